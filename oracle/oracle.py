@@ -1,0 +1,163 @@
+"""ctypes binding of the CPU oracle (oracle/mauve_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: the checker that tests/, __graft_entry__.smoke()
+and bench.py's CPU baseline compare the CUDA path against.  The product
+package never imports this module.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "lib", "libmauve_oracle.so")
+_lib = None
+
+
+def build(force=False):
+    """Compile oracle/mauve_oracle.c into oracle/lib/libmauve_oracle.so."""
+    src = os.path.join(_HERE, "mauve_oracle.c")
+    if not force and os.path.exists(LIB_PATH) and os.path.getmtime(LIB_PATH) >= os.path.getmtime(src):
+        return LIB_PATH
+    os.makedirs(os.path.dirname(LIB_PATH), exist_ok=True)
+    subprocess.check_call(["gcc", "-O2", "-fPIC", "-shared", "-o", LIB_PATH, src, "-lm", "-lpthread"])
+    return LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(LIB_PATH)
+        u64, i64, vp = ctypes.c_uint64, ctypes.c_int64, ctypes.c_void_p
+        L.mo_get_seed.restype = u64
+        L.mo_get_seed.argtypes = [ctypes.c_int, ctypes.c_int]
+        L.mo_seed_length.argtypes = [u64]
+        L.mo_seed_weight.argtypes = [u64]
+        L.mo_default_seed_weight.argtypes = [u64]
+        L.mo_default_seed_weight.restype = ctypes.c_uint
+        L.mo_pack.restype = i64
+        L.mo_pack.argtypes = [vp, u64, vp]
+        L.mo_seed_mers.restype = i64
+        L.mo_seed_mers.argtypes = [vp, u64, u64, vp]
+        L.mo_sml_build.restype = i64
+        L.mo_sml_build.argtypes = [vp, u64, u64, vp, vp]
+        L.mo_pairwise_matches.restype = i64
+        L.mo_pairwise_matches.argtypes = [vp, u64, vp, u64, u64, vp, u64]
+        L.mo_unique_pairs.restype = i64
+        L.mo_unique_pairs.argtypes = [vp, u64, vp, u64, u64, vp, vp, u64]
+        L.mo_nw_align.restype = i64
+        L.mo_nw_align.argtypes = [vp, ctypes.c_int, vp, ctypes.c_int, vp, vp]
+        L.mo_nw_score.restype = ctypes.c_int32
+        L.mo_nw_score.argtypes = [vp, ctypes.c_int, vp, ctypes.c_int]
+        L.mo_nw_batch.restype = i64
+        L.mo_nw_batch.argtypes = [vp, vp, vp, vp, i64, vp, vp, vp, vp, ctypes.c_int]
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _u8(seq):
+    if isinstance(seq, (bytes, bytearray)):
+        return np.frombuffer(bytes(seq), np.uint8)
+    return np.ascontiguousarray(seq, dtype=np.uint8)
+
+
+def get_seed(weight, rank):
+    return int(lib().mo_get_seed(weight, rank))
+
+
+def seed_length(seed):
+    return int(lib().mo_seed_length(seed))
+
+
+def seed_weight(seed):
+    return int(lib().mo_seed_weight(seed))
+
+
+def default_seed_weight(avg_len):
+    return int(lib().mo_default_seed_weight(avg_len))
+
+
+def pack(seq):
+    s = _u8(seq)
+    out = np.zeros(len(s) // 16 + 3, np.uint32)
+    n = lib().mo_pack(_p(s), len(s), _p(out))
+    if n < 0:
+        raise ValueError("gap character in genome sequence")
+    return out[:n]
+
+
+def seed_mers(seq, seed):
+    s = _u8(seq)
+    out = np.zeros(max(len(s), 1), np.uint64)
+    n = lib().mo_seed_mers(_p(s), len(s), seed, _p(out))
+    return out[:n]
+
+
+def sml_build(seq, seed):
+    s = _u8(seq)
+    pos = np.zeros(max(len(s), 1), np.uint32)
+    mer = np.zeros(max(len(s), 1), np.uint64)
+    n = lib().mo_sml_build(_p(s), len(s), seed, _p(pos), _p(mer))
+    return pos[:n], mer[:n]
+
+
+def unique_pairs(a, b, seed):
+    a, b = _u8(a), _u8(b)
+    cap = max(min(len(a), len(b)), 1)
+    pa = np.zeros(cap, np.uint32)
+    pb = np.zeros(cap, np.uint32)
+    n = lib().mo_unique_pairs(_p(a), len(a), _p(b), len(b), seed, _p(pa), _p(pb), cap)
+    if n < 0:
+        raise RuntimeError("mo_unique_pairs failed: %d" % n)
+    return pa[:n], pb[:n]
+
+
+def pairwise_matches(a, b, seed):
+    """(start0, start1, length) rows in the reference's MatchList order."""
+    a, b = _u8(a), _u8(b)
+    cap = max(min(len(a), len(b)), 16)
+    out = np.zeros(3 * cap, np.int64)
+    n = lib().mo_pairwise_matches(_p(a), len(a), _p(b), len(b), seed, _p(out), cap)
+    if n < 0:
+        raise RuntimeError("mo_pairwise_matches failed: %d" % n)
+    return out[: 3 * n].reshape(-1, 3)
+
+
+def nw_align(a, b):
+    """(path string of 'M'/'D'/'I', score) for base codes 0..3."""
+    a, b = _u8(a), _u8(b)
+    path = ctypes.create_string_buffer(len(a) + len(b) + 1)
+    score = ctypes.c_int32(0)
+    n = lib().mo_nw_align(_p(a), len(a), _p(b), len(b), path, ctypes.byref(score))
+    if n < 0:
+        raise ValueError("bad DP input")
+    return path.raw[:n].decode(), int(score.value)
+
+
+def nw_score(a, b):
+    a, b = _u8(a), _u8(b)
+    return int(lib().mo_nw_score(_p(a), len(a), _p(b), len(b)))
+
+
+def nw_batch(seq_a, off_a, seq_b, off_b, with_paths=True, nthreads=0):
+    """Batch of problems; returns (scores, path_len, paths, path_off)."""
+    seq_a, seq_b = _u8(seq_a), _u8(seq_b)
+    off_a = np.ascontiguousarray(off_a, np.uint64)
+    off_b = np.ascontiguousarray(off_b, np.uint64)
+    nprob = len(off_a) - 1
+    la = np.diff(off_a.astype(np.int64))
+    lb = np.diff(off_b.astype(np.int64))
+    path_off = np.zeros(nprob + 1, np.uint64)
+    path_off[1:] = np.cumsum(la + lb)
+    paths = np.zeros(int(path_off[-1]) if with_paths else 1, np.uint8)
+    plen = np.zeros(max(nprob, 1), np.int64)
+    scores = np.zeros(max(nprob, 1), np.int32)
+    lib().mo_nw_batch(_p(seq_a), _p(off_a), _p(seq_b), _p(off_b), nprob,
+                      _p(paths) if with_paths else None, _p(path_off), _p(plen), _p(scores), nthreads)
+    return scores[:nprob], plen[:nprob], paths, path_off

@@ -1,0 +1,37 @@
+// Test-only stand-in for the subset of boost::dynamic_bitset the reference's
+// match classes call (test/set/flip/resize/size and comparison).
+#pragma once
+#include <vector>
+#include <cstddef>
+namespace boost {
+template <class B = unsigned long, class A = void> class dynamic_bitset {
+  std::vector<bool> v_;
+ public:
+  typedef std::size_t size_type;
+  dynamic_bitset() {}
+  explicit dynamic_bitset(size_type n, unsigned long val = 0) : v_(n, false) {
+    for (size_type i = 0; i < n && i < 64; ++i) v_[i] = (val >> i) & 1UL;
+  }
+  size_type size() const { return v_.size(); }
+  bool test(size_type i) const { return v_[i]; }
+  dynamic_bitset& set(size_type i, bool b = true) { v_[i] = b; return *this; }
+  dynamic_bitset& set() { for (size_type i = 0; i < v_.size(); ++i) v_[i] = true; return *this; }
+  dynamic_bitset& reset(size_type i) { v_[i] = false; return *this; }
+  dynamic_bitset& reset() { for (size_type i = 0; i < v_.size(); ++i) v_[i] = false; return *this; }
+  dynamic_bitset& flip() { v_.flip(); return *this; }
+  dynamic_bitset& flip(size_type i) { v_[i] = !v_[i]; return *this; }
+  void resize(size_type n, bool b = false) { v_.resize(n, b); }
+  void clear() { v_.clear(); }
+  void push_back(bool b) { v_.push_back(b); }
+  bool operator[](size_type i) const { return v_[i]; }
+  std::vector<bool>::reference operator[](size_type i) { return v_[i]; }
+  size_type count() const { size_type c = 0; for (bool b : v_) c += b; return c; }
+  bool any() const { return count() > 0; }
+  bool none() const { return count() == 0; }
+  bool operator==(const dynamic_bitset& o) const { return v_ == o.v_; }
+  bool operator!=(const dynamic_bitset& o) const { return v_ != o.v_; }
+  bool operator<(const dynamic_bitset& o) const { return v_ < o.v_; }
+  dynamic_bitset& operator&=(const dynamic_bitset& o) { for (size_type i = 0; i < v_.size(); ++i) v_[i] = v_[i] && o.v_[i]; return *this; }
+  dynamic_bitset& operator|=(const dynamic_bitset& o) { for (size_type i = 0; i < v_.size(); ++i) v_[i] = v_[i] || o.v_[i]; return *this; }
+};
+}

@@ -1,0 +1,218 @@
+"""Seeded synthetic genome pairs and gap-alignment batches.
+
+The reference publishes no benchmark data; these generators produce inputs
+with the sizes and mutation spectra of the five workloads the build is
+measured on (numpy default_rng, fixed seeds, so every run sees the same
+bytes).  Sequences are ASCII uint8 arrays ('A','C','G','T'); DP batches are
+base codes 0..3.
+"""
+import numpy as np
+
+ACGT = np.frombuffer(b"ACGT", np.uint8)
+_COMP = np.zeros(256, np.uint8)
+for _x, _y in zip(b"ACGT", b"TGCA"):
+    _COMP[_x] = _y
+
+
+def random_bases(rng, n, gc=0.5):
+    p = [(1 - gc) / 2, gc / 2, gc / 2, (1 - gc) / 2]
+    return ACGT[rng.choice(4, size=n, p=p)].astype(np.uint8)
+
+
+def revcomp(s):
+    return _COMP[s[::-1]]
+
+
+def _substitute(rng, s, mask):
+    """Replace the masked bases with a different base (uniform over the other three)."""
+    idx = np.nonzero(mask)[0]
+    if len(idx) == 0:
+        return s
+    code = np.searchsorted(ACGT, s[idx])
+    code = np.where(code > 3, 0, code)
+    s = s.copy()
+    s[idx] = ACGT[(code + rng.integers(1, 4, len(idx))) % 4]
+    return s
+
+
+def _indels(rng, s, nindel, mean_len):
+    if nindel <= 0:
+        return s
+    pos = np.sort(rng.integers(0, len(s), nindel))
+    lens = rng.geometric(1.0 / mean_len, nindel)
+    ins = rng.random(nindel) < 0.5
+    parts, prev = [], 0
+    for p, l, i in zip(pos, lens, ins):
+        if p < prev:
+            continue
+        parts.append(s[prev:p])
+        if i:
+            parts.append(random_bases(rng, int(l)))
+            prev = p
+        else:
+            prev = min(len(s), p + int(l))
+    parts.append(s[prev:])
+    return np.concatenate(parts)
+
+
+def _rearrange(rng, s, n, len_range):
+    """n inversions or translocations of segments with lengths in len_range."""
+    s = s.copy()
+    for _ in range(n):
+        l = int(rng.integers(len_range[0], len_range[1] + 1))
+        if l >= len(s) // 2:
+            continue
+        p = int(rng.integers(0, len(s) - l))
+        if rng.random() < 0.5:
+            s[p:p + l] = revcomp(s[p:p + l])
+        else:
+            seg = s[p:p + l].copy()
+            rest = np.concatenate([s[:p], s[p + l:]])
+            q = int(rng.integers(0, len(rest)))
+            s = np.concatenate([rest[:q], seg, rest[q:]])
+    return s
+
+
+def mutate(rng, b, sub, nindel, mean_len, nrearr, rearr_len):
+    a = _substitute(rng, b, rng.random(len(b)) < sub)
+    a = _indels(rng, a, nindel, mean_len)
+    return _rearrange(rng, a, nrearr, rearr_len)
+
+
+def insert_repeats(rng, b, family_len, copies, families=1):
+    fams = [random_bases(rng, family_len) for _ in range(families)]
+    pos = np.sort(rng.integers(0, len(b), copies))
+    parts, prev = [], 0
+    for k, p in enumerate(pos):
+        parts.append(b[prev:p])
+        parts.append(fams[k % families])
+        prev = p
+    parts.append(b[prev:])
+    return np.concatenate(parts)
+
+
+def mutate_codes(rng, a, sub, nindel, mean_len):
+    """Mutate a base-code (0..3) sequence; never returns an empty sequence."""
+    s = ACGT[a]
+    s = _indels(rng, _substitute(rng, s, rng.random(len(s)) < sub), nindel, mean_len)
+    if len(s) == 0:
+        s = ACGT[rng.integers(0, 4, 1)]
+    return np.searchsorted(ACGT, s).astype(np.uint8)
+
+
+# ---------------------------------------------------------------- workloads
+
+def genome_pair_small(seed=0, n=1_000_000):
+    """Plain-method pair: B i.i.d. at GC 0.50; A = B + 0.5% substitutions,
+    50 indels (geometric mean 5, half insertions) and 2 inversions of 10 kbp."""
+    rng = np.random.default_rng(seed)
+    b = random_bases(rng, n, 0.50)
+    a = _substitute(rng, b, rng.random(n) < 0.005)
+    a = _indels(rng, a, 50, 5.0)
+    for _ in range(2):
+        p = int(rng.integers(0, len(a) - 10_000))
+        a[p:p + 10_000] = revcomp(a[p:p + 10_000])
+    return a, b
+
+
+def genome_pair_recoded(seed=1, n=4_600_000):
+    """Recoded-genome stand-in: B at GC 0.508 with 40 copies of one 1.3 kbp
+    repeat and 4,300 non-overlapping ORFs (mean 950 bp, multiple of 3);
+    A = B with 3% of ORF codon third positions substituted, 0.05% elsewhere,
+    200 indels (geometric mean 4) and 5 rearrangements of 5-50 kbp."""
+    rng = np.random.default_rng(seed)
+    core = random_bases(rng, n - 40 * 1300, 0.508)
+    b = insert_repeats(rng, core, 1300, 40)
+    norf = int(4300 * len(b) / 4_600_000)
+    lens = (np.maximum(rng.normal(950, 250, norf), 90) // 3 * 3).astype(np.int64)
+    total = int(lens.sum())
+    if total > 0.95 * len(b):
+        lens = (lens * (0.95 * len(b) / total) // 3 * 3).astype(np.int64)
+        total = int(lens.sum())
+    gaps = rng.multinomial(len(b) - total, np.ones(norf + 1) / (norf + 1))
+    in_orf3 = np.zeros(len(b), bool)
+    p = 0
+    for g, l in zip(gaps[:-1], lens):
+        p += int(g)
+        in_orf3[p + 2:p + l:3] = True
+        p += int(l)
+    in_orf = np.zeros(len(b), bool)
+    u = rng.random(len(b))
+    mask = np.where(in_orf3, u < 0.03, u < 0.0005)
+    del in_orf
+    a = _substitute(rng, b, mask)
+    a = _indels(rng, a, 200, 4.0)
+    a = _rearrange(rng, a, 5, (5_000, 50_000))
+    return a, b
+
+
+def genome_pair_large(seed=5, n=12_000_000, ncontig=16):
+    """Large pair: B = 12 Mbp in 16 contigs (0.2-1.5 Mbp) at GC 0.38 with
+    300 copies of 5 repeat families (0.3-6 kbp); A = B with 8%
+    substitutions, 2,000 indels (mean 6) and 1,000 rearrangements of
+    1-100 kbp.  Contigs are concatenated (the seed path sees one sequence)."""
+    rng = np.random.default_rng(seed)
+    fam_lens = rng.integers(300, 6001, 5)
+    rep_total = int(sum(fam_lens[k % 5] for k in range(300)))
+    core = random_bases(rng, n - rep_total, 0.38)
+    fams = [random_bases(rng, int(l), 0.38) for l in fam_lens]
+    pos = np.sort(rng.integers(0, len(core), 300))
+    parts, prev = [], 0
+    for k, p in enumerate(pos):
+        parts.append(core[prev:p])
+        parts.append(fams[k % 5])
+        prev = p
+    parts.append(core[prev:])
+    b = np.concatenate(parts)
+    a = _substitute(rng, b, rng.random(len(b)) < 0.08)
+    a = _indels(rng, a, 2000, 6.0)
+    a = _rearrange(rng, a, 1000, (1_000, 100_000))
+    return a, b
+
+
+def gap_batch(seed=3, nprob=200_000, lmin=10, lmax=20_000, max_div=0.30):
+    """Independent DP problems: lengths log-uniform on [lmin, lmax], the
+    second sequence derived from the first at divergence U(0, max_div)
+    (substitutions:indels 9:1, indel length geometric mean 3).
+    Returns concatenated base codes and offsets (nprob+1)."""
+    rng = np.random.default_rng(seed)
+    la = np.exp(rng.uniform(np.log(lmin), np.log(lmax), nprob)).astype(np.int64)
+    div = rng.uniform(0, max_div, nprob)
+    seq_a = rng.integers(0, 4, int(la.sum())).astype(np.uint8)
+    off_a = np.zeros(nprob + 1, np.int64)
+    off_a[1:] = np.cumsum(la)
+    pieces = []
+    for k in range(nprob):
+        a = seq_a[off_a[k]:off_a[k + 1]]
+        sub = 0.9 * div[k]
+        nind = rng.poisson(0.1 * div[k] * len(a) / 3.0)
+        pieces.append(_mutate_codes_fast(rng, a, sub, nind))
+    seq_b = np.concatenate(pieces)
+    off_b = np.zeros(nprob + 1, np.int64)
+    off_b[1:] = np.cumsum([len(x) for x in pieces])
+    return seq_a, off_a, seq_b, off_b
+
+
+def _mutate_codes_fast(rng, a, sub, nind):
+    m = rng.random(len(a)) < sub
+    b = a.copy()
+    b[m] = (b[m] + rng.integers(1, 4, int(m.sum()))) % 4
+    if nind:
+        pos = np.sort(rng.integers(0, len(b), nind))
+        lens = rng.geometric(1 / 3.0, nind)
+        ins = rng.random(nind) < 0.5
+        parts, prev = [], 0
+        for p, l, i in zip(pos, lens, ins):
+            if p < prev:
+                continue
+            parts.append(b[prev:p])
+            if i:
+                parts.append(rng.integers(0, 4, int(l)).astype(np.uint8))
+                prev = p
+            else:
+                prev = min(len(b), p + int(l))
+        parts.append(b[prev:])
+        b = np.concatenate(parts)
+    if len(b) == 0:
+        b = rng.integers(0, 4, 1).astype(np.uint8)
+    return b

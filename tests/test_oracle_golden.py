@@ -1,0 +1,57 @@
+"""Pins the CPU oracle to the golden fixtures made by the reference's own
+C++ code (tests/golden/make_golden.py)."""
+import numpy as np
+import pytest
+
+import oracle as O
+from conftest import load_golden
+
+
+def test_seed_table_and_default_weights():
+    g = load_golden("seeds.npz")
+    for wi, w in enumerate(range(3, 32)):
+        for r in range(6):
+            assert O.get_seed(w, r) == int(g["table"][wi, r]), (w, r)
+    for n, w in zip(g["lens"], g["weights"]):
+        assert O.default_seed_weight(int(n)) == int(w), n
+    # coding seed for the 1-4.6 Mbp genomes, solid 17-mer for 12 Mbp
+    assert O.get_seed(O.default_seed_weight(4_600_000), 3) == 0x16DF6D
+    assert O.get_seed(O.default_seed_weight(12_000_000), 3) == (1 << 17) - 1
+
+
+def test_sml_fill_and_sort_match_reference():
+    g = load_golden("sml.npz")
+    for k in range(int(g["count"])):
+        seq, seed = g["seq%d" % k], int(g["seed%d" % k])
+        np.testing.assert_array_equal(O.seed_mers(seq, seed), g["fill%d" % k])
+        pos, mer = O.sml_build(seq, seed)
+        rpos, rmer = g["pos%d" % k], g["mer%d" % k]
+        np.testing.assert_array_equal(mer, rmer)  # same sorted key sequence
+        # same (mer, pos) multiset; tie order inside equal mers is unspecified in the reference
+        ref = np.lexsort((rpos, rmer))
+        np.testing.assert_array_equal(pos, rpos[ref])
+
+
+def test_pairwise_match_lists_match_reference():
+    g = load_golden("matches.npz")
+    for k in range(int(g["count"])):
+        m = O.pairwise_matches(g["a%d" % k], g["b%d" % k], int(g["seed%d" % k]))
+        np.testing.assert_array_equal(m, g["m%d" % k], err_msg="case %d" % k)
+
+
+def test_gap_dp_paths_match_reference():
+    g = load_golden("gapdp.npz")
+    sa, sb, oa, ob, paths, op = g["seq_a"], g["seq_b"], g["off_a"], g["off_b"], g["paths"], g["off_p"]
+    for k in range(len(oa) - 1):
+        a, b = sa[oa[k]:oa[k + 1]], sb[ob[k]:ob[k + 1]]
+        path, score = O.nw_align(a, b)
+        assert path == paths[op[k]:op[k + 1]].tobytes().decode(), k
+        assert path.count("M") + path.count("D") == len(a)
+        assert path.count("M") + path.count("I") == len(b)
+
+
+def test_pack_layout():
+    w = O.pack(b"ACGTACGTACGTACGTC")
+    assert w[0] == 0x1B1B1B1B and w[1] == 0x40000000 and len(w) == 2 + 2
+    with pytest.raises(ValueError):
+        O.pack(b"AC-GT")
