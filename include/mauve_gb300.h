@@ -1,0 +1,126 @@
+/* mauve_gb300.h -- C ABI of the GB300 (sm_103a) pairwise anchoring and
+ * gap-alignment path of progressiveMauve.
+ *
+ * Plain C: POD pointers and sizes, an explicit CUDA stream passed as void*,
+ * integer status returns (0 = ok), no exceptions across the boundary.  The
+ * caller owns every input and output buffer; the library owns its device
+ * workspaces through an opaque handle.  Functions whose name ends in _dev
+ * take device pointers; the others take host pointers and do their own
+ * host<->device copies on the handle's stream.
+ *
+ * Reference citations are file:line within the mauve-py tree
+ * (LM/ = mauve/src/libMems/libMems/, MU/ = mauve/src/muscle/libMUSCLE/).
+ */
+#ifndef MAUVE_GB300_H
+#define MAUVE_GB300_H
+#include <stddef.h>
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. */
+#define MVG_OK 0
+#define MVG_ERR_ARG 1        /* invalid argument (null pointer, bad length, bad seed) */
+#define MVG_ERR_CUDA 2       /* a CUDA runtime call failed; see mvg_last_error() */
+#define MVG_ERR_GAP_CHAR 3   /* '-' in a genome sequence (LM/SortedMerList.cpp:433-437 throws) */
+#define MVG_ERR_BAD_BASE 4   /* gap-DP input code outside 0..3 */
+#define MVG_ERR_CAPACITY 5   /* caller's output buffer or a size limit is too small */
+#define MVG_ERR_NOMEM 6      /* device allocation failed */
+#define MVG_ERR_DEVICE 7     /* a kernel reported an internal error (watchdog, bound) */
+
+typedef struct mvg_context* mvg_handle;
+
+/* Creates a handle bound to CUDA device `device` with its own stream.
+ * Replaces nothing in the reference (which keeps no device state). */
+int mvg_create(mvg_handle* out, int device);
+int mvg_destroy(mvg_handle h);
+/* Human-readable description of the last error on this thread. */
+const char* mvg_last_error(void);
+/* The handle's CUDA stream (cudaStream_t as void*). */
+void* mvg_stream(mvg_handle h);
+/* Number of this library's kernels launched through the handle so far. */
+uint64_t mvg_kernel_launches(mvg_handle h);
+
+/* ---------------------------------------------------------------- seeds */
+
+/* getSeed(weight, rank) -- LM/SeedMasks.h:298-321 (pattern tables 44-260). */
+uint64_t mvg_get_seed(int weight, int rank);
+/* getDefaultSeedWeight -- LM/SeedMasks.h:389-401. */
+unsigned mvg_default_seed_weight(uint64_t avg_len);
+/* getSeedLength / getSeedWeight -- LM/SeedMasks.h:334-371. */
+int mvg_seed_length(uint64_t seed);
+int mvg_seed_weight(uint64_t seed);
+
+/* Sorted mer list construction: 2-bit packing (translate32,
+ * LM/SortedMerList.cpp:425-459), canonical spaced-seed mer per position
+ * (GetDnaSeedMer, :726-769; FillDnaSeedSML :771-784 / FillDnaSML :617-724)
+ * and the sort by mer (std::sort(bmer_lessthan), LM/MemorySML.cpp:45-60,
+ * LM/FileSML.cpp:429).  Replaces SortedMerList::Create (LM/SortedMerList.h:89).
+ * seq: n ASCII bases.  Writes n-L+1 positions sorted by canonical mer (ties
+ * by ascending position) and, if mer_out is not NULL, the canonical mers in
+ * the same order.  *count gets n-L+1 (0 if n < L). */
+int mvg_sml_build(mvg_handle h, const uint8_t* seq, uint64_t n, uint64_t seed,
+                  uint32_t* pos_out, uint64_t* mer_out, uint64_t cap, uint64_t* count);
+int mvg_sml_build_dev(mvg_handle h, const uint8_t* d_seq, uint64_t n, uint64_t seed,
+                      uint32_t* d_pos_out, uint64_t* d_mer_out, uint64_t cap, uint64_t* count);
+
+/* --------------------------------------------------------------- matches */
+
+/* Pairwise seed matching and maximal-match extension for two genomes:
+ * PairwiseMatchFinder::FindMatches as progressiveMauve calls it
+ * (MA/progressiveMauve.cpp:500-503): SearchRange (LM/MatchFinder.cpp:172-340),
+ * unique-seed enumeration (LM/PairwiseMatchFinder.cpp:37-71), HashMatch /
+ * SetDirection / CalculateOffset / AddHashEntry (LM/MemHash.cpp:167-251),
+ * ExtendMatch (LM/MatchFinder.h:218-374) and GetMatchList order
+ * (LM/MemHash.h:182-203).  Replaces MemHash::FindMatches(MatchList&)
+ * (LM/MemHash.h:55).
+ * out receives 3 int64 per match: start in A, start in B (1-based; a
+ * negative B start means the reverse strand) and length, in the reference's
+ * MatchList order.  *count gets the number of matches; MVG_ERR_CAPACITY if
+ * it exceeds cap (then *count still holds the needed size). */
+int mvg_pairwise_matches(mvg_handle h, const uint8_t* seq_a, uint64_t na, const uint8_t* seq_b,
+                         uint64_t nb, uint64_t seed, int64_t* out, uint64_t cap, uint64_t* count);
+int mvg_pairwise_matches_dev(mvg_handle h, const uint8_t* d_seq_a, uint64_t na, const uint8_t* d_seq_b,
+                             uint64_t nb, uint64_t seed, int64_t* d_out, uint64_t cap, uint64_t* count);
+
+/* Match-finding statistics of the last mvg_pairwise_matches* call on h:
+ * stats[0] = unique seed pairs hashed, [1] = collisions (contained seeds),
+ * [2] = matches, [3] = non-empty hash buckets. */
+int mvg_pairwise_stats(mvg_handle h, uint64_t stats[4]);
+
+/* ---------------------------------------------------------------- gap DP */
+
+/* Batched global gap alignment: for each problem p, muscle NWSmall
+ * (MU/nwsmall.cpp:500-670) on two single-sequence DNA profiles built with
+ * MUSCLE's DNA defaults (NUC_SP + 60, MU/nucmx.cpp:8-25; gap open -400 split
+ * into -200 open / -200 close, MU/profilefrommsa.cpp:291-292; extend 0;
+ * TERMGAPS_Half, MU/termgaps.cpp:6-38), then BitTraceBack
+ * (MU/bittraceback.cpp:138-210).  Replaces muscle::GlobalAlign
+ * (MU/glbalign.cpp:69) per range.
+ * seq_a / seq_b: concatenated base codes 0..3 (A,C,G,T); off_a / off_b:
+ * nprob+1 offsets; every length must be >= 1.  scores[p] gets
+ * max(M,D,I) at (LA,LB).  If paths is not NULL, path p is written as edge
+ * letters 'M' (both), 'D' (A only), 'I' (B only) in column order at
+ * paths + path_off[p] (path_off[p+1]-path_off[p] >= LA+LB) and its length
+ * in path_len[p]. */
+int mvg_gapdp_batch(mvg_handle h, const uint8_t* seq_a, const uint64_t* off_a, const uint8_t* seq_b,
+                    const uint64_t* off_b, int64_t nprob, int32_t* scores, char* paths,
+                    const uint64_t* path_off, int64_t* path_len);
+int mvg_gapdp_batch_dev(mvg_handle h, const uint8_t* d_seq_a, const uint64_t* d_off_a, const uint8_t* d_seq_b,
+                        const uint64_t* d_off_b, int64_t nprob, int32_t* d_scores, char* d_paths,
+                        const uint64_t* d_path_off, int64_t* d_path_len);
+
+/* Device bytes the gap-DP traceback arena may use (default 32 GiB); problems
+ * run in waves that fit it. */
+int mvg_set_tb_arena(mvg_handle h, uint64_t bytes);
+
+/* Microbenchmark: sustained INT32 add/max throughput of this GPU, in
+ * operations per second, from a dependent-chain-free kernel timed with
+ * CUDA events.  Used as the roofline denominator for the gap DP. */
+int mvg_probe_int32_peak(mvg_handle h, double* ops_per_s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,320 @@
+// C ABI (include/mauve_gb300.h): handle lifetime, host-buffer wrappers,
+// error reporting and the grow-only device workspace.
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "mvg_internal.h"
+
+namespace mvg {
+
+static thread_local char g_last_error[512] = "";
+
+int report_error(int code, const char* msg) {
+  snprintf(g_last_error, sizeof(g_last_error), "%s", msg);
+  return code;
+}
+
+int report_cuda(cudaError_t e, const char* what) {
+  snprintf(g_last_error, sizeof(g_last_error), "%s: %s", what, cudaGetErrorString(e));
+  return e == cudaErrorMemoryAllocation ? MVG_ERR_NOMEM : MVG_ERR_CUDA;
+}
+
+void* Workspace::get(Ctx* c, int slot, size_t bytes) {
+  if (slot < 0 || slot >= kSlots) return nullptr;
+  if (bytes == 0) bytes = 16;
+  if (size[slot] >= bytes) return ptr[slot];
+  if (ptr[slot]) {
+    cudaStreamSynchronize(c->stream);
+    cudaFree(ptr[slot]);
+    ptr[slot] = nullptr;
+    size[slot] = 0;
+  }
+  size_t want = bytes + bytes / 8 + 256;  // headroom so near-equal sizes reuse
+  if (cudaMalloc(&ptr[slot], want) != cudaSuccess) {
+    cudaGetLastError();
+    ptr[slot] = nullptr;
+    return nullptr;
+  }
+  size[slot] = want;
+  return ptr[slot];
+}
+
+void Workspace::release() {
+  for (int i = 0; i < kSlots; ++i) {
+    if (ptr[i]) cudaFree(ptr[i]);
+    ptr[i] = nullptr;
+    size[i] = 0;
+  }
+}
+
+int check_device_error(Ctx* c) {
+  MVG_CUDA_TRY(cudaMemcpyAsync(c->h_err, c->d_err, 4, cudaMemcpyDeviceToHost, c->stream));
+  MVG_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  switch (*c->h_err) {
+    case kDevOk:
+      return 0;
+    case kDevGapChar:
+      return report_error(MVG_ERR_GAP_CHAR, "gap character '-' in genome sequence");
+    case kDevBadBase:
+      return report_error(MVG_ERR_BAD_BASE, "gap-DP base code outside 0..3");
+    case kDevCapacity:
+      return report_error(MVG_ERR_DEVICE, "device capacity bound exceeded");
+    default:
+      return report_error(MVG_ERR_DEVICE, "device kernel reported an error");
+  }
+}
+
+int upload_base_table();
+int upload_score_table();
+
+}  // namespace mvg
+
+using namespace mvg;
+
+struct mvg_context : public mvg::Ctx {};
+
+// Resolved seed patterns (weights 3..31, ranks 0..5): getSeed() over the
+// tables of LM/SeedMasks.h:44-260 with its solid fallbacks applied.
+static const uint64_t kSeedTable[29][6] = {
+    {0xb, 0x7, 0x7, 0x7, 0x7, 0x7},
+    {0x3b, 0xf, 0xf, 0xf, 0xf, 0xf},
+    {0x6b, 0x139, 0x193, 0x6b, 0x1f, 0x1f},
+    {0x58d, 0x653, 0x1ab, 0xdb, 0x3f, 0x3f},
+    {0x1953, 0x588d, 0x688b, 0x17d, 0x164d, 0x7f},
+    {0x3927, 0x1ca7, 0x6553, 0xb6d, 0xff, 0xff},
+    {0x7497, 0x1c927, 0x72a7, 0x6fb, 0x16ed, 0x1ff},
+    {0x1d297, 0x3a497, 0xe997, 0x6d5b, 0x3ff, 0x3ff},
+    {0x7954f, 0x75257, 0x1c9527, 0x5bed, 0x5b26d, 0x7ff},
+    {0x7954f, 0x3d32f, 0x768b7, 0x5b56d, 0xfff, 0xfff},
+    {0x792a4f, 0x1d64d7, 0x1d3597, 0x1b7db, 0x75ad7, 0x1fff},
+    {0x1e6acf, 0xf59af, 0x3d4caf, 0x35ad6b, 0x3fff, 0x3fff},
+    {0x7ac9af, 0x7b2a6f, 0x79aacf, 0x16df6d, 0x6b5d6b, 0x7fff},
+    {0xf599af, 0xee5a77, 0x7cd59f, 0xeb5ad7, 0xffff, 0xffff},
+    {0x6dbedb, 0x1ffff, 0x1ffff, 0x1ffff, 0x1ffff, 0x1ffff},
+    {0x3e6b59f, 0x3eb335f, 0x7b3566f, 0x3ffff, 0x3ffff, 0x3ffff},
+    {0x7b974ef, 0x7d6735f, 0x1edd74f, 0x7ffff, 0x7ffff, 0x7ffff},
+    {0x1f59b35f, 0x3edcedf, 0xfae675f, 0xfffff, 0xfffff, 0xfffff},
+    {0x7ddaddf, 0xaeb3f, 0x7eb76bf, 0x1fffff, 0x1fffff, 0x1fffff},
+    {0x3fffff, 0x3fffff, 0x3fffff, 0x3fffff, 0x3fffff, 0x3fffff},
+    {0x7fffff, 0x7fffff, 0x7fffff, 0x7fffff, 0x7fffff, 0x7fffff},
+    {0xffffff, 0xffffff, 0xffffff, 0xffffff, 0xffffff, 0xffffff},
+    {0x1ffffff, 0x1ffffff, 0x1ffffff, 0x1ffffff, 0x1ffffff, 0x1ffffff},
+    {0x3ffffff, 0x3ffffff, 0x3ffffff, 0x3ffffff, 0x3ffffff, 0x3ffffff},
+    {0x7ffffff, 0x7ffffff, 0x7ffffff, 0x7ffffff, 0x7ffffff, 0x7ffffff},
+    {0xfffffff, 0xfffffff, 0xfffffff, 0xfffffff, 0xfffffff, 0xfffffff},
+    {0x1fffffff, 0x1fffffff, 0x1fffffff, 0x1fffffff, 0x1fffffff, 0x1fffffff},
+    {0x3fffffff, 0x3fffffff, 0x3fffffff, 0x3fffffff, 0x3fffffff, 0x3fffffff},
+    {0x7fffffff, 0x7fffffff, 0x7fffffff, 0x7fffffff, 0x7fffffff, 0x7fffffff},
+};
+
+extern "C" {
+
+const char* mvg_last_error(void) { return g_last_error; }
+
+int mvg_create(mvg_handle* out, int device) {
+  if (!out) return report_error(MVG_ERR_ARG, "null handle pointer");
+  *out = nullptr;
+  MVG_CUDA_TRY(cudaSetDevice(device));
+  mvg_context* c = new mvg_context();
+  c->device = device;
+  cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMalloc(&c->d_err, 64);
+  if (e == cudaSuccess) e = cudaMallocHost(&c->h_err, 64);
+  if (e == cudaSuccess) e = cudaMallocHost(&c->h_scalars, 64);
+  if (e != cudaSuccess) {
+    delete c;
+    return report_cuda(e, "mvg_create");
+  }
+  int rc = upload_base_table();
+  if (!rc) rc = upload_score_table();
+  if (rc) {
+    delete c;
+    return rc;
+  }
+  MVG_CUDA_TRY(cudaMemset(c->d_err, 0, 64));
+  *out = c;
+  return 0;
+}
+
+int mvg_destroy(mvg_handle h) {
+  if (!h) return 0;
+  cudaSetDevice(h->device);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  h->ws.release();
+  if (h->d_err) cudaFree(h->d_err);
+  if (h->h_err) cudaFreeHost(h->h_err);
+  if (h->h_scalars) cudaFreeHost(h->h_scalars);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+  return 0;
+}
+
+void* mvg_stream(mvg_handle h) { return h ? (void*)h->stream : nullptr; }
+
+uint64_t mvg_kernel_launches(mvg_handle h) { return h ? h->launches : 0; }
+
+uint64_t mvg_get_seed(int weight, int rank) {
+  if (weight > 31) return 0xffffffffull;
+  if (rank > 5 || rank < 0) return (1ull << weight) - 1;  // includes SOLID_SEED = INT_MAX
+  if (weight < 3) return 0;
+  return kSeedTable[weight - 3][rank];
+}
+
+unsigned mvg_default_seed_weight(uint64_t avg_len) {
+  unsigned w = (unsigned)ceil((log((double)avg_len) / log(2.0)) / 1.5);
+  if (!(w & 1)) ++w;
+  w = w < 5 ? 0 : w;
+  if (avg_len == 0) w = 0;
+  return w > 31 ? 31 : w;
+}
+
+int mvg_seed_length(uint64_t seed) { return seed ? 64 - __builtin_clzll(seed) - __builtin_ctzll(seed) : 0; }
+int mvg_seed_weight(uint64_t seed) { return __builtin_popcountll(seed); }
+
+int mvg_sml_build_dev(mvg_handle h, const uint8_t* d_seq, uint64_t n, uint64_t seed, uint32_t* d_pos_out,
+                      uint64_t* d_mer_out, uint64_t cap, uint64_t* count) {
+  if (!h || !count || (!d_seq && n)) return report_error(MVG_ERR_ARG, "null argument");
+  MVG_CUDA_TRY(cudaSetDevice(h->device));
+  const SeedDesc s = make_seed_desc(seed);
+  if (s.L == 0 || s.L > 31) return report_error(MVG_ERR_ARG, "invalid seed pattern");
+  if (n >= 0xffffffffull) return report_error(MVG_ERR_ARG, "sequence longer than 2^32-1");
+  const uint64_t cnt = n >= (uint64_t)s.L ? n - s.L + 1 : 0;
+  *count = cnt;
+  if (cnt > cap) return report_error(MVG_ERR_CAPACITY, "SML output buffer too small");
+  uint32_t* g = (uint32_t*)h->ws.get(h, 20, packed_words(n) * 4);
+  if (!g) return report_error(MVG_ERR_NOMEM, "workspace allocation failed");
+  MVG_CUDA_TRY(cudaMemsetAsync(h->d_err, 0, 4, h->stream));
+  int rc = pack_sequence(h, d_seq, n, g);
+  if (rc) return rc;
+  if (cnt) {
+    rc = sml_sort(h, g, cnt, s, d_pos_out, d_mer_out, nullptr, 0);
+    if (rc) return rc;
+  }
+  return check_device_error(h);
+}
+
+int mvg_sml_build(mvg_handle h, const uint8_t* seq, uint64_t n, uint64_t seed, uint32_t* pos_out, uint64_t* mer_out,
+                  uint64_t cap, uint64_t* count) {
+  if (!h || !count || (!seq && n)) return report_error(MVG_ERR_ARG, "null argument");
+  MVG_CUDA_TRY(cudaSetDevice(h->device));
+  const int L = mvg_seed_length(seed);
+  const uint64_t cnt = (L && n >= (uint64_t)L) ? n - L + 1 : 0;
+  *count = cnt;
+  if (cnt > cap) return report_error(MVG_ERR_CAPACITY, "SML output buffer too small");
+  uint8_t* d_seq = (uint8_t*)h->ws.get(h, 46, n + 16);
+  uint32_t* d_pos = (uint32_t*)h->ws.get(h, 47, cnt * 4 + 16);
+  uint64_t* d_mer = mer_out ? (uint64_t*)h->ws.get(h, 9, cnt * 8 + 16) : nullptr;
+  if (!d_seq || !d_pos || (mer_out && !d_mer)) return report_error(MVG_ERR_NOMEM, "workspace allocation failed");
+  MVG_CUDA_TRY(cudaMemcpyAsync(d_seq, seq, n, cudaMemcpyHostToDevice, h->stream));
+  int rc = mvg_sml_build_dev(h, d_seq, n, seed, d_pos, d_mer, cap, count);
+  if (rc) return rc;
+  if (pos_out) MVG_CUDA_TRY(cudaMemcpyAsync(pos_out, d_pos, cnt * 4, cudaMemcpyDeviceToHost, h->stream));
+  if (mer_out) MVG_CUDA_TRY(cudaMemcpyAsync(mer_out, d_mer, cnt * 8, cudaMemcpyDeviceToHost, h->stream));
+  MVG_CUDA_TRY(cudaStreamSynchronize(h->stream));
+  return 0;
+}
+
+int mvg_pairwise_matches_dev(mvg_handle h, const uint8_t* d_seq_a, uint64_t na, const uint8_t* d_seq_b, uint64_t nb,
+                             uint64_t seed, int64_t* d_out, uint64_t cap, uint64_t* count) {
+  if (!h || !count || (!d_seq_a && na) || (!d_seq_b && nb) || (!d_out && cap))
+    return report_error(MVG_ERR_ARG, "null argument");
+  MVG_CUDA_TRY(cudaSetDevice(h->device));
+  return pairwise_matches_dev(h, d_seq_a, na, d_seq_b, nb, seed, d_out, cap, count);
+}
+
+int mvg_pairwise_matches(mvg_handle h, const uint8_t* seq_a, uint64_t na, const uint8_t* seq_b, uint64_t nb,
+                         uint64_t seed, int64_t* out, uint64_t cap, uint64_t* count) {
+  if (!h || !count || (!seq_a && na) || (!seq_b && nb) || (!out && cap)) return report_error(MVG_ERR_ARG, "null argument");
+  MVG_CUDA_TRY(cudaSetDevice(h->device));
+  uint8_t* da = (uint8_t*)h->ws.get(h, 46, na + 16);
+  uint8_t* db = (uint8_t*)h->ws.get(h, 47, nb + 16);
+  const uint64_t dcap = std::max<uint64_t>(cap, 1);
+  int64_t* dout = (int64_t*)h->ws.get(h, 57, dcap * 24);
+  if (!da || !db || !dout) return report_error(MVG_ERR_NOMEM, "workspace allocation failed");
+  MVG_CUDA_TRY(cudaMemcpyAsync(da, seq_a, na, cudaMemcpyHostToDevice, h->stream));
+  MVG_CUDA_TRY(cudaMemcpyAsync(db, seq_b, nb, cudaMemcpyHostToDevice, h->stream));
+  int rc = pairwise_matches_dev(h, da, na, db, nb, seed, dout, cap, count);
+  if (rc && rc != MVG_ERR_CAPACITY) return rc;
+  const uint64_t nout = std::min<uint64_t>(*count, cap);
+  if (nout) MVG_CUDA_TRY(cudaMemcpyAsync(out, dout, nout * 24, cudaMemcpyDeviceToHost, h->stream));
+  MVG_CUDA_TRY(cudaStreamSynchronize(h->stream));
+  return rc;
+}
+
+int mvg_pairwise_stats(mvg_handle h, uint64_t stats[4]) {
+  if (!h || !stats) return report_error(MVG_ERR_ARG, "null argument");
+  stats[0] = h->stats.pairs;
+  stats[1] = h->stats.collisions;
+  stats[2] = h->stats.matches;
+  stats[3] = h->stats.buckets;
+  return 0;
+}
+
+int mvg_gapdp_batch_dev(mvg_handle h, const uint8_t* d_seq_a, const uint64_t* d_off_a, const uint8_t* d_seq_b,
+                        const uint64_t* d_off_b, int64_t nprob, int32_t* d_scores, char* d_paths,
+                        const uint64_t* d_path_off, int64_t* d_path_len) {
+  if (!h || nprob < 0 || (nprob && (!d_off_a || !d_off_b || !d_scores)) || (d_paths && (!d_path_off || !d_path_len)))
+    return report_error(MVG_ERR_ARG, "null argument");
+  if (nprob == 0) return 0;
+  MVG_CUDA_TRY(cudaSetDevice(h->device));
+  std::vector<uint64_t> oa(nprob + 1), ob(nprob + 1);
+  MVG_CUDA_TRY(cudaMemcpyAsync(oa.data(), d_off_a, (nprob + 1) * 8, cudaMemcpyDeviceToHost, h->stream));
+  MVG_CUDA_TRY(cudaMemcpyAsync(ob.data(), d_off_b, (nprob + 1) * 8, cudaMemcpyDeviceToHost, h->stream));
+  MVG_CUDA_TRY(cudaStreamSynchronize(h->stream));
+  return gapdp_batch_dev(h, d_seq_a, d_off_a, d_seq_b, d_off_b, nprob, d_scores, d_paths, d_path_off, d_path_len,
+                         oa.data(), ob.data());
+}
+
+int mvg_gapdp_batch(mvg_handle h, const uint8_t* seq_a, const uint64_t* off_a, const uint8_t* seq_b,
+                    const uint64_t* off_b, int64_t nprob, int32_t* scores, char* paths, const uint64_t* path_off,
+                    int64_t* path_len) {
+  if (!h || nprob < 0 || (nprob && (!off_a || !off_b || !scores || !seq_a || !seq_b)) ||
+      (paths && (!path_off || !path_len)))
+    return report_error(MVG_ERR_ARG, "null argument");
+  if (nprob == 0) return 0;
+  MVG_CUDA_TRY(cudaSetDevice(h->device));
+  const uint64_t na = off_a[nprob], nb = off_b[nprob];
+  const uint64_t np = paths ? path_off[nprob] : 0;
+  uint8_t* dsa = (uint8_t*)h->ws.get(h, 46, na + 16);
+  uint8_t* dsb = (uint8_t*)h->ws.get(h, 47, nb + 16);
+  uint64_t* doa = (uint64_t*)h->ws.get(h, 5, (nprob + 1) * 8);
+  uint64_t* dob = (uint64_t*)h->ws.get(h, 6, (nprob + 1) * 8);
+  int32_t* dsc = (int32_t*)h->ws.get(h, 7, nprob * 4);
+  char* dpa = paths ? (char*)h->ws.get(h, 9, np + 16) : nullptr;
+  uint64_t* dpo = paths ? (uint64_t*)h->ws.get(h, 8, (nprob + 1) * 8) : nullptr;
+  int64_t* dpl = paths ? (int64_t*)h->ws.get(h, 22, nprob * 8) : nullptr;
+  if (!dsa || !dsb || !doa || !dob || !dsc || (paths && (!dpa || !dpo || !dpl)))
+    return report_error(MVG_ERR_NOMEM, "workspace allocation failed");
+  MVG_CUDA_TRY(cudaMemcpyAsync(dsa, seq_a, na, cudaMemcpyHostToDevice, h->stream));
+  MVG_CUDA_TRY(cudaMemcpyAsync(dsb, seq_b, nb, cudaMemcpyHostToDevice, h->stream));
+  MVG_CUDA_TRY(cudaMemcpyAsync(doa, off_a, (nprob + 1) * 8, cudaMemcpyHostToDevice, h->stream));
+  MVG_CUDA_TRY(cudaMemcpyAsync(dob, off_b, (nprob + 1) * 8, cudaMemcpyHostToDevice, h->stream));
+  if (paths) MVG_CUDA_TRY(cudaMemcpyAsync(dpo, path_off, (nprob + 1) * 8, cudaMemcpyHostToDevice, h->stream));
+  int rc = gapdp_batch_dev(h, dsa, doa, dsb, dob, nprob, dsc, dpa, dpo, dpl, off_a, off_b);
+  if (rc) return rc;
+  MVG_CUDA_TRY(cudaMemcpyAsync(scores, dsc, nprob * 4, cudaMemcpyDeviceToHost, h->stream));
+  if (paths) {
+    MVG_CUDA_TRY(cudaMemcpyAsync(paths, dpa, np, cudaMemcpyDeviceToHost, h->stream));
+    MVG_CUDA_TRY(cudaMemcpyAsync(path_len, dpl, nprob * 8, cudaMemcpyDeviceToHost, h->stream));
+  }
+  MVG_CUDA_TRY(cudaStreamSynchronize(h->stream));
+  return 0;
+}
+
+int mvg_set_tb_arena(mvg_handle h, uint64_t bytes) {
+  if (!h || bytes < (1ull << 20)) return report_error(MVG_ERR_ARG, "arena must be at least 1 MiB");
+  h->tb_arena = bytes;
+  return 0;
+}
+
+int mvg_probe_int32_peak(mvg_handle h, double* ops_per_s) {
+  if (!h || !ops_per_s) return report_error(MVG_ERR_ARG, "null argument");
+  MVG_CUDA_TRY(cudaSetDevice(h->device));
+  return probe_int32_peak(h, ops_per_s);
+}
+
+}  // extern "C"

@@ -1,0 +1,491 @@
+// Pairwise seed matching and maximal-match extension (two genomes).
+//
+// The reference (PairwiseMatchFinder over MemHash) walks the two sorted mer
+// lists in key order, hashes every seed that is unique in both genomes into
+// one of 40,000 buckets by its generalised offset, skips a seed whose bucket
+// already holds a match containing it, and otherwise extends the seed to a
+// maximal spaced-seed match and inserts it in sorted position.  Only seeds
+// in the same bucket ever interact, so on the GPU:
+//
+//   k_unique_flags / k_compact_unique   per genome: keys unique under the
+//                                       seed mask (strand bit ignored)
+//   k_join                               merge-join of the two unique lists:
+//                                       the seed pairs, in ascending key
+//                                       order = the reference's hash order
+//   k_hash_pairs                         SetDirection + CalculateOffset +
+//                                       bucket id per pair
+//   stable radix sort by bucket          keeps key order inside a bucket
+//   k_bucket_warps                       one warp per bucket replays the
+//                                       reference's sequence of containment
+//                                       tests and inserts exactly: 32 seeds
+//                                       are tested at once against the
+//                                       current bucket, the first one not
+//                                       contained is extended warp-
+//                                       cooperatively (32 candidate windows
+//                                       per ballot) and inserted, and the
+//                                       seeds after it are re-tested
+//   k_emit                               GetMatchList order: bucket 0..39999,
+//                                       then bucket vector order
+#include "mvg_internal.h"
+#include "prim.cuh"
+
+namespace mvg {
+
+constexpr int kTableSize = 40000;  // LM/MemHash.h:30 DEFAULT_MEM_TABLE_SIZE
+
+struct Mhe {
+  int64_t s0, s1, len, off;
+};
+
+struct MatchCtx {
+  const uint32_t* g[2];
+  int64_t n[2];
+  SeedDesc s;
+};
+
+// ------------------------------------------------------------------ join
+
+template <typename K>
+__global__ void k_unique_flags(const K* __restrict__ keys, int64_t n, uint32_t* __restrict__ flag) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    uint64_t cur = (uint64_t)keys[i] >> 1;
+    bool u = true;
+    if (i > 0 && ((uint64_t)keys[i - 1] >> 1) == cur) u = false;
+    if (i + 1 < n && ((uint64_t)keys[i + 1] >> 1) == cur) u = false;
+    flag[i] = u;
+  }
+}
+
+template <typename K>
+__global__ void k_compact_unique(const K* __restrict__ keys, const uint32_t* __restrict__ pos, int64_t n,
+                                 const uint32_t* __restrict__ flag, const uint32_t* __restrict__ idx,
+                                 uint64_t* __restrict__ ukey, uint32_t* __restrict__ upos) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    if (flag[i]) {
+      uint32_t j = idx[i];
+      ukey[j] = (uint64_t)keys[i];  // seed bits << 1 | strand
+      upos[j] = pos[i];
+    }
+  }
+}
+
+// For each unique key of A, binary search the unique keys of B.
+__global__ void k_join(const uint64_t* __restrict__ ka, const uint32_t* __restrict__ nua_p, const uint64_t* __restrict__ kb,
+                       const uint32_t* __restrict__ nub_p, uint32_t* __restrict__ hit, int64_t cap_a) {
+  const int64_t na = *nua_p, nb = *nub_p;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < cap_a; i += (int64_t)gridDim.x * blockDim.x) {
+    uint32_t h = 0xffffffffu;
+    if (i < na) {
+      uint64_t key = ka[i] >> 1;
+      int64_t lo = 0, len = nb;
+      while (len > 0) {
+        int64_t half = len >> 1;
+        if ((kb[lo + half] >> 1) < key) {
+          lo = lo + half + 1;
+          len -= half + 1;
+        } else {
+          len = half;
+        }
+      }
+      if (lo < nb && (kb[lo] >> 1) == key) h = (uint32_t)lo;
+    }
+    hit[i] = h;
+  }
+}
+
+__global__ void k_hit_flags(const uint32_t* __restrict__ hit, int64_t n, uint32_t* __restrict__ flag) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    flag[i] = hit[i] != 0xffffffffu;
+}
+
+// One pair per hit: HashMatch (LM/MemHash.cpp:167-187) -> SetDirection
+// (:189-207) -> CalculateOffset (LM/MatchHashEntry.cpp:141-162) -> bucket.
+__global__ void k_hash_pairs(const uint64_t* __restrict__ ka, const uint32_t* __restrict__ pa, const uint64_t* __restrict__ kb,
+                             const uint32_t* __restrict__ pb, const uint32_t* __restrict__ hit,
+                             const uint32_t* __restrict__ flag, const uint32_t* __restrict__ idx, int64_t cap_a,
+                             const uint32_t* __restrict__ nua_p, int L, Mhe* __restrict__ mhe,
+                             uint32_t* __restrict__ bucket, uint32_t* __restrict__ order) {
+  const int64_t na = *nua_p;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < na && i < cap_a;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    if (!flag[i]) continue;
+    const uint32_t j = idx[i], h = hit[i];
+    Mhe m;
+    m.s0 = (int64_t)pa[i] + 1;
+    m.s1 = (int64_t)pb[h] + 1;
+    m.len = L;
+    const bool ref_forward = !(ka[i] & 1ull);
+    if (ref_forward == (bool)(kb[h] & 1ull)) m.s1 = -m.s1;
+    m.off = m.s1 - m.s0;
+    if (m.s1 < 0) m.off -= m.len;
+    const int64_t t = kTableSize;
+    bucket[j] = (uint32_t)(((m.off % t) + t) % t);
+    order[j] = j;
+    mhe[j] = m;
+  }
+}
+
+// ------------------------------------------------------- bucket replay
+
+// LM/MatchHashEntry.cpp:164-200 (Contains), two genomes, both present.
+__device__ __forceinline__ bool mhe_contains(const Mhe& c, const Mhe& m) {
+  if (c.off != m.off) return false;
+  const int64_t diff = m.s0 - c.s0;
+  if (c.s0 == 0) return false;
+  if (diff < 0 || (uint64_t)c.len < (uint64_t)(m.len + diff)) return false;
+  const int64_t diff_rc = m.len - c.len + diff;
+  const int64_t diff_i = m.s1 - c.s1;
+  if (m.s1 == 0 && c.s1 == 0) return true;
+  if (m.s1 < 0 && diff_rc == diff_i) return true;
+  return diff == diff_i;
+}
+
+// LM/MatchHashEntry.cpp:48-67 (strict_start_lessthan_ptr).
+__device__ __forceinline__ bool mhe_strict_lt(const Mhe& a, const Mhe& b, int L) {
+  int64_t x = a.s0 < 0 ? -a.s0 + a.len - L : a.s0;
+  int64_t y = b.s0 < 0 ? -b.s0 + b.len - L : b.s0;
+  if (x != y) return x < y;
+  x = a.s1 < 0 ? -a.s1 + a.len - L : a.s1;
+  y = b.s1 < 0 ? -b.s1 + b.len - L : b.s1;
+  if (x != y) return x < y;
+  return false;
+}
+
+// LM/MatchHashEntry.h:121-143 (MheCompare) for pairwise entries.
+__device__ __forceinline__ bool mhe_less(const Mhe& a, const Mhe& b, int L) {
+  if (mhe_contains(a, b) || mhe_contains(b, a)) return false;
+  return mhe_strict_lt(a, b, L);
+}
+
+// std::lower_bound's bisection: the comparator is not a strict weak order,
+// so the probe sequence decides which entry is tested and is kept exactly.
+__device__ __forceinline__ int64_t lower_bound_mhe(const Mhe* __restrict__ v, int64_t n, const Mhe& x, int L) {
+  int64_t first = 0, len = n;
+  while (len > 0) {
+    int64_t half = len >> 1, mid = first + half;
+    if (mhe_less(v[mid], x, L)) {
+      first = mid + 1;
+      len = len - half - 1;
+    } else {
+      len = half;
+    }
+  }
+  return first;
+}
+
+// Does the window pair after k steps of size J match?  State (st0, st1, len)
+// is the match before the steps; positive starts move left by k*J, the
+// length grows by k*J (LM/MatchFinder.h:265-318).
+__device__ __forceinline__ bool window_match(const MatchCtx& c, int64_t st0, int64_t st1, int64_t len, int64_t kJ) {
+  const int L = c.s.L;
+  const int64_t lk = len + kJ;
+  int64_t st[2] = {st0, st1};
+  uint64_t mer[2];
+  bool par[2];
+#pragma unroll
+  for (int q = 0; q < 2; ++q) {
+    int64_t sq = st[q] > 0 ? st[q] - kJ : st[q];
+    int64_t get = sq < 0 ? -sq + lk - L : sq;
+    uint64_t cm = canonical_mer(c.g[q], (uint64_t)(get - 1), c.s);
+    par[q] = sq < 0 ? (bool)(cm & 1ull) : !(cm & 1ull);
+    mer[q] = cm & c.s.seed_mask;
+  }
+  return mer[0] == mer[1] && par[0] == par[1];
+}
+
+// ExtendMatch (LM/MatchFinder.h:218-374) for two genomes, executed by a full
+// warp in lockstep.  Phases 0/1 jump by the seed length until the first
+// mismatching window (32 jumps per ballot); phases 2/3 try the L single-base
+// offsets at once and move to the furthest matching one; any such move
+// restarts the four phases.
+__device__ void warp_extend(const MatchCtx& c, Mhe& m) {
+  const int lane = threadIdx.x & 31;
+  const int L = c.s.L;
+  int64_t st0 = m.s0, st1 = m.s1, len = m.len;
+  bool extend_again = false;
+  for (int dir = 0; dir < 4; ++dir) {
+    int64_t maxlen = dir < 2 ? (int64_t)0xffffffffu : (int64_t)L;
+    if (st0 < 0) {
+      int64_t rc = c.n[0] - len + st0 + 1;
+      if (rc < maxlen) maxlen = rc;
+    } else if (st0 - 1 < maxlen) {
+      maxlen = st0 - 1;
+    }
+    if (st1 < 0) {
+      int64_t rc = c.n[1] - len + st1 + 1;
+      if (rc < maxlen) maxlen = rc;
+    } else if (st1 - 1 < maxlen) {
+      maxlen = st1 - 1;
+    }
+    int64_t moved = 0;
+    if (dir < 2) {
+      const int64_t nj = maxlen >= L ? maxlen / L : 0;
+      int64_t good = nj;
+      for (int64_t base = 1; base <= nj; base += 32) {
+        const int64_t k = base + lane;
+        bool bad = false;
+        if (k <= nj) bad = !window_match(c, st0, st1, len, k * L);
+        const unsigned mm = __ballot_sync(0xffffffffu, bad);
+        if (mm) {
+          good = base - 1 + (__ffs(mm) - 1);
+          break;
+        }
+      }
+      moved = good * L;
+    } else {
+      const int64_t msteps = maxlen > 0 ? (maxlen < L ? maxlen : L) : 0;
+      const int64_t k = lane + 1;
+      bool ok = false;
+      if (k <= msteps) ok = window_match(c, st0, st1, len, k);
+      const unsigned mb = __ballot_sync(0xffffffffu, ok);
+      const int limit = mb ? 32 - __clz(mb) : 0;
+      if (msteps > 0 && limit > 0) extend_again = true;
+      moved = limit;
+    }
+    len += moved;
+    if (st0 > 0) st0 -= moved;
+    if (st1 > 0) st1 -= moved;
+    st0 = -st0;  // Invert
+    st1 = -st1;
+    if (dir == 3 && extend_again) {
+      dir = -1;
+      extend_again = false;
+    }
+  }
+  m.s0 = st0;
+  m.s1 = st1;
+  m.len = len;
+}
+
+// One warp per bucket (taken in descending seed count).  ent: per-bucket
+// regions of capacity = the bucket's seed count.
+__global__ void __launch_bounds__(256) k_bucket_warps(MatchCtx c, const Mhe* __restrict__ mhe,
+                                                      const uint32_t* __restrict__ sorted_pair,
+                                                      const uint32_t* __restrict__ bstart, const uint32_t* __restrict__ bcount,
+                                                      const uint32_t* __restrict__ border, int nbuckets, Mhe* ent,
+                                                      uint32_t* __restrict__ nent_out, unsigned long long* __restrict__ coll) {
+  const int lane = threadIdx.x & 31;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  const int L = c.s.L;
+  for (int w = gw; w < nbuckets; w += nw) {
+    const uint32_t b = border[w];
+    const uint32_t cnt = bcount[b];
+    if (cnt == 0) continue;
+    Mhe* E = ent + bstart[b];
+    const uint32_t* sp = sorted_pair + bstart[b];
+    int64_t n = 0;
+    unsigned long long ncoll = 0;
+    for (uint32_t base = 0; base < cnt; base += 32) {
+      const uint32_t i = base + lane;
+      Mhe m = {0, 0, 0, 0};
+      if (i < cnt) m = mhe[sp[i]];
+      unsigned pending = __ballot_sync(0xffffffffu, i < cnt);
+      while (pending) {
+        bool coll_here = true;
+        if (pending & (1u << lane)) {
+          int64_t at = lower_bound_mhe(E, n, m, L);
+          coll_here = at != n && !mhe_less(E[at], m, L) && !mhe_less(m, E[at], L);
+        }
+        const unsigned fresh = __ballot_sync(0xffffffffu, (pending & (1u << lane)) && !coll_here);
+        if (!fresh) break;
+        const int f = __ffs(fresh) - 1;
+        ncoll += __popc(pending & ((1u << f) - 1u));
+        pending &= ~((2u << f) - 1u);
+        Mhe x;
+        x.s0 = __shfl_sync(0xffffffffu, m.s0, f);
+        x.s1 = __shfl_sync(0xffffffffu, m.s1, f);
+        x.len = __shfl_sync(0xffffffffu, m.len, f);
+        x.off = __shfl_sync(0xffffffffu, m.off, f);
+        warp_extend(c, x);
+        const int64_t at = lower_bound_mhe(E, n, x, L);
+        // shift E[at..n) right by one, 32 entries at a time from the end
+        for (int64_t hi = n - 1; hi >= at; hi -= 32) {
+          const int64_t k = hi - lane;
+          Mhe t;
+          if (k >= at) t = E[k];
+          __syncwarp();
+          if (k >= at) E[k + 1] = t;
+          __syncwarp();
+        }
+        if (lane == 0) E[at] = x;
+        __syncwarp();
+        ++n;
+      }
+      ncoll += __popc(pending);
+    }
+    if (lane == 0) {
+      nent_out[b] = (uint32_t)n;
+      atomicAdd(coll, ncoll);
+    }
+  }
+}
+
+__global__ void k_bucket_hist(const uint32_t* __restrict__ bucket, const uint32_t* __restrict__ npairs_p,
+                              uint32_t* __restrict__ cnt) {
+  const int64_t np = *npairs_p;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < np; i += (int64_t)gridDim.x * blockDim.x)
+    atomicAdd(&cnt[bucket[i]], 1u);
+}
+
+__global__ void k_lpt_keys(const uint32_t* __restrict__ cnt, uint32_t* __restrict__ key, uint32_t* __restrict__ id) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < kTableSize; i += gridDim.x * blockDim.x) {
+    key[i] = 0xffffffffu - cnt[i];
+    id[i] = i;
+  }
+}
+
+// GetMatchList (LM/MemHash.h:182-203): bucket order, then vector order.
+__global__ void k_emit(const Mhe* __restrict__ ent, const uint32_t* __restrict__ bstart, const uint32_t* __restrict__ nent,
+                       const uint32_t* __restrict__ ooff, int64_t* __restrict__ out, uint64_t cap) {
+  const int lane = threadIdx.x & 31;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  for (int b = gw; b < kTableSize; b += nw) {
+    const uint32_t n = nent[b];
+    const Mhe* E = ent + bstart[b];
+    for (uint32_t k = lane; k < n; k += 32) {
+      const uint64_t o = (uint64_t)ooff[b] + k;
+      if (o < cap) {
+        out[3 * o + 0] = E[k].s0;
+        out[3 * o + 1] = E[k].s1;
+        out[3 * o + 2] = E[k].len;
+      }
+    }
+  }
+}
+
+template <typename K>
+static int unique_list(Ctx* c, const SmlKeys& sk, int slot, uint64_t** ukey, uint32_t** upos, uint32_t** d_count) {
+  const int64_t n = (int64_t)sk.count;
+  Workspace& ws = c->ws;
+  uint32_t* flag = (uint32_t*)ws.get(c, slot + 0, (n + 1) * sizeof(uint32_t));
+  uint32_t* idx = (uint32_t*)ws.get(c, slot + 1, (n + 1) * sizeof(uint32_t));
+  uint32_t* scr = (uint32_t*)ws.get(c, slot + 2, scan_scratch_words(n + 1) * sizeof(uint32_t) + 64);
+  *ukey = (uint64_t*)ws.get(c, slot + 3, (n + 1) * sizeof(uint64_t));
+  *upos = (uint32_t*)ws.get(c, slot + 4, (n + 1) * sizeof(uint32_t));
+  if (!flag || !idx || !scr || !*ukey || !*upos) return report_error(MVG_ERR_NOMEM, "workspace allocation failed");
+  *d_count = scr + scan_scratch_words(n + 1);
+  if (n == 0) {
+    MVG_CUDA_TRY(cudaMemsetAsync(*d_count, 0, sizeof(uint32_t), c->stream));
+    return 0;
+  }
+  k_unique_flags<K><<<grid_for(n, 256), 256, 0, c->stream>>>((const K*)sk.keys, n, flag);
+  exclusive_scan(flag, idx, n, scr, *d_count, c->stream, &c->launches);
+  k_compact_unique<K><<<grid_for(n, 256), 256, 0, c->stream>>>((const K*)sk.keys, sk.pos, n, flag, idx, *ukey, *upos);
+  c->launches += 2;
+  return 0;
+}
+
+int pairwise_matches_dev(Ctx* c, const uint8_t* d_a, uint64_t na, const uint8_t* d_b, uint64_t nb, uint64_t seed,
+                         int64_t* d_out, uint64_t cap, uint64_t* count) {
+  const SeedDesc s = make_seed_desc(seed);
+  if (s.L == 0 || s.L > 31) return report_error(MVG_ERR_ARG, "invalid seed pattern");
+  if (na >= 0x7fffffffull || nb >= 0x7fffffffull) return report_error(MVG_ERR_ARG, "genome longer than 2^31-1");
+  c->stats = MatchStats();
+  *count = 0;
+  Workspace& ws = c->ws;
+  uint32_t* ga = (uint32_t*)ws.get(c, 20, packed_words(na) * 4);
+  uint32_t* gb = (uint32_t*)ws.get(c, 21, packed_words(nb) * 4);
+  if (!ga || !gb) return report_error(MVG_ERR_NOMEM, "workspace allocation failed");
+  MVG_CUDA_TRY(cudaMemsetAsync(c->d_err, 0, sizeof(uint32_t), c->stream));
+  int rc;
+  if ((rc = pack_sequence(c, d_a, na, ga))) return rc;
+  if ((rc = pack_sequence(c, d_b, nb, gb))) return rc;
+  const uint64_t ca = na >= (uint64_t)s.L ? na - s.L + 1 : 0;
+  const uint64_t cb = nb >= (uint64_t)s.L ? nb - s.L + 1 : 0;
+  if (ca == 0 || cb == 0) return check_device_error(c);
+  SmlKeys ska, skb;
+  if ((rc = sml_sort(c, ga, ca, s, nullptr, nullptr, &ska, 0))) return rc;
+  if ((rc = sml_sort(c, gb, cb, s, nullptr, nullptr, &skb, 52))) return rc;
+  uint64_t *uka, *ukb;
+  uint32_t *upa, *upb, *nua, *nub;
+  if (ska.wide) {
+    if ((rc = unique_list<uint64_t>(c, ska, 24, &uka, &upa, &nua))) return rc;
+    if ((rc = unique_list<uint64_t>(c, skb, 29, &ukb, &upb, &nub))) return rc;
+  } else {
+    if ((rc = unique_list<uint32_t>(c, ska, 24, &uka, &upa, &nua))) return rc;
+    if ((rc = unique_list<uint32_t>(c, skb, 29, &ukb, &upb, &nub))) return rc;
+  }
+  // join: capacity = unique count of A <= ca
+  const int64_t capa = (int64_t)ca;
+  uint32_t* hit = (uint32_t*)ws.get(c, 34, (capa + 1) * 4);
+  uint32_t* hflag = (uint32_t*)ws.get(c, 35, (capa + 1) * 4);
+  uint32_t* hidx = (uint32_t*)ws.get(c, 36, (capa + 1) * 4);
+  uint32_t* hscr = (uint32_t*)ws.get(c, 37, scan_scratch_words(capa + 1) * 4 + 64);
+  if (!hit || !hflag || !hidx || !hscr) return report_error(MVG_ERR_NOMEM, "workspace allocation failed");
+  uint32_t* d_npairs = hscr + scan_scratch_words(capa + 1);
+  k_join<<<grid_for(capa, 256), 256, 0, c->stream>>>(uka, nua, ukb, nub, hit, capa);
+  k_hit_flags<<<grid_for(capa, 256), 256, 0, c->stream>>>(hit, capa, hflag);
+  c->launches += 2;
+  exclusive_scan(hflag, hidx, capa, hscr, d_npairs, c->stream, &c->launches);
+  MVG_CUDA_TRY(cudaMemcpyAsync(c->h_scalars, d_npairs, 4, cudaMemcpyDeviceToHost, c->stream));
+  MVG_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  const int64_t npairs = (int64_t)(uint32_t)c->h_scalars[0];
+  if ((rc = check_device_error(c))) return rc;
+  c->stats.pairs = npairs;
+  if (npairs == 0) return 0;
+
+  Mhe* mhe = (Mhe*)ws.get(c, 38, npairs * sizeof(Mhe));
+  uint32_t* bk0 = (uint32_t*)ws.get(c, 39, npairs * 4);
+  uint32_t* bk1 = (uint32_t*)ws.get(c, 40, npairs * 4);
+  uint32_t* or0 = (uint32_t*)ws.get(c, 41, npairs * 4);
+  uint32_t* or1 = (uint32_t*)ws.get(c, 42, npairs * 4);
+  uint32_t* sscr = (uint32_t*)ws.get(c, 43, radix_scratch_words(npairs > kTableSize ? npairs : kTableSize) * 4);
+  // per-bucket tables: count, start, nent, lpt key/id x2, out offsets, scan scratch, totals
+  uint32_t* btab = (uint32_t*)ws.get(c, 44, (size_t)kTableSize * 4 * 10 + scan_scratch_words(kTableSize) * 4 + 256);
+  Mhe* ent = (Mhe*)ws.get(c, 45, npairs * sizeof(Mhe));
+  if (!mhe || !bk0 || !bk1 || !or0 || !or1 || !sscr || !btab || !ent)
+    return report_error(MVG_ERR_NOMEM, "workspace allocation failed");
+  uint32_t* bcount = btab;
+  uint32_t* bstart = btab + kTableSize;
+  uint32_t* nent = btab + 2 * kTableSize;
+  uint32_t* lk0 = btab + 3 * kTableSize;
+  uint32_t* li0 = btab + 4 * kTableSize;
+  uint32_t* lk1 = btab + 5 * kTableSize;
+  uint32_t* li1 = btab + 6 * kTableSize;
+  uint32_t* ooff = btab + 7 * kTableSize;
+  uint32_t* bscr = btab + 10 * kTableSize;
+  uint32_t* tot = bscr + scan_scratch_words(kTableSize);
+  unsigned long long* d_coll = (unsigned long long*)(tot + 4);
+
+  k_hash_pairs<<<grid_for(capa, 256), 256, 0, c->stream>>>(uka, upa, ukb, upb, hit, hflag, hidx, capa, nua, s.L, mhe,
+                                                            bk0, or0);
+  c->launches++;
+  int which = radix_sort_pairs<uint32_t>(bk0, or0, bk1, or1, npairs, 16, sscr, c->stream, &c->launches);
+  uint32_t* sorted_pair = which ? or1 : or0;
+  MVG_CUDA_TRY(cudaMemsetAsync(bcount, 0, (size_t)kTableSize * 4, c->stream));
+  MVG_CUDA_TRY(cudaMemsetAsync(nent, 0, (size_t)kTableSize * 4, c->stream));
+  MVG_CUDA_TRY(cudaMemsetAsync(d_coll, 0, 8, c->stream));
+  k_bucket_hist<<<grid_for(npairs, 256), 256, 0, c->stream>>>(bk0, d_npairs, bcount);
+  c->launches++;
+  exclusive_scan(bcount, bstart, kTableSize, bscr, tot, c->stream, &c->launches);
+  k_lpt_keys<<<grid_for(kTableSize, 256), 256, 0, c->stream>>>(bcount, lk0, li0);
+  c->launches++;
+  which = radix_sort_pairs<uint32_t>(lk0, li0, lk1, li1, kTableSize, 32, sscr, c->stream, &c->launches);
+  const uint32_t* border = which ? li1 : li0;
+  MatchCtx mc;
+  mc.g[0] = ga;
+  mc.g[1] = gb;
+  mc.n[0] = (int64_t)na;
+  mc.n[1] = (int64_t)nb;
+  mc.s = s;
+  k_bucket_warps<<<kTableSize / 8, 256, 0, c->stream>>>(mc, mhe, sorted_pair, bstart, bcount, border, kTableSize, ent,
+                                                         nent, d_coll);
+  c->launches++;
+  exclusive_scan(nent, ooff, kTableSize, bscr, tot + 1, c->stream, &c->launches);
+  k_emit<<<kTableSize / 8, 256, 0, c->stream>>>(ent, bstart, nent, ooff, d_out, cap);
+  c->launches++;
+  MVG_CUDA_TRY(cudaMemcpyAsync(c->h_scalars, tot + 1, 4, cudaMemcpyDeviceToHost, c->stream));
+  MVG_CUDA_TRY(cudaMemcpyAsync(c->h_scalars + 1, d_coll, 8, cudaMemcpyDeviceToHost, c->stream));
+  MVG_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  if ((rc = check_device_error(c))) return rc;
+  const uint64_t nm = (uint32_t)c->h_scalars[0];
+  c->stats.matches = nm;
+  c->stats.collisions = c->h_scalars[1];
+  *count = nm;
+  if (nm > cap) return report_error(MVG_ERR_CAPACITY, "match output buffer too small");
+  return 0;
+}
+
+}  // namespace mvg

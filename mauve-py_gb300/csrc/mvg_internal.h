@@ -1,0 +1,62 @@
+// Host-side internals shared by the translation units of libmauve_gb300.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "mvg_common.cuh"
+
+namespace mvg {
+
+struct Ctx;
+
+// Grow-only device buffers, one per slot, owned by the handle.  Calls reuse
+// them, so steady-state calls allocate nothing.
+struct Workspace {
+  static constexpr int kSlots = 64;
+  void* ptr[kSlots] = {};
+  size_t size[kSlots] = {};
+  void* get(Ctx* c, int slot, size_t bytes);
+  void release();
+};
+
+struct MatchStats {
+  uint64_t pairs = 0, collisions = 0, matches = 0, buckets = 0;
+};
+
+struct Ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  uint32_t* d_err = nullptr;     // device error word
+  uint32_t* h_err = nullptr;     // pinned mirror
+  uint64_t* h_scalars = nullptr; // pinned scalars for small device->host reads
+  uint64_t launches = 0;
+  uint64_t tb_arena = 32ull << 30;
+  Workspace ws;
+  MatchStats stats;
+};
+
+// Sorted keys of one genome kept on the device for the join.
+struct SmlKeys {
+  const void* keys = nullptr;  // uint32 or uint64 compact keys: (seed bits << 1) | strand
+  const uint32_t* pos = nullptr;
+  bool wide = false;
+  uint64_t count = 0;
+};
+
+inline uint64_t packed_words(uint64_t n) { return (n * 2) / 32 + (((n * 2) % 32) ? 1 : 0) + 2; }
+
+int upload_base_table();
+int grid_for(uint64_t n, int threads);
+int pack_sequence(Ctx* c, const uint8_t* d_seq, uint64_t n, uint32_t* d_packed);
+int sml_sort(Ctx* c, const uint32_t* d_packed, uint64_t count, const SeedDesc& s, uint32_t* d_pos_out,
+             uint64_t* d_mer_out, SmlKeys* keep, int slot_base);
+int check_device_error(Ctx* c);
+
+int pairwise_matches_dev(Ctx* c, const uint8_t* d_a, uint64_t na, const uint8_t* d_b, uint64_t nb, uint64_t seed,
+                         int64_t* d_out, uint64_t cap, uint64_t* count);
+int gapdp_batch_dev(Ctx* c, const uint8_t* d_sa, const uint64_t* d_oa, const uint8_t* d_sb, const uint64_t* d_ob,
+                    int64_t nprob, int32_t* d_scores, char* d_paths, const uint64_t* d_path_off, int64_t* d_path_len,
+                    const uint64_t* h_oa, const uint64_t* h_ob);
+int probe_int32_peak(Ctx* c, double* ops);
+
+}  // namespace mvg

@@ -1,0 +1,190 @@
+// Device primitives shared by the seed and match kernels: an exclusive scan
+// over uint32 and a stable LSD radix sort of (key, uint32 value) pairs.
+//
+// Radix sort, one 8-bit digit per pass:
+//   k_digit_hist   per-tile digit counts           (reads keys once)
+//   scan           exclusive scan of the digit-major count table
+//   k_digit_scatter stages the tile in shared memory in stable digit order,
+//                   then writes each digit's run contiguously (coalesced).
+// Stability inside a tile comes from ranking 256-element chunks in order with
+// __match_any_sync peer masks and per-warp counts, so equal digits keep their
+// input order and the whole sort is stable.
+#pragma once
+#include "mvg_common.cuh"
+
+namespace mvg {
+
+constexpr int kScanTile = 4096;  // elements per scan block (256 threads x 16)
+constexpr int kSortThreads = 256;
+constexpr int kSortTile = 2048;  // elements per sort block (8 chunks of 256)
+
+// ------------------------------------------------------------------ scan
+
+__device__ __forceinline__ uint32_t warp_incl_scan(uint32_t v) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    uint32_t t = __shfl_up_sync(0xffffffffu, v, d);
+    if (lane >= d) v += t;
+  }
+  return v;
+}
+
+// Block-wide exclusive scan of one value per thread (blockDim.x == 256).
+// Returns the exclusive prefix; *total gets the block sum.
+__device__ __forceinline__ uint32_t block_excl_scan256(uint32_t v, uint32_t* total) {
+  __shared__ uint32_t wsum[8];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  uint32_t inc = warp_incl_scan(v);
+  if (lane == 31) wsum[wid] = inc;
+  __syncthreads();
+  if (wid == 0) {
+    uint32_t x = lane < 8 ? wsum[lane] : 0;
+    uint32_t y = warp_incl_scan(x);
+    if (lane < 8) wsum[lane] = y - x;
+    if (lane == 7 && total) *total = y;
+  }
+  __syncthreads();
+  uint32_t r = wsum[wid] + inc - v;
+  __syncthreads();
+  return r;
+}
+
+// Pass 1: per-block sums of tiles of kScanTile elements.
+__global__ void k_scan_reduce(const uint32_t* __restrict__ in, int64_t n, uint32_t* __restrict__ bsum);
+// Pass 2: exclusive scan of the block sums (one block, loops over chunks).
+__global__ void k_scan_bsums(uint32_t* __restrict__ bsum, int64_t nb, uint32_t* __restrict__ total);
+// Pass 3: exclusive scan of each tile plus its block prefix.
+__global__ void k_scan_down(const uint32_t* in, int64_t n, const uint32_t* __restrict__ bsum, uint32_t* out);
+
+// Host side: exclusive scan of n uint32 into out (may alias in); *d_total
+// (device) gets the sum.  scratch needs scan_scratch_words(n) words.
+inline int64_t scan_scratch_words(int64_t n) { return (n + kScanTile - 1) / kScanTile + 1; }
+void exclusive_scan(const uint32_t* in, uint32_t* out, int64_t n, uint32_t* scratch, uint32_t* d_total,
+                    cudaStream_t st, uint64_t* launches);
+
+// ------------------------------------------------------------ radix sort
+
+template <typename K>
+__global__ void k_digit_hist(const K* __restrict__ keys, int64_t n, int shift, uint32_t* __restrict__ counts,
+                             int nblocks) {
+  __shared__ uint32_t h[256];
+  h[threadIdx.x] = 0;
+  __syncthreads();
+  const int64_t base = (int64_t)blockIdx.x * kSortTile;
+  const int64_t end = min(base + kSortTile, n);
+  for (int64_t i = base + threadIdx.x; i < end; i += kSortThreads) {
+    uint32_t d = (uint32_t)(keys[i] >> shift) & 255u;
+    atomicAdd(&h[d], 1u);
+  }
+  __syncthreads();
+  counts[(int64_t)threadIdx.x * nblocks + blockIdx.x] = h[threadIdx.x];
+}
+
+template <typename K>
+__global__ void __launch_bounds__(kSortThreads) k_digit_scatter(const K* __restrict__ kin, const uint32_t* __restrict__ vin,
+                                                                K* __restrict__ kout, uint32_t* __restrict__ vout, int64_t n,
+                                                                int shift, const uint32_t* __restrict__ counts,
+                                                                const uint32_t* __restrict__ offsets, int nblocks) {
+  __shared__ K skey[kSortTile];
+  __shared__ uint32_t sval[kSortTile];
+  __shared__ uint32_t wcnt[8][256];
+  __shared__ uint32_t run[256];
+  __shared__ uint32_t lstart[256];
+  __shared__ uint32_t gbase[256];
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const int64_t base = (int64_t)blockIdx.x * kSortTile;
+  const int tile_n = (int)min((int64_t)kSortTile, n - base);
+
+  uint32_t mycount = counts[(int64_t)tid * nblocks + blockIdx.x];
+  gbase[tid] = offsets[(int64_t)tid * nblocks + blockIdx.x];
+  uint32_t ls = block_excl_scan256(mycount, nullptr);
+  lstart[tid] = ls;
+  run[tid] = 0;
+#pragma unroll
+  for (int w = 0; w < 8; ++w) wcnt[w][tid] = 0;
+  __syncthreads();
+
+  const uint32_t lt_mask = (1u << lane) - 1u;
+  for (int c = 0; c < kSortTile; c += kSortThreads) {
+    const int li = c + tid;
+    const bool valid = li < tile_n;
+    K key = 0;
+    uint32_t val = 0, d = 256u + (uint32_t)lane;  // invalid lanes get private digits
+    if (valid) {
+      key = kin[base + li];
+      val = vin[base + li];
+      d = (uint32_t)(key >> shift) & 255u;
+    }
+    uint32_t peers = __match_any_sync(0xffffffffu, d);
+    uint32_t lrank = __popc(peers & lt_mask);
+    if (valid && lrank == 0) wcnt[wid][d] = __popc(peers);
+    __syncthreads();
+    if (valid) {
+      uint32_t r = run[d] + lrank;
+      for (int w = 0; w < wid; ++w) r += wcnt[w][d];
+      const uint32_t lp = lstart[d] + r;
+      skey[lp] = key;
+      sval[lp] = val;
+    }
+    __syncthreads();
+    {
+      uint32_t s = 0;
+#pragma unroll
+      for (int w = 0; w < 8; ++w) {
+        s += wcnt[w][tid];
+        wcnt[w][tid] = 0;
+      }
+      run[tid] += s;
+    }
+    __syncthreads();
+    if (c + kSortThreads >= tile_n) break;
+  }
+  for (int i = tid; i < tile_n; i += kSortThreads) {
+    K key = skey[i];
+    uint32_t d = (uint32_t)(key >> shift) & 255u;
+    int64_t o = (int64_t)gbase[d] + (i - (int)lstart[d]);
+    kout[o] = key;
+    vout[o] = sval[i];
+  }
+}
+
+// Stable LSD radix sort of (keys, vals) on bits [0, nbits).  Ping-pongs
+// between the input arrays and the alternates; returns which buffer holds
+// the result (0 = keys/vals, 1 = alt).  scratch: radix_scratch_words(n).
+inline int64_t radix_scratch_words(int64_t n) {
+  int64_t nb = (n + kSortTile - 1) / kSortTile;
+  return 2 * 256 * nb + scan_scratch_words(256 * nb) + 2;
+}
+
+template <typename K>
+int radix_sort_pairs(K* keys, uint32_t* vals, K* keys_alt, uint32_t* vals_alt, int64_t n, int nbits,
+                     uint32_t* scratch, cudaStream_t st, uint64_t* launches) {
+  if (n <= 0) return 0;
+  const int nb = (int)((n + kSortTile - 1) / kSortTile);
+  uint32_t* counts = scratch;
+  uint32_t* offsets = scratch + (int64_t)256 * nb;
+  uint32_t* sscr = offsets + (int64_t)256 * nb;
+  uint32_t* total = sscr + scan_scratch_words((int64_t)256 * nb);
+  K* ka = keys;
+  K* kb = keys_alt;
+  uint32_t* va = vals;
+  uint32_t* vb = vals_alt;
+  int which = 0;
+  for (int shift = 0; shift < nbits; shift += 8) {
+    k_digit_hist<K><<<nb, kSortThreads, 0, st>>>(ka, n, shift, counts, nb);
+    exclusive_scan(counts, offsets, (int64_t)256 * nb, sscr, total, st, launches);
+    k_digit_scatter<K><<<nb, kSortThreads, 0, st>>>(ka, va, kb, vb, n, shift, counts, offsets, nb);
+    if (launches) *launches += 2;
+    K* tk = ka;
+    ka = kb;
+    kb = tk;
+    uint32_t* tv = va;
+    va = vb;
+    vb = tv;
+    which ^= 1;
+  }
+  return which;
+}
+
+}  // namespace mvg

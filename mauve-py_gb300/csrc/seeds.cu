@@ -1,0 +1,175 @@
+// Seed path: 2-bit packing, spaced-seed canonical mers and the sorted mer
+// list (SML) build.
+//
+//   k_pack          ASCII bases -> 2-bit MSB-first uint32 words, 16 bases per
+//                   thread from one 128-bit load (translate32,
+//                   LM/SortedMerList.cpp:425-459; table :29-47).
+//   k_seed_keys     canonical spaced-seed mer of every position
+//                   (GetSeedMer/RevCompMer/GetDnaSeedMer, :597-615, 726-769),
+//                   emitted as a compact sort key: the 2w seed bits then the
+//                   strand bit, (2w+1) bits in all, which orders exactly like
+//                   the reference's 64-bit bmer.mer.
+//   radix sort      stable LSD over those 2w+1 bits (prim.cuh).
+#include <string.h>
+
+#include "mvg_internal.h"
+#include "prim.cuh"
+
+namespace mvg {
+
+// translate32's table (LM/SortedMerList.cpp:29-47): every byte not listed
+// maps to 0 (A).  Bit 7 of an entry flags '-', which the reference rejects.
+__constant__ uint8_t c_base_table[256];
+
+static void init_base_table_host(uint8_t* t) {
+  memset(t, 0, 256);
+  const char* c1 = "cCbByY";
+  const char* c2 = "gGsSkK";
+  for (const char* p = c1; *p; ++p) t[(uint8_t)*p] = 1;
+  for (const char* p = c2; *p; ++p) t[(uint8_t)*p] = 2;
+  t[(uint8_t)'t'] = 3;
+  t[(uint8_t)'T'] = 3;
+  t[(uint8_t)'-'] = 0x80;
+}
+
+int upload_base_table() {
+  uint8_t t[256];
+  init_base_table_host(t);
+  MVG_CUDA_TRY(cudaMemcpyToSymbol(c_base_table, t, 256));
+  return 0;
+}
+
+SeedDesc make_seed_desc(uint64_t pattern) {
+  SeedDesc s;
+  memset(&s, 0, sizeof(s));
+  s.pattern = pattern;
+  s.L = pattern ? 64 - __builtin_clzll(pattern) - __builtin_ctzll(pattern) : 0;
+  s.w = __builtin_popcountll(pattern);
+  s.seed_mask = s.w ? (~0ull << (64 - 2 * s.w)) : 0;
+  int out = 0;
+  for (int k = 0; k < s.L;) {
+    if (pattern & (1ull << (s.L - 1 - k))) {
+      int st = k;
+      while (k < s.L && (pattern & (1ull << (s.L - 1 - k)))) ++k;
+      s.run_start[s.nruns] = (int8_t)st;
+      s.run_len[s.nruns] = (int8_t)(k - st);
+      s.run_out[s.nruns] = (int8_t)out;
+      out += k - st;
+      s.nruns++;
+    } else {
+      ++k;
+    }
+  }
+  return s;
+}
+
+// One thread per output word: 16 bases, one 128-bit load when aligned.
+__global__ void k_pack(const uint8_t* __restrict__ seq, uint64_t n, uint32_t* __restrict__ out, uint64_t words,
+                       uint32_t* err) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  const bool aligned = (((uintptr_t)seq) & 15) == 0;
+  for (uint64_t w = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; w < words; w += stride) {
+    const uint64_t b0 = w * 16;
+    uint32_t word = 0, bad = 0;
+    if (b0 + 16 <= n && aligned) {
+      uint4 v = __ldg(reinterpret_cast<const uint4*>(seq + b0));
+      uint32_t parts[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          uint32_t t = c_base_table[(parts[q] >> (8 * k)) & 255u];
+          bad |= t;
+          word |= (t & 3u) << (30 - 2 * (q * 4 + k));
+        }
+      }
+    } else {
+      for (int k = 0; k < 16; ++k) {
+        uint64_t i = b0 + k;
+        if (i < n) {
+          uint32_t t = c_base_table[seq[i]];
+          bad |= t;
+          word |= (t & 3u) << (30 - 2 * k);
+        }
+      }
+    }
+    if (bad & 0x80u) set_error(err, kDevGapChar);
+    out[w] = word;
+  }
+}
+
+// Canonical mer per position -> (2w+1)-bit key and the position.
+template <typename K>
+__global__ void k_seed_keys(const uint32_t* __restrict__ g, uint64_t count, SeedDesc s, K* __restrict__ keys,
+                            uint32_t* __restrict__ pos) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  const int shift = 64 - 2 * s.w;
+  for (uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < count; p += stride) {
+    uint64_t m = canonical_mer(g, p, s);
+    keys[p] = (K)(((m >> shift) << 1) | (m & 1ull));
+    pos[p] = (uint32_t)p;
+  }
+}
+
+template <typename K>
+__global__ void k_key_to_mer(const K* __restrict__ keys, uint64_t count, int w, uint64_t* __restrict__ mer) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += stride) {
+    uint64_t k = (uint64_t)keys[i];
+    mer[i] = ((k >> 1) << (64 - 2 * w)) | (k & 1ull);
+  }
+}
+
+int grid_for(uint64_t n, int threads) {
+  uint64_t b = (n + threads - 1) / threads;
+  const uint64_t cap = 152ull * 16;  // 16 resident blocks per SM on 152 SMs
+  if (b > cap) b = cap;
+  return (int)(b ? b : 1);
+}
+
+int pack_sequence(Ctx* c, const uint8_t* d_seq, uint64_t n, uint32_t* d_packed) {
+  const uint64_t words = packed_words(n);
+  k_pack<<<grid_for(words, 256), 256, 0, c->stream>>>(d_seq, n, d_packed, words, c->d_err);
+  c->launches++;
+  MVG_CUDA_TRY(cudaGetLastError());
+  return 0;
+}
+
+template <typename K>
+static int sml_sort_impl(Ctx* c, const uint32_t* d_packed, uint64_t count, const SeedDesc& s, uint32_t* d_pos_out,
+                         uint64_t* d_mer_out, SmlKeys* keep, int sb) {
+  const int nbits = 2 * s.w + 1;
+  Workspace& ws = c->ws;
+  K* k0 = (K*)ws.get(c, sb + 0, count * sizeof(K));
+  K* k1 = (K*)ws.get(c, sb + 1, count * sizeof(K));
+  uint32_t* v0 = (uint32_t*)ws.get(c, sb + 2, count * sizeof(uint32_t));
+  uint32_t* v1 = (uint32_t*)ws.get(c, sb + 3, count * sizeof(uint32_t));
+  uint32_t* scr = (uint32_t*)ws.get(c, sb + 4, radix_scratch_words(count) * sizeof(uint32_t));
+  if (!k0 || !k1 || !v0 || !v1 || !scr) return report_error(MVG_ERR_NOMEM, "workspace allocation failed");
+  k_seed_keys<K><<<grid_for(count, 256), 256, 0, c->stream>>>(d_packed, count, s, k0, v0);
+  c->launches++;
+  int which = radix_sort_pairs<K>(k0, v0, k1, v1, (int64_t)count, nbits, scr, c->stream, &c->launches);
+  K* ks = which ? k1 : k0;
+  uint32_t* vs = which ? v1 : v0;
+  if (d_pos_out) MVG_CUDA_TRY(cudaMemcpyAsync(d_pos_out, vs, count * sizeof(uint32_t), cudaMemcpyDeviceToDevice, c->stream));
+  if (d_mer_out) {
+    k_key_to_mer<K><<<grid_for(count, 256), 256, 0, c->stream>>>(ks, count, s.w, d_mer_out);
+    c->launches++;
+  }
+  if (keep) {
+    keep->keys = ks;
+    keep->pos = vs;
+    keep->wide = sizeof(K) == 8;
+    keep->count = count;
+  }
+  MVG_CUDA_TRY(cudaGetLastError());
+  return 0;
+}
+
+int sml_sort(Ctx* c, const uint32_t* d_packed, uint64_t count, const SeedDesc& s, uint32_t* d_pos_out,
+             uint64_t* d_mer_out, SmlKeys* keep, int slot_base) {
+  if (2 * s.w + 1 <= 32) return sml_sort_impl<uint32_t>(c, d_packed, count, s, d_pos_out, d_mer_out, keep, slot_base);
+  return sml_sort_impl<uint64_t>(c, d_packed, count, s, d_pos_out, d_mer_out, keep, slot_base);
+}
+
+}  // namespace mvg

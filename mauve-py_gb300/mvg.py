@@ -1,0 +1,232 @@
+"""Python binding of libmauve_gb300 (the C ABI in include/mauve_gb300.h).
+
+Mirrors the reference's seams for the pairwise anchoring and gap-alignment
+path of progressiveMauve:
+
+  SortedMerList.create(seq, seed)      -> SortedMerList::Create + Read order
+                                          (libMems/SortedMerList.h:89)
+  pairwise_matches(a, b, seed)         -> PairwiseMatchFinder::FindMatches
+                                          (libMems/MemHash.h:55), the match
+                                          list as (start0, start1, length) rows
+  gap_align_batch(...)                 -> muscle::GlobalAlign per range
+                                          (muscle/libMUSCLE/glbalign.cpp:69)
+
+Every call runs on the GPU through the compiled library; there is no CPU
+fallback.  Importing this module on a machine without the built library or
+without a CUDA device raises.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libmauve_gb300.so")
+
+MVG_OK = 0
+_ERRORS = {1: ValueError, 2: RuntimeError, 3: ValueError, 4: ValueError, 5: OverflowError, 6: MemoryError,
+           7: RuntimeError}
+
+CODING_SEED = 3  # libMems/SeedMasks.h:262
+SOLID_SEED = 2 ** 31 - 1
+
+_lib = None
+EXPORTS = ["mvg_create", "mvg_destroy", "mvg_last_error", "mvg_stream", "mvg_kernel_launches", "mvg_get_seed",
+           "mvg_default_seed_weight", "mvg_seed_length", "mvg_seed_weight", "mvg_sml_build", "mvg_sml_build_dev",
+           "mvg_pairwise_matches", "mvg_pairwise_matches_dev", "mvg_pairwise_stats", "mvg_gapdp_batch",
+           "mvg_gapdp_batch_dev", "mvg_set_tb_arena", "mvg_probe_int32_peak"]
+
+
+def load_library(path=LIB_PATH):
+    """Loads the shared library (raises OSError if it is not built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise OSError("libmauve_gb300.so is not built (run __graft_entry__.build())")
+    L = ctypes.CDLL(path)
+    vp, u64, i64, ci = ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int64, ctypes.c_int
+    sig = {
+        "mvg_create": (ci, [ctypes.POINTER(vp), ci]),
+        "mvg_destroy": (ci, [vp]),
+        "mvg_last_error": (ctypes.c_char_p, []),
+        "mvg_stream": (vp, [vp]),
+        "mvg_kernel_launches": (u64, [vp]),
+        "mvg_get_seed": (u64, [ci, ci]),
+        "mvg_default_seed_weight": (ctypes.c_uint, [u64]),
+        "mvg_seed_length": (ci, [u64]),
+        "mvg_seed_weight": (ci, [u64]),
+        "mvg_sml_build": (ci, [vp, vp, u64, u64, vp, vp, u64, ctypes.POINTER(u64)]),
+        "mvg_sml_build_dev": (ci, [vp, vp, u64, u64, vp, vp, u64, ctypes.POINTER(u64)]),
+        "mvg_pairwise_matches": (ci, [vp, vp, u64, vp, u64, u64, vp, u64, ctypes.POINTER(u64)]),
+        "mvg_pairwise_matches_dev": (ci, [vp, vp, u64, vp, u64, u64, vp, u64, ctypes.POINTER(u64)]),
+        "mvg_pairwise_stats": (ci, [vp, vp]),
+        "mvg_gapdp_batch": (ci, [vp, vp, vp, vp, vp, i64, vp, vp, vp, vp]),
+        "mvg_gapdp_batch_dev": (ci, [vp, vp, vp, vp, vp, i64, vp, vp, vp, vp]),
+        "mvg_set_tb_arena": (ci, [vp, u64]),
+        "mvg_probe_int32_peak": (ci, [vp, ctypes.POINTER(ctypes.c_double)]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def _check(rc):
+    if rc != MVG_OK:
+        msg = load_library().mvg_last_error().decode(errors="replace")
+        raise _ERRORS.get(rc, RuntimeError)("libmauve_gb300 error %d: %s" % (rc, msg))
+
+
+def _ptr(a):
+    return ctypes.c_void_p(a.ctypes.data) if a is not None else None
+
+
+def _u8(seq):
+    if isinstance(seq, (bytes, bytearray)):
+        return np.frombuffer(bytes(seq), np.uint8)
+    if isinstance(seq, str):
+        return np.frombuffer(seq.encode(), np.uint8)
+    return np.ascontiguousarray(seq, dtype=np.uint8)
+
+
+def get_seed(weight, rank=0):
+    """getSeed (libMems/SeedMasks.h:298-321)."""
+    return int(load_library().mvg_get_seed(weight, rank))
+
+
+def default_seed_weight(avg_len):
+    """getDefaultSeedWeight (libMems/SeedMasks.h:389-401)."""
+    return int(load_library().mvg_default_seed_weight(avg_len))
+
+
+def seed_length(seed):
+    return int(load_library().mvg_seed_length(seed))
+
+
+def seed_weight(seed):
+    return int(load_library().mvg_seed_weight(seed))
+
+
+class Context:
+    """A CUDA device, a stream and the device workspaces (opaque handle)."""
+
+    def __init__(self, device=0):
+        L = load_library()
+        h = ctypes.c_void_p()
+        _check(L.mvg_create(ctypes.byref(h), device))
+        self._h = h
+        self.device = device
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def stream(self):
+        return load_library().mvg_stream(self._h)
+
+    def kernel_launches(self):
+        return int(load_library().mvg_kernel_launches(self._h))
+
+    def close(self):
+        if self._h:
+            load_library().mvg_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ------------------------------------------------------------ seeds
+    def sml_build(self, seq, seed, with_mers=True):
+        """Sorted mer list: (positions sorted by canonical mer, canonical mers)."""
+        s = _u8(seq)
+        L = seed_length(seed)
+        cnt = len(s) - L + 1 if len(s) >= L else 0
+        pos = np.zeros(max(cnt, 1), np.uint32)
+        mer = np.zeros(max(cnt, 1), np.uint64) if with_mers else None
+        out = ctypes.c_uint64(0)
+        _check(load_library().mvg_sml_build(self._h, _ptr(s), len(s), seed, _ptr(pos), _ptr(mer), cnt,
+                                            ctypes.byref(out)))
+        return pos[:cnt], (mer[:cnt] if with_mers else None)
+
+    def sml_build_dev(self, d_seq_ptr, n, seed, d_pos_ptr, d_mer_ptr, cap):
+        out = ctypes.c_uint64(0)
+        _check(load_library().mvg_sml_build_dev(self._h, d_seq_ptr, n, seed, d_pos_ptr, d_mer_ptr, cap,
+                                                ctypes.byref(out)))
+        return int(out.value)
+
+    # ---------------------------------------------------------- matches
+    def pairwise_matches(self, a, b, seed, cap=None):
+        """MatchList of the genome pair as int64 rows (start0, start1, length)."""
+        a, b = _u8(a), _u8(b)
+        if cap is None:
+            cap = max(min(len(a), len(b)) // 4, 1024)
+        while True:
+            out = np.zeros(3 * cap, np.int64)
+            cnt = ctypes.c_uint64(0)
+            rc = load_library().mvg_pairwise_matches(self._h, _ptr(a), len(a), _ptr(b), len(b), seed, _ptr(out),
+                                                     cap, ctypes.byref(cnt))
+            if rc == 5 and cnt.value > cap:
+                cap = int(cnt.value)
+                continue
+            _check(rc)
+            return out[: 3 * cnt.value].reshape(-1, 3)
+
+    def pairwise_matches_dev(self, d_a, na, d_b, nb, seed, d_out, cap):
+        cnt = ctypes.c_uint64(0)
+        _check(load_library().mvg_pairwise_matches_dev(self._h, d_a, na, d_b, nb, seed, d_out, cap,
+                                                       ctypes.byref(cnt)))
+        return int(cnt.value)
+
+    def pairwise_stats(self):
+        st = np.zeros(4, np.uint64)
+        _check(load_library().mvg_pairwise_stats(self._h, _ptr(st)))
+        return dict(pairs=int(st[0]), collisions=int(st[1]), matches=int(st[2]), buckets=int(st[3]))
+
+    # ----------------------------------------------------------- gap DP
+    def set_tb_arena(self, nbytes):
+        _check(load_library().mvg_set_tb_arena(self._h, int(nbytes)))
+
+    def gap_align_batch(self, seq_a, off_a, seq_b, off_b, with_paths=True):
+        """Batched NWSmall.  Returns (scores int32[n], paths list of str or None)."""
+        seq_a, seq_b = _u8(seq_a), _u8(seq_b)
+        off_a = np.ascontiguousarray(off_a, np.uint64)
+        off_b = np.ascontiguousarray(off_b, np.uint64)
+        n = len(off_a) - 1
+        scores = np.zeros(max(n, 1), np.int32)
+        if with_paths:
+            la = np.diff(off_a.astype(np.int64))
+            lb = np.diff(off_b.astype(np.int64))
+            path_off = np.zeros(n + 1, np.uint64)
+            path_off[1:] = np.cumsum(la + lb)
+            paths = np.zeros(int(path_off[-1]) + 1, np.uint8)
+            plen = np.zeros(max(n, 1), np.int64)
+            _check(load_library().mvg_gapdp_batch(self._h, _ptr(seq_a), _ptr(off_a), _ptr(seq_b), _ptr(off_b), n,
+                                                  _ptr(scores), _ptr(paths), _ptr(path_off), _ptr(plen)))
+            raw = paths.tobytes()
+            out = [raw[int(path_off[k]):int(path_off[k]) + int(plen[k])].decode() for k in range(n)]
+            return scores[:n], out
+        _check(load_library().mvg_gapdp_batch(self._h, _ptr(seq_a), _ptr(off_a), _ptr(seq_b), _ptr(off_b), n,
+                                              _ptr(scores), None, None, None))
+        return scores[:n], None
+
+    def gap_align_batch_raw(self, seq_a, off_a, seq_b, off_b, scores, paths, path_off, path_len):
+        """Host-buffer call with caller-owned numpy outputs (no per-call Python decoding)."""
+        n = len(off_a) - 1
+        _check(load_library().mvg_gapdp_batch(self._h, _ptr(seq_a), _ptr(off_a), _ptr(seq_b), _ptr(off_b), n,
+                                              _ptr(scores), _ptr(paths), _ptr(path_off), _ptr(path_len)))
+
+    def gap_align_batch_dev(self, d_sa, d_oa, d_sb, d_ob, n, d_scores, d_paths, d_path_off, d_path_len):
+        _check(load_library().mvg_gapdp_batch_dev(self._h, d_sa, d_oa, d_sb, d_ob, n, d_scores, d_paths, d_path_off,
+                                                  d_path_len))
+
+    def probe_int32_peak(self):
+        v = ctypes.c_double(0)
+        _check(load_library().mvg_probe_int32_peak(self._h, ctypes.byref(v)))
+        return float(v.value)

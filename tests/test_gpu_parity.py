@@ -1,0 +1,210 @@
+"""GPU parity: the CUDA path (through the C ABI) against the reference's golden
+fixtures and the CPU oracle.  Integer / index work, so every comparison is
+bit-exact."""
+import numpy as np
+import pytest
+
+import mvg
+import oracle as O
+import synth
+from conftest import load_golden
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    import build as pkg_build
+    pkg_build.build()
+    c = mvg.Context(0)
+    yield c
+    c.close()
+
+
+# ------------------------------------------------------------------ SML
+
+def test_sml_matches_reference_fixtures(ctx):
+    g = load_golden("sml.npz")
+    for k in range(int(g["count"])):
+        seq, seed = g["seq%d" % k], int(g["seed%d" % k])
+        pos, mer = ctx.sml_build(seq, seed)
+        rpos, rmer = g["pos%d" % k], g["mer%d" % k]
+        np.testing.assert_array_equal(mer, rmer)
+        np.testing.assert_array_equal(pos, rpos[np.lexsort((rpos, rmer))])
+
+
+@pytest.mark.parametrize("n,weight,rank", [(200_000, 15, 3), (150_000, 17, 3), (100_000, 11, 0), (5, 15, 3),
+                                           (21, 15, 3), (22, 15, 3), (65_537, 9, 0)])
+def test_sml_matches_oracle(ctx, n, weight, rank):
+    rng = np.random.default_rng(n + weight)
+    seq = synth.random_bases(rng, n, 0.45)
+    seed = mvg.get_seed(weight, rank)
+    pos, mer = ctx.sml_build(seq, seed)
+    opos, omer = O.sml_build(seq, seed)
+    np.testing.assert_array_equal(pos, opos)
+    np.testing.assert_array_equal(mer, omer)
+
+
+def test_sml_rejects_gap_character(ctx):
+    with pytest.raises(ValueError):
+        ctx.sml_build(b"ACGTACGTACGTACGTACGTACG-ACGTACGT", mvg.get_seed(15, 3))
+
+
+def test_sml_unaligned_input_and_iupac(ctx):
+    rng = np.random.default_rng(3)
+    buf = synth.random_bases(rng, 50_001, 0.5)
+    buf[rng.choice(50_001, 500, replace=False)] = np.frombuffer(b"NnRYacgtKMSWBb" * 36, np.uint8)[:500]
+    seq = buf[1:]  # not 16-byte aligned
+    seed = mvg.get_seed(15, 3)
+    pos, mer = ctx.sml_build(seq, seed)
+    opos, omer = O.sml_build(seq, seed)
+    np.testing.assert_array_equal(pos, opos)
+    np.testing.assert_array_equal(mer, omer)
+
+
+# -------------------------------------------------------------- matches
+
+def test_matches_reference_fixtures(ctx):
+    g = load_golden("matches.npz")
+    for k in range(int(g["count"])):
+        m = ctx.pairwise_matches(g["a%d" % k], g["b%d" % k], int(g["seed%d" % k]))
+        np.testing.assert_array_equal(m, g["m%d" % k], err_msg="case %d" % k)
+
+
+@pytest.mark.parametrize("seed_id", range(6))
+def test_matches_oracle_random_pairs(ctx, seed_id):
+    rng = np.random.default_rng(100 + seed_id)
+    n = int(rng.integers(20_000, 120_000))
+    b = synth.random_bases(rng, n, float(rng.uniform(0.35, 0.65)))
+    if seed_id % 2:
+        b = synth.insert_repeats(rng, b, int(rng.integers(100, 2000)), int(rng.integers(2, 30)))
+    a = synth.mutate(rng, b, float(rng.uniform(0, 0.1)), int(rng.integers(0, 80)), 4.0, int(rng.integers(0, 6)),
+                     (200, 5000))
+    w = mvg.default_seed_weight((len(a) + len(b)) // 2)
+    seed = mvg.get_seed(w, 3 if seed_id < 4 else 0)
+    m = ctx.pairwise_matches(a, b, seed)
+    om = O.pairwise_matches(a, b, seed)
+    np.testing.assert_array_equal(m, om)
+    st = ctx.pairwise_stats()
+    assert st["matches"] == len(m) and st["pairs"] == st["matches"] + st["collisions"]
+
+
+def test_matches_genome_pair_small_config(ctx):
+    """The 1 Mbp plain-method pair, end to end against the oracle."""
+    a, b = synth.genome_pair_small()
+    seed = mvg.get_seed(mvg.default_seed_weight((len(a) + len(b)) // 2), 3)
+    m = ctx.pairwise_matches(a, b, seed)
+    om = O.pairwise_matches(a, b, seed)
+    np.testing.assert_array_equal(m, om)
+
+
+def test_matches_degenerate_inputs(ctx):
+    seed = mvg.get_seed(15, 3)
+    assert ctx.pairwise_matches(b"ACGT", b"ACGTACGT", seed).shape == (0, 3)
+    rng = np.random.default_rng(9)
+    x = synth.random_bases(rng, 3000)
+    np.testing.assert_array_equal(ctx.pairwise_matches(x, x, seed), O.pairwise_matches(x, x, seed))
+    poly = np.frombuffer(b"A" * 5000, np.uint8)  # one key repeated: no unique seeds
+    assert ctx.pairwise_matches(poly, poly, seed).shape == (0, 3)
+
+
+# --------------------------------------------------------------- gap DP
+
+def _check_batch(ctx, sa, oa, sb, ob):
+    scores, paths = ctx.gap_align_batch(sa, oa, sb, ob)
+    oscores, oplen, opaths, opoff = O.nw_batch(sa, oa, sb, ob)
+    np.testing.assert_array_equal(scores, oscores)
+    raw = opaths.tobytes()
+    for k in range(len(oa) - 1):
+        assert paths[k] == raw[int(opoff[k]):int(opoff[k]) + int(oplen[k])].decode(), k
+
+
+def test_gapdp_reference_fixtures(ctx):
+    g = load_golden("gapdp.npz")
+    scores, paths = ctx.gap_align_batch(g["seq_a"], g["off_a"], g["seq_b"], g["off_b"])
+    for k in range(len(g["off_a"]) - 1):
+        assert paths[k] == g["paths"][g["off_p"][k]:g["off_p"][k + 1]].tobytes().decode(), k
+
+
+def test_gapdp_edge_shapes(ctx):
+    rng = np.random.default_rng(21)
+    shapes = [(1, 1), (1, 2), (2, 1), (1, 300), (300, 1), (127, 5), (128, 5), (129, 5), (256, 256), (257, 3),
+              (5, 129), (33, 33), (2, 2), (3, 1000), (1000, 3)]
+    a_list, b_list = [], []
+    for la, lb in shapes:
+        for _ in range(3):
+            a_list.append(rng.integers(0, 4, la).astype(np.uint8))
+            b_list.append(rng.integers(0, 4, lb).astype(np.uint8))
+    oa = np.concatenate([[0], np.cumsum([len(x) for x in a_list])]).astype(np.uint64)
+    ob = np.concatenate([[0], np.cumsum([len(x) for x in b_list])]).astype(np.uint64)
+    _check_batch(ctx, np.concatenate(a_list), oa, np.concatenate(b_list), ob)
+
+
+def test_gapdp_random_batch_vs_oracle(ctx):
+    sa, oa, sb, ob = synth.gap_batch(seed=31, nprob=400, lmin=1, lmax=3000)
+    _check_batch(ctx, sa, oa, sb, ob)
+
+
+def test_gapdp_small_arena_waves_identical(ctx):
+    sa, oa, sb, ob = synth.gap_batch(seed=32, nprob=60, lmin=200, lmax=2500)
+    s1, p1 = ctx.gap_align_batch(sa, oa, sb, ob)
+    ctx.set_tb_arena(4 << 20)  # forces many waves
+    try:
+        s2, p2 = ctx.gap_align_batch(sa, oa, sb, ob)
+    finally:
+        ctx.set_tb_arena(32 << 30)
+    np.testing.assert_array_equal(s1, s2)
+    assert p1 == p2
+
+
+def test_gapdp_scores_only_equals_with_paths(ctx):
+    sa, oa, sb, ob = synth.gap_batch(seed=33, nprob=100, lmin=1, lmax=1500)
+    s1, _ = ctx.gap_align_batch(sa, oa, sb, ob, with_paths=True)
+    s2, _ = ctx.gap_align_batch(sa, oa, sb, ob, with_paths=False)
+    np.testing.assert_array_equal(s1, s2)
+
+
+def test_gapdp_rejects_bad_codes_and_empty(ctx):
+    with pytest.raises(ValueError):
+        ctx.gap_align_batch(np.array([0, 5, 1], np.uint8), [0, 3], np.array([1, 2], np.uint8), [0, 2])
+    with pytest.raises(ValueError):
+        ctx.gap_align_batch(np.array([0, 1], np.uint8), [0, 0, 2], np.array([1, 2], np.uint8), [0, 1, 2])
+
+
+def test_gapdp_long_pair_property(ctx):
+    """A 12 kbp pair: path consumes both sequences, and the score re-derived
+    from the path with NWSmall's scoring equals the returned score."""
+    rng = np.random.default_rng(44)
+    a = rng.integers(0, 4, 12_000).astype(np.uint8)
+    b = synth.mutate_codes(rng, a, 0.2, 60, 3.0)
+    scores, paths = ctx.gap_align_batch(a, [0, len(a)], b, [0, len(b)])
+    p = paths[0]
+    assert p.count("M") + p.count("D") == len(a) and p.count("M") + p.count("I") == len(b)
+    assert int(scores[0]) == _path_score(a, b, p)
+    assert int(scores[0]) == O.nw_score(a, b)
+
+
+def _path_score(a, b, path):
+    """Score of an edge path under NWSmall's model (open -200 / close -200 per
+    gap, first-position open free, extend 0)."""
+    sp = np.array([[91, -114, -31, -123], [-114, 100, -125, -31], [-31, -125, 100, -114], [-123, -31, -114, 91]]) + 60
+    i = j = 0
+    s = 0
+    prev = None
+    for e in path:
+        if e == "M":
+            if prev in ("D", "I"):
+                s += -200  # close
+            s += int(sp[a[i], b[j]])
+            i += 1
+            j += 1
+        elif e == "D":
+            if prev != "D":
+                s += 0 if i == 0 else -200  # open at A position i
+            i += 1
+        else:
+            if prev != "I":
+                s += 0 if j == 0 else -200
+            j += 1
+        prev = e
+    return s
