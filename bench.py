@@ -1,0 +1,392 @@
+#!/usr/bin/env python3
+"""Benchmark of the pairwise anchoring + gap-alignment path on one GB300.
+
+Step (the `value` workload): the anchoring path on the recoded-genome pair
+(B = 4.6 Mbp at GC 0.508 with 40 copies of a 1.3 kbp repeat and 4,300 ORFs;
+A = B with 3% ORF codon-third substitutions, 0.05% elsewhere, 200 indels,
+5 rearrangements): 2-bit packing, canonical coding-seed mers and radix sort
+for both genomes, unique-seed join, hashing, and the bucket-ordered
+extension / containment replay that yields the reference's match list.
+value = (|A| + |B|) / step time, in Mbp/s, inputs resident in HBM.
+e2e   = the same through the host-buffer C-ABI call (copies inside).
+
+The gap DP is measured in the same run on a batch drawn from the
+batched-gap-DP distribution (lengths log-uniform 10-20,000, divergence
+U(0,30%), subs:indels 9:1, indel mean 3): 20,000 pairs (10% of the
+200,000-pair batch), reported as GCUPS under "gap_dp".
+
+    python bench.py [--gpus N --steps K --warmup W] [--impl gb300|reference]
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (os.path.join(ROOT, "mauve-py_gb300"), os.path.join(ROOT, "oracle"), os.path.join(ROOT, "tests")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "Mbp/s aligned & gap-DP GCUPS: batched+learned-band vs plain GPU, bit-exact"
+WORKLOAD = ("recoded-genome pair: B 4.6 Mbp GC 0.508, 40x1.3 kbp repeat, 4,300 ORFs; A = B + 3% ORF codon-3rd "
+            "subs, 0.05% elsewhere, 200 indels (mean 4), 5 rearrangements 5-50 kbp; coding seed w=15 (0x16df6d)")
+GAP_WORKLOAD = ("batched gap DP: 20,000 pairs (10% of the 200,000-pair batch), lengths log-uniform 10-20,000, "
+                "divergence U(0,30%), subs:indels 9:1, indel mean 3")
+GAP_NPROB = 20_000
+L2_FLUSH_BYTES = 256 << 20
+OPS_PER_CELL = 10  # D: 2 add + max, I: 2 add + max, M: add + 2 max + add
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup(n_gpus):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def seeds_for(a, b):
+    import oracle as O
+    w = O.default_seed_weight((len(a) + len(b)) // 2)
+    return O.get_seed(w, 3), w
+
+
+# ------------------------------------------------------------- CPU side
+
+def cpu_anchoring(a, b, seed, steps):
+    """The oracle's restatement of the reference pipeline, single thread."""
+    import oracle as O
+    ts = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        m = O.pairwise_matches(a, b, seed)
+        ts.append(time.perf_counter() - t0)
+    return ts, m
+
+
+def cpu_gapdp_gcups(sa, oa, sb, ob, sample, threads):
+    import oracle as O
+    la = np.diff(oa.astype(np.int64))
+    order = np.argsort(la)
+    idx = np.sort(order[np.linspace(0, len(order) - 1, sample).astype(np.int64)])
+    a_parts = [sa[oa[k]:oa[k + 1]] for k in idx]
+    b_parts = [sb[ob[k]:ob[k + 1]] for k in idx]
+    soa = np.concatenate([[0], np.cumsum([len(x) for x in a_parts])]).astype(np.uint64)
+    sob = np.concatenate([[0], np.cumsum([len(x) for x in b_parts])]).astype(np.uint64)
+    cells = float(np.sum(np.diff(soa.astype(np.int64)) * np.diff(sob.astype(np.int64))))
+    t0 = time.perf_counter()
+    O.nw_batch(np.concatenate(a_parts), soa, np.concatenate(b_parts), sob, with_paths=True, nthreads=threads)
+    dt = time.perf_counter() - t0
+    return cells / dt / 1e9, cells, dt
+
+
+# ------------------------------------------------------------- arms
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return 0
+    import synth
+    a, b = synth.genome_pair_recoded()
+    seed, w = seeds_for(a, b)
+    cpu_anchoring(a, b, seed, args.warmup)
+    ts, m = cpu_anchoring(a, b, seed, args.steps)
+    mbp = (len(a) + len(b)) / 1e6
+    value = mbp * len(ts) / sum(ts)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": "Mbp/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * sum(ts) / len(ts), 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8/int64",
+        "data": "synthetic (seeded numpy)",
+        "config": {"workload": WORKLOAD, "matches": int(len(m))},
+        "cpu_baseline": {"value": round(value, 4), "unit": "Mbp/s", "cores": 1, "kind": "port",
+                         "sample": "the full pair each step; CPU restatement of the reference (oracle/), "
+                                   "single-threaded like the reference build"},
+        "e2e": {"value": round(value, 4), "unit": "Mbp/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gb300(args, world, rank, local):
+    import torch
+
+    import mvg
+    import synth
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    ctx = mvg.Context(local)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    dev = torch.device("cuda", local)
+
+    # ---- anchoring workload (weak scaling: each rank its own pair)
+    a, b = synth.genome_pair_recoded(seed=1 + rank)
+    seed, w = seeds_for(a, b)
+    na, nb = len(a), len(b)
+    d_a = torch.from_numpy(a).to(dev)
+    d_b = torch.from_numpy(b).to(dev)
+    cap = 1 << 20
+    d_out = torch.zeros(3 * cap, dtype=torch.int64, device=dev)
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
+    torch.cuda.synchronize()
+
+    def step():
+        return ctx.pairwise_matches_dev(d_a.data_ptr(), na, d_b.data_ptr(), nb, seed, d_out.data_ptr(), cap)
+
+    for _ in range(args.warmup):
+        nmatch = step()
+    ctx.set_profiling(True)
+    stage_tot = {}
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    sampler = ClockSampler(local)
+    launches0 = ctx.kernel_launches()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    sampler.start()
+    for k in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(k & 255)  # evict L2 between steps (untimed)
+        ev[k][0].record(stream)
+        nmatch = step()
+        ev[k][1].record(stream)
+        for name, t in ctx.stage_times().items():
+            stage_tot[name] = stage_tot.get(name, 0.0) + t
+    torch.cuda.synchronize()
+    launches = ctx.kernel_launches() - launches0
+    ms = [e0.elapsed_time(e1) for e0, e1 in ev]
+    tot_ms = sum(ms)
+    if world > 1:
+        t = torch.tensor([tot_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.barrier()
+        tot_ms = float(t.item())
+    clocks_anchor = sampler.stop()
+    ctx.set_profiling(False)
+    value = world * args.steps * (na + nb) / 1e6 / (tot_ms / 1e3)
+
+    # ---- e2e through the host-buffer C ABI (pinned inputs, copies inside)
+    pa = torch.from_numpy(a).pin_memory().numpy()
+    pb = torch.from_numpy(b).pin_memory().numpy()
+    host_out = torch.zeros(3 * cap, dtype=torch.int64).pin_memory().numpy()
+    import ctypes
+    cnt = ctypes.c_uint64(0)
+    L = mvg.load_library()
+
+    def e2e_step():
+        rc = L.mvg_pairwise_matches(ctx.handle, ctypes.c_void_p(pa.ctypes.data), na, ctypes.c_void_p(pb.ctypes.data),
+                                    nb, seed, ctypes.c_void_p(host_out.ctypes.data), cap, ctypes.byref(cnt))
+        mvg._check(rc)
+        return int(cnt.value)
+
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    e2e_ts = []
+    for k in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(k & 255)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        n_e2e = e2e_step()
+        e2e_ts.append(time.perf_counter() - t0)
+    e2e_s = sum(e2e_ts)
+    if world > 1:
+        t = torch.tensor([e2e_s], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = world * args.steps * (na + nb) / 1e6 / e2e_s
+    assert n_e2e == nmatch
+
+    # ---- gap DP batch
+    sa, oa, sb, ob = synth.gap_batch(seed=3 + rank, nprob=GAP_NPROB)
+    oa = oa.astype(np.uint64)
+    ob = ob.astype(np.uint64)
+    n = len(oa) - 1
+    cells = float(np.sum(np.diff(oa.astype(np.int64)) * np.diff(ob.astype(np.int64))))
+    path_off = np.zeros(n + 1, np.uint64)
+    path_off[1:] = np.cumsum(np.diff(oa.astype(np.int64)) + np.diff(ob.astype(np.int64)))
+    d_sa = torch.from_numpy(sa).to(dev)
+    d_sb = torch.from_numpy(sb).to(dev)
+    d_oa = torch.from_numpy(oa.view(np.int64)).to(dev)
+    d_ob = torch.from_numpy(ob.view(np.int64)).to(dev)
+    d_po = torch.from_numpy(path_off.view(np.int64)).to(dev)
+    d_sc = torch.zeros(n, dtype=torch.int32, device=dev)
+    d_paths = torch.zeros(int(path_off[-1]) + 16, dtype=torch.uint8, device=dev)
+    d_pl = torch.zeros(n, dtype=torch.int64, device=dev)
+    torch.cuda.synchronize()
+
+    def dp_step():
+        ctx.gap_align_batch_dev(d_sa.data_ptr(), d_oa.data_ptr(), d_sb.data_ptr(), d_ob.data_ptr(), n,
+                                d_sc.data_ptr(), d_paths.data_ptr(), d_po.data_ptr(), d_pl.data_ptr())
+
+    dp_steps = max(1, min(args.steps, 3))
+    for _ in range(max(1, min(args.warmup, 2))):
+        dp_step()
+    ctx.set_profiling(True)
+    dp_stage = {}
+    sampler = ClockSampler(local)
+    sampler.start()
+    dp_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(dp_steps)]
+    for k in range(dp_steps):
+        dp_ev[k][0].record(stream)
+        dp_step()
+        dp_ev[k][1].record(stream)
+        for name, t in ctx.stage_times().items():
+            dp_stage[name] = dp_stage.get(name, 0.0) + t
+    torch.cuda.synchronize()
+    clocks_dp = sampler.stop()
+    ctx.set_profiling(False)
+    dp_ms = sum(e0.elapsed_time(e1) for e0, e1 in dp_ev) / dp_steps
+    gcups = cells / (dp_ms / 1e3) / 1e9
+    int32_peak = ctx.probe_int32_peak()
+    dp_kernel_ms = dp_stage.get("dp", 0.0) / dp_steps
+    dp_achieved = cells * OPS_PER_CELL / (dp_kernel_ms / 1e3) if dp_kernel_ms else 0.0
+
+    if rank != 0:
+        if world > 1:
+            torch.distributed.barrier()
+        return 0
+
+    # ---- roofline of the anchoring step's stages
+    hbm_peak, peak_kind = peaks()
+    P = (2 * w + 1 + 7) // 8
+    per_base = 24.25 + 24 * P  # seed path bytes per base per genome
+    seed_ms = sum(stage_tot.get(k, 0.0) for k in ("pack", "sml_sort", "unique_join")) / args.steps
+    seed_bytes = per_base * (na + nb)
+    stages = {k: round(v / args.steps, 4) for k, v in stage_tot.items()}
+    dominant = max(stages, key=stages.get) if stages else None
+    roofline = {
+        "bound": "hbm", "kernel": "seed path (pack + seed keys + LSD radix sort + unique join), both genomes",
+        "achieved": round(seed_bytes / (seed_ms / 1e3) / 1e9, 2) if seed_ms else None,
+        "peak": hbm_peak, "unit": "GB/s", "peak_kind": peak_kind,
+        "frac": round(seed_bytes / (seed_ms / 1e3) / 1e9 / hbm_peak, 4) if seed_ms else None,
+        "traffic": None, "algorithmic_bytes": seed_bytes, "bytes_per_base": per_base,
+        "stage_ms": stages, "dominant_stage": dominant,
+    }
+
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": "Mbp/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(tot_ms / args.steps, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u8/int64", "data": "synthetic (seeded numpy)",
+        "config": {"workload": WORKLOAD, "bases": na + nb, "matches": int(nmatch),
+                   "l2": "flushed between timed steps (256 MiB device write, untimed)",
+                   "parallelism": "replicas: one genome pair per GPU"},
+        "roofline": roofline,
+        "e2e": {"value": round(e2e_value, 3), "unit": "Mbp/s", "h2d_bytes_per_step": na + nb,
+                "d2h_bytes_per_step": int(nmatch) * 24 + 12},
+        "gpu_launches": int(launches),
+        "clocks": clocks_anchor,
+        "gap_dp": {
+            "workload": GAP_WORKLOAD, "gcups": round(gcups, 2), "cells": cells, "ms_per_batch": round(dp_ms, 3),
+            "stage_ms": {k: round(v / dp_steps, 3) for k, v in dp_stage.items()},
+            "roofline": {"bound": "int32-alu", "achieved": round(dp_achieved / 1e12, 3), "unit": "Tops/s",
+                         "peak": round(int32_peak / 1e12, 3), "peak_kind": "measured (INT32 add/max probe)",
+                         "frac": round(dp_achieved / int32_peak, 4) if int32_peak else None,
+                         "ops_per_cell": OPS_PER_CELL},
+            "clocks": clocks_dp,
+        },
+    }
+    if world == 1 and not args.skip_cpu_baseline:
+        import multiprocessing
+        ts, _ = cpu_anchoring(a, b, seed, 1)
+        cpu_val = (na + nb) / 1e6 / ts[0]
+        threads = multiprocessing.cpu_count()
+        cg, ccells, cdt = cpu_gapdp_gcups(sa, oa, sb, ob, 400, threads)
+        line["cpu_baseline"] = {"value": round(cpu_val, 4), "unit": "Mbp/s", "cores": 1, "kind": "port",
+                                "sample": "the full 9.2 Mbp pair once (oracle restatement, one thread)"}
+        line["gap_dp"]["cpu_baseline"] = {"gcups": round(cg, 4), "cores": threads, "kind": "port",
+                                          "sample": "400 pairs spread over the length distribution, %.3g cells"
+                                                    % ccells}
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.barrier()
+    ctx.close()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--skip-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    world, rank, local = dist_setup(args.gpus)
+    if args.impl == "reference":
+        return run_reference(args, world, rank)
+    import build as pkg_build
+    pkg_build.build()
+    return run_gb300(args, world, rank, local)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -115,6 +115,14 @@ int mvg_gapdp_batch_dev(mvg_handle h, const uint8_t* d_seq_a, const uint64_t* d_
  * run in waves that fit it. */
 int mvg_set_tb_arena(mvg_handle h, uint64_t bytes);
 
+/* Per-stage timing with CUDA events on the handle's stream (off by default;
+ * no extra synchronisation).  After a call, mvg_stage_times gives the stage
+ * names (comma separated into names, of capacity names_cap) and each stage's
+ * milliseconds in ms[0..*n).  No counterpart in the reference (it prints
+ * progress only). */
+int mvg_set_profiling(mvg_handle h, int on);
+int mvg_stage_times(mvg_handle h, char* names, size_t names_cap, double* ms, int cap, int* n);
+
 /* Microbenchmark: sustained INT32 add/max throughput of this GPU, in
  * operations per second, from a dependent-chain-free kernel timed with
  * CUDA events.  Used as the roofline denominator for the gap DP. */

@@ -311,6 +311,35 @@ int mvg_set_tb_arena(mvg_handle h, uint64_t bytes) {
   return 0;
 }
 
+int mvg_set_profiling(mvg_handle h, int on) {
+  if (!h) return report_error(MVG_ERR_ARG, "null handle");
+  h->profiling = on != 0;
+  return 0;
+}
+
+int mvg_stage_times(mvg_handle h, char* names, size_t names_cap, double* ms, int cap, int* n) {
+  if (!h || !n || (cap && !ms) || (names_cap && !names)) return report_error(MVG_ERR_ARG, "null argument");
+  *n = 0;
+  if (names_cap) names[0] = 0;
+  if (h->nstage < 2) return 0;
+  MVG_CUDA_TRY(cudaEventSynchronize(h->ev[h->nstage - 1]));
+  size_t used = 0;
+  for (int k = 0; k + 1 < h->nstage && k < cap; ++k) {
+    float t = 0;
+    MVG_CUDA_TRY(cudaEventElapsedTime(&t, h->ev[k], h->ev[k + 1]));
+    ms[k] = t;
+    const size_t len = strlen(h->stage_name[k]);
+    if (names_cap && used + len + 2 < names_cap) {
+      if (used) names[used++] = ',';
+      memcpy(names + used, h->stage_name[k], len);
+      used += len;
+      names[used] = 0;
+    }
+    *n = k + 1;
+  }
+  return 0;
+}
+
 int mvg_probe_int32_peak(mvg_handle h, double* ops_per_s) {
   if (!h || !ops_per_s) return report_error(MVG_ERR_ARG, "null argument");
   MVG_CUDA_TRY(cudaSetDevice(h->device));

@@ -424,6 +424,7 @@ int gapdp_batch_dev(Ctx* c, const uint8_t* d_sa, const uint64_t* d_oa, const uin
   MVG_CUDA_TRY(cudaMemcpyAsync(d_order, ord.data(), (size_t)nprob * 4, cudaMemcpyHostToDevice, c->stream));
   MVG_CUDA_TRY(cudaMemcpyAsync(d_tboff, tboff.data(), (size_t)nprob * 8, cudaMemcpyHostToDevice, c->stream));
   MVG_CUDA_TRY(cudaMemsetAsync(c->d_err, 0, 4, c->stream));
+  stage_begin_call(c);
   for (size_t wv = 0; wv + 1 < wave_begin.size(); ++wv) {
     const int64_t w0 = wave_begin[wv], w1 = wave_begin[wv + 1];
     DpJob J;
@@ -442,14 +443,18 @@ int gapdp_batch_dev(Ctx* c, const uint8_t* d_sa, const uint64_t* d_oa, const uin
     J.counter = d_counter;
     J.err = c->d_err;
     MVG_CUDA_TRY(cudaMemsetAsync(d_counter, 0, 4, c->stream));
+    stage_mark(c, "dp");
     k_gapdp<<<grid, kDpThreads, 0, c->stream>>>(J);
+    stage_mark(c, "traceback");
     k_traceback<<<grid_for(J.nwork, 128), 128, 0, c->stream>>>(d_oa, d_ob, J.order, J.tb_off, J.nwork, tb, d_edge,
                                                                 d_path_off, d_paths, d_path_len, c->d_err);
+    stage_mark(c, "path_compact");
     k_path_compact<<<grid_for((int64_t)J.nwork * 32, 256), 256, 0, c->stream>>>(d_oa, d_ob, J.order, J.nwork,
                                                                                  d_path_off, d_paths, d_path_len);
     c->launches += 3;
     MVG_CUDA_TRY(cudaGetLastError());
   }
+  stage_end(c);
   MVG_CUDA_TRY(cudaStreamSynchronize(c->stream));
   return check_device_error(c);
 }

@@ -384,6 +384,8 @@ int pairwise_matches_dev(Ctx* c, const uint8_t* d_a, uint64_t na, const uint8_t*
   if (na >= 0x7fffffffull || nb >= 0x7fffffffull) return report_error(MVG_ERR_ARG, "genome longer than 2^31-1");
   c->stats = MatchStats();
   *count = 0;
+  stage_begin_call(c);
+  stage_mark(c, "pack");
   Workspace& ws = c->ws;
   uint32_t* ga = (uint32_t*)ws.get(c, 20, packed_words(na) * 4);
   uint32_t* gb = (uint32_t*)ws.get(c, 21, packed_words(nb) * 4);
@@ -396,8 +398,10 @@ int pairwise_matches_dev(Ctx* c, const uint8_t* d_a, uint64_t na, const uint8_t*
   const uint64_t cb = nb >= (uint64_t)s.L ? nb - s.L + 1 : 0;
   if (ca == 0 || cb == 0) return check_device_error(c);
   SmlKeys ska, skb;
+  stage_mark(c, "sml_sort");
   if ((rc = sml_sort(c, ga, ca, s, nullptr, nullptr, &ska, 0))) return rc;
   if ((rc = sml_sort(c, gb, cb, s, nullptr, nullptr, &skb, 52))) return rc;
+  stage_mark(c, "unique_join");
   uint64_t *uka, *ukb;
   uint32_t *upa, *upb, *nua, *nub;
   if (ska.wide) {
@@ -447,8 +451,10 @@ int pairwise_matches_dev(Ctx* c, const uint8_t* d_a, uint64_t na, const uint8_t*
   uint32_t* ooff = btab + 7 * kTableSize;
   uint32_t* bscr = btab + 10 * kTableSize;
   uint32_t* tot = bscr + scan_scratch_words(kTableSize);
-  unsigned long long* d_coll = (unsigned long long*)(tot + 4);
+  // 64-bit counter: round up to an 8-byte boundary (the table above is uint32)
+  unsigned long long* d_coll = (unsigned long long*)(((uintptr_t)(tot + 4) + 7) & ~(uintptr_t)7);
 
+  stage_mark(c, "hash_bucket_sort");
   k_hash_pairs<<<grid_for(capa, 256), 256, 0, c->stream>>>(uka, upa, ukb, upb, hit, hflag, hidx, capa, nua, s.L, mhe,
                                                             bk0, or0);
   c->launches++;
@@ -470,12 +476,15 @@ int pairwise_matches_dev(Ctx* c, const uint8_t* d_a, uint64_t na, const uint8_t*
   mc.n[0] = (int64_t)na;
   mc.n[1] = (int64_t)nb;
   mc.s = s;
+  stage_mark(c, "bucket_replay");
   k_bucket_warps<<<kTableSize / 8, 256, 0, c->stream>>>(mc, mhe, sorted_pair, bstart, bcount, border, kTableSize, ent,
                                                          nent, d_coll);
   c->launches++;
+  stage_mark(c, "emit");
   exclusive_scan(nent, ooff, kTableSize, bscr, tot + 1, c->stream, &c->launches);
   k_emit<<<kTableSize / 8, 256, 0, c->stream>>>(ent, bstart, nent, ooff, d_out, cap);
   c->launches++;
+  stage_end(c);
   MVG_CUDA_TRY(cudaMemcpyAsync(c->h_scalars, tot + 1, 4, cudaMemcpyDeviceToHost, c->stream));
   MVG_CUDA_TRY(cudaMemcpyAsync(c->h_scalars + 1, d_coll, 8, cudaMemcpyDeviceToHost, c->stream));
   MVG_CUDA_TRY(cudaStreamSynchronize(c->stream));

@@ -23,6 +23,9 @@ struct MatchStats {
   uint64_t pairs = 0, collisions = 0, matches = 0, buckets = 0;
 };
 
+// Optional per-stage CUDA-event timing on the handle's stream (off by default).
+constexpr int kMaxStages = 24;
+
 struct Ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -33,7 +36,24 @@ struct Ctx {
   uint64_t tb_arena = 32ull << 30;
   Workspace ws;
   MatchStats stats;
+  bool profiling = false;
+  cudaEvent_t ev[kMaxStages + 1] = {};
+  const char* stage_name[kMaxStages] = {};
+  int nstage = -1;  // -1: no stage recorded yet in this call
 };
+
+// Marks the start of a named stage (and the end of the previous one).
+inline void stage_mark(Ctx* c, const char* name) {
+  if (!c->profiling) return;
+  if (c->nstage < 0) c->nstage = 0;
+  if (c->nstage >= kMaxStages) return;
+  if (!c->ev[c->nstage]) cudaEventCreate(&c->ev[c->nstage]);
+  cudaEventRecord(c->ev[c->nstage], c->stream);
+  c->stage_name[c->nstage] = name;
+  c->nstage++;
+}
+inline void stage_begin_call(Ctx* c) { c->nstage = -1; }
+inline void stage_end(Ctx* c) { stage_mark(c, "end"); }
 
 // Sorted keys of one genome kept on the device for the join.
 struct SmlKeys {

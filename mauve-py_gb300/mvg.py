@@ -34,7 +34,8 @@ _lib = None
 EXPORTS = ["mvg_create", "mvg_destroy", "mvg_last_error", "mvg_stream", "mvg_kernel_launches", "mvg_get_seed",
            "mvg_default_seed_weight", "mvg_seed_length", "mvg_seed_weight", "mvg_sml_build", "mvg_sml_build_dev",
            "mvg_pairwise_matches", "mvg_pairwise_matches_dev", "mvg_pairwise_stats", "mvg_gapdp_batch",
-           "mvg_gapdp_batch_dev", "mvg_set_tb_arena", "mvg_probe_int32_peak"]
+           "mvg_gapdp_batch_dev", "mvg_set_tb_arena", "mvg_probe_int32_peak", "mvg_set_profiling",
+           "mvg_stage_times"]
 
 
 def load_library(path=LIB_PATH):
@@ -65,6 +66,8 @@ def load_library(path=LIB_PATH):
         "mvg_gapdp_batch_dev": (ci, [vp, vp, vp, vp, vp, i64, vp, vp, vp, vp]),
         "mvg_set_tb_arena": (ci, [vp, u64]),
         "mvg_probe_int32_peak": (ci, [vp, ctypes.POINTER(ctypes.c_double)]),
+        "mvg_set_profiling": (ci, [vp, ci]),
+        "mvg_stage_times": (ci, [vp, ctypes.c_char_p, ctypes.c_size_t, vp, ci, ctypes.POINTER(ci)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -225,6 +228,20 @@ class Context:
     def gap_align_batch_dev(self, d_sa, d_oa, d_sb, d_ob, n, d_scores, d_paths, d_path_off, d_path_len):
         _check(load_library().mvg_gapdp_batch_dev(self._h, d_sa, d_oa, d_sb, d_ob, n, d_scores, d_paths, d_path_off,
                                                   d_path_len))
+
+    def set_profiling(self, on=True):
+        _check(load_library().mvg_set_profiling(self._h, 1 if on else 0))
+
+    def stage_times(self):
+        """{stage name: total ms} of the last call (profiling must be on)."""
+        names = ctypes.create_string_buffer(4096)
+        ms = np.zeros(64, np.float64)
+        n = ctypes.c_int(0)
+        _check(load_library().mvg_stage_times(self._h, names, 4096, _ptr(ms), 64, ctypes.byref(n)))
+        out = {}
+        for name, t in zip(names.value.decode().split(",") if n.value else [], ms[:n.value]):
+            out[name] = out.get(name, 0.0) + float(t)
+        return out
 
     def probe_int32_peak(self):
         v = ctypes.c_double(0)
