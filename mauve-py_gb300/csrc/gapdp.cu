@@ -39,21 +39,28 @@ constexpr int kDpThreads = 256;
 
 enum : uint32_t { TB_MM = 0, TB_DM = 1, TB_IM = 2, TB_MD = 4, TB_MI = 8 };
 
-// NUC_SP + 60, packed: entry (a,b) = byte b of kScoreRow[a], biased by +64.
+// NUC_SP + 60 (range -65..160), packed: entry (a,b) = byte b of
+// c_score_rows[a], stored with a +80 bias so every byte is in 15..240.
+constexpr int kScoreBias = 80;
 __constant__ uint32_t c_score_rows[4];
 
-static void score_rows_host(uint32_t* rows) {
+static bool score_rows_host(uint32_t* rows) {
   const int sp[4][4] = {{91, -114, -31, -123}, {-114, 100, -125, -31}, {-31, -125, 100, -114}, {-123, -31, -114, 91}};
   for (int a = 0; a < 4; ++a) {
     uint32_t r = 0;
-    for (int b = 0; b < 4; ++b) r |= (uint32_t)(sp[a][b] + 60 + 64) << (8 * b);
+    for (int b = 0; b < 4; ++b) {
+      const int v = sp[a][b] + 60 + kScoreBias;
+      if (v < 0 || v > 255) return false;
+      r |= (uint32_t)v << (8 * b);
+    }
     rows[a] = r;
   }
+  return true;
 }
 
 int upload_score_table() {
   uint32_t rows[4];
-  score_rows_host(rows);
+  if (!score_rows_host(rows)) return report_error(MVG_ERR_ARG, "score table does not fit the packed byte layout");
   MVG_CUDA_TRY(cudaMemcpyToSymbol(c_score_rows, rows, sizeof(rows)));
   return 0;
 }
@@ -76,7 +83,7 @@ struct DpJob {
 };
 
 __device__ __forceinline__ int32_t score_ab(uint32_t row_a, uint32_t b) {
-  return (int32_t)((row_a >> (8 * b)) & 255u) - 64;
+  return (int32_t)((row_a >> (8 * b)) & 255u) - kScoreBias;
 }
 
 __global__ void __launch_bounds__(kDpThreads, 2) k_gapdp(DpJob J) {
