@@ -379,6 +379,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--skip-cpu-baseline", action="store_true")
+    ap.add_argument("--only", choices=["all", "anchor", "gapdp"], default="all",
+                    help="run one half only (small cases for profiler captures)")
+    ap.add_argument("--pair", choices=["recoded", "small"], default="recoded",
+                    help="genome pair: recoded 4.6 Mbp (default) or the 1 Mbp plain-method pair")
+    ap.add_argument("--gap-nprob", type=int, default=GAP_NPROB)
     args = ap.parse_args()
     world, rank, local = dist_setup(args.gpus)
     if args.impl == "reference":
