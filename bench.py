@@ -122,7 +122,7 @@ def seeds_for(a, b):
 def cpu_anchoring(a, b, seed, steps):
     """The oracle's restatement of the reference pipeline, single thread."""
     import oracle as O
-    ts = []
+    ts, m = [], None
     for _ in range(steps):
         t0 = time.perf_counter()
         m = O.pairwise_matches(a, b, seed)
@@ -186,185 +186,199 @@ def run_gb300(args, world, rank, local):
     ctx = mvg.Context(local)
     stream = torch.cuda.ExternalStream(ctx.stream)
     dev = torch.device("cuda", local)
-
-    # ---- anchoring workload (weak scaling: each rank its own pair)
-    a, b = synth.genome_pair_recoded(seed=1 + rank)
-    seed, w = seeds_for(a, b)
-    na, nb = len(a), len(b)
-    d_a = torch.from_numpy(a).to(dev)
-    d_b = torch.from_numpy(b).to(dev)
-    cap = 1 << 20
-    d_out = torch.zeros(3 * cap, dtype=torch.int64, device=dev)
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
-    torch.cuda.synchronize()
 
-    def step():
-        return ctx.pairwise_matches_dev(d_a.data_ptr(), na, d_b.data_ptr(), nb, seed, d_out.data_ptr(), cap)
-
-    for _ in range(args.warmup):
-        nmatch = step()
-    ctx.set_profiling(True)
-    stage_tot = {}
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    sampler = ClockSampler(local)
-    launches0 = ctx.kernel_launches()
-    if world > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
-    sampler.start()
-    for k in range(args.steps):
-        with torch.cuda.stream(stream):
-            flush.fill_(k & 255)  # evict L2 between steps (untimed)
-        ev[k][0].record(stream)
-        nmatch = step()
-        ev[k][1].record(stream)
-        for name, t in ctx.stage_times().items():
-            stage_tot[name] = stage_tot.get(name, 0.0) + t
-    torch.cuda.synchronize()
-    launches = ctx.kernel_launches() - launches0
-    ms = [e0.elapsed_time(e1) for e0, e1 in ev]
-    tot_ms = sum(ms)
-    if world > 1:
-        t = torch.tensor([tot_ms], device=dev)
+    def max_over_ranks(x):
+        if world == 1:
+            return x
+        t = torch.tensor([x], device=dev, dtype=torch.float64)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        torch.distributed.barrier()
-        tot_ms = float(t.item())
-    clocks_anchor = sampler.stop()
-    ctx.set_profiling(False)
-    value = world * args.steps * (na + nb) / 1e6 / (tot_ms / 1e3)
+        return float(t.item())
 
-    # ---- e2e through the host-buffer C ABI (pinned inputs, copies inside)
-    pa = torch.from_numpy(a).pin_memory().numpy()
-    pb = torch.from_numpy(b).pin_memory().numpy()
-    host_out = torch.zeros(3 * cap, dtype=torch.int64).pin_memory().numpy()
-    import ctypes
-    cnt = ctypes.c_uint64(0)
-    L = mvg.load_library()
+    line = {"metric": METRIC, "unit": "Mbp/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8/int64",
+            "data": "synthetic (seeded numpy)"}
+    launches = 0
 
-    def e2e_step():
-        rc = L.mvg_pairwise_matches(ctx.handle, ctypes.c_void_p(pa.ctypes.data), na, ctypes.c_void_p(pb.ctypes.data),
-                                    nb, seed, ctypes.c_void_p(host_out.ctypes.data), cap, ctypes.byref(cnt))
-        mvg._check(rc)
-        return int(cnt.value)
-
-    for _ in range(max(1, args.warmup)):
-        e2e_step()
-    e2e_ts = []
-    for k in range(args.steps):
-        with torch.cuda.stream(stream):
-            flush.fill_(k & 255)
+    if args.only in ("all", "anchor"):
+        # ---- anchoring workload (weak scaling: each rank its own pair)
+        if args.pair == "small":
+            a, b = synth.genome_pair_small(seed=rank)
+            workload = "plain-method pair: 1 Mbp i.i.d. GC 0.50, A = B + 0.5% subs, 50 indels, 2 x 10 kbp inversions"
+        else:
+            a, b = synth.genome_pair_recoded(seed=1 + rank)
+            workload = WORKLOAD
+        seed, w = seeds_for(a, b)
+        na, nb = len(a), len(b)
+        d_a = torch.from_numpy(a).to(dev)
+        d_b = torch.from_numpy(b).to(dev)
+        cap = 1 << 20
+        d_out = torch.zeros(3 * cap, dtype=torch.int64, device=dev)
         torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        n_e2e = e2e_step()
-        e2e_ts.append(time.perf_counter() - t0)
-    e2e_s = sum(e2e_ts)
-    if world > 1:
-        t = torch.tensor([e2e_s], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e_value = world * args.steps * (na + nb) / 1e6 / e2e_s
-    assert n_e2e == nmatch
 
-    # ---- gap DP batch
-    sa, oa, sb, ob = synth.gap_batch(seed=3 + rank, nprob=GAP_NPROB)
-    oa = oa.astype(np.uint64)
-    ob = ob.astype(np.uint64)
-    n = len(oa) - 1
-    cells = float(np.sum(np.diff(oa.astype(np.int64)) * np.diff(ob.astype(np.int64))))
-    path_off = np.zeros(n + 1, np.uint64)
-    path_off[1:] = np.cumsum(np.diff(oa.astype(np.int64)) + np.diff(ob.astype(np.int64)))
-    d_sa = torch.from_numpy(sa).to(dev)
-    d_sb = torch.from_numpy(sb).to(dev)
-    d_oa = torch.from_numpy(oa.view(np.int64)).to(dev)
-    d_ob = torch.from_numpy(ob.view(np.int64)).to(dev)
-    d_po = torch.from_numpy(path_off.view(np.int64)).to(dev)
-    d_sc = torch.zeros(n, dtype=torch.int32, device=dev)
-    d_paths = torch.zeros(int(path_off[-1]) + 16, dtype=torch.uint8, device=dev)
-    d_pl = torch.zeros(n, dtype=torch.int64, device=dev)
-    torch.cuda.synchronize()
+        def step():
+            return ctx.pairwise_matches_dev(d_a.data_ptr(), na, d_b.data_ptr(), nb, seed, d_out.data_ptr(), cap)
 
-    def dp_step():
-        ctx.gap_align_batch_dev(d_sa.data_ptr(), d_oa.data_ptr(), d_sb.data_ptr(), d_ob.data_ptr(), n,
-                                d_sc.data_ptr(), d_paths.data_ptr(), d_po.data_ptr(), d_pl.data_ptr())
-
-    dp_steps = max(1, min(args.steps, 3))
-    for _ in range(max(1, min(args.warmup, 2))):
-        dp_step()
-    ctx.set_profiling(True)
-    dp_stage = {}
-    sampler = ClockSampler(local)
-    sampler.start()
-    dp_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(dp_steps)]
-    for k in range(dp_steps):
-        dp_ev[k][0].record(stream)
-        dp_step()
-        dp_ev[k][1].record(stream)
-        for name, t in ctx.stage_times().items():
-            dp_stage[name] = dp_stage.get(name, 0.0) + t
-    torch.cuda.synchronize()
-    clocks_dp = sampler.stop()
-    ctx.set_profiling(False)
-    dp_ms = sum(e0.elapsed_time(e1) for e0, e1 in dp_ev) / dp_steps
-    gcups = cells / (dp_ms / 1e3) / 1e9
-    int32_peak = ctx.probe_int32_peak()
-    dp_kernel_ms = dp_stage.get("dp", 0.0) / dp_steps
-    dp_achieved = cells * OPS_PER_CELL / (dp_kernel_ms / 1e3) if dp_kernel_ms else 0.0
-
-    if rank != 0:
+        for _ in range(args.warmup):
+            nmatch = step()
+        ctx.set_profiling(True)
+        stage_tot = {}
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        sampler = ClockSampler(local)
+        launches0 = ctx.kernel_launches()
         if world > 1:
             torch.distributed.barrier()
-        return 0
+        torch.cuda.synchronize()
+        sampler.start()
+        for k in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(k & 255)  # evict L2 between steps (untimed)
+            ev[k][0].record(stream)
+            nmatch = step()
+            ev[k][1].record(stream)
+            for name, t in ctx.stage_times().items():
+                stage_tot[name] = stage_tot.get(name, 0.0) + t
+        torch.cuda.synchronize()
+        launches += ctx.kernel_launches() - launches0
+        tot_ms = max_over_ranks(sum(e0.elapsed_time(e1) for e0, e1 in ev))
+        if world > 1:
+            torch.distributed.barrier()
+        clocks_anchor = sampler.stop()
+        ctx.set_profiling(False)
+        value = world * args.steps * (na + nb) / 1e6 / (tot_ms / 1e3)
 
-    # ---- roofline of the anchoring step's stages
-    hbm_peak, peak_kind = peaks()
-    P = (2 * w + 1 + 7) // 8
-    per_base = 24.25 + 24 * P  # seed path bytes per base per genome
-    seed_ms = sum(stage_tot.get(k, 0.0) for k in ("pack", "sml_sort", "unique_join")) / args.steps
-    seed_bytes = per_base * (na + nb)
-    stages = {k: round(v / args.steps, 4) for k, v in stage_tot.items()}
-    dominant = max(stages, key=stages.get) if stages else None
-    roofline = {
-        "bound": "hbm", "kernel": "seed path (pack + seed keys + LSD radix sort + unique join), both genomes",
-        "achieved": round(seed_bytes / (seed_ms / 1e3) / 1e9, 2) if seed_ms else None,
-        "peak": hbm_peak, "unit": "GB/s", "peak_kind": peak_kind,
-        "frac": round(seed_bytes / (seed_ms / 1e3) / 1e9 / hbm_peak, 4) if seed_ms else None,
-        "traffic": None, "algorithmic_bytes": seed_bytes, "bytes_per_base": per_base,
-        "stage_ms": stages, "dominant_stage": dominant,
-    }
+        # ---- e2e through the host-buffer C ABI (pinned inputs, copies inside)
+        import ctypes
+        pa = torch.from_numpy(a).pin_memory().numpy()
+        pb = torch.from_numpy(b).pin_memory().numpy()
+        host_out = torch.zeros(3 * cap, dtype=torch.int64).pin_memory().numpy()
+        cnt = ctypes.c_uint64(0)
+        L = mvg.load_library()
 
-    line = {
-        "metric": METRIC, "value": round(value, 3), "unit": "Mbp/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": round(tot_ms / args.steps, 4), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "u8/int64", "data": "synthetic (seeded numpy)",
-        "config": {"workload": WORKLOAD, "bases": na + nb, "matches": int(nmatch),
-                   "l2": "flushed between timed steps (256 MiB device write, untimed)",
-                   "parallelism": "replicas: one genome pair per GPU"},
-        "roofline": roofline,
-        "e2e": {"value": round(e2e_value, 3), "unit": "Mbp/s", "h2d_bytes_per_step": na + nb,
-                "d2h_bytes_per_step": int(nmatch) * 24 + 12},
-        "gpu_launches": int(launches),
-        "clocks": clocks_anchor,
-        "gap_dp": {
-            "workload": GAP_WORKLOAD, "gcups": round(gcups, 2), "cells": cells, "ms_per_batch": round(dp_ms, 3),
+        def e2e_step():
+            rc = L.mvg_pairwise_matches(ctx.handle, ctypes.c_void_p(pa.ctypes.data), na,
+                                        ctypes.c_void_p(pb.ctypes.data), nb, seed,
+                                        ctypes.c_void_p(host_out.ctypes.data), cap, ctypes.byref(cnt))
+            mvg._check(rc)
+            return int(cnt.value)
+
+        for _ in range(max(1, args.warmup)):
+            e2e_step()
+        e2e_s = 0.0
+        for k in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(k & 255)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            n_e2e = e2e_step()
+            e2e_s += time.perf_counter() - t0
+        e2e_s = max_over_ranks(e2e_s)
+        assert n_e2e == nmatch
+        e2e_value = world * args.steps * (na + nb) / 1e6 / e2e_s
+
+        hbm_peak, peak_kind = peaks()
+        P = (2 * w + 1 + 7) // 8
+        per_base = 24.25 + 24 * P  # seed path bytes per base per genome
+        seed_ms = sum(stage_tot.get(k, 0.0) for k in ("pack", "sml_sort", "unique_join")) / args.steps
+        seed_bytes = per_base * (na + nb)
+        stages = {k: round(v / args.steps, 4) for k, v in stage_tot.items()}
+        line.update({
+            "value": round(value, 3), "ms_per_step": round(tot_ms / args.steps, 4),
+            "config": {"workload": workload, "bases": na + nb, "matches": int(nmatch), "seed_weight": w,
+                       "l2": "flushed between timed steps (256 MiB device write, untimed)",
+                       "parallelism": "replicas: one genome pair per GPU"},
+            "roofline": {
+                "bound": "hbm", "kernel": "seed path (pack + seed keys + LSD radix sort + unique join), both genomes",
+                "achieved": round(seed_bytes / (seed_ms / 1e3) / 1e9, 2) if seed_ms else None,
+                "peak": hbm_peak, "unit": "GB/s", "peak_kind": peak_kind,
+                "frac": round(seed_bytes / (seed_ms / 1e3) / 1e9 / hbm_peak, 4) if seed_ms else None,
+                "traffic": None, "algorithmic_bytes": seed_bytes, "bytes_per_base": per_base,
+                "stage_ms": stages, "dominant_stage": max(stages, key=stages.get) if stages else None},
+            "e2e": {"value": round(e2e_value, 3), "unit": "Mbp/s", "h2d_bytes_per_step": na + nb,
+                    "d2h_bytes_per_step": int(nmatch) * 24 + 12},
+            "clocks": clocks_anchor,
+        })
+
+    if args.only in ("all", "gapdp"):
+        sa, oa, sb, ob = synth.gap_batch(seed=3 + rank, nprob=args.gap_nprob)
+        oa = oa.astype(np.uint64)
+        ob = ob.astype(np.uint64)
+        n = len(oa) - 1
+        cells = float(np.sum(np.diff(oa.astype(np.int64)) * np.diff(ob.astype(np.int64))))
+        path_off = np.zeros(n + 1, np.uint64)
+        path_off[1:] = np.cumsum(np.diff(oa.astype(np.int64)) + np.diff(ob.astype(np.int64)))
+        d_sa = torch.from_numpy(sa).to(dev)
+        d_sb = torch.from_numpy(sb).to(dev)
+        d_oa = torch.from_numpy(oa.view(np.int64)).to(dev)
+        d_ob = torch.from_numpy(ob.view(np.int64)).to(dev)
+        d_po = torch.from_numpy(path_off.view(np.int64)).to(dev)
+        d_sc = torch.zeros(n, dtype=torch.int32, device=dev)
+        d_paths = torch.zeros(int(path_off[-1]) + 16, dtype=torch.uint8, device=dev)
+        d_pl = torch.zeros(n, dtype=torch.int64, device=dev)
+        torch.cuda.synchronize()
+
+        def dp_step():
+            ctx.gap_align_batch_dev(d_sa.data_ptr(), d_oa.data_ptr(), d_sb.data_ptr(), d_ob.data_ptr(), n,
+                                    d_sc.data_ptr(), d_paths.data_ptr(), d_po.data_ptr(), d_pl.data_ptr())
+
+        dp_steps = max(1, min(args.steps, 3))
+        for _ in range(max(1, min(args.warmup, 2))):
+            dp_step()
+        ctx.set_profiling(True)
+        dp_stage = {}
+        sampler = ClockSampler(local)
+        launches0 = ctx.kernel_launches()
+        sampler.start()
+        dp_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                 for _ in range(dp_steps)]
+        for k in range(dp_steps):
+            dp_ev[k][0].record(stream)
+            dp_step()
+            dp_ev[k][1].record(stream)
+            for name, t in ctx.stage_times().items():
+                dp_stage[name] = dp_stage.get(name, 0.0) + t
+        torch.cuda.synchronize()
+        launches += ctx.kernel_launches() - launches0
+        clocks_dp = sampler.stop()
+        ctx.set_profiling(False)
+        dp_ms = max_over_ranks(sum(e0.elapsed_time(e1) for e0, e1 in dp_ev) / dp_steps)
+        gcups = world * cells / (dp_ms / 1e3) / 1e9
+        int32_peak = ctx.probe_int32_peak()
+        dp_kernel_ms = dp_stage.get("dp", 0.0) / dp_steps
+        dp_achieved = cells * OPS_PER_CELL / (dp_kernel_ms / 1e3) if dp_kernel_ms else 0.0
+        line["gap_dp"] = {
+            "workload": GAP_WORKLOAD if args.gap_nprob == GAP_NPROB else "%d pairs from the same distribution"
+                                                                          % args.gap_nprob,
+            "gcups": round(gcups, 2), "cells": cells, "ms_per_batch": round(dp_ms, 3),
             "stage_ms": {k: round(v / dp_steps, 3) for k, v in dp_stage.items()},
             "roofline": {"bound": "int32-alu", "achieved": round(dp_achieved / 1e12, 3), "unit": "Tops/s",
                          "peak": round(int32_peak / 1e12, 3), "peak_kind": "measured (INT32 add/max probe)",
                          "frac": round(dp_achieved / int32_peak, 4) if int32_peak else None,
                          "ops_per_cell": OPS_PER_CELL},
             "clocks": clocks_dp,
-        },
-    }
+        }
+        if args.only == "gapdp":
+            line.update({"value": round(gcups, 2), "unit": "GCUPS", "ms_per_step": round(dp_ms, 3)})
+
+    line["gpu_launches"] = int(launches)
+    if rank != 0:
+        if world > 1:
+            torch.distributed.barrier()
+        ctx.close()
+        return 0
     if world == 1 and not args.skip_cpu_baseline:
         import multiprocessing
-        ts, _ = cpu_anchoring(a, b, seed, 1)
-        cpu_val = (na + nb) / 1e6 / ts[0]
-        threads = multiprocessing.cpu_count()
-        cg, ccells, cdt = cpu_gapdp_gcups(sa, oa, sb, ob, 400, threads)
-        line["cpu_baseline"] = {"value": round(cpu_val, 4), "unit": "Mbp/s", "cores": 1, "kind": "port",
-                                "sample": "the full 9.2 Mbp pair once (oracle restatement, one thread)"}
-        line["gap_dp"]["cpu_baseline"] = {"gcups": round(cg, 4), "cores": threads, "kind": "port",
-                                          "sample": "400 pairs spread over the length distribution, %.3g cells"
-                                                    % ccells}
+        if args.only in ("all", "anchor"):
+            ts, _ = cpu_anchoring(a, b, seed, 1)
+            line["cpu_baseline"] = {"value": round((na + nb) / 1e6 / ts[0], 4), "unit": "Mbp/s", "cores": 1,
+                                    "kind": "port",
+                                    "sample": "the full pair once (oracle restatement, one thread)"}
+        if args.only in ("all", "gapdp"):
+            threads = multiprocessing.cpu_count()
+            cg, ccells, cdt = cpu_gapdp_gcups(sa, oa, sb, ob, 400, threads)
+            line["gap_dp"]["cpu_baseline"] = {"gcups": round(cg, 4), "cores": threads, "kind": "port",
+                                              "sample": "400 pairs spread over the length distribution, %.3g cells"
+                                                        % ccells}
     print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.barrier()

@@ -111,8 +111,9 @@ int mvg_gapdp_batch_dev(mvg_handle h, const uint8_t* d_seq_a, const uint64_t* d_
                         const uint64_t* d_off_b, int64_t nprob, int32_t* d_scores, char* d_paths,
                         const uint64_t* d_path_off, int64_t* d_path_len);
 
-/* Device bytes the gap-DP traceback arena may use (default 32 GiB); problems
- * run in waves that fit it. */
+/* Upper bound on the device bytes the gap-DP traceback arena may use.  Each
+ * call uses min(bound, 60% of free device memory); problems run in waves of
+ * mixed sizes that fit it.  Default: no bound beyond the 60% cap. */
 int mvg_set_tb_arena(mvg_handle h, uint64_t bytes);
 
 /* Per-stage timing with CUDA events on the handle's stream (off by default;

@@ -87,9 +87,17 @@ __device__ __forceinline__ int32_t score_ab(uint32_t row_a, uint32_t b) {
 }
 
 __global__ void __launch_bounds__(kDpThreads, 2) k_gapdp(DpJob J) {
+  // Per-warp shared rings: B codes (lane t at step s reads B[s - t]) and the
+  // row above the strip (lane 0 at step s reads rowbuf[s + 1]).  Both are
+  // filled one 32-step chunk ahead, so no load sits on a step's critical path.
+  __shared__ uint8_t sB[kDpThreads / 32][128];
+  __shared__ int4 sR[kDpThreads / 32][64];
   const int lane = threadIdx.x & 31;
+  const int wib = threadIdx.x >> 5;
   const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   int4* rowbuf = J.rowbuf + gw * J.rowbuf_stride;
+  uint8_t* ringB = sB[wib];
+  int4* ringR = sR[wib];
   for (;;) {
     int w = 0;
     if (lane == 0) w = (int)atomicAdd(J.counter, 1u);
@@ -104,28 +112,32 @@ __global__ void __launch_bounds__(kDpThreads, 2) k_gapdp(DpJob J) {
     const int S = LB + 31;                              // steps per strip
     const int wpl = (S * kRows + 7) / 8;                // TB words per lane per strip
     const int nstrips = (LA + kStripRows - 1) / kStripRows;
-    // end cell owner
     const int end_strip = (LA - 1) / kStripRows;
     const int end_lane = ((LA - 1) % kStripRows) / kRows;
     const int end_r = (LA - 1) % kRows;
+    uint32_t bad = 0;
 
     for (int k = 0; k < nstrips; ++k) {
       const int row0 = k * kStripRows;
       uint32_t arow[kRows];
       int32_t goA[kRows];
-      bool rvalid[kRows];
 #pragma unroll
       for (int r = 0; r < kRows; ++r) {
         const int i = row0 + lane * kRows + r + 1;
-        rvalid[r] = i <= LA;
-        uint32_t ac = rvalid[r] ? A[i - 1] : 0u;
-        if (ac > 3u) {
-          set_error(J.err, kDevBadBase);
-          ac = 0;
-        }
-        arow[r] = c_score_rows[ac];
+        uint32_t ac = i <= LA ? A[i - 1] : 0u;
+        bad |= ac;
+        arow[r] = c_score_rows[ac & 3u];
         goA[r] = (i == 1) ? 0 : kGap;
       }
+      // prime the rings: B[0..63], rowbuf[1..64]
+      __syncwarp();
+      ringB[lane] = lane < LB ? B[lane] : 0;
+      ringB[32 + lane] = 32 + lane < LB ? B[32 + lane] : 0;
+      if (k > 0) {
+        ringR[(1 + lane) & 63] = 1 + lane <= LB ? rowbuf[1 + lane] : make_int4(kNeg, kNeg, kNeg, 0);
+        ringR[(33 + lane) & 63] = 33 + lane <= LB ? rowbuf[33 + lane] : make_int4(kNeg, kNeg, kNeg, 0);
+      }
+      __syncwarp();
       // left state (column j-1) per row; column 0 = (NEG, 0, NEG)
       int32_t lM[kRows], lD[kRows], lI[kRows];
 #pragma unroll
@@ -139,39 +151,45 @@ __global__ void __launch_bounds__(kDpThreads, 2) k_gapdp(DpJob J) {
       int32_t dgM, dgD, dgI;                       // row above, previous column
       uint32_t acc = 0;
       uint32_t* tbs = tb + (int64_t)k * wpl * 32;
-      __syncwarp();
       for (int s = 0; s < S; ++s) {
+        if ((s & 31) == 0 && s > 0) {
+          // refill one chunk ahead: B[s+32 .. s+63], rowbuf[s+33 .. s+64]
+          __syncwarp();
+          const int xb = s + 32 + lane;
+          ringB[xb & 127] = xb < LB ? B[xb] : 0;
+          if (k > 0) {
+            const int xr = s + 33 + lane;
+            ringR[xr & 63] = xr <= LB ? rowbuf[xr] : make_int4(kNeg, kNeg, kNeg, 0);
+          }
+          __syncwarp();
+        }
         const int j = s - lane + 1;
         const int32_t rM = __shfl_up_sync(0xffffffffu, pubM, 1);
         const int32_t rD = __shfl_up_sync(0xffffffffu, pubD, 1);
         const int32_t rI = __shfl_up_sync(0xffffffffu, pubI, 1);
+        const uint32_t bc = ringB[(s - lane) & 127];
         dgM = upM;
         dgD = upD;
         dgI = upI;
         if (lane == 0) {
-          if (k == 0) {  // row 0: M(0,0)=0, M(0,j)=NEG; D(0,.)=NEG; I(0,0)=NEG, I(0,j)=0
-            upM = j == 0 ? 0 : kNeg;
+          if (k == 0) {  // row 0: M(0,j)=NEG, D(0,j)=NEG, I(0,j)=0 for j>=1
+            upM = kNeg;
             upD = kNeg;
-            upI = j == 0 ? kNeg : 0;
-          } else if (j <= LB) {
-            const int4 v = rowbuf[j];
+            upI = 0;
+            if (s == 0) {  // column 0 of row 0: M(0,0)=0, D(0,0)=I(0,0)=NEG
+              dgM = 0;
+              dgD = kNeg;
+              dgI = kNeg;
+            }
+          } else {
+            const int4 v = ringR[(s + 1) & 63];
             upM = v.x;
             upD = v.y;
             upI = v.z;
-          }
-          if (s == 0) {  // diag of column 1 = column 0 of the row above
-            dgM = k == 0 ? 0 : kNeg;
-            dgD = k == 0 ? kNeg : 0;
-            dgI = kNeg;
-            if (k == 0) {
-              upM = kNeg;
-              upD = kNeg;
-              upI = 0;
-            } else {
-              const int4 v = rowbuf[1];
-              upM = v.x;
-              upD = v.y;
-              upI = v.z;
+            if (s == 0) {  // column 0 of a row >= 1: (NEG, 0, NEG)
+              dgM = kNeg;
+              dgD = 0;
+              dgI = kNeg;
             }
           }
         } else {
@@ -181,11 +199,7 @@ __global__ void __launch_bounds__(kDpThreads, 2) k_gapdp(DpJob J) {
         }
         uint32_t nibs = 0;
         if (j >= 1 && j <= LB) {
-          uint32_t bc = B[j - 1];
-          if (bc > 3u) {
-            set_error(J.err, kDevBadBase);
-            bc = 0;
-          }
+          bad |= bc;
           const int32_t goB = j == 1 ? 0 : kGap;
           int32_t cuM = upM, cuD = upD;               // (i-1, j)
           int32_t cdM = dgM, cdD = dgD, cdI = dgI;    // (i-1, j-1)
@@ -201,26 +215,18 @@ __global__ void __launch_bounds__(kDpThreads, 2) k_gapdp(DpJob J) {
             const int32_t I = mi ? MI : lI[r];
             // M(i,j) = s + max(M, D + close, I + close) at (i-1,j-1), tie M > D > I
             const int32_t DM = cdD + kGap, IM = cdI + kGap;
-            int32_t best;
-            uint32_t tm;
-            if (cdM >= DM && cdM >= IM) {
-              best = cdM;
-              tm = TB_MM;
-            } else if (DM >= IM) {
-              best = DM;
-              tm = TB_DM;
-            } else {
-              best = IM;
-              tm = TB_IM;
-            }
-            int32_t M = score_ab(arow[r], bc) + best;
+            const int32_t DI = max(DM, IM);
+            const int32_t best = max(cdM, DI);
+            const uint32_t tm = cdM >= DI ? TB_MM : (DM >= IM ? TB_DM : TB_IM);
+            int32_t M = score_ab(arow[r], bc & 3u) + best;
+            uint32_t tmm = tm;
             if (LA == 1 && j == 1 && k == 0 && lane == 0 && r == 0) {
               // NWSmall's last-row special case (MU/nwsmall.cpp:616-624) with
               // LA == 1: open + close of position 0, close not zeroed.
-              M = score_ab(arow[0], bc) + kGap;
-              tm = TB_DM;
+              M = score_ab(arow[0], bc & 3u) + kGap;
+              tmm = TB_DM;
             }
-            nibs |= (tm | (dd ? 0u : TB_MD) | (mi ? TB_MI : 0u)) << (4 * r);
+            nibs |= (tmm | (dd ? 0u : TB_MD) | (mi ? TB_MI : 0u)) << (4 * r);
             // the row below in this lane sees this row as "up" and the old left as "diag"
             cdM = lM[r];
             cdD = lD[r];
@@ -244,7 +250,6 @@ __global__ void __launch_bounds__(kDpThreads, 2) k_gapdp(DpJob J) {
               J.scores[p] = sc;
               J.end_edge[p] = (uint8_t)e;
             }
-            (void)rvalid;
           }
           pubM = lM[kRows - 1];
           pubD = lD[kRows - 1];
@@ -264,6 +269,7 @@ __global__ void __launch_bounds__(kDpThreads, 2) k_gapdp(DpJob J) {
       }
       __syncwarp();
     }
+    if (bad > 3u) set_error(J.err, kDevBadBase);
   }
 }
 
@@ -410,22 +416,53 @@ int gapdp_batch_dev(Ctx* c, const uint8_t* d_sa, const uint64_t* d_oa, const uin
     d_path_off = d_tmp_poff;
     d_path_len = d_tmp_plen;
   }
-  // waves that fit the traceback arena
-  std::vector<uint64_t> tboff(nprob);
-  std::vector<int64_t> wave_begin;
-  uint64_t acc = 0, arena_need = 0;
-  for (int64_t w = 0; w < nprob; ++w) {
-    const uint64_t b = tb_bytes_for(la[ord[w]], lb[ord[w]]);
-    if (b > c->tb_arena) return report_error(MVG_ERR_CAPACITY, "one gap-DP problem exceeds the traceback arena");
-    if (w == 0 || acc + b > c->tb_arena) {
-      wave_begin.push_back(w);
-      acc = 0;
+  // Waves that fit the traceback arena.  Problems are dealt round-robin from
+  // the size-sorted list, so every wave holds the same mix of sizes (enough
+  // problems to fill every warp) and stays largest-first inside.
+  uint64_t arena = c->tb_arena;
+  {
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess) {
+      size_t have = c->ws.size[18] + free_b;  // the arena slot itself may be re-allocated
+      uint64_t cap = (uint64_t)(have * 0.6);
+      if (arena > cap) arena = cap;
     }
-    tboff[w] = acc;
-    acc += (b + 255) & ~255ull;
-    arena_need = std::max(arena_need, acc);
+  }
+  std::vector<uint64_t> bytes(nprob);
+  uint64_t total_tb = 0, max_tb = 0;
+  for (int64_t w = 0; w < nprob; ++w) {
+    bytes[w] = (tb_bytes_for(la[ord[w]], lb[ord[w]]) + 255) & ~255ull;
+    total_tb += bytes[w];
+    max_tb = std::max(max_tb, bytes[w]);
+  }
+  if (max_tb > arena) return report_error(MVG_ERR_CAPACITY, "one gap-DP problem exceeds the traceback arena");
+  int64_t nwaves = (int64_t)((total_tb + arena - 1) / arena);
+  std::vector<uint32_t> wave_ord;
+  std::vector<uint64_t> tboff;
+  std::vector<int64_t> wave_begin;
+  uint64_t arena_need = 0;
+  for (;;) {
+    wave_ord.clear();
+    tboff.clear();
+    wave_begin.clear();
+    arena_need = 0;
+    bool fits = true;
+    for (int64_t v = 0; v < nwaves && fits; ++v) {
+      wave_begin.push_back((int64_t)wave_ord.size());
+      uint64_t acc = 0;
+      for (int64_t w = v; w < nprob; w += nwaves) {
+        wave_ord.push_back(ord[w]);
+        tboff.push_back(acc);
+        acc += bytes[w];
+      }
+      if (acc > arena) fits = false;
+      arena_need = std::max(arena_need, acc);
+    }
+    if (fits) break;
+    ++nwaves;
   }
   wave_begin.push_back(nprob);
+  ord.swap(wave_ord);
   uint32_t* tb = (uint32_t*)ws.get(c, 18, arena_need);
   if (!tb) return report_error(MVG_ERR_NOMEM, "traceback arena allocation failed");
   MVG_CUDA_TRY(cudaMemcpyAsync(d_order, ord.data(), (size_t)nprob * 4, cudaMemcpyHostToDevice, c->stream));

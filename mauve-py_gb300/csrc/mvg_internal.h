@@ -33,7 +33,7 @@ struct Ctx {
   uint32_t* h_err = nullptr;     // pinned mirror
   uint64_t* h_scalars = nullptr; // pinned scalars for small device->host reads
   uint64_t launches = 0;
-  uint64_t tb_arena = 32ull << 30;
+  uint64_t tb_arena = ~0ull;  // capped per call at 60% of free device memory
   Workspace ws;
   MatchStats stats;
   bool profiling = false;

@@ -152,7 +152,7 @@ def test_gapdp_small_arena_waves_identical(ctx):
     try:
         s2, p2 = ctx.gap_align_batch(sa, oa, sb, ob)
     finally:
-        ctx.set_tb_arena(32 << 30)
+        ctx.set_tb_arena(1 << 62)
     np.testing.assert_array_equal(s1, s2)
     assert p1 == p2
 
