@@ -111,10 +111,71 @@ int mvg_gapdp_batch_dev(mvg_handle h, const uint8_t* d_seq_a, const uint64_t* d_
                         const uint64_t* d_off_b, int64_t nprob, int32_t* d_scores, char* d_paths,
                         const uint64_t* d_path_off, int64_t* d_path_len);
 
+/* Banded gap DP with an exactness check and full-DP fallback.  Problem p is
+ * first aligned inside the diagonal band of half-width band_half[p] around
+ * j = i*LB/LA + band_delta[p] (host arrays).  The banded result is kept only
+ * if its score is strictly above an upper bound on every path that leaves
+ * the band (best exit-cell score + 160 per remaining diagonal step); then its
+ * path equals the full NWSmall path.  Otherwise the problem is re-run through
+ * the full DP.  Output is therefore always identical to mvg_gapdp_batch.
+ * used_band[p] (host, may be NULL) gets 1 when the band was accepted;
+ * *cells (may be NULL) gets the DP cells actually computed.  No counterpart in
+ * the reference (a new method behind GlobalAlign, MU/glbalign.cpp:69). */
+int mvg_gapdp_banded(mvg_handle h, const uint8_t* seq_a, const uint64_t* off_a, const uint8_t* seq_b,
+                     const uint64_t* off_b, int64_t nprob, const int32_t* band_delta, const int32_t* band_half,
+                     int32_t* scores, char* paths, const uint64_t* path_off, int64_t* path_len,
+                     uint8_t* used_band, uint64_t* cells);
+int mvg_gapdp_banded_dev(mvg_handle h, const uint8_t* d_seq_a, const uint64_t* d_off_a, const uint8_t* d_seq_b,
+                         const uint64_t* d_off_b, int64_t nprob, const int32_t* band_delta,
+                         const int32_t* band_half, int32_t* d_scores, char* d_paths, const uint64_t* d_path_off,
+                         int64_t* d_path_len, uint8_t* used_band, uint64_t* cells);
+
+/* Full DP (as mvg_gapdp_batch_dev, scores into d_scores) that also writes each
+ * optimal path's envelope: d_env[2p], d_env[2p+1] = min and max over the
+ * path's cells (rows >= 1) of j - floor(i*LB/LA).  Training labels for the
+ * band proposal; no counterpart in the reference. */
+int mvg_gapdp_envelope_dev(mvg_handle h, const uint8_t* d_seq_a, const uint64_t* d_off_a, const uint8_t* d_seq_b,
+                           const uint64_t* d_off_b, int64_t nprob, int32_t* d_scores, int32_t* d_env);
+
+/* ------------------------------------------------ band-proposal network */
+
+/* The band proposal for mvg_gapdp_banded: a 528 -> 256 -> 256 -> 256 -> 2
+ * MLP (GELU, BF16 weights and activations, FP32 accumulation on the tensor
+ * cores, FP32 master weights and Adam state), one per handle.  Its input per
+ * gap is the 4-mer spectra of both sequences (2 x 256) and their log lengths;
+ * its outputs are the band's diagonal offset / 100 and log(1 + half-width).
+ * No counterpart in the reference.
+ * Parameters are a flat fp32 array of mvg_mlp_num_params() values:
+ * W1[256x528], b1[256], W2[256x256], b2, W3[256x256], b3, W4[2x256], b4[2]. */
+int64_t mvg_mlp_num_params(void);
+int mvg_mlp_set_params(mvg_handle h, const float* params);
+int mvg_mlp_get_params(mvg_handle h, float* params);
+/* Features of nprob gaps (device inputs) into d_x_bf16 [nprob x 528] (bf16). */
+int mvg_band_features_dev(mvg_handle h, const uint8_t* d_seq_a, const uint64_t* d_off_a, const uint8_t* d_seq_b,
+                          const uint64_t* d_off_b, int64_t nprob, void* d_x_bf16);
+/* Forward pass: d_out [n x 2] (fp32, device). */
+int mvg_mlp_forward_dev(mvg_handle h, const void* d_x_bf16, int64_t n, float* d_out);
+/* Mean-squared-error loss against d_target [n x 2] and its gradient with
+ * respect to every parameter (host, flat layout; may be NULL). */
+int mvg_mlp_grad_dev(mvg_handle h, const void* d_x_bf16, const float* d_target, int64_t n, float* grads,
+                     float* loss);
+/* One Adam step (beta 0.9/0.999, eps 1e-8) on a minibatch; step counts from 1. */
+int mvg_mlp_train_step_dev(mvg_handle h, const void* d_x_bf16, const float* d_target, int64_t n, float lr,
+                           int step, float* loss);
+/* Features + forward + mapping to integer bands: delta = round(100 * o0),
+ * half = ceil(alpha * (exp(o1) - 1) + beta); host outputs. */
+int mvg_band_propose_dev(mvg_handle h, const uint8_t* d_seq_a, const uint64_t* d_off_a, const uint8_t* d_seq_b,
+                         const uint64_t* d_off_b, int64_t nprob, float alpha, float beta, int32_t* band_delta,
+                         int32_t* band_half);
+
 /* Upper bound on the device bytes the gap-DP traceback arena may use.  Each
  * call uses min(bound, 60% of free device memory); problems run in waves of
  * mixed sizes that fit it.  Default: no bound beyond the 60% cap. */
 int mvg_set_tb_arena(mvg_handle h, uint64_t bytes);
+
+/* Gap-DP kernel shape: rows per lane (4 or 8; strips of 32*rows rows).  The
+ * default is the tuned choice committed in mauve-py_gb300/dp_tuning.json. */
+int mvg_set_dp_rows(mvg_handle h, int rows);
 
 /* Per-stage timing with CUDA events on the handle's stream (off by default;
  * no extra synchronisation).  After a call, mvg_stage_times gives the stage

@@ -1,0 +1,118 @@
+"""Learned band proposal for the gap DP.
+
+A small MLP (528 -> 256 -> 256 -> 256 -> 2, GELU; kernels in csrc/mlp.cu,
+BF16 tensor-core GEMMs with FP32 accumulation) predicts, for each gap, the
+diagonal offset and half-width of a band for mvg_gapdp_banded.  The banded
+DP keeps a result only when it provably equals the full DP, so a proposal
+that is too narrow costs a fallback, never a wrong answer.
+
+Labels come from the exact full DP run on the GPU: the optimal path's
+envelope (extreme deviations from the diagonal j = i*LB/LA) gives the
+offset, and the half-width is the larger of the envelope half-width and
+the width the exactness check needs, min(LA, LB) - score/160 (an exit
+reached from the free row-0 insertion run at column h is bounded by
+160 * (min(LA, LB) - h)).  Targets: offset / 100 and log(1 + half-width).
+"""
+import ctypes
+
+import numpy as np
+
+import mvg
+
+N_IN, N_HID, N_OUT = 528, 256, 2
+DELTA_SCALE = 100.0
+MAX_PAIR = 160
+
+
+def init_params(seed=0):
+    """He-initialised flat fp32 parameters in the library's layout."""
+    rng = np.random.default_rng(seed)
+    parts = []
+    dims = [(N_HID, N_IN), (N_HID, N_HID), (N_HID, N_HID), (N_OUT, N_HID)]
+    for k, (o, i) in enumerate(dims):
+        std = np.sqrt(2.0 / i) if k < 3 else np.sqrt(1.0 / i)
+        parts.append(rng.normal(0, std, (o, i)).astype(np.float32).ravel())
+        parts.append(np.zeros(o, np.float32))
+    p = np.concatenate(parts)
+    assert p.size == int(mvg.load_library().mvg_mlp_num_params())
+    return p
+
+
+def labels_from_full_dp(la, lb, scores, env, margin=8):
+    """(offset target, log(1 + half) target, offset, half) from full-DP results."""
+    la = la.astype(np.int64)
+    lb = lb.astype(np.int64)
+    lo, hi = env[:, 0].astype(np.int64), env[:, 1].astype(np.int64)
+    delta = (lo + hi) // 2
+    half_env = (hi - lo + 1) // 2 + margin
+    need = np.minimum(la, lb) - scores.astype(np.int64) // MAX_PAIR + margin
+    half = np.maximum(half_env, need)
+    half = np.clip(half, 0, np.maximum(la, lb))
+    t = np.stack([delta / DELTA_SCALE, np.log1p(half)], axis=1).astype(np.float32)
+    return t, delta.astype(np.int32), half.astype(np.int32)
+
+
+class BandNet:
+    """The band-proposal network bound to one library context."""
+
+    def __init__(self, ctx, params=None, seed=0):
+        self.ctx = ctx
+        self.step = 0
+        self.set_params(init_params(seed) if params is None else params)
+
+    def set_params(self, params):
+        params = np.ascontiguousarray(params, np.float32)
+        mvg._check(mvg.load_library().mvg_mlp_set_params(self.ctx.handle, mvg._ptr(params)))
+        self.step = 0
+
+    def get_params(self):
+        p = np.zeros(int(mvg.load_library().mvg_mlp_num_params()), np.float32)
+        mvg._check(mvg.load_library().mvg_mlp_get_params(self.ctx.handle, mvg._ptr(p)))
+        return p
+
+    # device-pointer calls (inputs resident on the GPU)
+    def features_dev(self, d_sa, d_oa, d_sb, d_ob, n, d_x):
+        mvg._check(mvg.load_library().mvg_band_features_dev(self.ctx.handle, d_sa, d_oa, d_sb, d_ob, n, d_x))
+
+    def forward_dev(self, d_x, n, d_out):
+        mvg._check(mvg.load_library().mvg_mlp_forward_dev(self.ctx.handle, d_x, n, d_out))
+
+    def grad_dev(self, d_x, d_t, n):
+        g = np.zeros(int(mvg.load_library().mvg_mlp_num_params()), np.float32)
+        loss = ctypes.c_float(0)
+        mvg._check(mvg.load_library().mvg_mlp_grad_dev(self.ctx.handle, d_x, d_t, n, mvg._ptr(g), ctypes.byref(loss)))
+        return g, float(loss.value)
+
+    def train_step_dev(self, d_x, d_t, n, lr):
+        self.step += 1
+        loss = ctypes.c_float(0)
+        mvg._check(mvg.load_library().mvg_mlp_train_step_dev(self.ctx.handle, d_x, d_t, n, ctypes.c_float(lr),
+                                                             self.step, ctypes.byref(loss)))
+        return float(loss.value)
+
+    def propose_dev(self, d_sa, d_oa, d_sb, d_ob, n, alpha=1.0, beta=8.0):
+        delta = np.zeros(max(n, 1), np.int32)
+        half = np.zeros(max(n, 1), np.int32)
+        mvg._check(mvg.load_library().mvg_band_propose_dev(self.ctx.handle, d_sa, d_oa, d_sb, d_ob, n,
+                                                           ctypes.c_float(alpha), ctypes.c_float(beta),
+                                                           mvg._ptr(delta), mvg._ptr(half)))
+        return delta[:n], half[:n]
+
+
+def full_dp_labels_dev(ctx, d_sa, d_oa, d_sb, d_ob, n, margin=8, torch_device=None):
+    """Runs the exact full DP on device inputs and returns (targets, delta, half, scores) on the host."""
+    import torch
+    d_sc = torch.zeros(n, dtype=torch.int32, device=torch_device)
+    d_env = torch.zeros(2 * n, dtype=torch.int32, device=torch_device)
+    mvg._check(mvg.load_library().mvg_gapdp_envelope_dev(ctx.handle, d_sa, d_oa, d_sb, d_ob, n, d_sc.data_ptr(),
+                                                         d_env.data_ptr()))
+    return d_sc.cpu().numpy(), d_env.cpu().numpy().reshape(-1, 2)
+
+
+def heuristic_band(la, lb, frac=0.1, extra=32):
+    """The band without the network: centred on the diagonal, half-width
+    |LA - LB| + frac * min(LA, LB) + extra."""
+    la = np.asarray(la, np.int64)
+    lb = np.asarray(lb, np.int64)
+    half = np.abs(la - lb) + (frac * np.minimum(la, lb)).astype(np.int64) + extra
+    return np.zeros(len(la), np.int32), half.astype(np.int32)

@@ -144,6 +144,7 @@ int mvg_destroy(mvg_handle h) {
   if (!h) return 0;
   cudaSetDevice(h->device);
   if (h->stream) cudaStreamSynchronize(h->stream);
+  mlp_release(h);
   h->ws.release();
   if (h->d_err) cudaFree(h->d_err);
   if (h->h_err) cudaFreeHost(h->h_err);
@@ -305,9 +306,84 @@ int mvg_gapdp_batch(mvg_handle h, const uint8_t* seq_a, const uint64_t* off_a, c
   return 0;
 }
 
+int mvg_gapdp_envelope_dev(mvg_handle h, const uint8_t* d_seq_a, const uint64_t* d_off_a, const uint8_t* d_seq_b,
+                           const uint64_t* d_off_b, int64_t nprob, int32_t* d_scores, int32_t* d_env) {
+  if (!h || nprob < 0 || (nprob && (!d_off_a || !d_off_b || !d_scores || !d_env)))
+    return report_error(MVG_ERR_ARG, "null argument");
+  if (nprob == 0) return 0;
+  MVG_CUDA_TRY(cudaSetDevice(h->device));
+  std::vector<uint64_t> oa(nprob + 1), ob(nprob + 1);
+  MVG_CUDA_TRY(cudaMemcpyAsync(oa.data(), d_off_a, (nprob + 1) * 8, cudaMemcpyDeviceToHost, h->stream));
+  MVG_CUDA_TRY(cudaMemcpyAsync(ob.data(), d_off_b, (nprob + 1) * 8, cudaMemcpyDeviceToHost, h->stream));
+  MVG_CUDA_TRY(cudaStreamSynchronize(h->stream));
+  return gapdp_batch_dev(h, d_seq_a, d_off_a, d_seq_b, d_off_b, nprob, d_scores, nullptr, nullptr, nullptr, oa.data(),
+                         ob.data(), d_env);
+}
+
+int mvg_gapdp_banded_dev(mvg_handle h, const uint8_t* d_seq_a, const uint64_t* d_off_a, const uint8_t* d_seq_b,
+                         const uint64_t* d_off_b, int64_t nprob, const int32_t* band_delta, const int32_t* band_half,
+                         int32_t* d_scores, char* d_paths, const uint64_t* d_path_off, int64_t* d_path_len,
+                         uint8_t* used_band, uint64_t* cells) {
+  if (!h || nprob < 0 || (nprob && (!d_off_a || !d_off_b || !d_scores || !band_delta || !band_half)) ||
+      (d_paths && (!d_path_off || !d_path_len)))
+    return report_error(MVG_ERR_ARG, "null argument");
+  if (nprob == 0) return 0;
+  MVG_CUDA_TRY(cudaSetDevice(h->device));
+  std::vector<uint64_t> oa(nprob + 1), ob(nprob + 1);
+  MVG_CUDA_TRY(cudaMemcpyAsync(oa.data(), d_off_a, (nprob + 1) * 8, cudaMemcpyDeviceToHost, h->stream));
+  MVG_CUDA_TRY(cudaMemcpyAsync(ob.data(), d_off_b, (nprob + 1) * 8, cudaMemcpyDeviceToHost, h->stream));
+  MVG_CUDA_TRY(cudaStreamSynchronize(h->stream));
+  return gapdp_banded_dev(h, d_seq_a, d_off_a, d_seq_b, d_off_b, nprob, band_delta, band_half, d_scores, d_paths,
+                          d_path_off, d_path_len, used_band, oa.data(), ob.data(), cells);
+}
+
+int mvg_gapdp_banded(mvg_handle h, const uint8_t* seq_a, const uint64_t* off_a, const uint8_t* seq_b,
+                     const uint64_t* off_b, int64_t nprob, const int32_t* band_delta, const int32_t* band_half,
+                     int32_t* scores, char* paths, const uint64_t* path_off, int64_t* path_len, uint8_t* used_band,
+                     uint64_t* cells) {
+  if (!h || nprob < 0 || (nprob && (!off_a || !off_b || !scores || !seq_a || !seq_b || !band_delta || !band_half)) ||
+      (paths && (!path_off || !path_len)))
+    return report_error(MVG_ERR_ARG, "null argument");
+  if (nprob == 0) return 0;
+  MVG_CUDA_TRY(cudaSetDevice(h->device));
+  const uint64_t na = off_a[nprob], nb = off_b[nprob];
+  const uint64_t np = paths ? path_off[nprob] : 0;
+  uint8_t* dsa = (uint8_t*)h->ws.get(h, 46, na + 16);
+  uint8_t* dsb = (uint8_t*)h->ws.get(h, 47, nb + 16);
+  uint64_t* doa = (uint64_t*)h->ws.get(h, 5, (nprob + 1) * 8);
+  uint64_t* dob = (uint64_t*)h->ws.get(h, 6, (nprob + 1) * 8);
+  int32_t* dsc = (int32_t*)h->ws.get(h, 7, nprob * 4);
+  char* dpa = paths ? (char*)h->ws.get(h, 9, np + 16) : nullptr;
+  uint64_t* dpo = paths ? (uint64_t*)h->ws.get(h, 8, (nprob + 1) * 8) : nullptr;
+  int64_t* dpl = paths ? (int64_t*)h->ws.get(h, 22, nprob * 8) : nullptr;
+  if (!dsa || !dsb || !doa || !dob || !dsc || (paths && (!dpa || !dpo || !dpl)))
+    return report_error(MVG_ERR_NOMEM, "workspace allocation failed");
+  MVG_CUDA_TRY(cudaMemcpyAsync(dsa, seq_a, na, cudaMemcpyHostToDevice, h->stream));
+  MVG_CUDA_TRY(cudaMemcpyAsync(dsb, seq_b, nb, cudaMemcpyHostToDevice, h->stream));
+  MVG_CUDA_TRY(cudaMemcpyAsync(doa, off_a, (nprob + 1) * 8, cudaMemcpyHostToDevice, h->stream));
+  MVG_CUDA_TRY(cudaMemcpyAsync(dob, off_b, (nprob + 1) * 8, cudaMemcpyHostToDevice, h->stream));
+  if (paths) MVG_CUDA_TRY(cudaMemcpyAsync(dpo, path_off, (nprob + 1) * 8, cudaMemcpyHostToDevice, h->stream));
+  int rc = gapdp_banded_dev(h, dsa, doa, dsb, dob, nprob, band_delta, band_half, dsc, dpa, dpo, dpl, used_band, off_a,
+                            off_b, cells);
+  if (rc) return rc;
+  MVG_CUDA_TRY(cudaMemcpyAsync(scores, dsc, nprob * 4, cudaMemcpyDeviceToHost, h->stream));
+  if (paths) {
+    MVG_CUDA_TRY(cudaMemcpyAsync(paths, dpa, np, cudaMemcpyDeviceToHost, h->stream));
+    MVG_CUDA_TRY(cudaMemcpyAsync(path_len, dpl, nprob * 8, cudaMemcpyDeviceToHost, h->stream));
+  }
+  MVG_CUDA_TRY(cudaStreamSynchronize(h->stream));
+  return 0;
+}
+
 int mvg_set_tb_arena(mvg_handle h, uint64_t bytes) {
   if (!h || bytes < (1ull << 20)) return report_error(MVG_ERR_ARG, "arena must be at least 1 MiB");
   h->tb_arena = bytes;
+  return 0;
+}
+
+int mvg_set_dp_rows(mvg_handle h, int rows) {
+  if (!h || (rows != 4 && rows != 8)) return report_error(MVG_ERR_ARG, "rows per lane must be 4 or 8");
+  h->dp_rows = rows;
   return 0;
 }
 

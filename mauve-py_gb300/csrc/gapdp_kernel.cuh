@@ -1,0 +1,324 @@
+// The NWSmall wavefront kernel, full or banded (included by gapdp.cu).
+//
+// One warp per problem; persistent warps pull problems from a counter.  The
+// DP matrix is cut into strips of 32*R rows; lane t owns rows [t*R, t*R+R)
+// of the strip and sweeps the strip's columns on an anti-diagonal wavefront
+// (lane t runs t columns behind lane 0).  Each step a lane computes an R x 1
+// column segment: the cells above it arrive from lane t-1 by __shfl_up_sync,
+// the row above the strip comes from a per-warp row buffer written by lane 31
+// of the previous strip.  B codes and row-buffer entries are staged in
+// per-warp shared rings one 32-step chunk ahead.  Traceback nibbles
+// (MU/types.h:30-43: 2 bits M source, 1 bit D<-M, 1 bit I<-M) are packed 8 per
+// word, lane-minor, so each flush is one coalesced 128-byte warp store.
+//
+// Per cell the recurrences use Hopper/Blackwell DPX max-with-predicate
+// (__vibmax_s32), which yields each maximum and its tie-broken traceback bit
+// in one instruction.  The steady part of a strip (every lane inside the
+// strip's columns) runs without per-step bounds checks; only the 31-step
+// ramp-up and ramp-down of the wavefront take the checked path.
+//
+// Banded mode: strip k only spans columns [jlo_k, jhi_k] of a diagonal band
+// (band.h), everything outside is -infinity, and the kernel also computes an
+// upper bound on every path that leaves the band: the best exit-cell score
+// plus 160 (the largest NUC_SP + 60 entry) per remaining diagonal step.  A
+// banded result is accepted only when its score is strictly above that bound;
+// then the reference's optimal path provably stays in the band and every
+// traceback decision along it is the same as in the full DP.
+#pragma once
+#include "band.h"
+#include "mvg_common.cuh"
+
+namespace mvg {
+
+constexpr int32_t kNeg = -(1 << 29);
+constexpr int32_t kGap = -200;           // half of gap open -400
+constexpr int32_t kMaxPair = 160;        // max NUC_SP + 60 (C/C, G/G)
+constexpr int kDpThreads = 256;
+
+enum : uint32_t { TB_MM = 0, TB_DM = 1, TB_IM = 2, TB_MD = 4, TB_MI = 8 };
+
+// NUC_SP + 60 (range -65..160), packed: entry (a,b) = byte b of
+// c_score_rows[a], stored with a +80 bias so every byte is in 15..240.
+constexpr int kScoreBias = 80;
+__constant__ uint32_t c_score_rows[4];  // this header has one includer (gapdp.cu)
+
+struct DpJob {
+  const uint8_t* sa;
+  const uint64_t* oa;
+  const uint8_t* sb;
+  const uint64_t* ob;
+  const uint32_t* order;   // problem ids of this wave, largest first
+  const uint64_t* tb_off;  // byte offset of each wave slot's traceback bits
+  int nwork;
+  uint32_t* tb;
+  int4* rowbuf;
+  int64_t rowbuf_stride;  // int4 entries per warp
+  int32_t* scores;
+  uint8_t* end_edge;  // 'M','D','I' per problem
+  const int32_t* band_delta;  // banded mode: per problem
+  const int32_t* band_half;
+  uint8_t* accept;            // banded mode: 1 if the band result is exact
+  unsigned* counter;
+};
+
+__host__ __device__ __forceinline__ int tb_words_per_lane(int W, int R) { return band_words_per_lane(W, R); }
+
+template <int R>
+struct DpLane {
+  uint32_t arow[R];      // packed score row of A[i-1] per owned row
+  int32_t lM[R], lD[R], lI[R];  // left neighbour (previous column) per row
+};
+
+// One wavefront step of one lane: rows r = 0..R-1 of column j.  Returns the
+// R traceback nibbles.  (up*) = cells (i0-1, j), (dg*) = cells (i0-1, j-1).
+template <int R>
+__device__ __forceinline__ uint32_t dp_column(DpLane<R>& L, int32_t upM, int32_t upD, int32_t dgM, int32_t dgD,
+                                              int32_t dgI, uint32_t bsel, int32_t goB, int32_t goA0) {
+  int32_t cuM = upM, cuD = upD;            // (i-1, j)
+  int32_t cdM = dgM, cdD = dgD, cdI = dgI;  // (i-1, j-1)
+  uint32_t nibs = 0;
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const int32_t goA = r == 0 ? goA0 : kGap;  // only row 1 of the matrix opens for free
+    // D(i,j) = max(M(i-1,j) + open, D(i-1,j)), ties to the M branch
+    bool dm;
+    const int32_t D = __vibmax_s32(cuM + goA, cuD, &dm);
+    // I(i,j) = max(M(i,j-1) + open, I(i,j-1)), ties to the M branch
+    bool mi;
+    const int32_t I = __vibmax_s32(L.lM[r] + goB, L.lI[r], &mi);
+    // M(i,j) = s + max(M, D + close, I + close) at (i-1,j-1), tie M > D > I;
+    // both closes are -200, so max(D, I) is taken before adding the close.
+    bool dge, mge;
+    const int32_t DI = __vibmax_s32(cdD, cdI, &dge) + kGap;
+    const int32_t best = __vibmax_s32(cdM, DI, &mge);
+    const int32_t M = best + (int32_t)__byte_perm(L.arow[r], 0u, bsel) - kScoreBias;
+    const uint32_t tm = mge ? TB_MM : (dge ? TB_DM : TB_IM);
+    nibs |= (tm | (dm ? TB_MD : 0u) | (mi ? TB_MI : 0u)) << (4 * r);
+    cdM = L.lM[r];
+    cdD = L.lD[r];
+    cdI = L.lI[r];
+    cuM = M;
+    cuD = D;
+    L.lM[r] = M;
+    L.lD[r] = D;
+    L.lI[r] = I;
+  }
+  return nibs;
+}
+
+template <bool BANDED, int R>
+__global__ void __launch_bounds__(kDpThreads, 2) k_gapdp_t(DpJob J) {
+  constexpr int SR = 32 * R;  // rows per strip
+  __shared__ uint8_t sB[kDpThreads / 32][128];
+  __shared__ int4 sR[kDpThreads / 32][64];
+  const int lane = threadIdx.x & 31;
+  const int wib = threadIdx.x >> 5;
+  const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int4* rowbuf = J.rowbuf + gw * J.rowbuf_stride;
+  uint8_t* ringB = sB[wib];
+  int4* ringR = sR[wib];
+  const int4 kNegCell = make_int4(kNeg, kNeg, kNeg, 0);
+  for (;;) {
+    int w = 0;
+    if (lane == 0) w = (int)atomicAdd(J.counter, 1u);
+    w = __shfl_sync(0xffffffffu, w, 0);
+    if (w >= J.nwork) break;
+    const uint32_t p = J.order[w];
+    const uint64_t a0 = J.oa[p], b0 = J.ob[p];
+    const int LA = (int)(J.oa[p + 1] - a0), LB = (int)(J.ob[p + 1] - b0);
+    const uint8_t* A = J.sa + a0;
+    const uint8_t* B = J.sb + b0;
+    uint32_t* tbs = J.tb + J.tb_off[w] / 4;
+    const int nstrips = (LA + SR - 1) / SR;
+    const int end_strip = (LA - 1) / SR;
+    const int end_lane = ((LA - 1) % SR) / R;
+    const int end_r = (LA - 1) % R;
+    const Band band = BANDED ? make_band(LA, LB, J.band_delta[p], J.band_half[p], SR) : make_full(LA, LB, SR);
+    int32_t bound = kNeg;  // best score of any path leaving the band
+    int prev_lo = 1, prev_hi = LB;  // column range of the strip above
+
+    for (int k = 0; k < nstrips; ++k) {
+      const int row0 = k * SR;
+      int jlo = 1, jhi = LB, next_lo = 1;
+      if (BANDED) {
+        jlo = band_lo(band, k);
+        jhi = band_hi(band, k);
+        next_lo = k + 1 < nstrips ? band_lo(band, k + 1) : 1;
+      }
+      const int W = jhi - jlo + 1;
+      const int S = W + 31;
+      const int wpl = tb_words_per_lane(W, R);
+      DpLane<R> L;
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const int i = row0 + lane * R + r + 1;
+        L.arow[r] = c_score_rows[(i <= LA ? A[i - 1] : 0u) & 3u];
+      }
+      const int32_t goA0 = (row0 + lane * R + 1 == 1) ? 0 : kGap;
+      // Row above this strip at absolute column x: row 0 for the first strip,
+      // else the previous strip's computed columns, its left boundary or -inf.
+      auto above = [&](int x) -> int4 {
+        if (k == 0) return x == 0 ? make_int4(0, kNeg, kNeg, 0) : make_int4(kNeg, kNeg, 0, 0);
+        if (x >= prev_lo && x <= prev_hi) return rowbuf[x];
+        if (x == prev_lo - 1) return prev_lo == 1 ? make_int4(kNeg, 0, kNeg, 0) : kNegCell;
+        return kNegCell;
+      };
+      // prime the rings: B[jlo-1 .. jlo+62], row above at columns jlo .. jlo+63
+      __syncwarp();
+      ringB[lane] = jlo - 1 + lane < LB ? B[jlo - 1 + lane] : 0;
+      ringB[32 + lane] = jlo + 31 + lane < LB ? B[jlo + 31 + lane] : 0;
+      ringR[lane] = above(jlo + lane);
+      ringR[32 + lane] = above(jlo + 32 + lane);
+      const int4 dg0 = above(jlo - 1);
+      __syncwarp();
+      // left state (column jlo-1) per row: column 0 = (NEG, 0, NEG), else -inf
+      const int32_t leftD = jlo == 1 ? 0 : kNeg;
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        L.lM[r] = kNeg;
+        L.lD[r] = leftD;
+        L.lI[r] = kNeg;
+      }
+      int32_t pubM = kNeg, pubD = leftD, pubI = kNeg;  // bottom row, last computed column
+      int32_t upM = kNeg, upD = kNeg, upI = kNeg;      // row above, current column
+      uint32_t acc = 0;
+      const bool bottom_exit = BANDED && lane == 31 && row0 + SR < LA;
+      const int32_t rem_rows = LA - (row0 + SR);
+
+      // one step; CHECKED handles the wavefront's ramp-up and ramp-down
+      auto step = [&](int s, bool checked) {
+        if ((s & 31) == 0 && s > 0) {
+          // refill one chunk ahead: B at offsets s+32 .. s+63, row above at s+32 .. s+63
+          __syncwarp();
+          const int xb = jlo - 1 + s + 32 + lane;
+          ringB[(s + 32 + lane) & 127] = xb < LB ? B[xb] : 0;
+          ringR[(s + 32 + lane) & 63] = above(jlo + s + 32 + lane);
+          __syncwarp();
+        }
+        const int jj = s - lane;  // column offset inside the strip
+        const int j = jlo + jj;   // absolute column
+        const int32_t rM = __shfl_up_sync(0xffffffffu, pubM, 1);
+        const int32_t rD = __shfl_up_sync(0xffffffffu, pubD, 1);
+        const int32_t rI = __shfl_up_sync(0xffffffffu, pubI, 1);
+        const int4 v = ringR[s & 63];
+        int32_t dgM = upM, dgD = upD, dgI = upI;
+        if (s == 0 && lane == 0) {
+          dgM = dg0.x;
+          dgD = dg0.y;
+          dgI = dg0.z;
+        }
+        upM = lane == 0 ? v.x : rM;
+        upD = lane == 0 ? v.y : rD;
+        upI = lane == 0 ? v.z : rI;
+        const uint32_t bsel = (uint32_t)ringB[jj & 127] | 0x4440u;
+        const int32_t goB = j == 1 ? 0 : kGap;
+        uint32_t nibs = 0;
+        if (!checked || (jj >= 0 && jj < W)) {
+          nibs = dp_column<R>(L, upM, upD, dgM, dgD, dgI, bsel, goB, goA0);
+          if (checked && s == 0 && lane == 0 && k == 0 && LA == 1) {
+            // NWSmall's last-row special case (MU/nwsmall.cpp:616-624) with
+            // LA == 1: M(1,1) adds the open and close of position 0, and the
+            // close of a one-position profile is not zeroed.
+            L.lM[0] = (int32_t)__byte_perm(L.arow[0], 0u, bsel) - kScoreBias + kGap;
+            nibs = (nibs & ~3u) | TB_DM;
+          }
+          pubM = L.lM[R - 1];
+          pubD = L.lD[R - 1];
+          pubI = L.lI[R - 1];
+          if (lane == 31 && k + 1 < nstrips) rowbuf[j] = make_int4(pubM, pubD, pubI, 0);
+          if (BANDED && bottom_exit && j < next_lo) {
+            const int32_t best = max(pubM, max(pubD, pubI));
+            bound = max(bound, best + kMaxPair * min(rem_rows, LB - j));
+          }
+        } else if (jj == -1) {
+          pubM = kNeg;
+          pubD = leftD;
+          pubI = kNeg;
+        }
+        if (R == 8) {
+          tbs[s * 32 + lane] = nibs;
+        } else {  // R == 4: one word every 2 steps
+          acc |= nibs << (16 * (s & 1));
+          if ((s & 1) || s == S - 1) {
+            tbs[(s >> 1) * 32 + lane] = acc;
+            acc = 0;
+          }
+        }
+      };
+
+      if (W >= 32) {
+        int s = 0;
+        for (; s < 31; ++s) step(s, true);
+        for (; s < W; ++s) step(s, false);
+        for (; s < S; ++s) step(s, true);
+      } else {
+        for (int s = 0; s < S; ++s) step(s, true);
+      }
+      __syncwarp();
+      // after the sweep each lane holds its rows' cells at column jhi
+      if (k == end_strip && lane == end_lane) {
+        int32_t eM = kNeg, eD = kNeg, eI = kNeg;
+#pragma unroll
+        for (int r = 0; r < R; ++r)
+          if (r == end_r) {
+            eM = L.lM[r];
+            eD = L.lD[r];
+            eI = L.lI[r];
+          }
+        int32_t sc = eM;
+        char e = 'M';
+        if (eD > sc) {
+          sc = eD;
+          e = 'D';
+        }
+        if (eI > sc) {
+          sc = eI;
+          e = 'I';
+        }
+        J.scores[p] = sc;
+        J.end_edge[p] = (uint8_t)e;
+      }
+      if (BANDED && jhi < LB) {  // right-edge exits: an I step leaves the band
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+          const int i = row0 + lane * R + r + 1;
+          if (i <= LA) {
+            const int32_t best = max(L.lM[r], max(L.lD[r], L.lI[r]));
+            bound = max(bound, best + kMaxPair * min(LA - i, LB - jhi));
+          }
+        }
+      }
+      tbs += (int64_t)wpl * 32;
+      prev_lo = jlo;
+      prev_hi = jhi;
+    }
+    if (BANDED) {
+      // paths along row 0 past the band, or down column 0 past it
+      if (lane == 0) {
+        const int hi0 = band_hi(band, 0);
+        if (hi0 < LB) bound = max(bound, kMaxPair * min(LA, LB - hi0));
+        const int last_col0 = band_last_row_at_col1(band, LA);
+        if (last_col0 < LA) bound = max(bound, kMaxPair * min(LA - last_col0, LB));
+      }
+#pragma unroll
+      for (int d = 16; d > 0; d >>= 1) bound = max(bound, __shfl_xor_sync(0xffffffffu, bound, d));
+      __syncwarp();
+      if (lane == 0) J.accept[p] = J.scores[p] > bound ? 1 : 0;
+    }
+  }
+}
+
+// Flags any byte above 3 in a concatenated code buffer.
+__global__ void k_check_codes(const uint8_t* __restrict__ s, uint64_t n, uint32_t* err) {
+  uint32_t bad = 0;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  const uint64_t n16 = (((uintptr_t)s & 15) == 0) ? n / 16 : 0;
+  for (uint64_t q = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; q < n16; q += stride) {
+    const uint4 v = reinterpret_cast<const uint4*>(s)[q];
+    bad |= (v.x | v.y | v.z | v.w) & 0xfcfcfcfcu;
+  }
+  for (uint64_t i = n16 * 16 + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) bad |= s[i] & 0xfcu;
+  if (bad) set_error(err, kDevBadBase);
+}
+
+}  // namespace mvg

@@ -321,6 +321,178 @@ __global__ void __launch_bounds__(256) k_bucket_warps(MatchCtx c, const Mhe* __r
   }
 }
 
+// Buckets with at least kBigBucket seeds get a whole CTA: 256 seeds are tested
+// per round against the bucket's entries held in shared memory (spilled to
+// the bucket's global region if they outgrow kCtaCap).  The first seed of the
+// round that is not contained is extended by its warp and inserted; later
+// seeds of the round are re-tested, exactly as in the sequential replay.
+// CTAs past the big buckets run the warp-per-bucket replay, 8 buckets each.
+constexpr uint32_t kBigBucket = 512;
+constexpr int kCtaCap = 768;
+
+__global__ void __launch_bounds__(256) k_bucket_replay(MatchCtx c, const Mhe* __restrict__ mhe,
+                                                       const uint32_t* __restrict__ sorted_pair,
+                                                       const uint32_t* __restrict__ bstart,
+                                                       const uint32_t* __restrict__ bcount,
+                                                       const uint32_t* __restrict__ border, Mhe* ent,
+                                                       uint32_t* __restrict__ nent_out,
+                                                       unsigned long long* __restrict__ coll) {
+  __shared__ Mhe sE[kCtaCap];
+  __shared__ unsigned wmask[8];
+  __shared__ Mhe s_x;
+  __shared__ long long s_at;
+  __shared__ int s_nbig;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const int L = c.s.L;
+  if (tid == 0) {  // buckets are sorted by descending seed count: count the big ones
+    int lo = 0, len = kTableSize;
+    while (len > 0) {
+      int half = len >> 1;
+      if (bcount[border[lo + half]] >= kBigBucket) {
+        lo += half + 1;
+        len -= half + 1;
+      } else {
+        len = half;
+      }
+    }
+    s_nbig = lo;
+  }
+  __syncthreads();
+  const int nbig = s_nbig;
+  if ((int)blockIdx.x >= nbig) {
+    // ------------------------------------------------ warp per bucket
+    const int idx = nbig + ((int)blockIdx.x - nbig) * 8 + wid;
+    if (idx >= kTableSize) return;
+    const uint32_t b = border[idx];
+    const uint32_t cnt = bcount[b];
+    if (cnt == 0) return;
+    Mhe* E = ent + bstart[b];
+    const uint32_t* sp = sorted_pair + bstart[b];
+    int64_t n = 0;
+    unsigned long long ncoll = 0;
+    for (uint32_t base = 0; base < cnt; base += 32) {
+      const uint32_t i = base + lane;
+      Mhe m = {0, 0, 0, 0};
+      if (i < cnt) m = mhe[sp[i]];
+      unsigned pending = __ballot_sync(0xffffffffu, i < cnt);
+      while (pending) {
+        bool coll_here = true;
+        if (pending & (1u << lane)) {
+          int64_t at = lower_bound_mhe(E, n, m, L);
+          coll_here = at != n && !mhe_less(E[at], m, L) && !mhe_less(m, E[at], L);
+        }
+        const unsigned fresh = __ballot_sync(0xffffffffu, (pending & (1u << lane)) && !coll_here);
+        if (!fresh) break;
+        const int f = __ffs(fresh) - 1;
+        ncoll += __popc(pending & ((1u << f) - 1u));
+        pending &= ~((2u << f) - 1u);
+        Mhe x;
+        x.s0 = __shfl_sync(0xffffffffu, m.s0, f);
+        x.s1 = __shfl_sync(0xffffffffu, m.s1, f);
+        x.len = __shfl_sync(0xffffffffu, m.len, f);
+        x.off = __shfl_sync(0xffffffffu, m.off, f);
+        warp_extend(c, x);
+        const int64_t at = lower_bound_mhe(E, n, x, L);
+        for (int64_t hi = n - 1; hi >= at; hi -= 32) {
+          const int64_t k = hi - lane;
+          Mhe t;
+          if (k >= at) t = E[k];
+          __syncwarp();
+          if (k >= at) E[k + 1] = t;
+          __syncwarp();
+        }
+        if (lane == 0) E[at] = x;
+        __syncwarp();
+        ++n;
+      }
+      ncoll += __popc(pending);
+    }
+    if (lane == 0) {
+      nent_out[b] = (uint32_t)n;
+      atomicAdd(coll, ncoll);
+    }
+    return;
+  }
+  // ------------------------------------------------------- CTA per bucket
+  const uint32_t b = border[blockIdx.x];
+  const uint32_t cnt = bcount[b];
+  Mhe* G = ent + bstart[b];
+  const uint32_t* sp = sorted_pair + bstart[b];
+  Mhe* E = sE;
+  bool spilled = false;
+  int64_t n = 0;
+  unsigned long long ncoll = 0;
+  for (uint32_t base = 0; base < cnt; base += 256) {
+    const uint32_t i = base + tid;
+    Mhe m = {0, 0, 0, 0};
+    bool pending = i < cnt;
+    if (pending) m = mhe[sp[i]];
+    for (;;) {
+      bool fresh = false;
+      if (pending) {
+        const int64_t at = lower_bound_mhe(E, n, m, L);
+        fresh = !(at != n && !mhe_less(E[at], m, L) && !mhe_less(m, E[at], L));
+      }
+      const unsigned wm = __ballot_sync(0xffffffffu, fresh);
+      if (lane == 0) wmask[wid] = wm;
+      __syncthreads();
+      int f = -1;
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const unsigned v = wmask[q];
+        if (f < 0 && v) f = q * 32 + __ffs(v) - 1;
+      }
+      if (f < 0) {
+        if (pending) ++ncoll;
+        pending = false;
+        __syncthreads();  // every thread has read wmask before the next round rewrites it
+        break;
+      }
+      if (pending && tid < f) {
+        ++ncoll;
+        pending = false;
+      }
+      if (tid == f) {
+        s_x = m;
+        pending = false;
+      }
+      __syncthreads();
+      if (wid == (f >> 5)) {
+        Mhe x = s_x;
+        warp_extend(c, x);
+        const int64_t at = lower_bound_mhe(E, n, x, L);
+        if (lane == 0) {
+          s_x = x;
+          s_at = at;
+        }
+      }
+      __syncthreads();
+      if (!spilled && n == kCtaCap) {  // move the entries to the bucket's global region
+        for (int k = tid; k < n; k += 256) G[k] = sE[k];
+        __syncthreads();
+        E = G;
+        spilled = true;
+      }
+      const int64_t at = s_at;
+      for (int64_t hi = n - 1; hi >= at; hi -= 256) {
+        const int64_t k = hi - tid;
+        Mhe t;
+        if (k >= at) t = E[k];
+        __syncthreads();
+        if (k >= at) E[k + 1] = t;
+        __syncthreads();
+      }
+      if (tid == 0) E[at] = s_x;
+      ++n;
+      __syncthreads();
+    }
+  }
+  if (!spilled)
+    for (int k = tid; k < n; k += 256) G[k] = sE[k];
+  if (tid == 0) nent_out[b] = (uint32_t)n;
+  if (ncoll) atomicAdd(coll, ncoll);
+}
+
 __global__ void k_bucket_hist(const uint32_t* __restrict__ bucket, const uint32_t* __restrict__ npairs_p,
                               uint32_t* __restrict__ cnt) {
   const int64_t np = *npairs_p;
@@ -477,8 +649,7 @@ int pairwise_matches_dev(Ctx* c, const uint8_t* d_a, uint64_t na, const uint8_t*
   mc.n[1] = (int64_t)nb;
   mc.s = s;
   stage_mark(c, "bucket_replay");
-  k_bucket_warps<<<kTableSize / 8, 256, 0, c->stream>>>(mc, mhe, sorted_pair, bstart, bcount, border, kTableSize, ent,
-                                                         nent, d_coll);
+  k_bucket_replay<<<kTableSize, 256, 0, c->stream>>>(mc, mhe, sorted_pair, bstart, bcount, border, ent, nent, d_coll);
   c->launches++;
   stage_mark(c, "emit");
   exclusive_scan(nent, ooff, kTableSize, bscr, tot + 1, c->stream, &c->launches);

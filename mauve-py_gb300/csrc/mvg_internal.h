@@ -34,6 +34,7 @@ struct Ctx {
   uint64_t* h_scalars = nullptr; // pinned scalars for small device->host reads
   uint64_t launches = 0;
   uint64_t tb_arena = ~0ull;  // capped per call at 60% of free device memory
+  int dp_rows = 8;            // gap-DP rows per lane (4 or 8), see dp_tuning.h
   Workspace ws;
   MatchStats stats;
   bool profiling = false;
@@ -76,7 +77,12 @@ int pairwise_matches_dev(Ctx* c, const uint8_t* d_a, uint64_t na, const uint8_t*
                          int64_t* d_out, uint64_t cap, uint64_t* count);
 int gapdp_batch_dev(Ctx* c, const uint8_t* d_sa, const uint64_t* d_oa, const uint8_t* d_sb, const uint64_t* d_ob,
                     int64_t nprob, int32_t* d_scores, char* d_paths, const uint64_t* d_path_off, int64_t* d_path_len,
-                    const uint64_t* h_oa, const uint64_t* h_ob);
+                    const uint64_t* h_oa, const uint64_t* h_ob, int32_t* d_env = nullptr);
+int gapdp_banded_dev(Ctx* c, const uint8_t* d_sa, const uint64_t* d_oa, const uint8_t* d_sb, const uint64_t* d_ob,
+                     int64_t nprob, const int32_t* h_delta, const int32_t* h_half, int32_t* d_scores, char* d_paths,
+                     const uint64_t* d_path_off, int64_t* d_path_len, uint8_t* h_used_band, const uint64_t* h_oa,
+                     const uint64_t* h_ob, uint64_t* banded_cells);
 int probe_int32_peak(Ctx* c, double* ops);
+void mlp_release(const void* h);
 
 }  // namespace mvg

@@ -35,7 +35,11 @@ EXPORTS = ["mvg_create", "mvg_destroy", "mvg_last_error", "mvg_stream", "mvg_ker
            "mvg_default_seed_weight", "mvg_seed_length", "mvg_seed_weight", "mvg_sml_build", "mvg_sml_build_dev",
            "mvg_pairwise_matches", "mvg_pairwise_matches_dev", "mvg_pairwise_stats", "mvg_gapdp_batch",
            "mvg_gapdp_batch_dev", "mvg_set_tb_arena", "mvg_probe_int32_peak", "mvg_set_profiling",
-           "mvg_stage_times"]
+           "mvg_stage_times", "mvg_gapdp_banded", "mvg_gapdp_banded_dev", "mvg_set_dp_rows", "mvg_mlp_num_params",
+           "mvg_mlp_set_params", "mvg_mlp_get_params", "mvg_band_features_dev", "mvg_mlp_forward_dev",
+           "mvg_mlp_grad_dev", "mvg_mlp_train_step_dev", "mvg_band_propose_dev", "mvg_gapdp_envelope_dev"]
+
+TUNING_PATH = os.path.join(HERE, "dp_tuning.json")
 
 
 def load_library(path=LIB_PATH):
@@ -66,6 +70,18 @@ def load_library(path=LIB_PATH):
         "mvg_gapdp_batch_dev": (ci, [vp, vp, vp, vp, vp, i64, vp, vp, vp, vp]),
         "mvg_set_tb_arena": (ci, [vp, u64]),
         "mvg_probe_int32_peak": (ci, [vp, ctypes.POINTER(ctypes.c_double)]),
+        "mvg_gapdp_banded": (ci, [vp, vp, vp, vp, vp, i64, vp, vp, vp, vp, vp, vp, vp, ctypes.POINTER(u64)]),
+        "mvg_gapdp_banded_dev": (ci, [vp, vp, vp, vp, vp, i64, vp, vp, vp, vp, vp, vp, vp, ctypes.POINTER(u64)]),
+        "mvg_set_dp_rows": (ci, [vp, ci]),
+        "mvg_gapdp_envelope_dev": (ci, [vp, vp, vp, vp, vp, i64, vp, vp]),
+        "mvg_mlp_num_params": (i64, []),
+        "mvg_mlp_set_params": (ci, [vp, vp]),
+        "mvg_mlp_get_params": (ci, [vp, vp]),
+        "mvg_band_features_dev": (ci, [vp, vp, vp, vp, vp, i64, vp]),
+        "mvg_mlp_forward_dev": (ci, [vp, vp, i64, vp]),
+        "mvg_mlp_grad_dev": (ci, [vp, vp, vp, i64, vp, vp]),
+        "mvg_mlp_train_step_dev": (ci, [vp, vp, vp, i64, ctypes.c_float, ci, vp]),
+        "mvg_band_propose_dev": (ci, [vp, vp, vp, vp, vp, i64, ctypes.c_float, ctypes.c_float, vp, vp]),
         "mvg_set_profiling": (ci, [vp, ci]),
         "mvg_stage_times": (ci, [vp, ctypes.c_char_p, ctypes.c_size_t, vp, ci, ctypes.POINTER(ci)]),
     }
@@ -122,6 +138,13 @@ class Context:
         _check(L.mvg_create(ctypes.byref(h), device))
         self._h = h
         self.device = device
+        if os.path.exists(TUNING_PATH):  # committed autotuner choice
+            import json
+            with open(TUNING_PATH) as f:
+                self.set_dp_rows(int(json.load(f).get("rows_per_lane", 8)))
+
+    def set_dp_rows(self, rows):
+        _check(load_library().mvg_set_dp_rows(self._h, int(rows)))
 
     @property
     def handle(self):
@@ -218,6 +241,48 @@ class Context:
         _check(load_library().mvg_gapdp_batch(self._h, _ptr(seq_a), _ptr(off_a), _ptr(seq_b), _ptr(off_b), n,
                                               _ptr(scores), None, None, None))
         return scores[:n], None
+
+    def gap_align_banded(self, seq_a, off_a, seq_b, off_b, band_delta, band_half, with_paths=True):
+        """Banded NWSmall with the exactness check and full-DP fallback.
+        Returns (scores, paths or None, used_band bool[n], cells computed)."""
+        seq_a, seq_b = _u8(seq_a), _u8(seq_b)
+        off_a = np.ascontiguousarray(off_a, np.uint64)
+        off_b = np.ascontiguousarray(off_b, np.uint64)
+        n = len(off_a) - 1
+        delta = np.ascontiguousarray(band_delta, np.int32)
+        half = np.ascontiguousarray(band_half, np.int32)
+        scores = np.zeros(max(n, 1), np.int32)
+        used = np.zeros(max(n, 1), np.uint8)
+        cells = ctypes.c_uint64(0)
+        if with_paths:
+            la = np.diff(off_a.astype(np.int64))
+            lb = np.diff(off_b.astype(np.int64))
+            path_off = np.zeros(n + 1, np.uint64)
+            path_off[1:] = np.cumsum(la + lb)
+            paths = np.zeros(int(path_off[-1]) + 1, np.uint8)
+            plen = np.zeros(max(n, 1), np.int64)
+            _check(load_library().mvg_gapdp_banded(self._h, _ptr(seq_a), _ptr(off_a), _ptr(seq_b), _ptr(off_b), n,
+                                                   _ptr(delta), _ptr(half), _ptr(scores), _ptr(paths),
+                                                   _ptr(path_off), _ptr(plen), _ptr(used), ctypes.byref(cells)))
+            raw = paths.tobytes()
+            out = [raw[int(path_off[k]):int(path_off[k]) + int(plen[k])].decode() for k in range(n)]
+            return scores[:n], out, used[:n].astype(bool), int(cells.value)
+        _check(load_library().mvg_gapdp_banded(self._h, _ptr(seq_a), _ptr(off_a), _ptr(seq_b), _ptr(off_b), n,
+                                               _ptr(delta), _ptr(half), _ptr(scores), None, None, None, _ptr(used),
+                                               ctypes.byref(cells)))
+        return scores[:n], None, used[:n].astype(bool), int(cells.value)
+
+    def gap_align_banded_dev(self, d_sa, d_oa, d_sb, d_ob, n, band_delta, band_half, d_scores, d_paths, d_path_off,
+                             d_path_len):
+        """Device-buffer banded call; band arrays and the returned used-band flags are host numpy arrays."""
+        delta = np.ascontiguousarray(band_delta, np.int32)
+        half = np.ascontiguousarray(band_half, np.int32)
+        used = np.zeros(max(n, 1), np.uint8)
+        cells = ctypes.c_uint64(0)
+        _check(load_library().mvg_gapdp_banded_dev(self._h, d_sa, d_oa, d_sb, d_ob, n, _ptr(delta), _ptr(half),
+                                                   d_scores, d_paths, d_path_off, d_path_len, _ptr(used),
+                                                   ctypes.byref(cells)))
+        return used[:n].astype(bool), int(cells.value)
 
     def gap_align_batch_raw(self, seq_a, off_a, seq_b, off_b, scores, paths, path_off, path_len):
         """Host-buffer call with caller-owned numpy outputs (no per-call Python decoding)."""

@@ -1,0 +1,240 @@
+#!/usr/bin/env python3
+"""Trains the band-proposal network on the GPU and evaluates it.
+
+    python mauve-py_gb300/train_bandnet.py [--train 1000000 --eval 200000]
+                                           [--out mauve-py_gb300/bandnet_weights.npz]
+
+1. Draws training and held-out gaps like the recoded-genome pair's
+   (tests/synth.py gap_batch_recoded).
+2. Labels them with the exact full DP (mvg_gapdp_envelope_dev): optimal
+   score and path envelope -> band offset and the half-width the exactness
+   check needs.
+3. Trains with the library's own forward/backward/Adam kernels.
+4. Calibrates the half-width margin (alpha, beta) on a validation split for
+   the fewest DP cells including fallbacks.
+5. Evaluates on the held-out gaps: plain full DP vs learned band vs the band
+   without the network, all with identical output (checked), and writes the
+   weights, calibration and metrics.
+"""
+import argparse
+import json
+import os
+import sys
+import time
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+for _p in (HERE, os.path.join(ROOT, "tests")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+import bandnet  # noqa: E402
+import mvg  # noqa: E402
+
+
+class DeviceBatch:
+    """Gap batch resident on the GPU (torch tensors for memory, raw pointers for the C ABI)."""
+
+    def __init__(self, sa, oa, sb, ob, dev):
+        import torch
+        self.n = len(oa) - 1
+        self.la = np.diff(oa).astype(np.int64)
+        self.lb = np.diff(ob).astype(np.int64)
+        self.oa, self.ob = oa.astype(np.uint64), ob.astype(np.uint64)
+        self.sa = torch.from_numpy(sa).to(dev)
+        self.sb = torch.from_numpy(sb).to(dev)
+        self.doa = torch.from_numpy(self.oa.view(np.int64)).to(dev)
+        self.dob = torch.from_numpy(self.ob.view(np.int64)).to(dev)
+        self.cells = float(np.sum(self.la * self.lb))
+
+    def ptrs(self):
+        return self.sa.data_ptr(), self.doa.data_ptr(), self.sb.data_ptr(), self.dob.data_ptr()
+
+
+def subset(sa, oa, sb, ob, idx):
+    a = [sa[oa[k]:oa[k + 1]] for k in idx]
+    b = [sb[ob[k]:ob[k + 1]] for k in idx]
+    noa = np.concatenate([[0], np.cumsum([len(x) for x in a])]).astype(np.int64)
+    nob = np.concatenate([[0], np.cumsum([len(x) for x in b])]).astype(np.int64)
+    return np.concatenate(a), noa, np.concatenate(b), nob
+
+
+def label(ctx, batch, chunk=100_000):
+    scores = np.zeros(batch.n, np.int32)
+    env = np.zeros((batch.n, 2), np.int32)
+    for s in range(0, batch.n, chunk):
+        e = min(batch.n, s + chunk)
+        sub = DeviceBatch(*subset_host(batch, s, e), batch.sa.device)
+        sc, en = bandnet.full_dp_labels_dev(ctx, *sub.ptrs(), sub.n, torch_device=batch.sa.device)
+        scores[s:e] = sc
+        env[s:e] = en
+    return scores, env
+
+
+def subset_host(batch, s, e):
+    sa = batch.sa[int(batch.oa[s]):int(batch.oa[e])].cpu().numpy()
+    sb = batch.sb[int(batch.ob[s]):int(batch.ob[e])].cpu().numpy()
+    oa = (batch.oa[s:e + 1] - batch.oa[s]).astype(np.int64)
+    ob = (batch.ob[s:e + 1] - batch.ob[s]).astype(np.int64)
+    return sa, oa, sb, ob
+
+
+def timed_banded(ctx, batch, delta, half):
+    """(seconds, used-band flags, cells) of the banded DP with fallback, paths on device."""
+    import torch
+    n = batch.n
+    path_off = np.zeros(n + 1, np.uint64)
+    path_off[1:] = np.cumsum(batch.la + batch.lb)
+    d_po = torch.from_numpy(path_off.view(np.int64)).to(batch.sa.device)
+    d_paths = torch.zeros(int(path_off[-1]) + 16, dtype=torch.uint8, device=batch.sa.device)
+    d_pl = torch.zeros(n, dtype=torch.int64, device=batch.sa.device)
+    d_sc = torch.zeros(n, dtype=torch.int32, device=batch.sa.device)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    used, cells = ctx.gap_align_banded_dev(*batch.ptrs(), n, delta, half, d_sc.data_ptr(), d_paths.data_ptr(),
+                                           d_po.data_ptr(), d_pl.data_ptr())
+    torch.cuda.synchronize()
+    return time.perf_counter() - t0, used, cells, d_sc, d_paths, d_pl, path_off
+
+
+def timed_full(ctx, batch):
+    import torch
+    n = batch.n
+    path_off = np.zeros(n + 1, np.uint64)
+    path_off[1:] = np.cumsum(batch.la + batch.lb)
+    d_po = torch.from_numpy(path_off.view(np.int64)).to(batch.sa.device)
+    d_paths = torch.zeros(int(path_off[-1]) + 16, dtype=torch.uint8, device=batch.sa.device)
+    d_pl = torch.zeros(n, dtype=torch.int64, device=batch.sa.device)
+    d_sc = torch.zeros(n, dtype=torch.int32, device=batch.sa.device)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ctx.gap_align_batch_dev(*batch.ptrs(), n, d_sc.data_ptr(), d_paths.data_ptr(), d_po.data_ptr(), d_pl.data_ptr())
+    torch.cuda.synchronize()
+    return time.perf_counter() - t0, d_sc, d_paths, d_pl
+
+
+def band_cells(la, lb, delta, half, srows):
+    """Host copy of the band geometry's cell count (same formula as band.h)."""
+    tot = 0
+    for a, b, d, h in zip(la, lb, delta, half):
+        ns = (a + srows - 1) // srows
+        for k in range(ns):
+            lo = 1 if k == 0 else min(max((k * srows + 1) * b // a + d - h, 1), b)
+            last = min((k + 1) * srows, a)
+            hi = b if k == ns - 1 else min(max(last * b // a + d + h + 1, 1), b)
+            tot += (min(srows, a - k * srows)) * (hi - lo + 1)
+    return tot
+
+
+def train(args):
+    import torch
+    import synth
+    dev = torch.device("cuda", 0)
+    ctx = mvg.Context(0)
+    t_all = time.time()
+    n_tr, n_ev = args.train, args.eval
+    sa, oa, sb, ob = synth.gap_batch_recoded(seed=args.seed, nprob=n_tr + n_ev)
+    tr = DeviceBatch(*subset(sa, oa, sb, ob, np.arange(n_tr)), dev)
+    ev = DeviceBatch(*subset(sa, oa, sb, ob, np.arange(n_tr, n_tr + n_ev)), dev)
+    del sa, sb
+    print("data", tr.n, ev.n, "%.1fs" % (time.time() - t_all), flush=True)
+    t0 = time.time()
+    sc_tr, env_tr = label(ctx, tr)
+    print("labels %.1fs (%.3g cells)" % (time.time() - t0, tr.cells), flush=True)
+    T, _, _ = bandnet.labels_from_full_dp(tr.la, tr.lb, sc_tr, env_tr)
+    X = torch.zeros((tr.n, bandnet.N_IN), dtype=torch.bfloat16, device=dev)
+    net = bandnet.BandNet(ctx, seed=args.seed)
+    net.features_dev(*tr.ptrs(), tr.n, X.data_ptr())
+    Tg = torch.from_numpy(T).to(dev)
+    nval = max(1, tr.n // 20)
+    perm = np.random.default_rng(args.seed).permutation(tr.n)
+    val_idx, fit_idx = perm[:nval], perm[nval:]
+    fit_idx_t = torch.from_numpy(fit_idx).to(dev)
+    t0 = time.time()
+    losses = []
+    step = 0
+    for ep in range(args.epochs):
+        order = fit_idx_t[torch.randperm(len(fit_idx_t), device=dev)]
+        lr = args.lr * (0.5 ** ep)
+        for s in range(0, len(order), args.batch):
+            idx = order[s:s + args.batch]
+            xb = X.index_select(0, idx).contiguous()
+            tb = Tg.index_select(0, idx).contiguous()
+            loss = net.train_step_dev(xb.data_ptr(), tb.data_ptr(), len(idx), lr)
+            step += 1
+            if step % 50 == 0:
+                losses.append((step, loss))
+        print("epoch %d loss %.4f" % (ep, losses[-1][1] if losses else float("nan")), flush=True)
+    train_s = time.time() - t0
+    # calibrate alpha / beta on the validation split: fewest cells incl. fallback
+    vi = torch.from_numpy(val_idx).to(dev)
+    out = torch.zeros((len(val_idx), 2), dtype=torch.float32, device=dev)
+    net.forward_dev(X.index_select(0, vi).contiguous().data_ptr(), len(val_idx), out.data_ptr())
+    o = out.cpu().numpy()
+    la_v, lb_v = tr.la[val_idx], tr.lb[val_idx]
+    _, dstar, hstar = bandnet.labels_from_full_dp(la_v, lb_v, sc_tr[val_idx], env_tr[val_idx])
+    best = None
+    srows = 32 * 8
+    for alpha in (1.0, 1.25, 1.5, 2.0):
+        for beta in (0.0, 16.0, 48.0, 128.0):
+            d = np.rint(o[:, 0] * bandnet.DELTA_SCALE).astype(np.int64)
+            h = np.ceil(alpha * np.expm1(np.minimum(o[:, 1], 13)) + beta).astype(np.int64)
+            ok = (np.abs(d - dstar) + hstar <= h)  # band covers the label band: a good proxy for acceptance
+            cost = np.where(ok, 0, la_v * lb_v).astype(float)
+            sample = np.arange(0, len(la_v), max(1, len(la_v) // 2000))
+            cost_band = band_cells(la_v[sample], lb_v[sample], d[sample], h[sample], srows) * (len(la_v) / len(sample))
+            total = cost_band + cost.sum()
+            if best is None or total < best[0]:
+                best = (total, alpha, beta, float(ok.mean()))
+    _, alpha, beta, cover = best
+    print("calibrated alpha %.2f beta %.1f (validation cover %.3f)" % (alpha, beta, cover), flush=True)
+    params = net.get_params()
+    # held-out evaluation: full vs learned band vs band without the network
+    res = {"train_gaps": tr.n, "eval_gaps": ev.n, "train_seconds": train_s, "steps": step,
+           "loss_curve": losses[-20:], "alpha": alpha, "beta": beta}
+    tf, sc_f, p_f, pl_f = timed_full(ctx, ev)
+    tf, sc_f, p_f, pl_f = timed_full(ctx, ev)  # second run: warm
+    t_prop0 = time.perf_counter()
+    dl, hl = net.propose_dev(*ev.ptrs(), ev.n, alpha, beta)
+    torch.cuda.synchronize()
+    t_prop = time.perf_counter() - t_prop0
+    tl, used_l, cells_l, sc_l, p_l, pl_l, _ = timed_banded(ctx, ev, dl, hl)
+    dh, hh = bandnet.heuristic_band(ev.la, ev.lb)
+    th, used_h, cells_h, sc_h, p_h, pl_h, _ = timed_banded(ctx, ev, dh, hh)
+    same_l = bool(torch.equal(sc_f, sc_l) and torch.equal(pl_f, pl_l) and torch.equal(p_f, p_l))
+    same_h = bool(torch.equal(sc_f, sc_h) and torch.equal(pl_f, pl_h) and torch.equal(p_f, p_h))
+    res.update({
+        "eval_cells_full": ev.cells,
+        "full": {"seconds": tf, "gcups": ev.cells / tf / 1e9},
+        "learned": {"seconds": tl + t_prop, "dp_seconds": tl, "propose_seconds": t_prop,
+                    "effective_gcups": ev.cells / (tl + t_prop) / 1e9, "accept_rate": float(used_l.mean()),
+                    "fallback_rate": float(1 - used_l.mean()), "cells": cells_l, "identical_to_full": same_l},
+        "no_network": {"seconds": th, "effective_gcups": ev.cells / th / 1e9, "accept_rate": float(used_h.mean()),
+                       "fallback_rate": float(1 - used_h.mean()), "cells": cells_h, "identical_to_full": same_h},
+    })
+    res["speedup_learned_vs_full"] = tf / (tl + t_prop)
+    res["speedup_no_network_vs_full"] = tf / th
+    print(json.dumps(res, indent=1), flush=True)
+    np.savez(args.out, params=params, alpha=np.float32(alpha), beta=np.float32(beta))
+    with open(os.path.splitext(args.out)[0] + "_eval.json", "w") as f:
+        json.dump(res, f, indent=1)
+    print("total %.1fs" % (time.time() - t_all))
+    return res
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--train", type=int, default=1_000_000)
+    ap.add_argument("--eval", type=int, default=200_000)
+    ap.add_argument("--epochs", type=int, default=4)
+    ap.add_argument("--batch", type=int, default=4096)
+    ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--seed", type=int, default=4)
+    ap.add_argument("--out", default=os.path.join(HERE, "bandnet_weights.npz"))
+    train(ap.parse_args())
+
+
+if __name__ == "__main__":
+    main()

@@ -193,6 +193,65 @@ def gap_batch(seed=3, nprob=200_000, lmin=10, lmax=20_000, max_div=0.30):
     return seq_a, off_a, seq_b, off_b
 
 
+def gap_batch_recoded(seed=4, nprob=1_000_000, lmin=20, lmax=5000, unrelated=0.1):
+    """Inter-anchor gaps drawn like the recoded-genome pair's: lengths
+    log-uniform on [lmin, lmax]; 90% homologous with substitutions U(0.5%, 3%)
+    and Poisson(0.0005 L) indels (geometric mean 4); 10% divergent gap
+    content (divergence U(25%, 40%), indel share 10%).  Vectorised over the
+    whole batch.  Returns concatenated base codes and offsets."""
+    rng = np.random.default_rng(seed)
+    la = np.exp(rng.uniform(np.log(lmin), np.log(lmax), nprob)).astype(np.int64)
+    off_a = np.zeros(nprob + 1, np.int64)
+    off_a[1:] = np.cumsum(la)
+    total = int(off_a[-1])
+    seq_a = rng.integers(0, 4, total).astype(np.uint8)
+    far = rng.random(nprob) < unrelated
+    sub = np.where(far, rng.uniform(0.25, 0.40, nprob) * 0.9, rng.uniform(0.005, 0.03, nprob))
+    ind_rate = np.where(far, rng.uniform(0.25, 0.40, nprob) * 0.1 / 3.0, 0.0005)
+    gid = np.repeat(np.arange(nprob), la)
+    b = seq_a.copy()
+    m = rng.random(total) < sub[gid]
+    b[m] = (b[m] + rng.integers(1, 4, int(m.sum()))) % 4
+    nind = rng.poisson(ind_rate * la)
+    eg = np.repeat(np.arange(nprob), nind)  # gap of each indel event
+    pos = off_a[eg] + (rng.random(len(eg)) * la[eg]).astype(np.int64)
+    lens = rng.geometric(0.25, len(eg))
+    ins = rng.random(len(eg)) < 0.5
+    order = np.argsort(pos, kind="stable")
+    pos, lens, ins, eg = pos[order], lens[order], ins[order], eg[order]
+    keep = np.ones(total, bool)
+    add_at, add_len = [], []
+    delta_len = np.zeros(nprob, np.int64)
+    for p, l, i, g in zip(pos, lens, ins, eg):
+        if i:
+            add_at.append(p)
+            add_len.append(int(l))
+            delta_len[g] += l
+        else:
+            e = min(p + int(l), int(off_a[g + 1]))
+            delta_len[g] -= int(keep[p:e].sum())
+            keep[p:e] = False
+    lb = la + delta_len
+    empty = lb <= 0
+    if empty.any():  # never return an empty sequence: keep the gap's first base
+        for g in np.nonzero(empty)[0]:
+            keep[off_a[g]] = True
+            delta_len[g] += 1
+        lb = la + delta_len
+    pieces, prev = [], 0
+    inserts = sorted(zip(add_at, add_len))
+    for p, l in inserts:
+        pieces.append(b[prev:p][keep[prev:p]])
+        pieces.append(rng.integers(0, 4, l).astype(np.uint8))
+        prev = p
+    pieces.append(b[prev:][keep[prev:]])
+    seq_b = np.concatenate(pieces)
+    off_b = np.zeros(nprob + 1, np.int64)
+    off_b[1:] = np.cumsum(lb)
+    assert off_b[-1] == len(seq_b)
+    return seq_a, off_a, seq_b, off_b
+
+
 def _mutate_codes_fast(rng, a, sub, nind):
     m = rng.random(len(a)) < sub
     b = a.copy()

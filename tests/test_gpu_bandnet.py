@@ -1,0 +1,138 @@
+"""GPU tests of the banded gap DP and the band-proposal network."""
+import numpy as np
+import pytest
+
+import bandnet
+import bandnet_ref as REF
+import mvg
+import oracle as O
+import synth
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    import build as pkg_build
+    pkg_build.build()
+    c = mvg.Context(0)
+    yield c
+    c.close()
+
+
+def _dev(arrs):
+    import torch
+    return [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in arrs]
+
+
+def _batch_ptrs(sa, oa, sb, ob):
+    t = _dev([sa, oa.astype(np.int64), sb, ob.astype(np.int64)])
+    return t, [x.data_ptr() for x in t]
+
+
+@pytest.mark.parametrize("rows", [4, 8])
+def test_banded_output_identical_to_full(ctx, rows):
+    ctx.set_dp_rows(rows)
+    try:
+        rng = np.random.default_rng(rows)
+        sa, oa, sb, ob = synth.gap_batch_recoded(seed=11, nprob=300, lmin=1, lmax=1500)
+        n = len(oa) - 1
+        la, lb = np.diff(oa), np.diff(ob)
+        s_full, p_full = ctx.gap_align_batch(sa, oa, sb, ob)
+        for delta, half in [bandnet.heuristic_band(la, lb),
+                            (rng.integers(-40, 40, n).astype(np.int32), rng.integers(0, 60, n).astype(np.int32)),
+                            (np.zeros(n, np.int32), np.zeros(n, np.int32))]:
+            s, p, used, cells = ctx.gap_align_banded(sa, oa, sb, ob, delta, half)
+            np.testing.assert_array_equal(s, s_full)
+            assert p == p_full
+        oscores, _, _, _ = O.nw_batch(sa, oa, sb, ob, with_paths=False)
+        np.testing.assert_array_equal(s_full, oscores)
+    finally:
+        ctx.set_dp_rows(8)
+
+
+def test_band_with_label_width_is_accepted_on_close_gaps(ctx):
+    sa, oa, sb, ob = synth.gap_batch_recoded(seed=12, nprob=400, lmin=50, lmax=3000, unrelated=0.0)
+    la, lb = np.diff(oa), np.diff(ob)
+    t, ptrs = _batch_ptrs(sa, oa, sb, ob)
+    scores, env = bandnet.full_dp_labels_dev(ctx, *ptrs, len(la), torch_device=t[0].device)
+    _, delta, half = bandnet.labels_from_full_dp(la, lb, scores, env, margin=16)
+    s, p, used, cells = ctx.gap_align_banded(sa, oa, sb, ob, delta, half, with_paths=False)
+    np.testing.assert_array_equal(s, scores)
+    assert used.mean() > 0.9
+    assert cells < 0.5 * float(np.sum(la * lb))
+
+
+def test_envelope_matches_oracle_paths(ctx):
+    sa, oa, sb, ob = synth.gap_batch(seed=13, nprob=50, lmin=1, lmax=800)
+    t, ptrs = _batch_ptrs(sa, oa, sb, ob)
+    scores, env = bandnet.full_dp_labels_dev(ctx, *ptrs, 50, torch_device=t[0].device)
+    for k in range(50):
+        a, b = sa[oa[k]:oa[k + 1]], sb[ob[k]:ob[k + 1]]
+        path, sc = O.nw_align(a, b)
+        assert sc == scores[k]
+        i = j = 0
+        devs = []
+        for e in path:
+            i += e != "I"
+            j += e != "D"
+            if i >= 1:
+                devs.append(j - (i * len(b)) // len(a))
+        assert (min(devs), max(devs)) == tuple(env[k]), k
+
+
+def test_features_match_reference(ctx):
+    import torch
+    sa, oa, sb, ob = synth.gap_batch(seed=14, nprob=40, lmin=1, lmax=400)
+    t, ptrs = _batch_ptrs(sa, oa, sb, ob)
+    X = torch.zeros((40, bandnet.N_IN), dtype=torch.bfloat16, device=t[0].device)
+    net = bandnet.BandNet(ctx)
+    net.features_dev(*ptrs, 40, X.data_ptr())
+    ref = REF.features(sa, oa, sb, ob)
+    np.testing.assert_allclose(X.float().cpu().numpy(), ref, rtol=1e-2, atol=1e-3)
+
+
+def test_mlp_gradients_match_cpu_oracle(ctx):
+    """Loss and every parameter block's gradient against the float64 CPU
+    reference (same bf16 roundings); tolerance 2e-2 relative in norm."""
+    import torch
+    sa, oa, sb, ob = synth.gap_batch_recoded(seed=15, nprob=96, lmin=20, lmax=600)
+    t, ptrs = _batch_ptrs(sa, oa, sb, ob)
+    net = bandnet.BandNet(ctx, seed=3)
+    n = 96
+    X = torch.zeros((n, bandnet.N_IN), dtype=torch.bfloat16, device=t[0].device)
+    net.features_dev(*ptrs, n, X.data_ptr())
+    rng = np.random.default_rng(0)
+    T = rng.normal(0, 1, (n, 2)).astype(np.float32)
+    g, loss = net.grad_dev(X.data_ptr(), torch.from_numpy(T).cuda().data_ptr(), n)
+    Xh = X.float().cpu().numpy().astype(np.float64)
+    rloss, rg = REF.loss_and_grads(net.get_params(), Xh, T.astype(np.float64))
+    assert abs(loss - rloss) <= 2e-2 * abs(rloss) + 1e-6
+    sizes = [256 * 528, 256, 256 * 256, 256, 256 * 256, 256, 2 * 256, 2]
+    off = 0
+    for s in sizes:
+        a, b = g[off:off + s], rg[off:off + s]
+        assert np.linalg.norm(a - b) <= 2e-2 * np.linalg.norm(b) + 1e-7, (off, s)
+        off += s
+    # forward agrees too
+    out = torch.zeros((n, 2), dtype=torch.float32, device=t[0].device)
+    net.forward_dev(X.data_ptr(), n, out.data_ptr())
+    np.testing.assert_allclose(out.cpu().numpy(), REF.forward(net.get_params(), Xh), rtol=2e-2, atol=2e-2)
+
+
+def test_training_reduces_loss(ctx):
+    import torch
+    sa, oa, sb, ob = synth.gap_batch_recoded(seed=16, nprob=3000, lmin=20, lmax=2000)
+    la, lb = np.diff(oa), np.diff(ob)
+    t, ptrs = _batch_ptrs(sa, oa, sb, ob)
+    scores, env = bandnet.full_dp_labels_dev(ctx, *ptrs, len(la), torch_device=t[0].device)
+    T, _, _ = bandnet.labels_from_full_dp(la, lb, scores, env)
+    n = len(la)
+    X = torch.zeros((n, bandnet.N_IN), dtype=torch.bfloat16, device=t[0].device)
+    net = bandnet.BandNet(ctx, seed=1)
+    net.features_dev(*ptrs, n, X.data_ptr())
+    Tg = torch.from_numpy(T).cuda()
+    first = net.train_step_dev(X.data_ptr(), Tg.data_ptr(), n, 1e-3)
+    for _ in range(150):
+        last = net.train_step_dev(X.data_ptr(), Tg.data_ptr(), n, 1e-3)
+    assert last < 0.5 * first
