@@ -493,11 +493,29 @@ __global__ void __launch_bounds__(256) k_bucket_replay(MatchCtx c, const Mhe* __
   if (ncoll) atomicAdd(coll, ncoll);
 }
 
-__global__ void k_bucket_hist(const uint32_t* __restrict__ bucket, const uint32_t* __restrict__ npairs_p,
-                              uint32_t* __restrict__ cnt) {
-  const int64_t np = *npairs_p;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < np; i += (int64_t)gridDim.x * blockDim.x)
-    atomicAdd(&cnt[bucket[i]], 1u);
+// Segment of each bucket in the bucket-sorted pair list: two lower_bounds.
+__global__ void k_bucket_bounds(const uint32_t* __restrict__ sorted_bucket, int64_t np, uint32_t* __restrict__ start,
+                                uint32_t* __restrict__ cnt) {
+  for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < kTableSize; b += gridDim.x * blockDim.x) {
+    int64_t lo[2];
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const uint32_t key = (uint32_t)b + q;
+      int64_t first = 0, len = np;
+      while (len > 0) {
+        const int64_t half = len >> 1;
+        if (sorted_bucket[first + half] < key) {
+          first += half + 1;
+          len -= half + 1;
+        } else {
+          len = half;
+        }
+      }
+      lo[q] = first;
+    }
+    start[b] = (uint32_t)lo[0];
+    cnt[b] = (uint32_t)(lo[1] - lo[0]);
+  }
 }
 
 __global__ void k_lpt_keys(const uint32_t* __restrict__ cnt, uint32_t* __restrict__ key, uint32_t* __restrict__ id) {
@@ -632,12 +650,11 @@ int pairwise_matches_dev(Ctx* c, const uint8_t* d_a, uint64_t na, const uint8_t*
   c->launches++;
   int which = radix_sort_pairs<uint32_t>(bk0, or0, bk1, or1, npairs, 16, sscr, c->stream, &c->launches);
   uint32_t* sorted_pair = which ? or1 : or0;
-  MVG_CUDA_TRY(cudaMemsetAsync(bcount, 0, (size_t)kTableSize * 4, c->stream));
+  const uint32_t* sorted_bucket = which ? bk1 : bk0;
   MVG_CUDA_TRY(cudaMemsetAsync(nent, 0, (size_t)kTableSize * 4, c->stream));
   MVG_CUDA_TRY(cudaMemsetAsync(d_coll, 0, 8, c->stream));
-  k_bucket_hist<<<grid_for(npairs, 256), 256, 0, c->stream>>>(bk0, d_npairs, bcount);
+  k_bucket_bounds<<<grid_for(kTableSize, 256), 256, 0, c->stream>>>(sorted_bucket, npairs, bstart, bcount);
   c->launches++;
-  exclusive_scan(bcount, bstart, kTableSize, bscr, tot, c->stream, &c->launches);
   k_lpt_keys<<<grid_for(kTableSize, 256), 256, 0, c->stream>>>(bcount, lk0, li0);
   c->launches++;
   which = radix_sort_pairs<uint32_t>(lk0, li0, lk1, li1, kTableSize, 32, sscr, c->stream, &c->launches);
