@@ -65,6 +65,23 @@ int mvg_sml_build(mvg_handle h, const uint8_t* seq, uint64_t n, uint64_t seed,
 int mvg_sml_build_dev(mvg_handle h, const uint8_t* d_seq, uint64_t n, uint64_t seed,
                       uint32_t* d_pos_out, uint64_t* d_mer_out, uint64_t cap, uint64_t* count);
 
+/* Sorted mer list build that allocates no device memory.  No counterpart in
+ * the reference.  Some callers cannot call cudaMalloc when they need a sorted
+ * mer list.  One example is a process whose other runtime reserved the
+ * device's memory for its own pool up front.  Another is a latency-bound
+ * loop that cannot take cudaMalloc's implicit device-wide synchronisation.
+ * This call needs no handle.  It takes device input/output pointers like
+ * mvg_sml_build_dev and a CUDA stream (void*, NULL = default stream).  It
+ * produces the same output.  Its scratch is one static device array of
+ * about 6.3 MB that every GPU loading the library holds until exit, which
+ * limits n to 262,144 bases; longer input returns MVG_ERR_CAPACITY.  The first
+ * call on a device looks up that array's device address (with the device
+ * current) and uploads the base table, so make it before any stream capture.
+ * All calls share the array: calls whose GPU work overlaps (other streams or
+ * host threads) race and must be serialised by the caller. */
+int mvg_sml_build_noalloc(const uint8_t* d_seq, uint64_t n, uint64_t seed, uint32_t* d_pos_out,
+                          uint64_t* d_mer_out, uint64_t cap, uint64_t* count, void* stream);
+
 /* --------------------------------------------------------------- matches */
 
 /* Pairwise seed matching and maximal-match extension for two genomes:

@@ -72,6 +72,10 @@ int pack_sequence(Ctx* c, const uint8_t* d_seq, uint64_t n, uint32_t* d_packed);
 int sml_sort(Ctx* c, const uint32_t* d_packed, uint64_t count, const SeedDesc& s, uint32_t* d_pos_out,
              uint64_t* d_mer_out, SmlKeys* keep, int slot_base);
 int check_device_error(Ctx* c);
+size_t sml_key_bytes(const SeedDesc& s);
+int sml_build_into(const uint8_t* d_seq, uint64_t n, uint64_t count, const SeedDesc& s, uint32_t* packed, void* k0,
+                   void* k1, uint32_t* v0, uint32_t* v1, uint32_t* scr, uint32_t* d_pos_out, uint64_t* d_mer_out,
+                   cudaStream_t st, uint32_t* d_err, uint64_t* launches);
 
 int pairwise_matches_dev(Ctx* c, const uint8_t* d_a, uint64_t na, const uint8_t* d_b, uint64_t nb, uint64_t seed,
                          int64_t* d_out, uint64_t cap, uint64_t* count);

@@ -166,6 +166,44 @@ static int sml_sort_impl(Ctx* c, const uint32_t* d_packed, uint64_t count, const
   return 0;
 }
 
+// The whole SML build on caller-provided device buffers (no workspace, no
+// allocation): pack, seed keys, radix sort, positions and mers out.
+// packed: packed_words(n) words; k0/k1: count keys of sml_key_bytes(s) each;
+// v0/v1: count uint32; scr: radix_scratch_words(count) words.
+template <typename K>
+static int sml_build_into_impl(const uint8_t* d_seq, uint64_t n, uint64_t count, const SeedDesc& s, uint32_t* packed,
+                               void* k0, void* k1, uint32_t* v0, uint32_t* v1, uint32_t* scr, uint32_t* d_pos_out,
+                               uint64_t* d_mer_out, cudaStream_t st, uint32_t* d_err, uint64_t* launches) {
+  const uint64_t words = packed_words(n);
+  k_pack<<<grid_for(words, 256), 256, 0, st>>>(d_seq, n, packed, words, d_err);
+  ++*launches;
+  if (count == 0) return 0;
+  k_seed_keys<K><<<grid_for(count, 256), 256, 0, st>>>(packed, count, s, (K*)k0, v0);
+  ++*launches;
+  const int which = radix_sort_pairs<K>((K*)k0, v0, (K*)k1, v1, (int64_t)count, 2 * s.w + 1, scr, st, launches);
+  K* ks = which ? (K*)k1 : (K*)k0;
+  uint32_t* vs = which ? v1 : v0;
+  if (d_pos_out) MVG_CUDA_TRY(cudaMemcpyAsync(d_pos_out, vs, count * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st));
+  if (d_mer_out) {
+    k_key_to_mer<K><<<grid_for(count, 256), 256, 0, st>>>(ks, count, s.w, d_mer_out);
+    ++*launches;
+  }
+  MVG_CUDA_TRY(cudaGetLastError());
+  return 0;
+}
+
+size_t sml_key_bytes(const SeedDesc& s) { return 2 * s.w + 1 <= 32 ? 4 : 8; }
+
+int sml_build_into(const uint8_t* d_seq, uint64_t n, uint64_t count, const SeedDesc& s, uint32_t* packed, void* k0,
+                   void* k1, uint32_t* v0, uint32_t* v1, uint32_t* scr, uint32_t* d_pos_out, uint64_t* d_mer_out,
+                   cudaStream_t st, uint32_t* d_err, uint64_t* launches) {
+  if (sml_key_bytes(s) == 4)
+    return sml_build_into_impl<uint32_t>(d_seq, n, count, s, packed, k0, k1, v0, v1, scr, d_pos_out, d_mer_out, st,
+                                         d_err, launches);
+  return sml_build_into_impl<uint64_t>(d_seq, n, count, s, packed, k0, k1, v0, v1, scr, d_pos_out, d_mer_out, st,
+                                       d_err, launches);
+}
+
 int sml_sort(Ctx* c, const uint32_t* d_packed, uint64_t count, const SeedDesc& s, uint32_t* d_pos_out,
              uint64_t* d_mer_out, SmlKeys* keep, int slot_base) {
   if (2 * s.w + 1 <= 32) return sml_sort_impl<uint32_t>(c, d_packed, count, s, d_pos_out, d_mer_out, keep, slot_base);

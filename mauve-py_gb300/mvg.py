@@ -37,7 +37,8 @@ EXPORTS = ["mvg_create", "mvg_destroy", "mvg_last_error", "mvg_stream", "mvg_ker
            "mvg_gapdp_batch_dev", "mvg_set_tb_arena", "mvg_probe_int32_peak", "mvg_set_profiling",
            "mvg_stage_times", "mvg_gapdp_banded", "mvg_gapdp_banded_dev", "mvg_set_dp_rows", "mvg_mlp_num_params",
            "mvg_mlp_set_params", "mvg_mlp_get_params", "mvg_band_features_dev", "mvg_mlp_forward_dev",
-           "mvg_mlp_grad_dev", "mvg_mlp_train_step_dev", "mvg_band_propose_dev", "mvg_gapdp_envelope_dev"]
+           "mvg_mlp_grad_dev", "mvg_mlp_train_step_dev", "mvg_band_propose_dev", "mvg_gapdp_envelope_dev",
+           "mvg_sml_build_noalloc"]
 
 TUNING_PATH = os.path.join(HERE, "dp_tuning.json")
 
