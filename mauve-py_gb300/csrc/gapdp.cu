@@ -222,22 +222,30 @@ static int run_dp(Ctx* c, const DpInputs& in, const std::vector<uint32_t>& ids, 
   int64_t nwaves = (int64_t)((total_tb + arena - 1) / arena);
   std::vector<uint32_t> order;
   std::vector<uint64_t> tboff;
-  std::vector<int64_t> wave_begin;
+  std::vector<int64_t> wave_begin, wave_nbig;
   uint64_t arena_need = 0;
   for (;;) {
     order.clear();
     tboff.clear();
     wave_begin.clear();
+    wave_nbig.clear();
     arena_need = 0;
     bool fits = true;
     for (int64_t v = 0; v < nwaves && fits; ++v) {
       wave_begin.push_back((int64_t)order.size());
       uint64_t acc = 0;
-      for (int64_t q = v; q < nwork; q += nwaves) {
-        order.push_back(ids[idx[q]]);
-        tboff.push_back(acc);
-        acc += bytes[idx[q]];
-      }
+      // large problems (solved by a whole CTA) first, then the rest; each part largest first
+      int64_t nb = 0;
+      for (int pass = 0; pass < 2; ++pass)
+        for (int64_t q = v; q < nwork; q += nwaves) {
+          const bool big = (la[ids[idx[q]]] + 32 * rows - 1) / (32 * rows) >= kCoopMinStrips;
+          if (big != (pass == 0)) continue;
+          order.push_back(ids[idx[q]]);
+          tboff.push_back(acc);
+          acc += bytes[idx[q]];
+          nb += big;
+        }
+      wave_nbig.push_back(nb);
       if (acc > arena) fits = false;
       arena_need = std::max(arena_need, acc);
     }
@@ -277,6 +285,7 @@ static int run_dp(Ctx* c, const DpInputs& in, const std::vector<uint32_t>& ids, 
     J.order = d_order + w0;
     J.tb_off = d_tboff + w0;
     J.nwork = (int)(w1 - w0);
+    J.nbig = (int)wave_nbig[wv];
     J.tb = tb;
     J.rowbuf = rowbuf;
     J.rowbuf_stride = rb_stride;
@@ -286,7 +295,8 @@ static int run_dp(Ctx* c, const DpInputs& in, const std::vector<uint32_t>& ids, 
     J.band_half = d_half;
     J.accept = d_accept;
     J.counter = d_counter;
-    MVG_CUDA_TRY(cudaMemsetAsync(d_counter, 0, 4, c->stream));
+    J.err = c->d_err;
+    MVG_CUDA_TRY(cudaMemsetAsync(d_counter, 0, 8, c->stream));
     stage_mark(c, banded ? "dp_banded" : "dp");
     kern<<<grid, kDpThreads, 0, c->stream>>>(J);
     stage_mark(c, "traceback");

@@ -1,15 +1,23 @@
 // The NWSmall wavefront kernel, full or banded (included by gapdp.cu).
 //
-// One warp per problem; persistent warps pull problems from a counter.  The
-// DP matrix is cut into strips of 32*R rows; lane t owns rows [t*R, t*R+R)
-// of the strip and sweeps the strip's columns on an anti-diagonal wavefront
-// (lane t runs t columns behind lane 0).  Each step a lane computes an R x 1
-// column segment: the cells above it arrive from lane t-1 by __shfl_up_sync,
-// the row above the strip comes from a per-warp row buffer written by lane 31
-// of the previous strip.  B codes and row-buffer entries are staged in
-// per-warp shared rings one 32-step chunk ahead.  Traceback nibbles
-// (MU/types.h:30-43: 2 bits M source, 1 bit D<-M, 1 bit I<-M) are packed 8 per
-// word, lane-minor, so each flush is one coalesced 128-byte warp store.
+// The DP matrix is cut into strips of 32*R rows; lane t of a warp owns rows
+// [t*R, t*R+R) of a strip and sweeps the strip's columns on an anti-diagonal
+// wavefront (lane t runs t columns behind lane 0).  Each step a lane computes
+// an R x 1 column segment: the cells above it arrive from lane t-1 by
+// __shfl_up_sync, the row above the strip comes from a row buffer written by
+// lane 31 of the warp that ran the previous strip.  B codes and row-buffer
+// entries are staged in per-warp shared rings one 32-step chunk ahead.
+// Traceback nibbles (MU/types.h:30-43: 2 bits M source, 1 bit D<-M, 1 bit
+// I<-M) are packed 8 per word, lane-minor, so each flush is one coalesced
+// 128-byte warp store.
+//
+// Work split: persistent CTAs first take the large problems (the front of
+// the wave's list, at least kCoopMinStrips strips) one per CTA: warp w runs
+// strips w, w+8, w+16, ... as a pipeline, each warp consuming the bottom row
+// its predecessor publishes in a per-CTA buffer; progress is exchanged
+// through shared-memory counters every 32 steps, and every wait is bounded
+// (a watchdog error instead of a hang).  Then each warp takes small problems
+// on its own.
 //
 // Per cell the recurrences use Hopper/Blackwell DPX max-with-predicate
 // (__vibmax_s32), which yields each maximum and its tie-broken traceback bit
@@ -34,6 +42,9 @@ constexpr int32_t kNeg = -(1 << 29);
 constexpr int32_t kGap = -200;           // half of gap open -400
 constexpr int32_t kMaxPair = 160;        // max NUC_SP + 60 (C/C, G/G)
 constexpr int kDpThreads = 256;
+constexpr int kDpWarps = kDpThreads / 32;
+constexpr int kCoopMinStrips = 16;       // problems with at least this many strips use a whole CTA
+constexpr long long kSpinLimit = 1ll << 26;  // bounded waits (about a second)
 
 enum : uint32_t { TB_MM = 0, TB_DM = 1, TB_IM = 2, TB_MD = 4, TB_MI = 8 };
 
@@ -47,25 +58,27 @@ struct DpJob {
   const uint64_t* oa;
   const uint8_t* sb;
   const uint64_t* ob;
-  const uint32_t* order;   // problem ids of this wave, largest first
+  const uint32_t* order;   // problem ids of this wave: large problems first, each part largest first
   const uint64_t* tb_off;  // byte offset of each wave slot's traceback bits
   int nwork;
+  int nbig;                // the first nbig slots are solved by whole CTAs
   uint32_t* tb;
   int4* rowbuf;
-  int64_t rowbuf_stride;  // int4 entries per warp
+  int64_t rowbuf_stride;  // int4 entries per row buffer (one per warp)
   int32_t* scores;
   uint8_t* end_edge;  // 'M','D','I' per problem
   const int32_t* band_delta;  // banded mode: per problem
   const int32_t* band_half;
   uint8_t* accept;            // banded mode: 1 if the band result is exact
-  unsigned* counter;
+  unsigned* counter;          // [0] large-problem claims (per CTA), [1] small-problem claims (per warp)
+  uint32_t* err;
 };
 
 __host__ __device__ __forceinline__ int tb_words_per_lane(int W, int R) { return band_words_per_lane(W, R); }
 
 template <int R>
 struct DpLane {
-  uint32_t arow[R];      // packed score row of A[i-1] per owned row
+  uint32_t arow[R];             // packed score row of A[i-1] per owned row
   int32_t lM[R], lD[R], lI[R];  // left neighbour (previous column) per row
 };
 
@@ -106,205 +119,290 @@ __device__ __forceinline__ uint32_t dp_column(DpLane<R>& L, int32_t upM, int32_t
   return nibs;
 }
 
+// Shared state of one CTA.
+struct DpShared {
+  uint8_t ringB[kDpWarps][128];
+  int4 ringR[kDpWarps][64];
+  volatile unsigned long long prog[kDpWarps];  // cooperative mode: (strip << 21) | last column published
+  int bound;                                   // cooperative mode: CTA-wide band-exit bound
+  int abort;                                   // cooperative mode: a wait gave up
+  int claim;
+};
+
+// Solves problem slot w.  Strips kstart, kstart + kstep, ... are run by this
+// warp; coop = true when the CTA's warps share the problem.
 template <bool BANDED, int R>
-__global__ void __launch_bounds__(kDpThreads, 2) k_gapdp_t(DpJob J) {
-  constexpr int SR = 32 * R;  // rows per strip
-  __shared__ uint8_t sB[kDpThreads / 32][128];
-  __shared__ int4 sR[kDpThreads / 32][64];
+__device__ void dp_solve(const DpJob& J, DpShared& sh, int w, int kstart, int kstep, bool coop, int4* rowbuf_base,
+                         int4* own_rowbuf) {
+  constexpr int SR = 32 * R;
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
-  const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  int4* rowbuf = J.rowbuf + gw * J.rowbuf_stride;
-  uint8_t* ringB = sB[wib];
-  int4* ringR = sR[wib];
+  uint8_t* ringB = sh.ringB[wib];
+  int4* ringR = sh.ringR[wib];
   const int4 kNegCell = make_int4(kNeg, kNeg, kNeg, 0);
-  for (;;) {
-    int w = 0;
-    if (lane == 0) w = (int)atomicAdd(J.counter, 1u);
-    w = __shfl_sync(0xffffffffu, w, 0);
-    if (w >= J.nwork) break;
-    const uint32_t p = J.order[w];
-    const uint64_t a0 = J.oa[p], b0 = J.ob[p];
-    const int LA = (int)(J.oa[p + 1] - a0), LB = (int)(J.ob[p + 1] - b0);
-    const uint8_t* A = J.sa + a0;
-    const uint8_t* B = J.sb + b0;
-    uint32_t* tbs = J.tb + J.tb_off[w] / 4;
-    const int nstrips = (LA + SR - 1) / SR;
-    const int end_strip = (LA - 1) / SR;
-    const int end_lane = ((LA - 1) % SR) / R;
-    const int end_r = (LA - 1) % R;
-    const Band band = BANDED ? make_band(LA, LB, J.band_delta[p], J.band_half[p], SR) : make_full(LA, LB, SR);
-    int32_t bound = kNeg;  // best score of any path leaving the band
-    int prev_lo = 1, prev_hi = LB;  // column range of the strip above
+  const uint32_t p = J.order[w];
+  const uint64_t a0 = J.oa[p], b0 = J.ob[p];
+  const int LA = (int)(J.oa[p + 1] - a0), LB = (int)(J.ob[p + 1] - b0);
+  const uint8_t* A = J.sa + a0;
+  const uint8_t* B = J.sb + b0;
+  const int nstrips = (LA + SR - 1) / SR;
+  const int end_strip = (LA - 1) / SR;
+  const int end_lane = ((LA - 1) % SR) / R;
+  const int end_r = (LA - 1) % R;
+  const Band band = BANDED ? make_band(LA, LB, J.band_delta[p], J.band_half[p], SR) : make_full(LA, LB, SR);
+  int32_t bound = kNeg;  // best score of any path leaving the band (this warp's part)
+  uint32_t* tbs = J.tb + J.tb_off[w] / 4;
+  for (int k = 0; k < kstart; ++k) tbs += (int64_t)tb_words_per_lane(band_hi(band, k) - band_lo(band, k) + 1, R) * 32;
 
-    for (int k = 0; k < nstrips; ++k) {
-      const int row0 = k * SR;
-      int jlo = 1, jhi = LB, next_lo = 1;
-      if (BANDED) {
-        jlo = band_lo(band, k);
-        jhi = band_hi(band, k);
-        next_lo = k + 1 < nstrips ? band_lo(band, k + 1) : 1;
+  for (int k = kstart; k < nstrips; k += kstep) {
+    const int row0 = k * SR;
+    const int jlo = band_lo(band, k), jhi = band_hi(band, k);
+    const int next_lo = k + 1 < nstrips ? band_lo(band, k + 1) : 1;
+    const int prev_lo = k > 0 ? band_lo(band, k - 1) : 1, prev_hi = k > 0 ? band_hi(band, k - 1) : LB;
+    const int W = jhi - jlo + 1;
+    const int S = W + 31;
+    const int wpl = tb_words_per_lane(W, R);
+    // row buffers: the one this strip reads (previous strip's bottom row) and the one it writes
+    int4* rb_in = coop ? rowbuf_base + (int64_t)((k - 1) & (kDpWarps - 1)) * J.rowbuf_stride : own_rowbuf;
+    int4* rb_out = coop ? rowbuf_base + (int64_t)(k & (kDpWarps - 1)) * J.rowbuf_stride : own_rowbuf;
+    const int producer = (k - 1) & (kDpWarps - 1);
+    // cooperative mode: wait until the previous strip published column `col`
+    auto wait_for = [&](int col) -> bool {
+      if (!coop || k == 0) return true;
+      if (col > prev_hi) col = prev_hi;
+      if (col < prev_lo) return true;
+      const unsigned long long need = ((unsigned long long)(k - 1) << 21) | (unsigned long long)col;
+      bool ok = true;
+      if (lane == 0) {
+        long long spins = 0;
+        while (sh.prog[producer] < need) {
+          if (*(volatile int*)&sh.abort || ++spins > kSpinLimit) {
+            ok = false;
+            break;
+          }
+        }
+        if (!ok) {
+          *(volatile int*)&sh.abort = 1;
+          set_error(J.err, kDevWatchdog);
+        }
+        __threadfence_block();
       }
-      const int W = jhi - jlo + 1;
-      const int S = W + 31;
-      const int wpl = tb_words_per_lane(W, R);
-      DpLane<R> L;
+      return __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
+    };
+    auto publish = [&](int col) {
+      if (!coop) return;
+      __syncwarp();
+      if (lane == 31) {
+        __threadfence_block();
+        sh.prog[wib] = ((unsigned long long)k << 21) | (unsigned long long)col;
+      }
+    };
+    DpLane<R> L;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const int i = row0 + lane * R + r + 1;
+      L.arow[r] = c_score_rows[(i <= LA ? A[i - 1] : 0u) & 3u];
+    }
+    const int32_t goA0 = (row0 + lane * R + 1 == 1) ? 0 : kGap;
+    // Row above this strip at absolute column x: row 0 for the first strip,
+    // else the previous strip's computed columns, its left boundary or -inf.
+    auto above = [&](int x) -> int4 {
+      if (k == 0) return x == 0 ? make_int4(0, kNeg, kNeg, 0) : make_int4(kNeg, kNeg, 0, 0);
+      if (x >= prev_lo && x <= prev_hi) return rb_in[x];
+      if (x == prev_lo - 1) return prev_lo == 1 ? make_int4(kNeg, 0, kNeg, 0) : kNegCell;
+      return kNegCell;
+    };
+    if (!wait_for(jlo + 63)) return;
+    // prime the rings: B[jlo-1 .. jlo+62], row above at columns jlo .. jlo+63
+    __syncwarp();
+    ringB[lane] = jlo - 1 + lane < LB ? B[jlo - 1 + lane] : 0;
+    ringB[32 + lane] = jlo + 31 + lane < LB ? B[jlo + 31 + lane] : 0;
+    ringR[lane] = above(jlo + lane);
+    ringR[32 + lane] = above(jlo + 32 + lane);
+    const int4 dg0 = above(jlo - 1);
+    __syncwarp();
+    // left state (column jlo-1) per row: column 0 = (NEG, 0, NEG), else -inf
+    const int32_t leftD = jlo == 1 ? 0 : kNeg;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      L.lM[r] = kNeg;
+      L.lD[r] = leftD;
+      L.lI[r] = kNeg;
+    }
+    int32_t pubM = kNeg, pubD = leftD, pubI = kNeg;  // bottom row, last computed column
+    int32_t upM = kNeg, upD = kNeg, upI = kNeg;      // row above, current column
+    uint32_t acc = 0;
+    const bool bottom_exit = BANDED && lane == 31 && row0 + SR < LA;
+    const int32_t rem_rows = LA - (row0 + SR);
+    const bool writes_row = k + 1 < nstrips;
+    bool alive = true;
+
+    // one step; `checked` handles the wavefront's ramp-up and ramp-down
+    auto step = [&](int s, bool checked) {
+      if ((s & 31) == 0 && s > 0) {
+        if ((s & 31) == 0 && writes_row && s >= 32) publish(jlo + s - 32);  // columns <= jlo+s-32 are written
+        if (!wait_for(jlo + s + 63)) {
+          alive = false;
+          return;
+        }
+        // refill one chunk ahead: B at offsets s+32 .. s+63, row above at s+32 .. s+63
+        __syncwarp();
+        const int xb = jlo - 1 + s + 32 + lane;
+        ringB[(s + 32 + lane) & 127] = xb < LB ? B[xb] : 0;
+        ringR[(s + 32 + lane) & 63] = above(jlo + s + 32 + lane);
+        __syncwarp();
+      }
+      const int jj = s - lane;  // column offset inside the strip
+      const int j = jlo + jj;   // absolute column
+      const int32_t rM = __shfl_up_sync(0xffffffffu, pubM, 1);
+      const int32_t rD = __shfl_up_sync(0xffffffffu, pubD, 1);
+      const int32_t rI = __shfl_up_sync(0xffffffffu, pubI, 1);
+      const int4 v = ringR[s & 63];
+      int32_t dgM = upM, dgD = upD, dgI = upI;
+      if (s == 0 && lane == 0) {
+        dgM = dg0.x;
+        dgD = dg0.y;
+        dgI = dg0.z;
+      }
+      upM = lane == 0 ? v.x : rM;
+      upD = lane == 0 ? v.y : rD;
+      upI = lane == 0 ? v.z : rI;
+      const uint32_t bsel = (uint32_t)ringB[jj & 127] | 0x4440u;
+      const int32_t goB = j == 1 ? 0 : kGap;
+      uint32_t nibs = 0;
+      if (!checked || (jj >= 0 && jj < W)) {
+        nibs = dp_column<R>(L, upM, upD, dgM, dgD, dgI, bsel, goB, goA0);
+        if (checked && s == 0 && lane == 0 && k == 0 && LA == 1) {
+          // NWSmall's last-row special case (MU/nwsmall.cpp:616-624) with
+          // LA == 1: M(1,1) adds the open and close of position 0, and the
+          // close of a one-position profile is not zeroed.
+          L.lM[0] = (int32_t)__byte_perm(L.arow[0], 0u, bsel) - kScoreBias + kGap;
+          nibs = (nibs & ~3u) | TB_DM;
+        }
+        pubM = L.lM[R - 1];
+        pubD = L.lD[R - 1];
+        pubI = L.lI[R - 1];
+        if (lane == 31 && writes_row) rb_out[j] = make_int4(pubM, pubD, pubI, 0);
+        if (BANDED && bottom_exit && j < next_lo) {
+          const int32_t best = max(pubM, max(pubD, pubI));
+          bound = max(bound, best + kMaxPair * min(rem_rows, LB - j));
+        }
+      } else if (jj == -1) {
+        pubM = kNeg;
+        pubD = leftD;
+        pubI = kNeg;
+      }
+      if (R == 8) {
+        tbs[s * 32 + lane] = nibs;
+      } else {  // R == 4: one word every 2 steps
+        acc |= nibs << (16 * (s & 1));
+        if ((s & 1) || s == S - 1) {
+          tbs[(s >> 1) * 32 + lane] = acc;
+          acc = 0;
+        }
+      }
+    };
+
+    if (W >= 32) {
+      int s = 0;
+      for (; s < 31 && alive; ++s) step(s, true);
+      for (; s < W && alive; ++s) step(s, false);
+      for (; s < S && alive; ++s) step(s, true);
+    } else {
+      for (int s = 0; s < S && alive; ++s) step(s, true);
+    }
+    if (!alive) return;
+    if (writes_row) publish(jhi);  // whole bottom row written
+    __syncwarp();
+    // after the sweep each lane holds its rows' cells at column jhi
+    if (k == end_strip && lane == end_lane) {
+      int32_t eM = kNeg, eD = kNeg, eI = kNeg;
+#pragma unroll
+      for (int r = 0; r < R; ++r)
+        if (r == end_r) {
+          eM = L.lM[r];
+          eD = L.lD[r];
+          eI = L.lI[r];
+        }
+      int32_t sc = eM;
+      char e = 'M';
+      if (eD > sc) {
+        sc = eD;
+        e = 'D';
+      }
+      if (eI > sc) {
+        sc = eI;
+        e = 'I';
+      }
+      J.scores[p] = sc;
+      J.end_edge[p] = (uint8_t)e;
+    }
+    if (BANDED && jhi < LB) {  // right-edge exits: an I step leaves the band
 #pragma unroll
       for (int r = 0; r < R; ++r) {
         const int i = row0 + lane * R + r + 1;
-        L.arow[r] = c_score_rows[(i <= LA ? A[i - 1] : 0u) & 3u];
-      }
-      const int32_t goA0 = (row0 + lane * R + 1 == 1) ? 0 : kGap;
-      // Row above this strip at absolute column x: row 0 for the first strip,
-      // else the previous strip's computed columns, its left boundary or -inf.
-      auto above = [&](int x) -> int4 {
-        if (k == 0) return x == 0 ? make_int4(0, kNeg, kNeg, 0) : make_int4(kNeg, kNeg, 0, 0);
-        if (x >= prev_lo && x <= prev_hi) return rowbuf[x];
-        if (x == prev_lo - 1) return prev_lo == 1 ? make_int4(kNeg, 0, kNeg, 0) : kNegCell;
-        return kNegCell;
-      };
-      // prime the rings: B[jlo-1 .. jlo+62], row above at columns jlo .. jlo+63
-      __syncwarp();
-      ringB[lane] = jlo - 1 + lane < LB ? B[jlo - 1 + lane] : 0;
-      ringB[32 + lane] = jlo + 31 + lane < LB ? B[jlo + 31 + lane] : 0;
-      ringR[lane] = above(jlo + lane);
-      ringR[32 + lane] = above(jlo + 32 + lane);
-      const int4 dg0 = above(jlo - 1);
-      __syncwarp();
-      // left state (column jlo-1) per row: column 0 = (NEG, 0, NEG), else -inf
-      const int32_t leftD = jlo == 1 ? 0 : kNeg;
-#pragma unroll
-      for (int r = 0; r < R; ++r) {
-        L.lM[r] = kNeg;
-        L.lD[r] = leftD;
-        L.lI[r] = kNeg;
-      }
-      int32_t pubM = kNeg, pubD = leftD, pubI = kNeg;  // bottom row, last computed column
-      int32_t upM = kNeg, upD = kNeg, upI = kNeg;      // row above, current column
-      uint32_t acc = 0;
-      const bool bottom_exit = BANDED && lane == 31 && row0 + SR < LA;
-      const int32_t rem_rows = LA - (row0 + SR);
-
-      // one step; CHECKED handles the wavefront's ramp-up and ramp-down
-      auto step = [&](int s, bool checked) {
-        if ((s & 31) == 0 && s > 0) {
-          // refill one chunk ahead: B at offsets s+32 .. s+63, row above at s+32 .. s+63
-          __syncwarp();
-          const int xb = jlo - 1 + s + 32 + lane;
-          ringB[(s + 32 + lane) & 127] = xb < LB ? B[xb] : 0;
-          ringR[(s + 32 + lane) & 63] = above(jlo + s + 32 + lane);
-          __syncwarp();
-        }
-        const int jj = s - lane;  // column offset inside the strip
-        const int j = jlo + jj;   // absolute column
-        const int32_t rM = __shfl_up_sync(0xffffffffu, pubM, 1);
-        const int32_t rD = __shfl_up_sync(0xffffffffu, pubD, 1);
-        const int32_t rI = __shfl_up_sync(0xffffffffu, pubI, 1);
-        const int4 v = ringR[s & 63];
-        int32_t dgM = upM, dgD = upD, dgI = upI;
-        if (s == 0 && lane == 0) {
-          dgM = dg0.x;
-          dgD = dg0.y;
-          dgI = dg0.z;
-        }
-        upM = lane == 0 ? v.x : rM;
-        upD = lane == 0 ? v.y : rD;
-        upI = lane == 0 ? v.z : rI;
-        const uint32_t bsel = (uint32_t)ringB[jj & 127] | 0x4440u;
-        const int32_t goB = j == 1 ? 0 : kGap;
-        uint32_t nibs = 0;
-        if (!checked || (jj >= 0 && jj < W)) {
-          nibs = dp_column<R>(L, upM, upD, dgM, dgD, dgI, bsel, goB, goA0);
-          if (checked && s == 0 && lane == 0 && k == 0 && LA == 1) {
-            // NWSmall's last-row special case (MU/nwsmall.cpp:616-624) with
-            // LA == 1: M(1,1) adds the open and close of position 0, and the
-            // close of a one-position profile is not zeroed.
-            L.lM[0] = (int32_t)__byte_perm(L.arow[0], 0u, bsel) - kScoreBias + kGap;
-            nibs = (nibs & ~3u) | TB_DM;
-          }
-          pubM = L.lM[R - 1];
-          pubD = L.lD[R - 1];
-          pubI = L.lI[R - 1];
-          if (lane == 31 && k + 1 < nstrips) rowbuf[j] = make_int4(pubM, pubD, pubI, 0);
-          if (BANDED && bottom_exit && j < next_lo) {
-            const int32_t best = max(pubM, max(pubD, pubI));
-            bound = max(bound, best + kMaxPair * min(rem_rows, LB - j));
-          }
-        } else if (jj == -1) {
-          pubM = kNeg;
-          pubD = leftD;
-          pubI = kNeg;
-        }
-        if (R == 8) {
-          tbs[s * 32 + lane] = nibs;
-        } else {  // R == 4: one word every 2 steps
-          acc |= nibs << (16 * (s & 1));
-          if ((s & 1) || s == S - 1) {
-            tbs[(s >> 1) * 32 + lane] = acc;
-            acc = 0;
-          }
-        }
-      };
-
-      if (W >= 32) {
-        int s = 0;
-        for (; s < 31; ++s) step(s, true);
-        for (; s < W; ++s) step(s, false);
-        for (; s < S; ++s) step(s, true);
-      } else {
-        for (int s = 0; s < S; ++s) step(s, true);
-      }
-      __syncwarp();
-      // after the sweep each lane holds its rows' cells at column jhi
-      if (k == end_strip && lane == end_lane) {
-        int32_t eM = kNeg, eD = kNeg, eI = kNeg;
-#pragma unroll
-        for (int r = 0; r < R; ++r)
-          if (r == end_r) {
-            eM = L.lM[r];
-            eD = L.lD[r];
-            eI = L.lI[r];
-          }
-        int32_t sc = eM;
-        char e = 'M';
-        if (eD > sc) {
-          sc = eD;
-          e = 'D';
-        }
-        if (eI > sc) {
-          sc = eI;
-          e = 'I';
-        }
-        J.scores[p] = sc;
-        J.end_edge[p] = (uint8_t)e;
-      }
-      if (BANDED && jhi < LB) {  // right-edge exits: an I step leaves the band
-#pragma unroll
-        for (int r = 0; r < R; ++r) {
-          const int i = row0 + lane * R + r + 1;
-          if (i <= LA) {
-            const int32_t best = max(L.lM[r], max(L.lD[r], L.lI[r]));
-            bound = max(bound, best + kMaxPair * min(LA - i, LB - jhi));
-          }
+        if (i <= LA) {
+          const int32_t best = max(L.lM[r], max(L.lD[r], L.lI[r]));
+          bound = max(bound, best + kMaxPair * min(LA - i, LB - jhi));
         }
       }
-      tbs += (int64_t)wpl * 32;
-      prev_lo = jlo;
-      prev_hi = jhi;
     }
-    if (BANDED) {
-      // paths along row 0 past the band, or down column 0 past it
-      if (lane == 0) {
-        const int hi0 = band_hi(band, 0);
-        if (hi0 < LB) bound = max(bound, kMaxPair * min(LA, LB - hi0));
-        const int last_col0 = band_last_row_at_col1(band, LA);
-        if (last_col0 < LA) bound = max(bound, kMaxPair * min(LA - last_col0, LB));
-      }
+    // advance the traceback pointer past this warp's strip and the skipped ones
+    for (int q = k; q < k + kstep && q < nstrips; ++q)
+      tbs += (int64_t)tb_words_per_lane(band_hi(band, q) - band_lo(band, q) + 1, R) * 32;
+  }
+  if (BANDED) {
+    // paths along row 0 past the band, or down column 0 past it (added once)
+    if (lane == 0 && kstart == 0) {
+      const int hi0 = band_hi(band, 0);
+      if (hi0 < LB) bound = max(bound, kMaxPair * min(LA, LB - hi0));
+      const int last_col0 = band_last_row_at_col1(band, LA);
+      if (last_col0 < LA) bound = max(bound, kMaxPair * min(LA - last_col0, LB));
+    }
 #pragma unroll
-      for (int d = 16; d > 0; d >>= 1) bound = max(bound, __shfl_xor_sync(0xffffffffu, bound, d));
+    for (int d = 16; d > 0; d >>= 1) bound = max(bound, __shfl_xor_sync(0xffffffffu, bound, d));
+    if (coop) {
+      if (lane == 0) atomicMax(&sh.bound, bound);
+    } else {
       __syncwarp();
       if (lane == 0) J.accept[p] = J.scores[p] > bound ? 1 : 0;
     }
+  }
+}
+
+template <bool BANDED, int R>
+__global__ void __launch_bounds__(kDpThreads, 2) k_gapdp_t(DpJob J) {
+  __shared__ DpShared sh;
+  const int lane = threadIdx.x & 31;
+  const int wib = threadIdx.x >> 5;
+  int4* rowbuf_cta = J.rowbuf + (int64_t)blockIdx.x * kDpWarps * J.rowbuf_stride;
+  int4* own_rowbuf = rowbuf_cta + (int64_t)wib * J.rowbuf_stride;
+  // phase 1: large problems, one per CTA, strips pipelined across the warps
+  for (;;) {
+    if (threadIdx.x == 0) sh.claim = (int)atomicAdd(&J.counter[0], 1u);
+    if (lane == 0) sh.prog[wib] = 0ull;
+    if (threadIdx.x == 0) {
+      sh.bound = kNeg;
+      sh.abort = 0;
+    }
+    __syncthreads();
+    const int w = sh.claim;
+    if (w >= J.nbig) break;
+    dp_solve<BANDED, R>(J, sh, w, wib, kDpWarps, true, rowbuf_cta, own_rowbuf);
+    __syncthreads();
+    if (BANDED && threadIdx.x == 0) {
+      const uint32_t p = J.order[w];
+      J.accept[p] = (!sh.abort && J.scores[p] > sh.bound) ? 1 : 0;
+    }
+    __syncthreads();
+  }
+  // phase 2: small problems, one per warp
+  for (;;) {
+    int w = 0;
+    if (lane == 0) w = J.nbig + (int)atomicAdd(&J.counter[1], 1u);
+    w = __shfl_sync(0xffffffffu, w, 0);
+    if (w >= J.nwork) break;
+    dp_solve<BANDED, R>(J, sh, w, 0, 1, false, rowbuf_cta, own_rowbuf);
   }
 }
 
