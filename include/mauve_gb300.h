@@ -190,9 +190,10 @@ int mvg_band_propose_dev(mvg_handle h, const uint8_t* d_seq_a, const uint64_t* d
  * mixed sizes that fit it.  Default: no bound beyond the 60% cap. */
 int mvg_set_tb_arena(mvg_handle h, uint64_t bytes);
 
-/* Gap-DP kernel shape: rows per lane (4 or 8; strips of 32*rows rows).  The
- * default is the tuned choice committed in mauve-py_gb300/dp_tuning.json. */
-int mvg_set_dp_rows(mvg_handle h, int rows);
+/* Gap-DP kernel shape: rows per lane for the full DP (4 or 8) and for banded
+ * passes (2, 4 or 8); strips are 32*rows rows.  The Python binding applies
+ * the tuned choice committed in mauve-py_gb300/dp_tuning.json. */
+int mvg_set_dp_rows(mvg_handle h, int full_rows, int band_rows);
 
 /* Per-stage timing with CUDA events on the handle's stream (off by default;
  * no extra synchronisation).  After a call, mvg_stage_times gives the stage

@@ -50,6 +50,7 @@ template __global__ void k_gapdp_t<false, 4>(DpJob);
 template __global__ void k_gapdp_t<true, 4>(DpJob);
 template __global__ void k_gapdp_t<false, 8>(DpJob);
 template __global__ void k_gapdp_t<true, 8>(DpJob);
+template __global__ void k_gapdp_t<true, 2>(DpJob);
 
 // BitTraceBack from (LA, LB); writes the path reversed at the end of the
 // problem's path slot and its length.  Banded problems index their strips
@@ -186,7 +187,9 @@ static int run_dp(Ctx* c, const DpInputs& in, const std::vector<uint32_t>& ids, 
   const int64_t nwork = (int64_t)ids.size();
   if (nwork == 0) return 0;
   const bool banded = d_delta != nullptr;
-  const int rows = c->dp_rows;
+  // banded passes may use shorter strips: the staircase of a narrow band
+  // widens by the diagonal's drift over one strip
+  const int rows = banded ? c->band_rows : c->dp_rows;
   std::vector<uint64_t> bytes(nwork), cells(nwork);
   int64_t maxlb = 0;
   for (int64_t w = 0; w < nwork; ++w) {
@@ -256,8 +259,9 @@ static int run_dp(Ctx* c, const DpInputs& in, const std::vector<uint32_t>& ids, 
 
   int dev_sms = 0;
   MVG_CUDA_TRY(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, c->device));
-  void (*kern)(DpJob) = rows == 8 ? (banded ? k_gapdp_t<true, 8> : k_gapdp_t<false, 8>)
-                                  : (banded ? k_gapdp_t<true, 4> : k_gapdp_t<false, 4>);
+  void (*kern)(DpJob) = rows == 8   ? (banded ? k_gapdp_t<true, 8> : k_gapdp_t<false, 8>)
+                        : rows == 4 ? (banded ? k_gapdp_t<true, 4> : k_gapdp_t<false, 4>)
+                                    : k_gapdp_t<true, 2>;
   int bps = 0;
   MVG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kern, kDpThreads, 0));
   if (bps < 1) bps = 1;
@@ -393,7 +397,7 @@ int gapdp_banded_dev(Ctx* c, const uint8_t* d_sa, const uint64_t* d_oa, const ui
   uint64_t bc = 0;
   for (int64_t p = 0; p < nprob; ++p) {
     if (hv[p] < 0) return report_error(MVG_ERR_ARG, "negative band half-width");
-    bc += band_cells(make_band((int)la[p], (int)lb[p], dv[p], hv[p], 32 * c->dp_rows));
+    bc += band_cells(make_band((int)la[p], (int)lb[p], dv[p], hv[p], 32 * c->band_rows));
   }
   int32_t* d_delta = (int32_t*)c->ws.get(c, 23, (size_t)nprob * 4);
   int32_t* d_half = (int32_t*)c->ws.get(c, 25, (size_t)nprob * 4);

@@ -294,10 +294,11 @@ __device__ void dp_solve(const DpJob& J, DpShared& sh, int w, int kstart, int ks
       }
       if (R == 8) {
         tbs[s * 32 + lane] = nibs;
-      } else {  // R == 4: one word every 2 steps
-        acc |= nibs << (16 * (s & 1));
-        if ((s & 1) || s == S - 1) {
-          tbs[(s >> 1) * 32 + lane] = acc;
+      } else {  // 8/R steps per 32-bit word
+        constexpr int kPer = 8 / R;
+        acc |= nibs << (4 * R * (s % kPer));
+        if ((s % kPer) == kPer - 1 || s == S - 1) {
+          tbs[(s / kPer) * 32 + lane] = acc;
           acc = 0;
         }
       }

@@ -34,7 +34,8 @@ struct Ctx {
   uint64_t* h_scalars = nullptr; // pinned scalars for small device->host reads
   uint64_t launches = 0;
   uint64_t tb_arena = ~0ull;  // capped per call at 60% of free device memory
-  int dp_rows = 8;            // gap-DP rows per lane (4 or 8), see dp_tuning.h
+  int dp_rows = 8;            // full gap-DP rows per lane (4 or 8)
+  int band_rows = 4;          // banded gap-DP rows per lane (2, 4 or 8)
   Workspace ws;
   MatchStats stats;
   bool profiling = false;

@@ -73,7 +73,7 @@ def load_library(path=LIB_PATH):
         "mvg_probe_int32_peak": (ci, [vp, ctypes.POINTER(ctypes.c_double)]),
         "mvg_gapdp_banded": (ci, [vp, vp, vp, vp, vp, i64, vp, vp, vp, vp, vp, vp, vp, ctypes.POINTER(u64)]),
         "mvg_gapdp_banded_dev": (ci, [vp, vp, vp, vp, vp, i64, vp, vp, vp, vp, vp, vp, vp, ctypes.POINTER(u64)]),
-        "mvg_set_dp_rows": (ci, [vp, ci]),
+        "mvg_set_dp_rows": (ci, [vp, ci, ci]),
         "mvg_gapdp_envelope_dev": (ci, [vp, vp, vp, vp, vp, i64, vp, vp]),
         "mvg_mlp_num_params": (i64, []),
         "mvg_mlp_set_params": (ci, [vp, vp]),
@@ -139,13 +139,17 @@ class Context:
         _check(L.mvg_create(ctypes.byref(h), device))
         self._h = h
         self.device = device
+        self.full_rows, self.band_rows = 8, 4
         if os.path.exists(TUNING_PATH):  # committed autotuner choice
             import json
             with open(TUNING_PATH) as f:
-                self.set_dp_rows(int(json.load(f).get("rows_per_lane", 8)))
+                t = json.load(f)
+            self.set_dp_rows(int(t.get("full_rows_per_lane", 8)), int(t.get("band_rows_per_lane", 4)))
 
-    def set_dp_rows(self, rows):
-        _check(load_library().mvg_set_dp_rows(self._h, int(rows)))
+    def set_dp_rows(self, full_rows, band_rows=None):
+        band_rows = self.band_rows if band_rows is None else band_rows
+        _check(load_library().mvg_set_dp_rows(self._h, int(full_rows), int(band_rows)))
+        self.full_rows, self.band_rows = int(full_rows), int(band_rows)
 
     @property
     def handle(self):

@@ -81,6 +81,12 @@ def subset_host(batch, s, e):
     return sa, oa, sb, ob
 
 
+def subset_host_idx(batch, idx):
+    sa = batch.sa.cpu().numpy()
+    sb = batch.sb.cpu().numpy()
+    return subset(sa, batch.oa.astype(np.int64), sb, batch.ob.astype(np.int64), idx)
+
+
 def timed_banded(ctx, batch, delta, half):
     """(seconds, used-band flags, cells) of the banded DP with fallback, paths on device."""
     import torch
@@ -168,28 +174,19 @@ def train(args):
                 losses.append((step, loss))
         print("epoch %d loss %.4f" % (ep, losses[-1][1] if losses else float("nan")), flush=True)
     train_s = time.time() - t0
-    # calibrate alpha / beta on the validation split: fewest cells incl. fallback
-    vi = torch.from_numpy(val_idx).to(dev)
-    out = torch.zeros((len(val_idx), 2), dtype=torch.float32, device=dev)
-    net.forward_dev(X.index_select(0, vi).contiguous().data_ptr(), len(val_idx), out.data_ptr())
-    o = out.cpu().numpy()
-    la_v, lb_v = tr.la[val_idx], tr.lb[val_idx]
-    _, dstar, hstar = bandnet.labels_from_full_dp(la_v, lb_v, sc_tr[val_idx], env_tr[val_idx])
+    # calibrate alpha / beta on the validation split by timing the exact
+    # banded DP (with its fallbacks) for each candidate margin
+    import synth  # noqa: F401
+    vb = DeviceBatch(*subset_host_idx(tr, np.sort(val_idx)), dev)
     best = None
-    srows = 32 * 8
     for alpha in (1.0, 1.25, 1.5, 2.0):
         for beta in (0.0, 16.0, 48.0, 128.0):
-            d = np.rint(o[:, 0] * bandnet.DELTA_SCALE).astype(np.int64)
-            h = np.ceil(alpha * np.expm1(np.minimum(o[:, 1], 13)) + beta).astype(np.int64)
-            ok = (np.abs(d - dstar) + hstar <= h)  # band covers the label band: a good proxy for acceptance
-            cost = np.where(ok, 0, la_v * lb_v).astype(float)
-            sample = np.arange(0, len(la_v), max(1, len(la_v) // 2000))
-            cost_band = band_cells(la_v[sample], lb_v[sample], d[sample], h[sample], srows) * (len(la_v) / len(sample))
-            total = cost_band + cost.sum()
-            if best is None or total < best[0]:
-                best = (total, alpha, beta, float(ok.mean()))
-    _, alpha, beta, cover = best
-    print("calibrated alpha %.2f beta %.1f (validation cover %.3f)" % (alpha, beta, cover), flush=True)
+            d, h = net.propose_dev(*vb.ptrs(), vb.n, alpha, beta)
+            secs, used, cells, *_ = timed_banded(ctx, vb, d, h)
+            if best is None or secs < best[0]:
+                best = (secs, alpha, beta, float(used.mean()), cells)
+    _, alpha, beta, acc_v, _ = best
+    print("calibrated alpha %.2f beta %.1f (validation accept %.3f)" % (alpha, beta, acc_v), flush=True)
     params = net.get_params()
     # held-out evaluation: full vs learned band vs band without the network
     res = {"train_gaps": tr.n, "eval_gaps": ev.n, "train_seconds": train_s, "steps": step,

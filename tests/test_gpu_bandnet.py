@@ -30,9 +30,9 @@ def _batch_ptrs(sa, oa, sb, ob):
     return t, [x.data_ptr() for x in t]
 
 
-@pytest.mark.parametrize("rows", [4, 8])
-def test_banded_output_identical_to_full(ctx, rows):
-    ctx.set_dp_rows(rows)
+@pytest.mark.parametrize("rows,band_rows", [(4, 2), (8, 4), (8, 8)])
+def test_banded_output_identical_to_full(ctx, rows, band_rows):
+    ctx.set_dp_rows(rows, band_rows)
     try:
         rng = np.random.default_rng(rows)
         sa, oa, sb, ob = synth.gap_batch_recoded(seed=11, nprob=300, lmin=1, lmax=1500)
@@ -48,7 +48,7 @@ def test_banded_output_identical_to_full(ctx, rows):
         oscores, _, _, _ = O.nw_batch(sa, oa, sb, ob, with_paths=False)
         np.testing.assert_array_equal(s_full, oscores)
     finally:
-        ctx.set_dp_rows(8)
+        ctx.set_dp_rows(8, 4)
 
 
 def test_band_with_label_width_is_accepted_on_close_gaps(ctx):
