@@ -47,8 +47,8 @@ def run(args):
         res["full"][rows] = {"seconds": secs, "gcups": full.cells / secs / 1e9}
     best_full = max(res["full"], key=lambda r: res["full"][r]["gcups"])
     band = DeviceBatch(*synth.gap_batch_recoded(seed=22, nprob=args.nprob * 5), dev)
-    if os.path.exists(WEIGHTS):
-        w = np.load(WEIGHTS)
+    if os.path.exists(args.weights):
+        w = np.load(args.weights)
         net = bandnet.BandNet(ctx, params=w["params"])
         d, h = net.propose_dev(*band.ptrs(), band.n, float(w["alpha"]), float(w["beta"]))
         src = "network"
@@ -74,6 +74,7 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--nprob", type=int, default=4000)
     ap.add_argument("--out", default=os.path.join(HERE, "dp_tuning.json"))
+    ap.add_argument("--weights", default=WEIGHTS)
     run(ap.parse_args())
 
 
