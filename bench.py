@@ -146,6 +146,75 @@ def cpu_gapdp_gcups(sa, oa, sb, ob, sample, threads):
     return cells / dt / 1e9, cells, dt
 
 
+WEIGHTS = os.path.join(ROOT, "mauve-py_gb300", "bandnet_weights.npz")
+LB_NPROB = 20_000
+
+
+def learned_band_section(ctx, args, dev, stream, rank):
+    """Plain full DP vs the learned band (network proposal + banded DP with
+    exactness check + full-DP fallback) on gaps drawn like the recoded-genome
+    pair's; both timed with CUDA events over whole calls, outputs compared."""
+    if not os.path.exists(WEIGHTS):
+        return None
+    import torch
+
+    import bandnet
+    import synth
+    w = np.load(WEIGHTS)
+    net = bandnet.BandNet(ctx, params=w["params"])
+    alpha, beta = float(w["alpha"]), float(w["beta"])
+    sa, oa, sb, ob = synth.gap_batch_recoded(seed=1000 + rank, nprob=LB_NPROB)
+    n = len(oa) - 1
+    la, lb = np.diff(oa), np.diff(ob)
+    cells = float(np.sum(la * lb))
+    path_off = np.zeros(n + 1, np.uint64)
+    path_off[1:] = np.cumsum(la + lb)
+    t = [torch.from_numpy(x).to(dev) for x in (sa, oa.astype(np.int64), sb, ob.astype(np.int64),
+                                             path_off.view(np.int64))]
+    ptrs = [x.data_ptr() for x in t[:4]]
+    bufs = []
+    for _ in range(2):
+        bufs.append((torch.zeros(n, dtype=torch.int32, device=dev),
+                     torch.zeros(int(path_off[-1]) + 16, dtype=torch.uint8, device=dev),
+                     torch.zeros(n, dtype=torch.int64, device=dev)))
+
+    def full(b):
+        ctx.gap_align_batch_dev(*ptrs, n, b[0].data_ptr(), b[1].data_ptr(), t[4].data_ptr(), b[2].data_ptr())
+
+    def learned(b):
+        d, h = net.propose_dev(*ptrs, n, alpha, beta)
+        return ctx.gap_align_banded_dev(*ptrs, n, d, h, b[0].data_ptr(), b[1].data_ptr(), t[4].data_ptr(),
+                                        b[2].data_ptr())
+
+    def timed(fn, b, reps):
+        out, ms = None, []
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record(stream)
+            out = fn(b)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        return min(ms), out
+
+    full(bufs[0])
+    learned(bufs[1])  # warm-up
+    ms_full, _ = timed(full, bufs[0], 3)
+    ms_band, (used, band_cells) = timed(learned, bufs[1], 3)
+    identical = all(bool(torch.equal(x, y)) for x, y in zip(bufs[0], bufs[1]))
+    return {
+        "workload": "%d gaps drawn like the recoded-genome pair's (lengths log-uniform 20-5000; 90%% at 0.5-3%% "
+                    "substitutions, 10%% divergent)" % n,
+        "cells_full": cells, "plain_full_ms": round(ms_full, 3), "plain_full_gcups": round(cells / ms_full / 1e6, 2),
+        "learned_ms": round(ms_band, 3), "learned_effective_gcups": round(cells / ms_band / 1e6, 2),
+        "speedup_vs_plain": round(ms_full / ms_band, 3), "accept_rate": round(float(used.mean()), 4),
+        "fallback_rate": round(1 - float(used.mean()), 4), "cells_computed": band_cells,
+        "identical_to_full": identical, "weights": "mauve-py_gb300/bandnet_weights.npz",
+        "margins": {"alpha": alpha, "beta": beta},
+    }
+
+
 # ------------------------------------------------------------- arms
 
 def run_reference(args, world, rank):
@@ -359,6 +428,9 @@ def run_gb300(args, world, rank, local):
         }
         if args.only == "gapdp":
             line.update({"value": round(gcups, 2), "unit": "GCUPS", "ms_per_step": round(dp_ms, 3)})
+        lb_section = learned_band_section(ctx, args, dev, stream, rank)
+        if lb_section:
+            line["gap_dp"]["learned_band"] = lb_section
 
     line["gpu_launches"] = int(launches)
     if rank != 0:

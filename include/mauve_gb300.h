@@ -28,6 +28,8 @@ extern "C" {
 #define MVG_ERR_CAPACITY 5   /* caller's output buffer or a size limit is too small */
 #define MVG_ERR_NOMEM 6      /* device allocation failed */
 #define MVG_ERR_DEVICE 7     /* a kernel reported an internal error (watchdog, bound) */
+#define MVG_ERR_RANGE 8      /* index outside the LUT or a sequence (the reference raises IndexError) */
+#define MVG_ERR_OVERFLOW 9   /* a LUT value does not fit int32 (numpy raises OverflowError) */
 
 typedef struct mvg_context* mvg_handle;
 
@@ -176,7 +178,9 @@ int mvg_mlp_forward_dev(mvg_handle h, const void* d_x_bf16, int64_t n, float* d_
  * respect to every parameter (host, flat layout; may be NULL). */
 int mvg_mlp_grad_dev(mvg_handle h, const void* d_x_bf16, const float* d_target, int64_t n, float* grads,
                      float* loss);
-/* One Adam step (beta 0.9/0.999, eps 1e-8) on a minibatch; step counts from 1. */
+/* One Adam step (beta 0.9/0.999, eps 1e-8) on a minibatch; step counts from 1.
+ * The gradient is scaled to global L2 norm <= 1; a minibatch whose gradient
+ * is not finite changes nothing (its loss is still returned). */
 int mvg_mlp_train_step_dev(mvg_handle h, const void* d_x_bf16, const float* d_target, int64_t n, float lr,
                            int step, float* loss);
 /* Features + forward + mapping to integer bands: delta = round(100 * o0),
@@ -184,6 +188,69 @@ int mvg_mlp_train_step_dev(mvg_handle h, const void* d_x_bf16, const float* d_ta
 int mvg_band_propose_dev(mvg_handle h, const uint8_t* d_seq_a, const uint64_t* d_off_a, const uint8_t* d_seq_b,
                          const uint64_t* d_off_b, int64_t nprob, float alpha, float beta, int32_t* band_delta,
                          int32_t* band_half);
+
+/* ------------------------------------------------------------ index LUT */
+
+/* Genome -> reference index LUT (int32, -1 = unmapped) as mauve.buildIndex
+ * builds it after parsing progressiveMauve's XMFA output.  Aligned blocks
+ * are passed flattened: block b's two gapped rows (genome = sequence 1,
+ * reference = sequence 2) are columns [col_off[b], col_off[b+1]) of
+ * genome_rows / ref_rows; genome_start / ref_start are the sub-alignments'
+ * start_idx as the XMFA parse gives them.  Callers pass only groups where
+ * both sequences are present (lookupSubAlignment, mauve/indexutils.pyx:17-24,
+ * returned both).  Limits: n <= 2^31-1 entries, fewer than 2^32-1 columns.
+ * The _dev forms take device pointers and run on the handle's stream. */
+
+/* mauve/buildindex.py:112-130: LUT of n entries from the blocks (later
+ * blocks and columns overwrite earlier ones; a write at genome index -1
+ * lands in lut[n-1] as a numpy index does).  MVG_ERR_RANGE / MVG_ERR_OVERFLOW
+ * where the reference raises IndexError / OverflowError; the LUT is then
+ * unspecified. */
+int mvg_lut_from_blocks(mvg_handle h, const int64_t* genome_start, const int64_t* ref_start, const uint64_t* col_off,
+                        const uint8_t* genome_rows, const uint8_t* ref_rows, uint64_t nblocks, int32_t* lut,
+                        uint64_t n);
+int mvg_lut_from_blocks_dev(mvg_handle h, const int64_t* d_genome_start, const int64_t* d_ref_start,
+                            const uint64_t* d_col_off, const uint8_t* d_genome_rows, const uint8_t* d_ref_rows,
+                            uint64_t nblocks, int32_t* d_lut, uint64_t n);
+/* mauve/indexutils.pyx:27-44 fixZeroIdx (in place).  MVG_ERR_RANGE where
+ * the Cython function raises IndexError. */
+int mvg_lut_fix_zero_idx(mvg_handle h, int32_t* lut, uint64_t n, const uint8_t* genome, uint64_t genome_len,
+                         const uint8_t* ref, uint64_t ref_len);
+int mvg_lut_fix_zero_idx_dev(mvg_handle h, int32_t* d_lut, uint64_t n, const uint8_t* d_genome, uint64_t genome_len,
+                             const uint8_t* d_ref, uint64_t ref_len);
+/* mauve/indexutils.pyx:47-75 fillGaps and :78-108 smoothEdges (in place,
+ * same result as the sequential passes). */
+int mvg_lut_fill_gaps(mvg_handle h, int32_t* lut, uint64_t n, int max_gap_width);
+int mvg_lut_fill_gaps_dev(mvg_handle h, int32_t* d_lut, uint64_t n, int max_gap_width);
+int mvg_lut_smooth_edges(mvg_handle h, int32_t* lut, uint64_t n, int smoothing_radius);
+int mvg_lut_smooth_edges_dev(mvg_handle h, int32_t* d_lut, uint64_t n, int smoothing_radius);
+/* mauve/indexutils.pyx:111-139 findGaps: fills like fillGaps(300) and writes
+ * gaps[n] (filled gap size at a gap start, -1 where none was found, else 0). */
+int mvg_lut_find_gaps(mvg_handle h, int32_t* lut, uint64_t n, int32_t* gaps);
+int mvg_lut_find_gaps_dev(mvg_handle h, int32_t* d_lut, uint64_t n, int32_t* d_gaps);
+/* mauve/indexutils.pyx:142-156 findEdges as its 0/1 byte mask (before the
+ * bit packing). */
+int mvg_lut_find_edges(mvg_handle h, const int32_t* lut, uint64_t n, uint8_t* edges);
+/* mauve/indexutils.pyx:159-175 findMismatches as a 0/1 byte mask of n
+ * entries.  A mapped index outside the reference is MVG_ERR_RANGE (the
+ * Cython function reads past its buffer there). */
+int mvg_lut_find_mismatches(mvg_handle h, const int32_t* lut, uint64_t n, const uint8_t* genome, uint64_t genome_len,
+                            const uint8_t* ref, uint64_t ref_len, uint8_t* mismatches);
+/* mauve/indexutils.pyx:178-186 findDuplicateMappings. */
+int mvg_lut_find_duplicate_mappings(mvg_handle h, const int32_t* lut, uint64_t n, int64_t* result);
+/* mauve/buildindex.py:111-138 after the XMFA parse: the LUT of n entries
+ * (the genome's length) from the blocks, then fixZeroIdx +
+ * fillGaps(max_gap_width) when fill_gaps, then smoothEdges(smoothing_radius)
+ * when smooth_edges.  genome / ref are read only when fill_gaps. */
+int mvg_build_index_lut(mvg_handle h, const int64_t* genome_start, const int64_t* ref_start, const uint64_t* col_off,
+                        const uint8_t* genome_rows, const uint8_t* ref_rows, uint64_t nblocks, const uint8_t* genome,
+                        uint64_t genome_len, const uint8_t* ref, uint64_t ref_len, int fill_gaps, int max_gap_width,
+                        int smooth_edges, int smoothing_radius, int32_t* lut, uint64_t n);
+int mvg_build_index_lut_dev(mvg_handle h, const int64_t* d_genome_start, const int64_t* d_ref_start,
+                            const uint64_t* d_col_off, const uint8_t* d_genome_rows, const uint8_t* d_ref_rows,
+                            uint64_t nblocks, const uint8_t* d_genome, uint64_t genome_len, const uint8_t* d_ref,
+                            uint64_t ref_len, int fill_gaps, int max_gap_width, int smooth_edges,
+                            int smoothing_radius, int32_t* d_lut, uint64_t n);
 
 /* Upper bound on the device bytes the gap-DP traceback arena may use.  Each
  * call uses min(bound, 60% of free device memory); problems run in waves of

@@ -21,6 +21,7 @@ import mvg
 
 N_IN, N_HID, N_OUT = 528, 256, 2
 DELTA_SCALE = 100.0
+DELTA_CLIP = 10.0
 MAX_PAIR = 160
 
 
@@ -48,7 +49,9 @@ def labels_from_full_dp(la, lb, scores, env, margin=8):
     need = np.minimum(la, lb) - scores.astype(np.int64) // MAX_PAIR + margin
     half = np.maximum(half_env, need)
     half = np.clip(half, 0, np.maximum(la, lb))
-    t = np.stack([delta / DELTA_SCALE, np.log1p(half)], axis=1).astype(np.float32)
+    # offsets beyond +-1000 columns are clipped in the target: such gaps need a
+    # band of most of the matrix and are decided by the half-width anyway
+    t = np.stack([np.clip(delta / DELTA_SCALE, -DELTA_CLIP, DELTA_CLIP), np.log1p(half)], axis=1).astype(np.float32)
     return t, delta.astype(np.int32), half.astype(np.int32)
 
 
@@ -72,18 +75,22 @@ class BandNet:
 
     # device-pointer calls (inputs resident on the GPU)
     def features_dev(self, d_sa, d_oa, d_sb, d_ob, n, d_x):
+        mvg.wait_producers()
         mvg._check(mvg.load_library().mvg_band_features_dev(self.ctx.handle, d_sa, d_oa, d_sb, d_ob, n, d_x))
 
     def forward_dev(self, d_x, n, d_out):
+        mvg.wait_producers()
         mvg._check(mvg.load_library().mvg_mlp_forward_dev(self.ctx.handle, d_x, n, d_out))
 
     def grad_dev(self, d_x, d_t, n):
+        mvg.wait_producers()
         g = np.zeros(int(mvg.load_library().mvg_mlp_num_params()), np.float32)
         loss = ctypes.c_float(0)
         mvg._check(mvg.load_library().mvg_mlp_grad_dev(self.ctx.handle, d_x, d_t, n, mvg._ptr(g), ctypes.byref(loss)))
         return g, float(loss.value)
 
     def train_step_dev(self, d_x, d_t, n, lr):
+        mvg.wait_producers()
         self.step += 1
         loss = ctypes.c_float(0)
         mvg._check(mvg.load_library().mvg_mlp_train_step_dev(self.ctx.handle, d_x, d_t, n, ctypes.c_float(lr),
@@ -91,6 +98,7 @@ class BandNet:
         return float(loss.value)
 
     def propose_dev(self, d_sa, d_oa, d_sb, d_ob, n, alpha=1.0, beta=8.0):
+        mvg.wait_producers()
         delta = np.zeros(max(n, 1), np.int32)
         half = np.zeros(max(n, 1), np.int32)
         mvg._check(mvg.load_library().mvg_band_propose_dev(self.ctx.handle, d_sa, d_oa, d_sb, d_ob, n,
@@ -104,6 +112,7 @@ def full_dp_labels_dev(ctx, d_sa, d_oa, d_sb, d_ob, n, margin=8, torch_device=No
     import torch
     d_sc = torch.zeros(n, dtype=torch.int32, device=torch_device)
     d_env = torch.zeros(2 * n, dtype=torch.int32, device=torch_device)
+    mvg.wait_producers()
     mvg._check(mvg.load_library().mvg_gapdp_envelope_dev(ctx.handle, d_sa, d_oa, d_sb, d_ob, n, d_sc.data_ptr(),
                                                          d_env.data_ptr()))
     return d_sc.cpu().numpy(), d_env.cpu().numpy().reshape(-1, 2)

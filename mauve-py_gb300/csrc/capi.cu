@@ -63,6 +63,10 @@ int check_device_error(Ctx* c) {
       return report_error(MVG_ERR_BAD_BASE, "gap-DP base code outside 0..3");
     case kDevCapacity:
       return report_error(MVG_ERR_DEVICE, "device capacity bound exceeded");
+    case kDevRange:
+      return report_error(MVG_ERR_RANGE, "index out of range");
+    case kDevOverflow:
+      return report_error(MVG_ERR_OVERFLOW, "LUT value does not fit int32");
     default:
       return report_error(MVG_ERR_DEVICE, "device kernel reported an error");
   }

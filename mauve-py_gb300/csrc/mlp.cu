@@ -35,6 +35,7 @@ constexpr int64_t kOffB3 = kOffW3 + (int64_t)kHid * kHid;
 constexpr int64_t kOffW4 = kOffB3 + kHid;
 constexpr int64_t kOffB4 = kOffW4 + (int64_t)kOut * kHid;
 constexpr int64_t kNumParams = kOffB4 + kOut;
+constexpr float kClipNorm = 1.0f;  // global gradient-norm clip of the Adam step
 
 struct MlpState {
   float* w = nullptr;     // master weights
@@ -215,11 +216,26 @@ __global__ void k_to_bf16(const float* __restrict__ x, __nv_bfloat16* __restrict
     y[e] = __float2bfloat16(x[e]);
 }
 
+// Sum of squares of the gradient into *sumsq (for norm clipping).
+__global__ void k_sumsq(const float* __restrict__ g, int64_t n, float* __restrict__ sumsq) {
+  float s = 0.f;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
+    s += g[e] * g[e];
+  for (int d = 16; d > 0; d >>= 1) s += __shfl_xor_sync(0xffffffffu, s, d);
+  if ((threadIdx.x & 31) == 0) atomicAdd(sumsq, s);
+}
+
+// Adam on the gradient scaled to global norm <= clip; a step whose gradient
+// norm is not finite leaves weights and moments untouched.
 __global__ void k_adam(float* __restrict__ w, __nv_bfloat16* __restrict__ wb, const float* __restrict__ g,
                        float* __restrict__ m, float* __restrict__ v, int64_t n, float lr, float b1, float b2, float eps,
-                       float c1, float c2) {
+                       float c1, float c2, const float* __restrict__ sumsq, float clip) {
+  const float ss = *sumsq;
+  if (!isfinite(ss)) return;
+  const float norm = sqrtf(ss);
+  const float scale = norm > clip ? clip / norm : 1.f;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x) {
-    const float ge = g[e];
+    const float ge = g[e] * scale;
     const float me = b1 * m[e] + (1.f - b1) * ge;
     const float ve = b2 * v[e] + (1.f - b2) * ge * ge;
     m[e] = me;
@@ -273,8 +289,10 @@ __global__ void __launch_bounds__(256) k_band_features(const uint8_t* __restrict
 __global__ void k_to_band(const float* __restrict__ o, int64_t n, float alpha, float beta, int32_t* __restrict__ delta,
                           int32_t* __restrict__ half) {
   for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
-    const float d = rintf(o[p * kOut] * kDeltaScale);
-    float h = ceilf(alpha * (expf(fminf(o[p * kOut + 1], 13.f)) - 1.f) + beta);
+    // a non-finite output proposes the whole matrix (centred, half 1e6)
+    const bool ok = isfinite(o[p * kOut]) && isfinite(o[p * kOut + 1]);
+    const float d = ok ? rintf(o[p * kOut] * kDeltaScale) : 0.f;
+    float h = ok ? ceilf(alpha * (expf(fminf(o[p * kOut + 1], 13.f)) - 1.f) + beta) : 1e6f;
     h = fminf(fmaxf(h, 0.f), 1e6f);
     delta[p] = (int32_t)fminf(fmaxf(d, -1e6f), 1e6f);
     half[p] = (int32_t)h;
@@ -507,9 +525,11 @@ int mvg_mlp_train_step_dev(mvg_handle h, const void* d_x_bf16, const float* d_ta
   mlp_backward(c, s, (const __nv_bfloat16*)d_x_bf16, d_target, n);
   const float b1 = 0.9f, b2 = 0.999f;
   const float c1 = 1.f - powf(b1, (float)step), c2 = 1.f - powf(b2, (float)step);
+  MVG_CUDA_TRY(cudaMemsetAsync(s.loss + 1, 0, 4, c->stream));
+  k_sumsq<<<grid_for(kNumParams, 256), 256, 0, c->stream>>>(s.g, kNumParams, s.loss + 1);
   k_adam<<<grid_for(kNumParams, 256), 256, 0, c->stream>>>(s.w, s.wb, s.g, s.m, s.v, kNumParams, lr, b1, b2, 1e-8f, c1,
-                                                           c2);
-  c->launches++;
+                                                           c2, s.loss + 1, kClipNorm);
+  c->launches += 2;
   if (h_loss) {
     float loss = 0;
     MVG_CUDA_TRY(cudaMemcpyAsync(&loss, s.loss, 4, cudaMemcpyDeviceToHost, c->stream));

@@ -19,6 +19,8 @@ enum DevError : uint32_t {
   kDevBadBase = 2,      // DP input code outside 0..3
   kDevCapacity = 3,     // an internal capacity bound was exceeded
   kDevWatchdog = 4,     // a bounded wait gave up
+  kDevRange = 5,        // LUT: an index outside the LUT or a sequence
+  kDevOverflow = 6,     // LUT: a value outside int32
 };
 
 __device__ __forceinline__ void set_error(uint32_t* err, uint32_t code) {

@@ -12,7 +12,7 @@ struct Ctx;
 // Grow-only device buffers, one per slot, owned by the handle.  Calls reuse
 // them, so steady-state calls allocate nothing.
 struct Workspace {
-  static constexpr int kSlots = 64;
+  static constexpr int kSlots = 96;
   void* ptr[kSlots] = {};
   size_t size[kSlots] = {};
   void* get(Ctx* c, int slot, size_t bytes);

@@ -17,6 +17,7 @@ without a CUDA device raises.
 """
 import ctypes
 import os
+import sys
 
 import numpy as np
 
@@ -25,7 +26,7 @@ LIB_PATH = os.path.join(HERE, "lib", "libmauve_gb300.so")
 
 MVG_OK = 0
 _ERRORS = {1: ValueError, 2: RuntimeError, 3: ValueError, 4: ValueError, 5: OverflowError, 6: MemoryError,
-           7: RuntimeError}
+           7: RuntimeError, 8: IndexError, 9: OverflowError}
 
 CODING_SEED = 3  # libMems/SeedMasks.h:262
 SOLID_SEED = 2 ** 31 - 1
@@ -38,7 +39,11 @@ EXPORTS = ["mvg_create", "mvg_destroy", "mvg_last_error", "mvg_stream", "mvg_ker
            "mvg_stage_times", "mvg_gapdp_banded", "mvg_gapdp_banded_dev", "mvg_set_dp_rows", "mvg_mlp_num_params",
            "mvg_mlp_set_params", "mvg_mlp_get_params", "mvg_band_features_dev", "mvg_mlp_forward_dev",
            "mvg_mlp_grad_dev", "mvg_mlp_train_step_dev", "mvg_band_propose_dev", "mvg_gapdp_envelope_dev",
-           "mvg_sml_build_noalloc"]
+           "mvg_sml_build_noalloc", "mvg_lut_from_blocks", "mvg_lut_from_blocks_dev", "mvg_lut_fix_zero_idx",
+           "mvg_lut_fix_zero_idx_dev", "mvg_lut_fill_gaps", "mvg_lut_fill_gaps_dev", "mvg_lut_smooth_edges",
+           "mvg_lut_smooth_edges_dev", "mvg_lut_find_gaps", "mvg_lut_find_gaps_dev", "mvg_lut_find_edges",
+           "mvg_lut_find_mismatches", "mvg_lut_find_duplicate_mappings", "mvg_build_index_lut",
+           "mvg_build_index_lut_dev"]
 
 TUNING_PATH = os.path.join(HERE, "dp_tuning.json")
 
@@ -85,6 +90,21 @@ def load_library(path=LIB_PATH):
         "mvg_band_propose_dev": (ci, [vp, vp, vp, vp, vp, i64, ctypes.c_float, ctypes.c_float, vp, vp]),
         "mvg_set_profiling": (ci, [vp, ci]),
         "mvg_stage_times": (ci, [vp, ctypes.c_char_p, ctypes.c_size_t, vp, ci, ctypes.POINTER(ci)]),
+        "mvg_lut_from_blocks": (ci, [vp, vp, vp, vp, vp, vp, u64, vp, u64]),
+        "mvg_lut_from_blocks_dev": (ci, [vp, vp, vp, vp, vp, vp, u64, vp, u64]),
+        "mvg_lut_fix_zero_idx": (ci, [vp, vp, u64, vp, u64, vp, u64]),
+        "mvg_lut_fix_zero_idx_dev": (ci, [vp, vp, u64, vp, u64, vp, u64]),
+        "mvg_lut_fill_gaps": (ci, [vp, vp, u64, ci]),
+        "mvg_lut_fill_gaps_dev": (ci, [vp, vp, u64, ci]),
+        "mvg_lut_smooth_edges": (ci, [vp, vp, u64, ci]),
+        "mvg_lut_smooth_edges_dev": (ci, [vp, vp, u64, ci]),
+        "mvg_lut_find_gaps": (ci, [vp, vp, u64, vp]),
+        "mvg_lut_find_gaps_dev": (ci, [vp, vp, u64, vp]),
+        "mvg_lut_find_edges": (ci, [vp, vp, u64, vp]),
+        "mvg_lut_find_mismatches": (ci, [vp, vp, u64, vp, u64, vp, u64, vp]),
+        "mvg_lut_find_duplicate_mappings": (ci, [vp, vp, u64, ctypes.POINTER(i64)]),
+        "mvg_build_index_lut": (ci, [vp, vp, vp, vp, vp, vp, u64, vp, u64, vp, u64, ci, ci, ci, ci, vp, u64]),
+        "mvg_build_index_lut_dev": (ci, [vp, vp, vp, vp, vp, vp, u64, vp, u64, vp, u64, ci, ci, ci, ci, vp, u64]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -98,6 +118,15 @@ def _check(rc):
     if rc != MVG_OK:
         msg = load_library().mvg_last_error().decode(errors="replace")
         raise _ERRORS.get(rc, RuntimeError)("libmauve_gb300 error %d: %s" % (rc, msg))
+
+
+def wait_producers():
+    """Device inputs reach the library as raw pointers, usually written by
+    torch kernels on torch's current stream, while the library runs on the
+    handle's own stream: finish that producer work before a device call."""
+    t = sys.modules.get("torch")
+    if t is not None and t.cuda.is_initialized():
+        t.cuda.current_stream().synchronize()
 
 
 def _ptr(a):
@@ -187,6 +216,7 @@ class Context:
         return pos[:cnt], (mer[:cnt] if with_mers else None)
 
     def sml_build_dev(self, d_seq_ptr, n, seed, d_pos_ptr, d_mer_ptr, cap):
+        wait_producers()
         out = ctypes.c_uint64(0)
         _check(load_library().mvg_sml_build_dev(self._h, d_seq_ptr, n, seed, d_pos_ptr, d_mer_ptr, cap,
                                                 ctypes.byref(out)))
@@ -210,6 +240,7 @@ class Context:
             return out[: 3 * cnt.value].reshape(-1, 3)
 
     def pairwise_matches_dev(self, d_a, na, d_b, nb, seed, d_out, cap):
+        wait_producers()
         cnt = ctypes.c_uint64(0)
         _check(load_library().mvg_pairwise_matches_dev(self._h, d_a, na, d_b, nb, seed, d_out, cap,
                                                        ctypes.byref(cnt)))
@@ -280,6 +311,7 @@ class Context:
     def gap_align_banded_dev(self, d_sa, d_oa, d_sb, d_ob, n, band_delta, band_half, d_scores, d_paths, d_path_off,
                              d_path_len):
         """Device-buffer banded call; band arrays and the returned used-band flags are host numpy arrays."""
+        wait_producers()
         delta = np.ascontiguousarray(band_delta, np.int32)
         half = np.ascontiguousarray(band_half, np.int32)
         used = np.zeros(max(n, 1), np.uint8)
@@ -296,6 +328,7 @@ class Context:
                                               _ptr(scores), _ptr(paths), _ptr(path_off), _ptr(path_len)))
 
     def gap_align_batch_dev(self, d_sa, d_oa, d_sb, d_ob, n, d_scores, d_paths, d_path_off, d_path_len):
+        wait_producers()
         _check(load_library().mvg_gapdp_batch_dev(self._h, d_sa, d_oa, d_sb, d_ob, n, d_scores, d_paths, d_path_off,
                                                   d_path_len))
 

@@ -150,6 +150,10 @@ def train(args):
     sc_tr, env_tr = label(ctx, tr)
     print("labels %.1fs (%.3g cells)" % (time.time() - t0, tr.cells), flush=True)
     T, _, _ = bandnet.labels_from_full_dp(tr.la, tr.lb, sc_tr, env_tr)
+    if not np.isfinite(T).all():
+        raise RuntimeError("non-finite training targets")
+    print("targets: |offset| max %.2f, log-half range %.2f..%.2f" % (np.abs(T[:, 0]).max(), T[:, 1].min(),
+                                                                      T[:, 1].max()), flush=True)
     X = torch.zeros((tr.n, bandnet.N_IN), dtype=torch.bfloat16, device=dev)
     net = bandnet.BandNet(ctx, seed=args.seed)
     net.features_dev(*tr.ptrs(), tr.n, X.data_ptr())
@@ -161,6 +165,7 @@ def train(args):
     t0 = time.time()
     losses = []
     step = 0
+    skipped = 0
     for ep in range(args.epochs):
         order = fit_idx_t[torch.randperm(len(fit_idx_t), device=dev)]
         lr = args.lr * (0.5 ** ep)
@@ -170,9 +175,21 @@ def train(args):
             tb = Tg.index_select(0, idx).contiguous()
             loss = net.train_step_dev(xb.data_ptr(), tb.data_ptr(), len(idx), lr)
             step += 1
+            if not np.isfinite(loss):
+                skipped += 1
+                if skipped == 1:
+                    out = torch.zeros((len(idx), 2), dtype=torch.float32, device=dev)
+                    net.forward_dev(xb.data_ptr(), len(idx), out.data_ptr())
+                    print("first non-finite minibatch at step %d: n %d, X finite %s, T finite %s, |T| max %.3g, "
+                          "output finite %s, |output| max %.3g, params finite %s" % (
+                              step, len(idx), bool(torch.isfinite(xb.float()).all()), bool(torch.isfinite(tb).all()),
+                              float(tb.abs().max()), bool(torch.isfinite(out).all()),
+                              float(out.abs().nan_to_num(0).max()), bool(np.isfinite(net.get_params()).all())),
+                          flush=True)
             if step % 50 == 0:
                 losses.append((step, loss))
-        print("epoch %d loss %.4f" % (ep, losses[-1][1] if losses else float("nan")), flush=True)
+        print("epoch %d loss %.4f (non-finite minibatches so far: %d)" % (
+            ep, losses[-1][1] if losses else float("nan"), skipped), flush=True)
     train_s = time.time() - t0
     # calibrate alpha / beta on the validation split by timing the exact
     # banded DP (with its fallbacks) for each candidate margin
@@ -190,7 +207,7 @@ def train(args):
     params = net.get_params()
     # held-out evaluation: full vs learned band vs band without the network
     res = {"train_gaps": tr.n, "eval_gaps": ev.n, "train_seconds": train_s, "steps": step,
-           "loss_curve": losses[-20:], "alpha": alpha, "beta": beta}
+           "loss_curve": losses[-20:], "nonfinite_minibatches": skipped, "alpha": alpha, "beta": beta}
     tf, sc_f, p_f, pl_f = timed_full(ctx, ev)
     tf, sc_f, p_f, pl_f = timed_full(ctx, ev)  # second run: warm
     t_prop0 = time.perf_counter()
@@ -213,6 +230,29 @@ def train(args):
     })
     res["speedup_learned_vs_full"] = tf / (tl + t_prop)
     res["speedup_no_network_vs_full"] = tf / th
+    # where the banded time goes: the accepted gaps' banded DP alone, and the
+    # full-DP cells of the gaps that fell back; plus the ceiling set by the
+    # label bands (the full DP's own envelope + margin) on the same gaps
+    gcups_full = ev.cells / tf / 1e9
+    for key, (d, h, used) in (("learned", (dl, hl, used_l)), ("no_network", (dh, hh, used_h))):
+        acc = np.nonzero(used)[0]
+        fb = np.nonzero(used == 0)[0]
+        if len(acc) == 0:
+            continue
+        sub = DeviceBatch(*subset_host_idx(ev, acc), dev)
+        ta, _, cells_a, *_ = timed_banded(ctx, sub, d[acc], h[acc])
+        fb_cells = float(np.sum(ev.la[fb].astype(np.float64) * ev.lb[fb]))
+        res[key].update({"accepted_band_seconds": ta, "accepted_band_cells": cells_a,
+                         "accepted_band_gcups": cells_a / ta / 1e9 if ta > 0 else None,
+                         "accepted_full_cells": float(np.sum(ev.la[acc].astype(np.float64) * ev.lb[acc])),
+                         "fallback_full_cells": fb_cells,
+                         "fallback_seconds_at_full_gcups": fb_cells / gcups_full / 1e9})
+        del sub
+    env = bandnet.full_dp_labels_dev(ctx, *ev.ptrs(), ev.n, torch_device=dev)
+    _, d_lab, h_lab = bandnet.labels_from_full_dp(ev.la, ev.lb, *env)
+    t_lab, used_lab, cells_lab, *_ = timed_banded(ctx, ev, d_lab, h_lab)
+    res["label_band"] = {"seconds": t_lab, "accept_rate": float(used_lab.mean()), "cells": cells_lab,
+                         "speedup_vs_full": tf / t_lab}
     print(json.dumps(res, indent=1), flush=True)
     np.savez(args.out, params=params, alpha=np.float32(alpha), beta=np.float32(beta))
     with open(os.path.splitext(args.out)[0] + "_eval.json", "w") as f:

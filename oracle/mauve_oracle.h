@@ -63,6 +63,23 @@ int64_t mo_nw_batch(const uint8_t* seq_a, const uint64_t* off_a, const uint8_t* 
                     const uint64_t* off_b, int64_t nprob, char* paths, const uint64_t* path_off,
                     int64_t* path_len, int32_t* scores, int nthreads);
 
+/* Index LUT (oracle/lut_oracle.c).  Genome -> reference LUT built from
+ * aligned blocks (buildindex.py:112-130) and the indexutils.pyx passes.
+ * Blocks: columns [col_off[b], col_off[b+1]) of the two gapped rows, start
+ * indices as the XMFA parse gives them.  -2 = IndexError, -3 = overflow. */
+int64_t mo_lut_from_blocks(const int64_t* g_start, const int64_t* r_start, const uint64_t* col_off,
+                           const uint8_t* g_rows, const uint8_t* r_rows, uint64_t nblocks,
+                           int32_t* lut, uint64_t n);
+int mo_fix_zero_idx(int32_t* lut, uint64_t n, const uint8_t* genome, uint64_t glen,
+                    const uint8_t* ref, uint64_t rlen);
+void mo_fill_gaps(int32_t* lut, uint64_t n, int max_gap_width);
+void mo_smooth_edges(int32_t* lut, uint64_t n, int smoothing_radius);
+void mo_find_gaps(int32_t* lut, uint64_t n, int32_t* gaps);
+void mo_find_edges(const int32_t* lut, uint64_t n, uint8_t* edges);
+int mo_find_mismatches(const int32_t* lut, uint64_t n, const uint8_t* genome, uint64_t glen,
+                       const uint8_t* ref, uint64_t rlen, uint8_t* mism);
+int64_t mo_find_duplicate_mappings(const int32_t* lut, uint64_t n, uint32_t* counts, uint64_t ncounts);
+
 #ifdef __cplusplus
 }
 #endif

@@ -17,11 +17,12 @@ _lib = None
 
 def build(force=False):
     """Compile oracle/mauve_oracle.c into oracle/lib/libmauve_oracle.so."""
-    src = os.path.join(_HERE, "mauve_oracle.c")
-    if not force and os.path.exists(LIB_PATH) and os.path.getmtime(LIB_PATH) >= os.path.getmtime(src):
+    srcs = [os.path.join(_HERE, f) for f in ("mauve_oracle.c", "lut_oracle.c", "mauve_oracle.h")]
+    if not force and os.path.exists(LIB_PATH) and all(
+            os.path.getmtime(LIB_PATH) >= os.path.getmtime(s) for s in srcs):
         return LIB_PATH
     os.makedirs(os.path.dirname(LIB_PATH), exist_ok=True)
-    subprocess.check_call(["gcc", "-O2", "-fPIC", "-shared", "-o", LIB_PATH, src, "-lm", "-lpthread"])
+    subprocess.check_call(["gcc", "-O2", "-fPIC", "-shared", "-o", LIB_PATH, *srcs[:2], "-lm", "-lpthread"])
     return LIB_PATH
 
 
@@ -53,6 +54,20 @@ def lib():
         L.mo_nw_score.argtypes = [vp, ctypes.c_int, vp, ctypes.c_int]
         L.mo_nw_batch.restype = i64
         L.mo_nw_batch.argtypes = [vp, vp, vp, vp, i64, vp, vp, vp, vp, ctypes.c_int]
+        L.mo_lut_from_blocks.restype = i64
+        L.mo_lut_from_blocks.argtypes = [vp, vp, vp, vp, vp, u64, vp, u64]
+        L.mo_fix_zero_idx.argtypes = [vp, u64, vp, u64, vp, u64]
+        L.mo_fill_gaps.argtypes = [vp, u64, ctypes.c_int]
+        L.mo_fill_gaps.restype = None
+        L.mo_smooth_edges.argtypes = [vp, u64, ctypes.c_int]
+        L.mo_smooth_edges.restype = None
+        L.mo_find_gaps.argtypes = [vp, u64, vp]
+        L.mo_find_gaps.restype = None
+        L.mo_find_edges.argtypes = [vp, u64, vp]
+        L.mo_find_edges.restype = None
+        L.mo_find_mismatches.argtypes = [vp, u64, vp, u64, vp, u64, vp]
+        L.mo_find_duplicate_mappings.restype = i64
+        L.mo_find_duplicate_mappings.argtypes = [vp, u64, vp, u64]
         _lib = L
     return _lib
 
@@ -161,3 +176,91 @@ def nw_batch(seq_a, off_a, seq_b, off_b, with_paths=True, nthreads=0):
     lib().mo_nw_batch(_p(seq_a), _p(off_a), _p(seq_b), _p(off_b), nprob,
                       _p(paths) if with_paths else None, _p(path_off), _p(plen), _p(scores), nthreads)
     return scores[:nprob], plen[:nprob], paths, path_off
+
+
+# ---- index LUT (lut_oracle.c) ------------------------------------------
+
+
+class LutIndexError(IndexError):
+    pass
+
+
+def _lut(lut):
+    if not (isinstance(lut, np.ndarray) and lut.dtype == np.int32 and lut.ndim == 1 and lut.flags.c_contiguous):
+        raise TypeError("LUT must be a contiguous 1-D int32 array")
+    return lut
+
+
+def _check(rc, what):
+    if rc == -2:
+        raise LutIndexError(what + ": index out of range")
+    if rc == -3:
+        raise OverflowError(what + ": value does not fit int32")
+    if rc < 0:
+        raise ValueError(what + ": error %d" % rc)
+    return rc
+
+
+def blocks_arrays(blocks):
+    """(g_start, r_start, col_off, g_rows, r_rows) from a list of
+    (genome_start, ref_start, genome_row, ref_row) blocks."""
+    gs = np.array([b[0] for b in blocks], np.int64)
+    rs = np.array([b[1] for b in blocks], np.int64)
+    lens = [len(b[2]) for b in blocks]
+    for b in blocks:
+        if len(b[2]) != len(b[3]):
+            raise ValueError("rows of a block differ in length")
+    off = np.zeros(len(blocks) + 1, np.uint64)
+    off[1:] = np.cumsum(lens, dtype=np.uint64)
+    g = np.frombuffer(b"".join(bytes(b[2]) for b in blocks), np.uint8).copy()
+    r = np.frombuffer(b"".join(bytes(b[3]) for b in blocks), np.uint8).copy()
+    return gs, rs, off, g, r
+
+
+def lut_from_blocks(blocks, genome_length):
+    gs, rs, off, g, r = blocks_arrays(blocks)
+    lut = np.empty(genome_length, np.int32)
+    _check(lib().mo_lut_from_blocks(_p(gs), _p(rs), _p(off), _p(g), _p(r), len(gs), _p(lut), genome_length),
+           "lut_from_blocks")
+    return lut
+
+
+def fix_zero_idx(lut, genome, ref):
+    g, r = _u8(genome), _u8(ref)
+    _check(lib().mo_fix_zero_idx(_p(_lut(lut)), len(lut), _p(g), len(g), _p(r), len(r)), "fix_zero_idx")
+
+
+def fill_gaps(lut, max_gap_width=300):
+    lib().mo_fill_gaps(_p(_lut(lut)), len(lut), int(max_gap_width))
+
+
+def smooth_edges(lut, smoothing_radius=20):
+    lib().mo_smooth_edges(_p(_lut(lut)), len(lut), int(smoothing_radius))
+
+
+def find_gaps(lut):
+    gaps = np.zeros(len(lut), np.int32)
+    lib().mo_find_gaps(_p(_lut(lut)), len(lut), _p(gaps))
+    return gaps
+
+
+def find_edges(lut):
+    e = np.zeros(len(lut), np.uint8)
+    lib().mo_find_edges(_p(_lut(lut)), len(lut), _p(e))
+    return e
+
+
+def find_mismatches(lut, genome, ref):
+    g, r = _u8(genome), _u8(ref)
+    m = np.zeros(len(lut), np.uint8)
+    _check(lib().mo_find_mismatches(_p(_lut(lut)), len(lut), _p(g), len(g), _p(r), len(r), _p(m)),
+           "find_mismatches")
+    return m
+
+
+def find_duplicate_mappings(lut):
+    _lut(lut)
+    nc = int(max(int(lut.max()), 0)) + 1 if len(lut) else 1
+    counts = np.zeros(nc, np.uint32)
+    return int(_check(lib().mo_find_duplicate_mappings(_p(lut), len(lut), _p(counts), nc), "find_duplicate_mappings")
+               if len(lut) else -1)

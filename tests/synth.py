@@ -275,3 +275,102 @@ def _mutate_codes_fast(rng, a, sub, nind):
     if len(b) == 0:
         b = rng.integers(0, 4, 1).astype(np.uint8)
     return b
+
+
+# ---------------------------------------------------------------- index LUT
+
+
+def lut_alignment(seed, n_ref=20000, sub=0.01, indel=0.002, nblocks=8, shuffle=True, extras=True):
+    """A pairwise alignment of a genome against a reference, cut into XMFA-
+    like sub-alignment groups.  Returns (groups, genome, ref): each group is
+    a list of (seq_num, start_idx, row) with seq_num 1 = genome, 2 =
+    reference and start_idx the 1-based position of the row's first base.
+    Columns come from a walk over the reference with substitutions, indels
+    (geometric lengths), occasional N and lowercase bases; extras adds a
+    genome-only group, a repeated (overwriting) block, a column gapped on
+    both sides, and a block whose genome row is all gaps with start 0."""
+    rng = np.random.default_rng(seed)
+    ref = rng.choice(np.frombuffer(b"ACGT", np.uint8), n_ref)
+    if extras:
+        ref[rng.random(n_ref) < 0.001] = ord("N")
+    cols_g, cols_r = [], []
+    i = 0
+    while i < n_ref:
+        u = rng.random()
+        if u < indel / 2:
+            k = int(rng.geometric(0.3))
+            for _ in range(k):
+                cols_g.append(int(rng.choice(np.frombuffer(b"ACGT", np.uint8))))
+                cols_r.append(ord("-"))
+        elif u < indel:
+            k = min(int(rng.geometric(0.3)), n_ref - i)
+            for _ in range(k):
+                cols_g.append(ord("-"))
+                cols_r.append(int(ref[i]))
+                i += 1
+        else:
+            b = int(ref[i])
+            if rng.random() < sub:
+                b = int(rng.choice([c for c in b"ACGT" if c != b]))
+            if extras and rng.random() < 0.0005:
+                b = b | 0x20 if 65 <= b <= 90 else b  # lowercase: compares unequal
+            cols_g.append(b)
+            cols_r.append(int(ref[i]))
+            i += 1
+    G = np.array(cols_g, np.uint8)
+    R = np.array(cols_r, np.uint8)
+    gpos = np.cumsum(G != ord("-"))  # 1-based genome position after each column
+    rpos = np.cumsum(R != ord("-"))
+    genome = G[G != ord("-")].tobytes()
+    cuts = np.sort(rng.choice(np.arange(1, len(G)), nblocks - 1, replace=False)) if nblocks > 1 else []
+    bounds = [0, *cuts.tolist(), len(G)] if nblocks > 1 else [0, len(G)]
+    groups = []
+    for a, e in zip(bounds[:-1], bounds[1:]):
+        g0 = int(gpos[a - 1]) + 1 if a > 0 else 1
+        r0 = int(rpos[a - 1]) + 1 if a > 0 else 1
+        groups.append([(1, g0, G[a:e].tobytes()), (2, r0, R[a:e].tobytes())])
+    if shuffle:
+        order = rng.permutation(len(groups))
+        groups = [groups[k] for k in order]
+    if extras:
+        groups.insert(int(rng.integers(0, len(groups) + 1)), [(1, 5, genome[4:200])])
+        k = int(rng.integers(0, len(groups)))
+        if len(groups[k]) == 2:
+            (s1, g0, rg), (s2, r0, rr) = groups[k]
+            # a copy shifted by one reference base, later in the list: it
+            # overwrites the first copy's entries
+            groups.append([(1, g0, rg), (2, r0 + 1, rr)])
+            # a column gapped on both sides inside the block
+            m = len(rg) // 2
+            groups[k] = [(1, g0, rg[:m] + b"-" + rg[m:]), (2, r0, rr[:m] + b"-" + rr[m:])]
+        groups.append([(1, 0, b"---"), (2, 7, b"A-C")])
+    return groups, genome, ref.tobytes()
+
+
+def lut_random(seed, n=5000, run_mean=60, p_gap=0.3, p_noise=0.05, p_island=0.2):
+    """A LUT made of consecutive runs separated by -1 gaps, shifted runs,
+    noisy single entries and mapped islands inside gaps (starts that a
+    neighbouring fill covers)."""
+    rng = np.random.default_rng(seed)
+    lut = np.empty(n, np.int32)
+    i, v = 0, int(rng.integers(0, 1000))
+    while i < n:
+        L = min(int(rng.geometric(1.0 / run_mean)), n - i)
+        lut[i:i + L] = v + np.arange(L)
+        i += L
+        v += L
+        r = rng.random()
+        if r < p_gap:
+            g = min(int(rng.geometric(1.0 / 12)), n - i)
+            lut[i:i + g] = -1
+            if g > 4 and rng.random() < p_island:
+                k = int(rng.integers(1, g - 1))
+                lut[i + k] = int(rng.integers(0, v + 100))
+            i += g
+            v += g + int(rng.integers(-3, 4)) * (rng.random() < 0.5)
+        elif r < p_gap + 0.2:
+            v += int(rng.integers(-50, 50))
+        v = max(v, 0)
+    noise = rng.random(n) < p_noise
+    lut[noise] = rng.integers(-1, max(2, int(lut.max()) + 10), int(noise.sum()))
+    return lut
