@@ -208,11 +208,131 @@ def learned_band_section(ctx, args, dev, stream, rank):
                     "substitutions, 10%% divergent)" % n,
         "cells_full": cells, "plain_full_ms": round(ms_full, 3), "plain_full_gcups": round(cells / ms_full / 1e6, 2),
         "learned_ms": round(ms_band, 3), "learned_effective_gcups": round(cells / ms_band / 1e6, 2),
-        "speedup_vs_plain": round(ms_full / ms_band, 3), "accept_rate": round(float(used.mean()), 4),
-        "fallback_rate": round(1 - float(used.mean()), 4), "cells_computed": band_cells,
+        "speedup_vs_plain": round(ms_full / ms_band, 3), "accept_rate": round(float((used == 1).mean()), 4),
+        "fallback_rate": round(float((used != 1).mean()), 4),
+        "fallback_split": {"rejected_by_check": round(float((used == 0).mean()), 4),
+                           "not_tried": round(float((used == 2).mean()), 4)},
+        "cells_computed": band_cells,
         "identical_to_full": identical, "weights": "mauve-py_gb300/bandnet_weights.npz",
         "margins": {"alpha": alpha, "beta": beta},
     }
+
+
+def mds42_section(ctx, dev, stream, flush):
+    """Anchoring on the reference's own recoded E. coli fixture pair
+    (tests/golden/mds42.npz, 3.98 Mbp each): device-resident throughput and
+    whether the match list equals the reference's."""
+    import torch
+
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from conftest import load_mds42
+    a, b, seed, want = load_mds42()
+    da, db = torch.from_numpy(a.copy()).to(dev), torch.from_numpy(b.copy()).to(dev)
+    out = torch.zeros(3 * (len(want) + 1024), dtype=torch.int64, device=dev)
+
+    def step():
+        return ctx.pairwise_matches_dev(da.data_ptr(), len(a), db.data_ptr(), len(b), seed, out.data_ptr(),
+                                        len(want) + 1024)
+
+    for _ in range(3):
+        n = step()
+    ms = []
+    for _ in range(5):
+        flush.zero_()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        n = step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    got = out[:3 * n].cpu().numpy().reshape(-1, 3)
+    t = sorted(ms)[len(ms) // 2]
+    return {"workload": "the reference's recoded E. coli fixture pair (mds42_recoded vs mds42_full, %.2f + %.2f Mbp), "
+                        "coding seed w=15" % (len(a) / 1e6, len(b) / 1e6),
+            "value": round((len(a) + len(b)) / 1e6 / (t / 1e3), 2), "unit": "Mbp/s", "ms": round(t, 3),
+            "matches": int(n), "identical_to_reference": bool(n == len(want) and np.array_equal(got, want))}
+
+
+LUT_NREF = 4_600_000
+
+
+def lut_section(ctx, args, dev, stream, rank, flush):
+    """buildIndex's LUT step on a genome-sized alignment: the LUT from the
+    aligned blocks, fixZeroIdx, fillGaps(300), smoothEdges(20).  value:
+    inputs resident on the device (CUDA events); e2e: the host C-ABI call
+    with host buffers (copies inside the timed region, wall clock)."""
+    import torch
+
+    import indexutils as iu
+    import synth
+    gs, rs, off, rg, rr, genome, ref = synth.lut_alignment_fast(31 + rank, n_ref=LUT_NREF, sub=0.02, indel=0.0005,
+                                                                nblocks=64)
+    n, ncols = len(genome), len(rg)
+    t = [torch.from_numpy(np.ascontiguousarray(x)).to(dev) for x in (gs, rs, off.view(np.int64), rg, rr, genome, ref)]
+    d_lut = torch.empty(n, dtype=torch.int32, device=dev)
+    ptrs = [x.data_ptr() for x in t]
+
+    def dev_step():
+        iu.buildIndexLutDev(*ptrs[:5], len(gs), ptrs[5], n, ptrs[6], len(ref), d_lut.data_ptr(), n, ctx=ctx)
+
+    blocks = iu.Blocks(gs, rs, off, rg, rr)
+    host_lut = None
+    for _ in range(max(3, args.warmup)):
+        dev_step()
+        host_lut = iu.buildIndexFromGroups(blocks, n, genome, ref, ctx=ctx)
+    reps = max(3, args.steps)
+    ms = []
+    launches0 = ctx.kernel_launches()
+    for _ in range(reps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        dev_step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    launches = (ctx.kernel_launches() - launches0) / reps
+    wall = []
+    for _ in range(reps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        host_lut = iu.buildIndexFromGroups(blocks, n, genome, ref, ctx=ctx)
+        wall.append(time.perf_counter() - t0)
+    dev_ms = sorted(ms)[len(ms) // 2]
+    e2e_s = sorted(wall)[len(wall) // 2]
+    same_paths = bool(np.array_equal(d_lut.cpu().numpy(), host_lut))
+    # algorithmic bytes: both rows once, the LUT written once and read by each clean-up pass
+    alg = 2.0 * ncols + 4.0 * n * 3
+    return {
+        "workload": "index LUT of a %.1f Mbp genome from %d aligned blocks (%d columns; 2%% substitutions, "
+                    "0.05%% indels), fixZeroIdx + fillGaps(300) + smoothEdges(20)" % (n / 1e6, len(gs), ncols),
+        "value": round(n / 1e6 / (dev_ms / 1e3), 2), "unit": "Mbp/s", "ms": round(dev_ms, 4),
+        "e2e": {"value": round(n / 1e6 / e2e_s, 2), "unit": "Mbp/s", "ms": round(e2e_s * 1e3, 3),
+                "h2d_bytes_per_step": int(2 * ncols + 16 * len(gs) + 8 + n + len(ref)),
+                "d2h_bytes_per_step": int(4 * n)},
+        "roofline": {"bound": "hbm", "achieved": round(alg / (dev_ms / 1e3) / 1e9, 2), "unit": "GB/s",
+                     "algorithmic_bytes": alg, "note": "launch- and sync-bound at this size"},
+        "gpu_launches_per_step": launches, "device_and_host_paths_identical": same_paths,
+        "_host_lut": host_lut, "_inputs": (gs, rs, off, rg, rr, genome, ref),
+    }
+
+
+def cpu_lut(inputs):
+    """The oracle's LUT path on one host thread (CPU baseline and check)."""
+    import oracle as O
+    gs, rs, off, rg, rr, genome, ref = inputs
+    n = len(genome)
+    lut = np.empty(n, np.int32)
+    t0 = time.perf_counter()
+    rc = O.lib().mo_lut_from_blocks(O._p(gs), O._p(rs), O._p(off), O._p(rg), O._p(rr), len(gs), O._p(lut), n)
+    O.fix_zero_idx(lut, genome, ref)
+    O.fill_gaps(lut, 300)
+    O.smooth_edges(lut, 20)
+    dt = time.perf_counter() - t0
+    return rc, lut, dt
 
 
 # ------------------------------------------------------------- arms
@@ -368,6 +488,9 @@ def run_gb300(args, world, rank, local):
             "clocks": clocks_anchor,
         })
 
+    if args.only in ("all", "anchor") and world == 1:
+        line["reference_fixture_pair"] = mds42_section(ctx, dev, stream, flush)
+
     if args.only in ("all", "gapdp"):
         sa, oa, sb, ob = synth.gap_batch(seed=3 + rank, nprob=args.gap_nprob)
         oa = oa.astype(np.uint64)
@@ -432,6 +555,14 @@ def run_gb300(args, world, rank, local):
         if lb_section:
             line["gap_dp"]["learned_band"] = lb_section
 
+    lut_sec = None
+    if args.only in ("all", "lut"):
+        lut_sec = lut_section(ctx, args, dev, stream, rank, flush)
+        launches += int(lut_sec["gpu_launches_per_step"])
+        line["index_lut"] = {k: v for k, v in lut_sec.items() if not k.startswith("_")}
+        if args.only == "lut":
+            line.update({"value": lut_sec["value"], "unit": "Mbp/s", "ms_per_step": lut_sec["ms"]})
+
     line["gpu_launches"] = int(launches)
     if rank != 0:
         if world > 1:
@@ -445,6 +576,12 @@ def run_gb300(args, world, rank, local):
             line["cpu_baseline"] = {"value": round((na + nb) / 1e6 / ts[0], 4), "unit": "Mbp/s", "cores": 1,
                                     "kind": "port",
                                     "sample": "the full pair once (oracle restatement, one thread)"}
+        if lut_sec is not None:
+            rc, cl, dt = cpu_lut(lut_sec["_inputs"])
+            line["index_lut"]["cpu_baseline"] = {
+                "value": round(len(cl) / 1e6 / dt, 2), "unit": "Mbp/s", "cores": 1, "kind": "port",
+                "sample": "the same alignment once (oracle restatement of buildindex.py:112-137, one thread)"}
+            line["index_lut"]["identical_to_oracle"] = bool(rc == 0 and np.array_equal(cl, lut_sec["_host_lut"]))
         if args.only in ("all", "gapdp"):
             threads = multiprocessing.cpu_count()
             cg, ccells, cdt = cpu_gapdp_gcups(sa, oa, sb, ob, 400, threads)
@@ -465,7 +602,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--skip-cpu-baseline", action="store_true")
-    ap.add_argument("--only", choices=["all", "anchor", "gapdp"], default="all",
+    ap.add_argument("--only", choices=["all", "anchor", "gapdp", "lut"], default="all",
                     help="run one half only (small cases for profiler captures)")
     ap.add_argument("--pair", choices=["recoded", "small"], default="recoded",
                     help="genome pair: recoded 4.6 Mbp (default) or the 1 Mbp plain-method pair")

@@ -134,12 +134,16 @@ int mvg_gapdp_batch_dev(mvg_handle h, const uint8_t* d_seq_a, const uint64_t* d_
  * first aligned inside the diagonal band of half-width band_half[p] around
  * j = i*LB/LA + band_delta[p] (host arrays).  The banded result is kept only
  * if its score is strictly above an upper bound on every path that leaves
- * the band (best exit-cell score + 160 per remaining diagonal step); then its
- * path equals the full NWSmall path.  Otherwise the problem is re-run through
- * the full DP.  Output is therefore always identical to mvg_gapdp_batch.
- * used_band[p] (host, may be NULL) gets 1 when the band was accepted;
- * *cells (may be NULL) gets the DP cells actually computed.  No counterpart in
- * the reference (a new method behind GlobalAlign, MU/glbalign.cpp:69). */
+ * the band (best exit-cell score + the sum of the best NUC_SP + 60 entry of
+ * each base the path would still have to consume, taking the smaller of the
+ * two sequences' sums); then its path equals the full NWSmall path.
+ * Otherwise the problem is re-run through the full DP.  A band whose strips
+ * cover at least half of the matrix is not tried.  Output is therefore always
+ * identical to mvg_gapdp_batch.  used_band[p] (host, may be NULL) gets 1 when
+ * the banded result was kept, 0 when the band was tried and rejected, 2 when
+ * it was not tried; *cells (may be NULL) gets the DP cells actually computed.
+ * No counterpart in the reference (a new method behind GlobalAlign,
+ * MU/glbalign.cpp:69). */
 int mvg_gapdp_banded(mvg_handle h, const uint8_t* seq_a, const uint64_t* off_a, const uint8_t* seq_b,
                      const uint64_t* off_b, int64_t nprob, const int32_t* band_delta, const int32_t* band_half,
                      int32_t* scores, char* paths, const uint64_t* path_off, int64_t* path_len,
@@ -199,7 +203,8 @@ int mvg_band_propose_dev(mvg_handle h, const uint8_t* d_seq_a, const uint64_t* d
  * start_idx as the XMFA parse gives them.  Callers pass only groups where
  * both sequences are present (lookupSubAlignment, mauve/indexutils.pyx:17-24,
  * returned both).  Limits: n <= 2^31-1 entries, fewer than 2^32-1 columns.
- * The _dev forms take device pointers and run on the handle's stream. */
+ * The _dev forms take device pointers and run on the handle's stream; like
+ * every entry point they return once their GPU work has finished. */
 
 /* mauve/buildindex.py:112-130: LUT of n entries from the blocks (later
  * blocks and columns overwrite earlier ones; a write at genome index -1
@@ -258,7 +263,7 @@ int mvg_build_index_lut_dev(mvg_handle h, const int64_t* d_genome_start, const i
 int mvg_set_tb_arena(mvg_handle h, uint64_t bytes);
 
 /* Gap-DP kernel shape: rows per lane for the full DP (4 or 8) and for banded
- * passes (2, 4 or 8); strips are 32*rows rows.  The Python binding applies
+ * passes (1, 2, 4 or 8); strips are 32*rows rows.  The Python binding applies
  * the tuned choice committed in mauve-py_gb300/dp_tuning.json. */
 int mvg_set_dp_rows(mvg_handle h, int full_rows, int band_rows);
 

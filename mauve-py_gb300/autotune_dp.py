@@ -4,7 +4,7 @@
     python mauve-py_gb300/autotune_dp.py [--nprob 4000]
 
 Knobs: rows per lane of the full-DP kernel (4 or 8: strips of 128 or 256
-rows) and of the banded kernel (2, 4 or 8).  The full DP is timed on a
+rows) and of the banded kernel (1, 2, 4 or 8).  The full DP is timed on a
 sample of the gap-DP distribution (lengths log-uniform 10-20,000,
 divergence U(0,30%)); the banded DP on gaps drawn like the recoded-genome
 pair's, with the trained band-proposal network's bands when weights are
@@ -55,12 +55,12 @@ def run(args):
     else:
         d, h = bandnet.heuristic_band(band.la, band.lb)
         src = "network-free band"
-    for rows in (2, 4, 8):
+    for rows in (1, 2, 4, 8):
         ctx.set_dp_rows(best_full, rows)
         timed_banded(ctx, band, d, h)  # warm
         secs, used, cells = min((timed_banded(ctx, band, d, h)[:3] for _ in range(2)), key=lambda t: t[0])
         res["banded"][rows] = {"seconds": secs, "effective_gcups": band.cells / secs / 1e9,
-                               "accept_rate": float(used.mean()), "cells": cells}
+                               "accept_rate": float((used == 1).mean()), "cells": cells}
     best_band = max(res["banded"], key=lambda r: res["banded"][r]["effective_gcups"])
     out = {"full_rows_per_lane": int(best_full), "band_rows_per_lane": int(best_band),
            "measured": res, "band_source": src, "gpu": torch.cuda.get_device_name(0),

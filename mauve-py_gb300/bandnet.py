@@ -9,9 +9,13 @@ that is too narrow costs a fallback, never a wrong answer.
 Labels come from the exact full DP run on the GPU: the optimal path's
 envelope (extreme deviations from the diagonal j = i*LB/LA) gives the
 offset, and the half-width is the larger of the envelope half-width and
-the width the exactness check needs, min(LA, LB) - score/160 (an exit
-reached from the free row-0 insertion run at column h is bounded by
-160 * (min(LA, LB) - h)).  Targets: offset / 100 and log(1 + half-width).
+an estimate of the width the exactness check needs.  The check bounds a
+path leaving the band by its exit score plus the sum of the best per-base
+scores of what remains; an exit k columns off the optimal path costs one
+gap (400) and forgoes about 155 per skipped base, so bands need roughly
+(best total - score - 400) / 155 columns each side, where best total =
+min over the two sequences of the sum of each base's best NUC_SP + 60
+entry.  Targets: offset / 100 and log(1 + half-width).
 """
 import ctypes
 
@@ -23,6 +27,17 @@ N_IN, N_HID, N_OUT = 528, 256, 2
 DELTA_SCALE = 100.0
 DELTA_CLIP = 10.0
 MAX_PAIR = 160
+# best NUC_SP + 60 entry per base code A, C, G, T (MU/nucmx.cpp:8-25 diagonal + 60)
+BASE_BEST = np.array([151, 160, 160, 151], np.int64)
+
+
+def best_totals(seq, off):
+    """Per problem: sum over its bases of BASE_BEST (the banded bound's total)."""
+    seq = np.asarray(seq)
+    off = np.asarray(off, np.int64)
+    v = BASE_BEST[seq & 3]
+    cs = np.concatenate([[0], np.cumsum(v)])
+    return cs[off[1:]] - cs[off[:-1]]
 
 
 def init_params(seed=0):
@@ -39,14 +54,17 @@ def init_params(seed=0):
     return p
 
 
-def labels_from_full_dp(la, lb, scores, env, margin=8):
-    """(offset target, log(1 + half) target, offset, half) from full-DP results."""
+def labels_from_full_dp(la, lb, scores, env, margin=8, totals=None):
+    """(offset target, log(1 + half) target, offset, half) from full-DP
+    results.  totals = (best_totals of A, of B); without them the need is
+    estimated with 160 per base."""
     la = la.astype(np.int64)
     lb = lb.astype(np.int64)
     lo, hi = env[:, 0].astype(np.int64), env[:, 1].astype(np.int64)
     delta = (lo + hi) // 2
     half_env = (hi - lo + 1) // 2 + margin
-    need = np.minimum(la, lb) - scores.astype(np.int64) // MAX_PAIR + margin
+    best = np.minimum(totals[0], totals[1]) if totals is not None else MAX_PAIR * np.minimum(la, lb)
+    need = np.maximum(best - scores.astype(np.int64) - 400, 0) // 155 + margin
     half = np.maximum(half_env, need)
     half = np.clip(half, 0, np.maximum(la, lb))
     # offsets beyond +-1000 columns are clipped in the target: such gaps need a

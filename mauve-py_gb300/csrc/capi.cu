@@ -386,8 +386,9 @@ int mvg_set_tb_arena(mvg_handle h, uint64_t bytes) {
 }
 
 int mvg_set_dp_rows(mvg_handle h, int full_rows, int band_rows) {
-  if (!h || (full_rows != 4 && full_rows != 8) || (band_rows != 2 && band_rows != 4 && band_rows != 8))
-    return report_error(MVG_ERR_ARG, "rows per lane: full DP 4 or 8, banded 2, 4 or 8");
+  if (!h || (full_rows != 4 && full_rows != 8) ||
+      (band_rows != 1 && band_rows != 2 && band_rows != 4 && band_rows != 8))
+    return report_error(MVG_ERR_ARG, "rows per lane: full DP 4 or 8, banded 1, 2, 4 or 8");
   h->dp_rows = full_rows;
   h->band_rows = band_rows;
   return 0;

@@ -25,17 +25,29 @@
 
 namespace mvg {
 
+// Best score of each base code, biased, one byte per code (the banded
+// kernel's bound).  The matrix is symmetric, so row and column maxima agree.
+static uint32_t g_base_max = 0;
+
 static bool score_rows_host(uint32_t* rows) {
   const int sp[4][4] = {{91, -114, -31, -123}, {-114, 100, -125, -31}, {-31, -125, 100, -114}, {-123, -31, -114, 91}};
+  uint32_t bm = 0;
   for (int a = 0; a < 4; ++a) {
     uint32_t r = 0;
+    int best = -1000;
     for (int b = 0; b < 4; ++b) {
       const int v = sp[a][b] + 60 + kScoreBias;
       if (v < 0 || v > 255) return false;
+      if (sp[a][b] != sp[b][a]) return false;
       r |= (uint32_t)v << (8 * b);
+      best = best > v ? best : v;
     }
+    // the bound sums these maxima over unused bases too: they must be >= 0
+    if (best - kScoreBias < 0) return false;
     rows[a] = r;
+    bm |= (uint32_t)best << (8 * a);
   }
+  g_base_max = bm;
   return true;
 }
 
@@ -51,6 +63,7 @@ template __global__ void k_gapdp_t<true, 4>(DpJob);
 template __global__ void k_gapdp_t<false, 8>(DpJob);
 template __global__ void k_gapdp_t<true, 8>(DpJob);
 template __global__ void k_gapdp_t<true, 2>(DpJob);
+template __global__ void k_gapdp_t<true, 1>(DpJob);
 
 // BitTraceBack from (LA, LB); writes the path reversed at the end of the
 // problem's path slot and its length.  Banded problems index their strips
@@ -261,7 +274,8 @@ static int run_dp(Ctx* c, const DpInputs& in, const std::vector<uint32_t>& ids, 
   MVG_CUDA_TRY(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, c->device));
   void (*kern)(DpJob) = rows == 8   ? (banded ? k_gapdp_t<true, 8> : k_gapdp_t<false, 8>)
                         : rows == 4 ? (banded ? k_gapdp_t<true, 4> : k_gapdp_t<false, 4>)
-                                    : k_gapdp_t<true, 2>;
+                        : rows == 2 ? k_gapdp_t<true, 2>
+                                    : k_gapdp_t<true, 1>;
   int bps = 0;
   MVG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kern, kDpThreads, 0));
   if (bps < 1) bps = 1;
@@ -298,6 +312,7 @@ static int run_dp(Ctx* c, const DpInputs& in, const std::vector<uint32_t>& ids, 
     J.band_delta = d_delta;
     J.band_half = d_half;
     J.accept = d_accept;
+    J.base_max = g_base_max;
     J.counter = d_counter;
     J.err = c->d_err;
     MVG_CUDA_TRY(cudaMemsetAsync(d_counter, 0, 8, c->stream));
@@ -395,9 +410,17 @@ int gapdp_banded_dev(Ctx* c, const uint8_t* d_sa, const uint64_t* d_oa, const ui
   if (!d_paths && (rc = scratch_paths(c, nprob, la, lb, in))) return rc;
   std::vector<int32_t> dv(h_delta, h_delta + nprob), hv(h_half, h_half + nprob);
   uint64_t bc = 0;
+  // a band covering at least half of its matrix saves little and may still
+  // fail its check: such problems go straight to the full DP
+  std::vector<uint32_t> ids;
+  ids.reserve(nprob);
   for (int64_t p = 0; p < nprob; ++p) {
     if (hv[p] < 0) return report_error(MVG_ERR_ARG, "negative band half-width");
-    bc += band_cells(make_band((int)la[p], (int)lb[p], dv[p], hv[p], 32 * c->band_rows));
+    const uint64_t cells = band_cells(make_band((int)la[p], (int)lb[p], dv[p], hv[p], 32 * c->band_rows));
+    if (2 * cells < (uint64_t)la[p] * (uint64_t)lb[p]) {
+      ids.push_back((uint32_t)p);
+      bc += cells;
+    }
   }
   int32_t* d_delta = (int32_t*)c->ws.get(c, 23, (size_t)nprob * 4);
   int32_t* d_half = (int32_t*)c->ws.get(c, 25, (size_t)nprob * 4);
@@ -408,19 +431,22 @@ int gapdp_banded_dev(Ctx* c, const uint8_t* d_sa, const uint64_t* d_oa, const ui
   MVG_CUDA_TRY(cudaMemsetAsync(d_accept, 0, (size_t)nprob, c->stream));
   MVG_CUDA_TRY(cudaMemsetAsync(c->d_err, 0, 4, c->stream));
   if ((rc = check_codes(c, d_sa, h_oa[nprob], d_sb, h_ob[nprob]))) return rc;
-  std::vector<uint32_t> ids(nprob);
-  std::iota(ids.begin(), ids.end(), 0u);
   stage_begin_call(c);
-  rc = run_dp(c, in, ids, la, lb, d_delta, d_half, &dv, &hv, d_accept);
-  if (rc) return rc;
+  if (!ids.empty()) {
+    rc = run_dp(c, in, ids, la, lb, d_delta, d_half, &dv, &hv, d_accept);
+    if (rc) return rc;
+  }
   std::vector<uint8_t> acc(nprob);
   MVG_CUDA_TRY(cudaMemcpyAsync(acc.data(), d_accept, (size_t)nprob, cudaMemcpyDeviceToHost, c->stream));
   MVG_CUDA_TRY(cudaStreamSynchronize(c->stream));
   std::vector<uint32_t> fallback;
+  std::vector<uint8_t> tried(nprob, 0);
+  for (uint32_t p : ids) tried[p] = 1;
   for (int64_t p = 0; p < nprob; ++p)
     if (!acc[p]) {
       fallback.push_back((uint32_t)p);
       bc += (uint64_t)la[p] * (uint64_t)lb[p];
+      if (!tried[p]) acc[p] = 2;  // not tried: the band covered at least half the matrix
     }
   // rejected bands: the full DP is both the fallback and the judge
   rc = run_dp(c, in, fallback, la, lb, nullptr, nullptr, nullptr, nullptr, nullptr);

@@ -28,10 +28,15 @@
 // Banded mode: strip k only spans columns [jlo_k, jhi_k] of a diagonal band
 // (band.h), everything outside is -infinity, and the kernel also computes an
 // upper bound on every path that leaves the band: the best exit-cell score
-// plus 160 (the largest NUC_SP + 60 entry) per remaining diagonal step.  A
-// banded result is accepted only when its score is strictly above that bound;
-// then the reference's optimal path provably stays in the band and every
-// traceback decision along it is the same as in the full DP.
+// plus the largest score the rest of the path could still collect.  From
+// cell (i, j) the rest consumes A[i..LA) and B[j..LB); gap steps score <= 0
+// and each match step pairs one base of each, scoring at most that base's
+// best NUC_SP + 60 entry, so the rest scores at most
+// min(sum of row maxima over A[i..LA), sum of column maxima over B[j..LB)).
+// Those suffix sums come from per-problem totals and running prefix sums.  A
+// banded result is accepted only when its score is strictly above the
+// bound; then the reference's optimal path provably stays in the band and
+// every traceback decision along it is the same as in the full DP.
 #pragma once
 #include "band.h"
 #include "mvg_common.cuh"
@@ -70,6 +75,7 @@ struct DpJob {
   const int32_t* band_delta;  // banded mode: per problem
   const int32_t* band_half;
   uint8_t* accept;            // banded mode: 1 if the band result is exact
+  uint32_t base_max;          // banded mode: best score of each base code, byte c = max + kScoreBias
   unsigned* counter;          // [0] large-problem claims (per CTA), [1] small-problem claims (per warp)
   uint32_t* err;
 };
@@ -119,6 +125,22 @@ __device__ __forceinline__ uint32_t dp_column(DpLane<R>& L, int32_t upM, int32_t
   return nibs;
 }
 
+// Sum over s[from, to) of each base's best score (warp-wide, every lane
+// gets the total).  base_max packs the biased maxima of codes 0..3.
+__device__ __forceinline__ int32_t warp_best_sum(const uint8_t* s, int from, int to, uint32_t base_max) {
+  const int lane = threadIdx.x & 31;
+  int32_t acc = 0;
+  for (int t = from + lane; t < to; t += 32) acc += (int32_t)__byte_perm(base_max, 0u, (s[t] & 3u) | 0x4440u) - kScoreBias;
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, d);
+  return acc;
+}
+
+// selector nibbles 1..3 = 4 pick zero bytes of the second operand
+__device__ __forceinline__ int32_t best_of(uint32_t base_max, uint32_t code) {
+  return (int32_t)__byte_perm(base_max, 0u, (code & 3u) | 0x4440u) - kScoreBias;
+}
+
 // Shared state of one CTA.
 struct DpShared {
   uint8_t ringB[kDpWarps][128];
@@ -151,6 +173,13 @@ __device__ void dp_solve(const DpJob& J, DpShared& sh, int w, int kstart, int ks
   const int end_r = (LA - 1) % R;
   const Band band = BANDED ? make_band(LA, LB, J.band_delta[p], J.band_half[p], SR) : make_full(LA, LB, SR);
   int32_t bound = kNeg;  // best score of any path leaving the band (this warp's part)
+  // banded mode: totals and running prefixes of the per-base best scores
+  int32_t totA = 0, totB = 0, pa = 0, pb_lo = 0, pb_hi = 0;
+  int pa_rows = 0, pb_lo_cols = 0, pb_hi_cols = 0;
+  if (BANDED) {
+    totA = warp_best_sum(A, 0, LA, J.base_max);
+    totB = warp_best_sum(B, 0, LB, J.base_max);
+  }
   uint32_t* tbs = J.tb + J.tb_off[w] / 4;
   for (int k = 0; k < kstart; ++k) tbs += (int64_t)tb_words_per_lane(band_hi(band, k) - band_lo(band, k) + 1, R) * 32;
 
@@ -204,6 +233,33 @@ __device__ void dp_solve(const DpJob& J, DpShared& sh, int w, int kstart, int ks
       L.arow[r] = c_score_rows[(i <= LA ? A[i - 1] : 0u) & 3u];
     }
     const int32_t goA0 = (row0 + lane * R + 1 == 1) ? 0 : kGap;
+    // banded mode: prefix of the row maxima up to each owned row, the
+    // strip's bottom row, and the column prefix at jlo-1 for lane 31
+    int32_t rowpre[R];
+    int32_t strip_pre = 0, run31 = 0;
+    if (BANDED) {
+      pa += warp_best_sum(A, pa_rows, row0, J.base_max);
+      pa_rows = row0;
+      int32_t lsum = 0;
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const int i = row0 + lane * R + r + 1;
+        lsum += i <= LA ? best_of(J.base_max, A[i - 1]) : 0;
+        rowpre[r] = lsum;
+      }
+      int32_t incl = lsum;
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        const int32_t t = __shfl_up_sync(0xffffffffu, incl, d);
+        if (lane >= d) incl += t;
+      }
+#pragma unroll
+      for (int r = 0; r < R; ++r) rowpre[r] += pa + incl - lsum;  // PA after row r
+      strip_pre = pa + __shfl_sync(0xffffffffu, incl, 31);
+      pb_lo += warp_best_sum(B, pb_lo_cols, jlo - 1, J.base_max);
+      pb_lo_cols = jlo - 1;
+      run31 = pb_lo;
+    }
     // Row above this strip at absolute column x: row 0 for the first strip,
     // else the previous strip's computed columns, its left boundary or -inf.
     auto above = [&](int x) -> int4 {
@@ -233,7 +289,6 @@ __device__ void dp_solve(const DpJob& J, DpShared& sh, int w, int kstart, int ks
     int32_t upM = kNeg, upD = kNeg, upI = kNeg;      // row above, current column
     uint32_t acc = 0;
     const bool bottom_exit = BANDED && lane == 31 && row0 + SR < LA;
-    const int32_t rem_rows = LA - (row0 + SR);
     const bool writes_row = k + 1 < nstrips;
     bool alive = true;
 
@@ -283,9 +338,12 @@ __device__ void dp_solve(const DpJob& J, DpShared& sh, int w, int kstart, int ks
         pubD = L.lD[R - 1];
         pubI = L.lI[R - 1];
         if (lane == 31 && writes_row) rb_out[j] = make_int4(pubM, pubD, pubI, 0);
-        if (BANDED && bottom_exit && j < next_lo) {
-          const int32_t best = max(pubM, max(pubD, pubI));
-          bound = max(bound, best + kMaxPair * min(rem_rows, LB - j));
+        if (BANDED && bottom_exit) {
+          run31 += best_of(J.base_max, bsel);  // prefix over B[0..j)
+          if (j < next_lo) {
+            const int32_t best = max(pubM, max(pubD, pubI));
+            bound = max(bound, best + min(totA - strip_pre, totB - run31));
+          }
         }
       } else if (jj == -1) {
         pubM = kNeg;
@@ -339,12 +397,14 @@ __device__ void dp_solve(const DpJob& J, DpShared& sh, int w, int kstart, int ks
       J.end_edge[p] = (uint8_t)e;
     }
     if (BANDED && jhi < LB) {  // right-edge exits: an I step leaves the band
+      pb_hi += warp_best_sum(B, pb_hi_cols, jhi, J.base_max);
+      pb_hi_cols = jhi;
 #pragma unroll
       for (int r = 0; r < R; ++r) {
         const int i = row0 + lane * R + r + 1;
         if (i <= LA) {
           const int32_t best = max(L.lM[r], max(L.lD[r], L.lI[r]));
-          bound = max(bound, best + kMaxPair * min(LA - i, LB - jhi));
+          bound = max(bound, best + min(totA - rowpre[r], totB - pb_hi));
         }
       }
     }
@@ -354,11 +414,15 @@ __device__ void dp_solve(const DpJob& J, DpShared& sh, int w, int kstart, int ks
   }
   if (BANDED) {
     // paths along row 0 past the band, or down column 0 past it (added once)
-    if (lane == 0 && kstart == 0) {
+    if (kstart == 0) {
       const int hi0 = band_hi(band, 0);
-      if (hi0 < LB) bound = max(bound, kMaxPair * min(LA, LB - hi0));
       const int last_col0 = band_last_row_at_col1(band, LA);
-      if (last_col0 < LA) bound = max(bound, kMaxPair * min(LA - last_col0, LB));
+      const int32_t pb0 = hi0 < LB ? warp_best_sum(B, 0, hi0, J.base_max) : 0;
+      const int32_t pa0 = last_col0 < LA ? warp_best_sum(A, 0, last_col0, J.base_max) : 0;
+      if (lane == 0) {
+        if (hi0 < LB) bound = max(bound, min(totA, totB - pb0));
+        if (last_col0 < LA) bound = max(bound, min(totA - pa0, totB));
+      }
     }
 #pragma unroll
     for (int d = 16; d > 0; d >>= 1) bound = max(bound, __shfl_xor_sync(0xffffffffu, bound, d));

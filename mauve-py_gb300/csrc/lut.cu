@@ -369,7 +369,7 @@ __global__ void k_count_dups(const uint32_t* __restrict__ counts, int64_t nc, un
 
 // Workspace slots of this file.
 enum : int {
-  kWsSegN = 46, kWsSegStart, kWsSegBlock, kWsSegG, kWsSegR, kWsScan, kWsKeys, kWsFlags, kWsCand, kWsReach, kWsLval,
+  kWsSegN = 70, kWsSegStart, kWsSegBlock, kWsSegG, kWsSegR, kWsScan, kWsKeys, kWsFlags, kWsCand, kWsReach, kWsLval,
   kWsHead, kWsActive, kWsCounts, kWsMeta,
   // host-API staging
   kWsHLut, kWsHAux, kWsHGenome, kWsHRef, kWsHRowG, kWsHRowR, kWsHStarts, kWsHOff
@@ -442,7 +442,10 @@ int lut_fix_zero_dev(Ctx* c, int32_t* d_lut, int64_t n, const uint8_t* d_genome,
 int lut_fill_dev(Ctx* c, int32_t* d_lut, int64_t n, int width, int mode, int32_t* d_gaps) {
   cudaStream_t st = c->stream;
   if (d_gaps && n > 0) MVG_CUDA_TRY(cudaMemsetAsync(d_gaps, 0, (size_t)n * 4, st));
-  if (n < 2 || width < 1) return 0;  // the reference loops never find a partner
+  if (n < 2 || width < 1) {  // the reference loops never find a partner
+    MVG_CUDA_TRY(cudaStreamSynchronize(st));
+    return 0;
+  }
   uint32_t* flags = wsu32(c, kWsFlags, (uint64_t)n);
   uint32_t* scr = wsu32(c, kWsScan, scan_scratch_words(n) + 8);
   if (!flags || !scr) return report_error(MVG_ERR_NOMEM, "LUT fill allocation failed");
@@ -451,7 +454,7 @@ int lut_fill_dev(Ctx* c, int32_t* d_lut, int64_t n, int width, int mode, int32_t
   exclusive_scan(flags, flags, n, scr, d_tot, st, &c->launches);
   c->launches++;
   uint32_t ncand = 0;
-  if (int rc = read_u32(c, d_tot, &ncand)) return rc;
+  if (int rc = read_u32(c, d_tot, &ncand)) return rc;  // synchronises the stream
   if (ncand == 0) return 0;
   int32_t* cand = (int32_t*)wsu32(c, kWsCand, ncand);
   int32_t* reach = (int32_t*)wsu32(c, kWsReach, ncand);
@@ -467,6 +470,9 @@ int lut_fill_dev(Ctx* c, int32_t* d_lut, int64_t n, int width, int mode, int32_t
   k_fill_apply<<<grid_for((uint64_t)ncand * 32, 256), 256, 0, st>>>(d_lut, cand, reach, lval, active, ncand, d_gaps);
   c->launches += 6;
   MVG_CUDA_TRY(cudaGetLastError());
+  // like every entry point, return once the LUT is final (callers read it
+  // on other streams)
+  MVG_CUDA_TRY(cudaStreamSynchronize(st));
   return 0;
 }
 
@@ -475,6 +481,7 @@ int lut_find_edges_dev(Ctx* c, const int32_t* d_lut, int64_t n, uint8_t* d_edges
   k_find_edges<<<grid_for((uint64_t)n, 256), 256, 0, c->stream>>>(d_lut, n, d_edges);
   c->launches++;
   MVG_CUDA_TRY(cudaGetLastError());
+  MVG_CUDA_TRY(cudaStreamSynchronize(c->stream));
   return 0;
 }
 

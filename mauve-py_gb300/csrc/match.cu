@@ -15,15 +15,16 @@
 //   k_hash_pairs                         SetDirection + CalculateOffset +
 //                                       bucket id per pair
 //   stable radix sort by bucket          keeps key order inside a bucket
-//   k_bucket_warps                       one warp per bucket replays the
+//   k_bucket_replay                      per bucket (a CTA for big buckets,
+//                                       a warp for the rest) replays the
 //                                       reference's sequence of containment
-//                                       tests and inserts exactly: 32 seeds
+//                                       tests and inserts exactly: many seeds
 //                                       are tested at once against the
 //                                       current bucket, the first one not
-//                                       contained is extended warp-
-//                                       cooperatively (32 candidate windows
-//                                       per ballot) and inserted, and the
-//                                       seeds after it are re-tested
+//                                       contained is extended by its warp
+//                                       (match bits of the diagonal cached
+//                                       in shared memory) and inserted, and
+//                                       the seeds after it are re-tested
 //   k_emit                               GetMatchList order: bucket 0..39999,
 //                                       then bucket vector order
 #include "mvg_internal.h"
@@ -173,37 +174,96 @@ __device__ __forceinline__ int64_t lower_bound_mhe(const Mhe* __restrict__ v, in
   return first;
 }
 
-// Does the window pair after k steps of size J match?  State (st0, st1, len)
-// is the match before the steps; positive starts move left by k*J, the
-// length grows by k*J (LM/MatchFinder.h:265-318).
-__device__ __forceinline__ bool window_match(const MatchCtx& c, int64_t st0, int64_t st1, int64_t len, int64_t kJ) {
-  const int L = c.s.L;
-  const int64_t lk = len + kJ;
-  int64_t st[2] = {st0, st1};
-  uint64_t mer[2];
-  bool par[2];
-#pragma unroll
-  for (int q = 0; q < 2; ++q) {
-    int64_t sq = st[q] > 0 ? st[q] - kJ : st[q];
-    int64_t get = sq < 0 ? -sq + lk - L : sq;
-    uint64_t cm = canonical_mer(c.g[q], (uint64_t)(get - 1), c.s);
-    par[q] = sq < 0 ? (bool)(cm & 1ull) : !(cm & 1ull);
-    mer[q] = cm & c.s.seed_mask;
-  }
-  return mer[0] == mer[1] && par[0] == par[1];
-}
-
 // ExtendMatch (LM/MatchFinder.h:218-374) for two genomes, executed by a full
 // warp in lockstep.  Phases 0/1 jump by the seed length until the first
-// mismatching window (32 jumps per ballot); phases 2/3 try the L single-base
-// offsets at once and move to the furthest matching one; any such move
-// restarts the four phases.
-__device__ void warp_extend(const MatchCtx& c, Mhe& m) {
+// mismatching window; phases 2/3 try the L single-base offsets and move to
+// the furthest matching one; any such move restarts the four phases.
+//
+// Every window pair the walk tests lies on the match's diagonal: in the
+// entry orientation S0, the pair tested at step size k from the current
+// left edge is the pair at displacement ML + k from the entry left edge (ML
+// = total moved in even phases), and in the inverted orientation the pair
+// at MR + k from the entry right edge (MR = total moved in odd phases);
+// positive starts move by exactly those amounts and negative starts stay.
+// So the walk reads match bits of the two sides, computed 1024 displacements
+// at a time into per-warp shared rings, instead of recomputing seed windows
+// in every phase.  For a same-strand pair a window pair matches iff the
+// pattern-selected bases are equal (equal canonical mers with equal strand
+// bits); other pairs use the canonical-mer test itself.
+constexpr int kExtRing = 128;    // words per side: the last 4096 displacements
+constexpr int kExtChunk = 1024;  // displacements per fill (32 per lane)
+
+struct ExtRing {
+  uint32_t w[2][kExtRing];
+};
+
+// 2-bit mask of the pattern's bases in a 64-bit window (base 0 in bits 63:62).
+__device__ __forceinline__ uint64_t pattern_mask64(const SeedDesc& s) {
+  uint64_t m = 0;
+  for (int r = 0; r < s.nruns; ++r)
+    for (int b = 0; b < s.run_len[r]; ++b) m |= 3ull << (62 - 2 * (s.run_start[r] + b));
+  return m;
+}
+
+// Window start (0-based) in genome q of the pair at displacement u from the
+// entry state's edge (st, len), or -1 outside the genome.
+__device__ __forceinline__ int64_t ext_start(int64_t st, int64_t len, int64_t u, int L, int64_t n) {
+  const int64_t sq = st > 0 ? st - u : st;
+  const int64_t get = sq < 0 ? -sq + len + u - L : sq;
+  const int64_t x = get - 1;
+  return (x >= 0 && x + L <= n) ? x : -1;
+}
+
+__device__ void ext_fill(const MatchCtx& c, int64_t st0, int64_t st1, int64_t len, int64_t u0, uint64_t pmask,
+                         uint32_t* ring) {
   const int lane = threadIdx.x & 31;
   const int L = c.s.L;
+  const bool same = (st0 > 0) == (st1 > 0);
+  uint32_t word = 0;
+  for (int t = 0; t < 32; ++t) {
+    const int64_t u = u0 + lane * 32 + t;
+    const int64_t xa = ext_start(st0, len, u, L, c.n[0]);
+    const int64_t xb = ext_start(st1, len, u, L, c.n[1]);
+    bool b = false;
+    if (u >= 1 && xa >= 0 && xb >= 0) {
+      if (same) {
+        b = ((window64(c.g[0], (uint64_t)xa) ^ window64(c.g[1], (uint64_t)xb)) & pmask) == 0;
+      } else {
+        const uint64_t ca = canonical_mer(c.g[0], (uint64_t)xa, c.s);
+        const uint64_t cb = canonical_mer(c.g[1], (uint64_t)xb, c.s);
+        const bool pa = st0 > 0 ? !(ca & 1ull) : (bool)(ca & 1ull);
+        const bool pb = st1 > 0 ? !(cb & 1ull) : (bool)(cb & 1ull);
+        b = (ca & c.s.seed_mask) == (cb & c.s.seed_mask) && pa == pb;
+      }
+    }
+    word |= (uint32_t)b << t;
+  }
+  ring[((u0 >> 5) + lane) & (kExtRing - 1)] = word;
+  __syncwarp();
+}
+
+__device__ void warp_extend(const MatchCtx& c, Mhe& m, ExtRing& R) {
+  const int lane = threadIdx.x & 31;
+  const int L = c.s.L;
+  const uint64_t pmask = pattern_mask64(c.s);
+  const int64_t e0 = m.s0, e1 = m.s1, elen = m.len;  // entry state S0
   int64_t st0 = m.s0, st1 = m.s1, len = m.len;
+  int64_t moved_side[2] = {0, 0};   // ML, MR
+  int64_t filled[2] = {0, 0};       // displacements [0, filled) of each side are in the ring
+  // bit of side sd at displacement u (u >= filled - 4096 holds for every query)
+  auto ensure = [&](int sd, int64_t umax) {
+    while (filled[sd] <= umax) {
+      if (sd == 0)
+        ext_fill(c, e0, e1, elen, filled[0], pmask, R.w[0]);
+      else
+        ext_fill(c, -e0, -e1, elen, filled[1], pmask, R.w[1]);
+      filled[sd] += kExtChunk;
+    }
+  };
+  auto bit = [&](int sd, int64_t u) -> bool { return (R.w[sd][(u >> 5) & (kExtRing - 1)] >> (u & 31)) & 1u; };
   bool extend_again = false;
   for (int dir = 0; dir < 4; ++dir) {
+    const int sd = dir & 1;
     int64_t maxlen = dir < 2 ? (int64_t)0xffffffffu : (int64_t)L;
     if (st0 < 0) {
       int64_t rc = c.n[0] - len + st0 + 1;
@@ -217,31 +277,34 @@ __device__ void warp_extend(const MatchCtx& c, Mhe& m) {
     } else if (st1 - 1 < maxlen) {
       maxlen = st1 - 1;
     }
+    const int64_t base = moved_side[sd];
     int64_t moved = 0;
     if (dir < 2) {
       const int64_t nj = maxlen >= L ? maxlen / L : 0;
       int64_t good = nj;
-      for (int64_t base = 1; base <= nj; base += 32) {
-        const int64_t k = base + lane;
-        bool bad = false;
-        if (k <= nj) bad = !window_match(c, st0, st1, len, k * L);
+      for (int64_t kb = 1; kb <= nj; kb += 32) {
+        const int64_t klast = kb + 31 < nj ? kb + 31 : nj;
+        ensure(sd, base + klast * L);
+        const int64_t k = kb + lane;
+        const bool bad = k <= nj && !bit(sd, base + k * L);
         const unsigned mm = __ballot_sync(0xffffffffu, bad);
         if (mm) {
-          good = base - 1 + (__ffs(mm) - 1);
+          good = kb - 1 + (__ffs(mm) - 1);
           break;
         }
       }
       moved = good * L;
     } else {
       const int64_t msteps = maxlen > 0 ? (maxlen < L ? maxlen : L) : 0;
+      if (msteps > 0) ensure(sd, base + msteps);
       const int64_t k = lane + 1;
-      bool ok = false;
-      if (k <= msteps) ok = window_match(c, st0, st1, len, k);
+      const bool ok = k <= msteps && bit(sd, base + k);
       const unsigned mb = __ballot_sync(0xffffffffu, ok);
       const int limit = mb ? 32 - __clz(mb) : 0;
       if (msteps > 0 && limit > 0) extend_again = true;
       moved = limit;
     }
+    moved_side[sd] += moved;
     len += moved;
     if (st0 > 0) st0 -= moved;
     if (st1 > 0) st1 -= moved;
@@ -255,70 +318,6 @@ __device__ void warp_extend(const MatchCtx& c, Mhe& m) {
   m.s0 = st0;
   m.s1 = st1;
   m.len = len;
-}
-
-// One warp per bucket (taken in descending seed count).  ent: per-bucket
-// regions of capacity = the bucket's seed count.
-__global__ void __launch_bounds__(256) k_bucket_warps(MatchCtx c, const Mhe* __restrict__ mhe,
-                                                      const uint32_t* __restrict__ sorted_pair,
-                                                      const uint32_t* __restrict__ bstart, const uint32_t* __restrict__ bcount,
-                                                      const uint32_t* __restrict__ border, int nbuckets, Mhe* ent,
-                                                      uint32_t* __restrict__ nent_out, unsigned long long* __restrict__ coll) {
-  const int lane = threadIdx.x & 31;
-  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int nw = (gridDim.x * blockDim.x) >> 5;
-  const int L = c.s.L;
-  for (int w = gw; w < nbuckets; w += nw) {
-    const uint32_t b = border[w];
-    const uint32_t cnt = bcount[b];
-    if (cnt == 0) continue;
-    Mhe* E = ent + bstart[b];
-    const uint32_t* sp = sorted_pair + bstart[b];
-    int64_t n = 0;
-    unsigned long long ncoll = 0;
-    for (uint32_t base = 0; base < cnt; base += 32) {
-      const uint32_t i = base + lane;
-      Mhe m = {0, 0, 0, 0};
-      if (i < cnt) m = mhe[sp[i]];
-      unsigned pending = __ballot_sync(0xffffffffu, i < cnt);
-      while (pending) {
-        bool coll_here = true;
-        if (pending & (1u << lane)) {
-          int64_t at = lower_bound_mhe(E, n, m, L);
-          coll_here = at != n && !mhe_less(E[at], m, L) && !mhe_less(m, E[at], L);
-        }
-        const unsigned fresh = __ballot_sync(0xffffffffu, (pending & (1u << lane)) && !coll_here);
-        if (!fresh) break;
-        const int f = __ffs(fresh) - 1;
-        ncoll += __popc(pending & ((1u << f) - 1u));
-        pending &= ~((2u << f) - 1u);
-        Mhe x;
-        x.s0 = __shfl_sync(0xffffffffu, m.s0, f);
-        x.s1 = __shfl_sync(0xffffffffu, m.s1, f);
-        x.len = __shfl_sync(0xffffffffu, m.len, f);
-        x.off = __shfl_sync(0xffffffffu, m.off, f);
-        warp_extend(c, x);
-        const int64_t at = lower_bound_mhe(E, n, x, L);
-        // shift E[at..n) right by one, 32 entries at a time from the end
-        for (int64_t hi = n - 1; hi >= at; hi -= 32) {
-          const int64_t k = hi - lane;
-          Mhe t;
-          if (k >= at) t = E[k];
-          __syncwarp();
-          if (k >= at) E[k + 1] = t;
-          __syncwarp();
-        }
-        if (lane == 0) E[at] = x;
-        __syncwarp();
-        ++n;
-      }
-      ncoll += __popc(pending);
-    }
-    if (lane == 0) {
-      nent_out[b] = (uint32_t)n;
-      atomicAdd(coll, ncoll);
-    }
-  }
 }
 
 // Buckets with at least kBigBucket seeds get a whole CTA: 256 seeds are tested
@@ -338,6 +337,7 @@ __global__ void __launch_bounds__(256) k_bucket_replay(MatchCtx c, const Mhe* __
                                                        uint32_t* __restrict__ nent_out,
                                                        unsigned long long* __restrict__ coll) {
   __shared__ Mhe sE[kCtaCap];
+  __shared__ ExtRing s_ring[8];
   __shared__ unsigned wmask[8];
   __shared__ Mhe s_x;
   __shared__ long long s_at;
@@ -391,7 +391,7 @@ __global__ void __launch_bounds__(256) k_bucket_replay(MatchCtx c, const Mhe* __
         x.s1 = __shfl_sync(0xffffffffu, m.s1, f);
         x.len = __shfl_sync(0xffffffffu, m.len, f);
         x.off = __shfl_sync(0xffffffffu, m.off, f);
-        warp_extend(c, x);
+        warp_extend(c, x, s_ring[wid]);
         const int64_t at = lower_bound_mhe(E, n, x, L);
         for (int64_t hi = n - 1; hi >= at; hi -= 32) {
           const int64_t k = hi - lane;
@@ -459,7 +459,7 @@ __global__ void __launch_bounds__(256) k_bucket_replay(MatchCtx c, const Mhe* __
       __syncthreads();
       if (wid == (f >> 5)) {
         Mhe x = s_x;
-        warp_extend(c, x);
+        warp_extend(c, x, s_ring[wid]);
         const int64_t at = lower_bound_mhe(E, n, x, L);
         if (lane == 0) {
           s_x = x;
@@ -625,7 +625,7 @@ int pairwise_matches_dev(Ctx* c, const uint8_t* d_a, uint64_t na, const uint8_t*
   uint32_t* bk1 = (uint32_t*)ws.get(c, 40, npairs * 4);
   uint32_t* or0 = (uint32_t*)ws.get(c, 41, npairs * 4);
   uint32_t* or1 = (uint32_t*)ws.get(c, 42, npairs * 4);
-  uint32_t* sscr = (uint32_t*)ws.get(c, 43, radix_scratch_words(npairs > kTableSize ? npairs : kTableSize) * 4);
+  uint32_t* sscr = (uint32_t*)ws.get(c, 43, sort_scratch_words(npairs > kTableSize ? npairs : kTableSize, 32) * 4);
   // per-bucket tables: count, start, nent, lpt key/id x2, out offsets, scan scratch, totals
   uint32_t* btab = (uint32_t*)ws.get(c, 44, (size_t)kTableSize * 4 * 10 + scan_scratch_words(kTableSize) * 4 + 256);
   Mhe* ent = (Mhe*)ws.get(c, 45, npairs * sizeof(Mhe));
@@ -648,7 +648,7 @@ int pairwise_matches_dev(Ctx* c, const uint8_t* d_a, uint64_t na, const uint8_t*
   k_hash_pairs<<<grid_for(capa, 256), 256, 0, c->stream>>>(uka, upa, ukb, upb, hit, hflag, hidx, capa, nua, s.L, mhe,
                                                             bk0, or0);
   c->launches++;
-  int which = radix_sort_pairs<uint32_t>(bk0, or0, bk1, or1, npairs, 16, sscr, c->stream, &c->launches);
+  int which = sort_pairs<uint32_t>(bk0, or0, bk1, or1, npairs, 16, sscr, c->stream, &c->launches, c->d_err);
   uint32_t* sorted_pair = which ? or1 : or0;
   const uint32_t* sorted_bucket = which ? bk1 : bk0;
   MVG_CUDA_TRY(cudaMemsetAsync(nent, 0, (size_t)kTableSize * 4, c->stream));
@@ -657,7 +657,7 @@ int pairwise_matches_dev(Ctx* c, const uint8_t* d_a, uint64_t na, const uint8_t*
   c->launches++;
   k_lpt_keys<<<grid_for(kTableSize, 256), 256, 0, c->stream>>>(bcount, lk0, li0);
   c->launches++;
-  which = radix_sort_pairs<uint32_t>(lk0, li0, lk1, li1, kTableSize, 32, sscr, c->stream, &c->launches);
+  which = sort_pairs<uint32_t>(lk0, li0, lk1, li1, kTableSize, 32, sscr, c->stream, &c->launches, c->d_err);
   const uint32_t* border = which ? li1 : li0;
   MatchCtx mc;
   mc.g[0] = ga;

@@ -70,4 +70,11 @@ void exclusive_scan(const uint32_t* in, uint32_t* out, int64_t n, uint32_t* scra
   if (launches) *launches += 3;
 }
 
+__global__ void __launch_bounds__(256) k_os_scan(uint32_t* __restrict__ ghist) {
+  uint32_t* g = ghist + blockIdx.x * 256;
+  const uint32_t v = g[threadIdx.x];
+  const uint32_t ex = block_excl_scan256(v, nullptr);
+  g[threadIdx.x] = ex;
+}
+
 }  // namespace mvg

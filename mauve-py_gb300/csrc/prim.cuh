@@ -187,4 +187,201 @@ int radix_sort_pairs(K* keys, uint32_t* vals, K* keys_alt, uint32_t* vals_alt, i
   return which;
 }
 
+// ------------------------------------------------- one-sweep radix sort
+//
+// Same stable LSD result as radix_sort_pairs, one kernel per 8-bit digit:
+//   k_os_hist   all passes' digit histograms in one read of the keys
+//   k_os_scan   exclusive scan of each pass's 256 counts
+//   k_os_pass   per tile (claimed in order through an atomic counter): keys
+//               and values held in registers, the tile's digit counts
+//               published at once, the counts of all earlier tiles gathered
+//               by decoupled look-back (each state word carries a flag and
+//               a 30-bit count in one 32-bit store), the tile ranked stably
+//               in shared memory and written out digit run by digit run.
+// A tile only waits for tiles claimed before it, which are already running,
+// so the look-back always finishes; each wait is still bounded and a give-up
+// raises kDevWatchdog.  n must stay below 2^30.
+namespace os {
+constexpr int kThreads = 256;
+constexpr int kItems = 8;
+constexpr int kTile = kThreads * kItems;
+constexpr uint32_t kAgg = 1u << 30, kPre = 2u << 30, kVal = (1u << 30) - 1;
+constexpr long long kSpin = 1ll << 22;
+}  // namespace os
+
+inline int64_t onesweep_scratch_words(int64_t n, int nbits) {
+  const int64_t npass = (nbits + 7) / 8;
+  const int64_t ntiles = (n + os::kTile - 1) / os::kTile;
+  return npass * ntiles * 256 + npass * 256 + npass + 16;
+}
+
+template <typename K>
+__global__ void __launch_bounds__(256) k_os_hist(const K* __restrict__ keys, int64_t n, int npass,
+                                                 uint32_t* __restrict__ ghist) {
+  __shared__ uint32_t h[8][256];
+  for (int p = 0; p < 8; ++p) h[p][threadIdx.x] = 0;
+  __syncthreads();
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const K k = keys[i];
+    for (int p = 0; p < npass; ++p) atomicAdd(&h[p][(uint32_t)(k >> (8 * p)) & 255u], 1u);
+  }
+  __syncthreads();
+  for (int p = 0; p < npass; ++p)
+    if (h[p][threadIdx.x]) atomicAdd(&ghist[p * 256 + threadIdx.x], h[p][threadIdx.x]);
+}
+
+// Exclusive scan of each pass's 256 digit counts (one block per pass).
+__global__ void k_os_scan(uint32_t* __restrict__ ghist);
+
+template <typename K>
+__global__ void __launch_bounds__(os::kThreads) k_os_pass(const K* __restrict__ kin, const uint32_t* __restrict__ vin,
+                                                         K* __restrict__ kout, uint32_t* __restrict__ vout, int64_t n,
+                                                         int shift, const uint32_t* __restrict__ gstart,
+                                                         uint32_t* state, uint32_t* tile_ctr, uint32_t* err) {
+  using namespace os;
+  __shared__ K skey[kTile];
+  __shared__ uint32_t sval[kTile];
+  __shared__ uint32_t wcnt[8][256];
+  __shared__ uint32_t cnt[256];
+  __shared__ uint32_t run[256];
+  __shared__ uint32_t lstart[256];
+  __shared__ uint32_t gbase[256];
+  __shared__ uint32_t s_tile;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  if (tid == 0) s_tile = atomicAdd(tile_ctr, 1u);
+  cnt[tid] = 0;
+  run[tid] = 0;
+#pragma unroll
+  for (int w = 0; w < 8; ++w) wcnt[w][tid] = 0;
+  __syncthreads();
+  const int64_t tile = s_tile;
+  const int64_t base = tile * kTile;
+  const int tile_n = (int)min((int64_t)kTile, n - base);
+  K key[kItems];
+  uint32_t val[kItems], dig[kItems];
+#pragma unroll
+  for (int c = 0; c < kItems; ++c) {
+    const int li = c * kThreads + tid;
+    if (li < tile_n) {
+      key[c] = kin[base + li];
+      val[c] = vin[base + li];
+      dig[c] = (uint32_t)(key[c] >> shift) & 255u;
+      atomicAdd(&cnt[dig[c]], 1u);
+    } else {
+      key[c] = 0;
+      val[c] = 0;
+      dig[c] = 256u + (uint32_t)lane;  // private digit: never shares a rank
+    }
+  }
+  __syncthreads();
+  // publish this tile's counts, then look back over earlier tiles
+  const uint32_t mine = cnt[tid];
+  uint32_t* st = state + tile * 256 + tid;
+  *(volatile uint32_t*)st = (tile == 0 ? kPre : kAgg) | mine;
+  uint32_t excl = 0;
+  for (int64_t t = tile - 1; t >= 0; --t) {
+    const volatile uint32_t* p = state + t * 256 + tid;
+    uint32_t v = *p;
+    long long spins = 0;
+    while ((v & ~kVal) == 0 && ++spins < kSpin) v = *p;
+    if ((v & ~kVal) == 0) {
+      set_error(err, kDevWatchdog);
+      break;
+    }
+    excl += v & kVal;
+    if (v & kPre) break;
+  }
+  if (tile > 0) *(volatile uint32_t*)st = kPre | (excl + mine);
+  gbase[tid] = gstart[tid] + excl;
+  lstart[tid] = block_excl_scan256(mine, nullptr);
+  __syncthreads();
+  // stable rank inside the tile: chunks of 256 in order, warps in order
+  const uint32_t lt_mask = (1u << lane) - 1u;
+#pragma unroll
+  for (int c = 0; c < kItems; ++c) {
+    const uint32_t d = dig[c];
+    const uint32_t peers = __match_any_sync(0xffffffffu, d);
+    const uint32_t lrank = __popc(peers & lt_mask);
+    if (d < 256u && lrank == 0) wcnt[wid][d] = __popc(peers);
+    __syncthreads();
+    if (d < 256u) {
+      uint32_t r = run[d] + lrank;
+      for (int w = 0; w < wid; ++w) r += wcnt[w][d];
+      const uint32_t lp = lstart[d] + r;
+      skey[lp] = key[c];
+      sval[lp] = val[c];
+    }
+    __syncthreads();
+    {
+      uint32_t s = 0;
+#pragma unroll
+      for (int w = 0; w < 8; ++w) {
+        s += wcnt[w][tid];
+        wcnt[w][tid] = 0;
+      }
+      run[tid] += s;
+    }
+    __syncthreads();
+  }
+  for (int i = tid; i < tile_n; i += kThreads) {
+    const K k = skey[i];
+    const uint32_t d = (uint32_t)(k >> shift) & 255u;
+    const int64_t o = (int64_t)gbase[d] + (i - (int)lstart[d]);
+    kout[o] = k;
+    vout[o] = sval[i];
+  }
+}
+
+// Stable LSD sort of (keys, vals) on bits [0, nbits); returns which buffer
+// holds the result (0 = keys/vals, 1 = alt).  scratch:
+// onesweep_scratch_words(n, nbits) words.  n < 2^30.
+template <typename K>
+int onesweep_sort_pairs(K* keys, uint32_t* vals, K* keys_alt, uint32_t* vals_alt, int64_t n, int nbits,
+                        uint32_t* scratch, cudaStream_t st, uint64_t* launches, uint32_t* err) {
+  if (n <= 0) return 0;
+  const int npass = (nbits + 7) / 8;
+  const int64_t ntiles = (n + os::kTile - 1) / os::kTile;
+  uint32_t* state = scratch;
+  uint32_t* ghist = state + (int64_t)npass * ntiles * 256;
+  uint32_t* ctr = ghist + npass * 256;
+  cudaMemsetAsync(scratch, 0, (size_t)onesweep_scratch_words(n, nbits) * 4, st);
+  int hb = (int)((n + 255) / 256);
+  if (hb > 152 * 8) hb = 152 * 8;
+  k_os_hist<K><<<hb, 256, 0, st>>>(keys, n, npass, ghist);
+  k_os_scan<<<npass, 256, 0, st>>>(ghist);
+  K* ka = keys;
+  K* kb = keys_alt;
+  uint32_t* va = vals;
+  uint32_t* vb = vals_alt;
+  int which = 0;
+  for (int p = 0; p < npass; ++p) {
+    k_os_pass<K><<<(unsigned)ntiles, os::kThreads, 0, st>>>(ka, va, kb, vb, n, 8 * p, ghist + p * 256,
+                                                            state + (int64_t)p * ntiles * 256, ctr + p, err);
+    K* tk = ka;
+    ka = kb;
+    kb = tk;
+    uint32_t* tv = va;
+    va = vb;
+    vb = tv;
+    which ^= 1;
+  }
+  if (launches) *launches += 2 + npass;
+  return which;
+}
+
+// The sort the workspace paths use: one-sweep below 2^30 elements, the
+// three-kernel passes above.  scratch: sort_scratch_words(n, nbits) words.
+inline int64_t sort_scratch_words(int64_t n, int nbits) {
+  const int64_t a = radix_scratch_words(n), b = onesweep_scratch_words(n, nbits);
+  return a > b ? a : b;
+}
+
+template <typename K>
+int sort_pairs(K* keys, uint32_t* vals, K* keys_alt, uint32_t* vals_alt, int64_t n, int nbits, uint32_t* scratch,
+               cudaStream_t st, uint64_t* launches, uint32_t* err) {
+  if (n < (int64_t)os::kVal)
+    return onesweep_sort_pairs<K>(keys, vals, keys_alt, vals_alt, n, nbits, scratch, st, launches, err);
+  return radix_sort_pairs<K>(keys, vals, keys_alt, vals_alt, n, nbits, scratch, st, launches);
+}
+
 }  // namespace mvg

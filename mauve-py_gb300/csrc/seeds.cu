@@ -144,11 +144,11 @@ static int sml_sort_impl(Ctx* c, const uint32_t* d_packed, uint64_t count, const
   K* k1 = (K*)ws.get(c, sb + 1, count * sizeof(K));
   uint32_t* v0 = (uint32_t*)ws.get(c, sb + 2, count * sizeof(uint32_t));
   uint32_t* v1 = (uint32_t*)ws.get(c, sb + 3, count * sizeof(uint32_t));
-  uint32_t* scr = (uint32_t*)ws.get(c, sb + 4, radix_scratch_words(count) * sizeof(uint32_t));
+  uint32_t* scr = (uint32_t*)ws.get(c, sb + 4, sort_scratch_words(count, nbits) * sizeof(uint32_t));
   if (!k0 || !k1 || !v0 || !v1 || !scr) return report_error(MVG_ERR_NOMEM, "workspace allocation failed");
   k_seed_keys<K><<<grid_for(count, 256), 256, 0, c->stream>>>(d_packed, count, s, k0, v0);
   c->launches++;
-  int which = radix_sort_pairs<K>(k0, v0, k1, v1, (int64_t)count, nbits, scr, c->stream, &c->launches);
+  int which = sort_pairs<K>(k0, v0, k1, v1, (int64_t)count, nbits, scr, c->stream, &c->launches, c->d_err);
   K* ks = which ? k1 : k0;
   uint32_t* vs = which ? v1 : v0;
   if (d_pos_out) MVG_CUDA_TRY(cudaMemcpyAsync(d_pos_out, vs, count * sizeof(uint32_t), cudaMemcpyDeviceToDevice, c->stream));

@@ -232,3 +232,16 @@ def buildIndexFromGroups(sub_alignment_groups, genome_length, genome_seq=None, r
         c.handle, *blocks.ptrs(), blocks.n, mvg._ptr(g), len(g), mvg._ptr(r), len(r), int(bool(fill_gaps)),
         int(max_gap_width), int(bool(smooth_edges)), int(smoothing_radius), mvg._ptr(lut), len(lut)))
     return lut
+
+
+def buildIndexLutDev(d_genome_start, d_ref_start, d_col_off, d_genome_rows, d_ref_rows, nblocks, d_genome,
+                     genome_len, d_ref, ref_len, d_lut, n, fill_gaps=True, max_gap_width=300, smooth_edges=True,
+                     smoothing_radius=20, ctx=None):
+    """buildIndexFromGroups on device buffers (raw pointers): inputs and the
+    n-entry int32 LUT stay in device memory."""
+    c = _ctx(ctx)
+    mvg.wait_producers()
+    mvg._check(mvg.load_library().mvg_build_index_lut_dev(
+        c.handle, d_genome_start, d_ref_start, d_col_off, d_genome_rows, d_ref_rows, nblocks, d_genome, genome_len,
+        d_ref, ref_len, int(bool(fill_gaps)), int(max_gap_width), int(bool(smooth_edges)), int(smoothing_radius),
+        d_lut, n))

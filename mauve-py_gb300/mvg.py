@@ -280,7 +280,8 @@ class Context:
 
     def gap_align_banded(self, seq_a, off_a, seq_b, off_b, band_delta, band_half, with_paths=True):
         """Banded NWSmall with the exactness check and full-DP fallback.
-        Returns (scores, paths or None, used_band bool[n], cells computed)."""
+        Returns (scores, paths or None, status uint8[n], cells computed); status
+        1 = banded result kept, 0 = band rejected (full DP), 2 = band not tried."""
         seq_a, seq_b = _u8(seq_a), _u8(seq_b)
         off_a = np.ascontiguousarray(off_a, np.uint64)
         off_b = np.ascontiguousarray(off_b, np.uint64)
@@ -302,15 +303,16 @@ class Context:
                                                    _ptr(path_off), _ptr(plen), _ptr(used), ctypes.byref(cells)))
             raw = paths.tobytes()
             out = [raw[int(path_off[k]):int(path_off[k]) + int(plen[k])].decode() for k in range(n)]
-            return scores[:n], out, used[:n].astype(bool), int(cells.value)
+            return scores[:n], out, used[:n].copy(), int(cells.value)
         _check(load_library().mvg_gapdp_banded(self._h, _ptr(seq_a), _ptr(off_a), _ptr(seq_b), _ptr(off_b), n,
                                                _ptr(delta), _ptr(half), _ptr(scores), None, None, None, _ptr(used),
                                                ctypes.byref(cells)))
-        return scores[:n], None, used[:n].astype(bool), int(cells.value)
+        return scores[:n], None, used[:n].copy(), int(cells.value)
 
     def gap_align_banded_dev(self, d_sa, d_oa, d_sb, d_ob, n, band_delta, band_half, d_scores, d_paths, d_path_off,
                              d_path_len):
-        """Device-buffer banded call; band arrays and the returned used-band flags are host numpy arrays."""
+        """Device-buffer banded call; band arrays and the returned status (1 kept, 0 rejected, 2 not
+        tried) are host numpy arrays."""
         wait_producers()
         delta = np.ascontiguousarray(band_delta, np.int32)
         half = np.ascontiguousarray(band_half, np.int32)
@@ -319,7 +321,7 @@ class Context:
         _check(load_library().mvg_gapdp_banded_dev(self._h, d_sa, d_oa, d_sb, d_ob, n, _ptr(delta), _ptr(half),
                                                    d_scores, d_paths, d_path_off, d_path_len, _ptr(used),
                                                    ctypes.byref(cells)))
-        return used[:n].astype(bool), int(cells.value)
+        return used[:n].copy(), int(cells.value)
 
     def gap_align_batch_raw(self, seq_a, off_a, seq_b, off_b, scores, paths, path_off, path_len):
         """Host-buffer call with caller-owned numpy outputs (no per-call Python decoding)."""

@@ -87,6 +87,13 @@ def subset_host_idx(batch, idx):
     return subset(sa, batch.oa.astype(np.int64), sb, batch.ob.astype(np.int64), idx)
 
 
+def status_rates(status):
+    """Shares of banded results kept (1), rejected by the check (0) and not
+    tried (2); fallback = everything that ran the full DP."""
+    return {"accept_rate": float((status == 1).mean()), "rejected_rate": float((status == 0).mean()),
+            "not_tried_rate": float((status == 2).mean()), "fallback_rate": float((status != 1).mean())}
+
+
 def timed_banded(ctx, batch, delta, half):
     """(seconds, used-band flags, cells) of the banded DP with fallback, paths on device."""
     import torch
@@ -142,6 +149,7 @@ def train(args):
     t_all = time.time()
     n_tr, n_ev = args.train, args.eval
     sa, oa, sb, ob = synth.gap_batch_recoded(seed=args.seed, nprob=n_tr + n_ev)
+    tot_a, tot_b = bandnet.best_totals(sa, oa), bandnet.best_totals(sb, ob)
     tr = DeviceBatch(*subset(sa, oa, sb, ob, np.arange(n_tr)), dev)
     ev = DeviceBatch(*subset(sa, oa, sb, ob, np.arange(n_tr, n_tr + n_ev)), dev)
     del sa, sb
@@ -149,7 +157,7 @@ def train(args):
     t0 = time.time()
     sc_tr, env_tr = label(ctx, tr)
     print("labels %.1fs (%.3g cells)" % (time.time() - t0, tr.cells), flush=True)
-    T, _, _ = bandnet.labels_from_full_dp(tr.la, tr.lb, sc_tr, env_tr)
+    T, _, _ = bandnet.labels_from_full_dp(tr.la, tr.lb, sc_tr, env_tr, totals=(tot_a[:n_tr], tot_b[:n_tr]))
     if not np.isfinite(T).all():
         raise RuntimeError("non-finite training targets")
     print("targets: |offset| max %.2f, log-half range %.2f..%.2f" % (np.abs(T[:, 0]).max(), T[:, 1].min(),
@@ -201,7 +209,7 @@ def train(args):
             d, h = net.propose_dev(*vb.ptrs(), vb.n, alpha, beta)
             secs, used, cells, *_ = timed_banded(ctx, vb, d, h)
             if best is None or secs < best[0]:
-                best = (secs, alpha, beta, float(used.mean()), cells)
+                best = (secs, alpha, beta, float((used == 1).mean()), cells)
     _, alpha, beta, acc_v, _ = best
     print("calibrated alpha %.2f beta %.1f (validation accept %.3f)" % (alpha, beta, acc_v), flush=True)
     params = net.get_params()
@@ -223,10 +231,10 @@ def train(args):
         "eval_cells_full": ev.cells,
         "full": {"seconds": tf, "gcups": ev.cells / tf / 1e9},
         "learned": {"seconds": tl + t_prop, "dp_seconds": tl, "propose_seconds": t_prop,
-                    "effective_gcups": ev.cells / (tl + t_prop) / 1e9, "accept_rate": float(used_l.mean()),
-                    "fallback_rate": float(1 - used_l.mean()), "cells": cells_l, "identical_to_full": same_l},
-        "no_network": {"seconds": th, "effective_gcups": ev.cells / th / 1e9, "accept_rate": float(used_h.mean()),
-                       "fallback_rate": float(1 - used_h.mean()), "cells": cells_h, "identical_to_full": same_h},
+                    "effective_gcups": ev.cells / (tl + t_prop) / 1e9, **status_rates(used_l), "cells": cells_l,
+                    "identical_to_full": same_l},
+        "no_network": {"seconds": th, "effective_gcups": ev.cells / th / 1e9, **status_rates(used_h),
+                       "cells": cells_h, "identical_to_full": same_h},
     })
     res["speedup_learned_vs_full"] = tf / (tl + t_prop)
     res["speedup_no_network_vs_full"] = tf / th
@@ -235,8 +243,8 @@ def train(args):
     # label bands (the full DP's own envelope + margin) on the same gaps
     gcups_full = ev.cells / tf / 1e9
     for key, (d, h, used) in (("learned", (dl, hl, used_l)), ("no_network", (dh, hh, used_h))):
-        acc = np.nonzero(used)[0]
-        fb = np.nonzero(used == 0)[0]
+        acc = np.nonzero(used == 1)[0]
+        fb = np.nonzero(used != 1)[0]
         if len(acc) == 0:
             continue
         sub = DeviceBatch(*subset_host_idx(ev, acc), dev)
@@ -249,9 +257,9 @@ def train(args):
                          "fallback_seconds_at_full_gcups": fb_cells / gcups_full / 1e9})
         del sub
     env = bandnet.full_dp_labels_dev(ctx, *ev.ptrs(), ev.n, torch_device=dev)
-    _, d_lab, h_lab = bandnet.labels_from_full_dp(ev.la, ev.lb, *env)
+    _, d_lab, h_lab = bandnet.labels_from_full_dp(ev.la, ev.lb, *env, totals=(tot_a[n_tr:], tot_b[n_tr:]))
     t_lab, used_lab, cells_lab, *_ = timed_banded(ctx, ev, d_lab, h_lab)
-    res["label_band"] = {"seconds": t_lab, "accept_rate": float(used_lab.mean()), "cells": cells_lab,
+    res["label_band"] = {"seconds": t_lab, **status_rates(used_lab), "cells": cells_lab,
                          "speedup_vs_full": tf / t_lab}
     print(json.dumps(res, indent=1), flush=True)
     np.savez(args.out, params=params, alpha=np.float32(alpha), beta=np.float32(beta))

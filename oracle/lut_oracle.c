@@ -81,7 +81,7 @@ static void run_fill(int32_t* lut, uint64_t n, int width, int smooth, int32_t* g
     uint64_t lower = idx - 1;
     int ok = 0;
     for (uint64_t up = idx + 1; up < n; ++up) {
-      if (up - idx > (uint64_t)width) break;
+      if ((int64_t)(up - idx) > (int64_t)width) break;
       if ((int32_t)((uint32_t)lut[up] - (uint32_t)lo) == (int32_t)(up - lower)) {
         for (uint64_t k = lower; k <= up; ++k) lut[k] = lo + (int32_t)(k - lower);
         if (gaps) gaps[idx] = (int32_t)(up - lower);

@@ -262,5 +262,9 @@ def find_duplicate_mappings(lut):
     _lut(lut)
     nc = int(max(int(lut.max()), 0)) + 1 if len(lut) else 1
     counts = np.zeros(nc, np.uint32)
-    return int(_check(lib().mo_find_duplicate_mappings(_p(lut), len(lut), _p(counts), nc), "find_duplicate_mappings")
-               if len(lut) else -1)
+    if len(lut) == 0:
+        return -1
+    rc = lib().mo_find_duplicate_mappings(_p(lut), len(lut), _p(counts), nc)
+    if rc == -2:
+        raise LutIndexError("find_duplicate_mappings: count table too small")
+    return int(rc)

@@ -16,3 +16,16 @@ def pytest_configure(config):
 def load_golden(name):
     import numpy as np
     return np.load(os.path.join(ROOT, "tests", "golden", name))
+
+
+def load_mds42():
+    """The reference's recoded E. coli fixture pair (ASCII bases), its seed
+    and the reference's match list (tests/golden/mds42.npz)."""
+    import numpy as np
+    g = load_golden("mds42.npz")
+
+    def unpack(p, n):
+        v = np.stack([(p >> 6) & 3, (p >> 4) & 3, (p >> 2) & 3, p & 3], axis=1).reshape(-1)[:n]
+        return np.frombuffer(b"ACGT", np.uint8)[v]
+
+    return (unpack(g["a"], int(g["na"])), unpack(g["b"], int(g["nb"])), int(g["seed"]), g["matches"])

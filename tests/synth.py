@@ -374,3 +374,63 @@ def lut_random(seed, n=5000, run_mean=60, p_gap=0.3, p_noise=0.05, p_island=0.2)
     noise = rng.random(n) < p_noise
     lut[noise] = rng.integers(-1, max(2, int(lut.max()) + 10), int(noise.sum()))
     return lut
+
+
+def lut_alignment_fast(seed, n_ref=4_600_000, sub=0.01, indel=0.0005, nblocks=64, shuffle=True):
+    """Vectorised lut_alignment without the extras, for genome-sized cases:
+    returns (gs, rs, col_off, genome_rows, ref_rows, genome, ref) with the
+    blocks already flattened (every block has both sequences)."""
+    rng = np.random.default_rng(seed)
+    acgt = np.frombuffer(b"ACGT", np.uint8)
+    R = rng.choice(acgt, n_ref)
+    Gc = R.copy()
+    m = rng.random(n_ref) < sub
+    Gc[m] = acgt[(np.searchsorted(acgt, Gc[m]) + rng.integers(1, 4, int(m.sum()))) % 4]
+    nev = rng.poisson(indel * n_ref)
+    pos = rng.integers(0, n_ref, nev)
+    lens = rng.geometric(0.3, nev)
+    ins = rng.random(nev) < 0.5
+    dele = np.zeros(n_ref + 1, np.int32)
+    np.add.at(dele, pos[~ins], 1)
+    np.add.at(dele, np.minimum(pos[~ins] + lens[~ins], n_ref), -1)
+    Gc[np.cumsum(dele[:-1]) > 0] = ord("-")
+    at = np.repeat(pos[ins], lens[ins])
+    G = np.insert(Gc, at, rng.choice(acgt, len(at)))
+    Rr = np.insert(R, at, np.full(len(at), ord("-"), np.uint8))
+    gpos = np.cumsum(G != ord("-"))
+    rpos = np.cumsum(Rr != ord("-"))
+    genome = G[G != ord("-")]
+    cuts = np.sort(rng.choice(np.arange(1, len(G)), nblocks - 1, replace=False))
+    bounds = np.concatenate([[0], cuts, [len(G)]])
+    order = rng.permutation(nblocks) if shuffle else np.arange(nblocks)
+    gs, rs, rows_g, rows_r = [], [], [], []
+    for b in order:
+        a, e = int(bounds[b]), int(bounds[b + 1])
+        gs.append(int(gpos[a - 1]) + 1 if a > 0 else 1)
+        rs.append(int(rpos[a - 1]) + 1 if a > 0 else 1)
+        rows_g.append(G[a:e])
+        rows_r.append(Rr[a:e])
+    off = np.zeros(nblocks + 1, np.uint64)
+    off[1:] = np.cumsum([len(x) for x in rows_g])
+    return (np.array(gs, np.int64), np.array(rs, np.int64), off, np.concatenate(rows_g), np.concatenate(rows_r),
+            genome, R)
+
+
+def xmfa_text(groups, width=80, crlf=False, seed=0):
+    """XMFA text of sub-alignment groups [(seq_num, start, row bytes)]:
+    '#' header lines, one '>' header per sub-alignment with an end
+    coordinate, strand and file name, rows wrapped at `width`, and an '='
+    line (with a score note on some) closing each group."""
+    rng = np.random.default_rng(seed)
+    nl = "\r\n" if crlf else "\n"
+    out = ["#FormatVersion Mauve1", "#Sequence1File\tgenome.fa", "#Sequence2File\tref.fa"]
+    for grp in groups:
+        for s, st, row in grp:
+            n = sum(1 for c in row if c != ord("-"))
+            end = st + n - 1 if n else 0
+            strand = "+" if rng.random() < 0.8 else "-"
+            out.append("> %d:%d-%d %s %s" % (s, st, end, strand, "genome.fa" if s == 1 else "ref.fa"))
+            txt = row.decode("latin-1")
+            out.extend(txt[k:k + width] for k in range(0, len(txt), width))
+        out.append("=" if rng.random() < 0.5 else "= score=%d" % int(rng.integers(0, 10 ** 6)))
+    return (nl.join(out) + nl).encode("latin-1")

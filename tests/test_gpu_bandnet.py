@@ -30,7 +30,7 @@ def _batch_ptrs(sa, oa, sb, ob):
     return t, [x.data_ptr() for x in t]
 
 
-@pytest.mark.parametrize("rows,band_rows", [(4, 2), (8, 4), (8, 8)])
+@pytest.mark.parametrize("rows,band_rows", [(4, 1), (4, 2), (8, 4), (8, 8)])
 def test_banded_output_identical_to_full(ctx, rows, band_rows):
     ctx.set_dp_rows(rows, band_rows)
     try:
@@ -56,10 +56,14 @@ def test_band_with_label_width_is_accepted_on_close_gaps(ctx):
     la, lb = np.diff(oa), np.diff(ob)
     t, ptrs = _batch_ptrs(sa, oa, sb, ob)
     scores, env = bandnet.full_dp_labels_dev(ctx, *ptrs, len(la), torch_device=t[0].device)
-    _, delta, half = bandnet.labels_from_full_dp(la, lb, scores, env, margin=16)
+    totals = (bandnet.best_totals(sa, oa), bandnet.best_totals(sb, ob))
+    _, delta, half = bandnet.labels_from_full_dp(la, lb, scores, env, margin=16, totals=totals)
     s, p, used, cells = ctx.gap_align_banded(sa, oa, sb, ob, delta, half, with_paths=False)
     np.testing.assert_array_equal(s, scores)
-    assert used.mean() > 0.9
+    tried = used != 2
+    assert tried.sum() > 100
+    # the label width must pass the exactness check
+    assert (used[tried] == 1).mean() > 0.9
     assert cells < 0.5 * float(np.sum(la * lb))
 
 

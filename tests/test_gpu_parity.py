@@ -98,6 +98,21 @@ def test_matches_genome_pair_small_config(ctx):
     np.testing.assert_array_equal(m, om)
 
 
+def test_matches_reference_mds42_pair(ctx):
+    """The reference's own recoded E. coli fixture pair (3.98 Mbp each,
+    29,403 matches): the GPU match list equals the reference's, bit for bit,
+    through the host and the device entry points."""
+    import torch
+    from conftest import load_mds42
+    a, b, seed, want = load_mds42()
+    np.testing.assert_array_equal(ctx.pairwise_matches(a, b, seed), want)
+    da, db = torch.from_numpy(a.copy()).cuda(), torch.from_numpy(b.copy()).cuda()
+    out = torch.zeros(3 * (len(want) + 16), dtype=torch.int64, device="cuda")
+    n = ctx.pairwise_matches_dev(da.data_ptr(), len(a), db.data_ptr(), len(b), seed, out.data_ptr(), len(want) + 16)
+    assert n == len(want)
+    np.testing.assert_array_equal(out[:3 * n].cpu().numpy().reshape(-1, 3), want)
+
+
 def test_matches_degenerate_inputs(ctx):
     seed = mvg.get_seed(15, 3)
     assert ctx.pairwise_matches(b"ACGT", b"ACGTACGT", seed).shape == (0, 3)

@@ -55,3 +55,12 @@ def test_pack_layout():
     assert w[0] == 0x1B1B1B1B and w[1] == 0x40000000 and len(w) == 2 + 2
     with pytest.raises(ValueError):
         O.pack(b"AC-GT")
+
+
+def test_oracle_matches_on_the_reference_mds42_pair():
+    """The reference's own recoded E. coli fixture pair (3.98 Mbp each):
+    the oracle's match list equals the reference's."""
+    from conftest import load_mds42
+    a, b, seed, want = load_mds42()
+    got = O.pairwise_matches(a, b, seed)
+    np.testing.assert_array_equal(got, want)
