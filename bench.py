@@ -163,6 +163,8 @@ def learned_band_section(ctx, args, dev, stream, rank):
     w = np.load(WEIGHTS)
     net = bandnet.BandNet(ctx, params=w["params"])
     alpha, beta = float(w["alpha"]), float(w["beta"])
+    whole = float(w["whole"]) if "whole" in w.files else 0.5
+    ctx.set_band_whole_fraction(whole)
     sa, oa, sb, ob = synth.gap_batch_recoded(seed=1000 + rank, nprob=LB_NPROB)
     n = len(oa) - 1
     la, lb = np.diff(oa), np.diff(ob)
@@ -214,7 +216,7 @@ def learned_band_section(ctx, args, dev, stream, rank):
                            "not_tried": round(float((used == 2).mean()), 4)},
         "cells_computed": band_cells,
         "identical_to_full": identical, "weights": "mauve-py_gb300/bandnet_weights.npz",
-        "margins": {"alpha": alpha, "beta": beta},
+        "margins": {"alpha": alpha, "beta": beta, "whole_fraction": whole},
     }
 
 

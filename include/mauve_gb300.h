@@ -138,7 +138,8 @@ int mvg_gapdp_batch_dev(mvg_handle h, const uint8_t* d_seq_a, const uint64_t* d_
  * each base the path would still have to consume, taking the smaller of the
  * two sequences' sums); then its path equals the full NWSmall path.
  * Otherwise the problem is re-run through the full DP.  A band whose strips
- * cover at least half of the matrix is not tried.  Output is therefore always
+ * cover at least half of the matrix (mvg_set_band_whole_fraction) is not
+ * banded: that problem runs over the whole matrix.  Output is therefore always
  * identical to mvg_gapdp_batch.  used_band[p] (host, may be NULL) gets 1 when
  * the banded result was kept, 0 when the band was tried and rejected, 2 when
  * it was not tried; *cells (may be NULL) gets the DP cells actually computed.
@@ -266,6 +267,11 @@ int mvg_set_tb_arena(mvg_handle h, uint64_t bytes);
  * passes (1, 2, 4 or 8); strips are 32*rows rows.  The Python binding applies
  * the tuned choice committed in mauve-py_gb300/dp_tuning.json. */
 int mvg_set_dp_rows(mvg_handle h, int full_rows, int band_rows);
+
+/* Banded passes: a proposed band whose strips cover at least `fraction` of
+ * its matrix (0 < fraction <= 1, default 0.5) is not banded; the problem
+ * runs over the whole matrix in the same launch (status 2). */
+int mvg_set_band_whole_fraction(mvg_handle h, double fraction);
 
 /* Per-stage timing with CUDA events on the handle's stream (off by default;
  * no extra synchronisation).  After a call, mvg_stage_times gives the stage

@@ -50,6 +50,8 @@ def run(args):
     if os.path.exists(args.weights):
         w = np.load(args.weights)
         net = bandnet.BandNet(ctx, params=w["params"])
+        if "whole" in w.files:
+            ctx.set_band_whole_fraction(float(w["whole"]))
         d, h = net.propose_dev(*band.ptrs(), band.n, float(w["alpha"]), float(w["beta"]))
         src = "network"
     else:

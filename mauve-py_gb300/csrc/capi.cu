@@ -394,6 +394,12 @@ int mvg_set_dp_rows(mvg_handle h, int full_rows, int band_rows) {
   return 0;
 }
 
+int mvg_set_band_whole_fraction(mvg_handle h, double fraction) {
+  if (!h || !(fraction > 0.0) || fraction > 1.0) return report_error(MVG_ERR_ARG, "fraction must be in (0, 1]");
+  h->band_whole = fraction;
+  return 0;
+}
+
 int mvg_set_profiling(mvg_handle h, int on) {
   if (!h) return report_error(MVG_ERR_ARG, "null handle");
   h->profiling = on != 0;

@@ -126,6 +126,12 @@ __global__ void k_traceback(const uint64_t* __restrict__ oa, const uint64_t* __r
         }
         const int nib = s * rows + r;
         bits = (T[base + (nib >> 3) * 32 + t] >> (4 * (nib & 7))) & 15u;
+        // the path runs right to left through the strip: start fetching the
+        // word 8 steps ahead (each step's word is otherwise a dependent miss)
+        if (s >= 8) {
+          const int nib_ahead = (s - 8) * rows + r;
+          asm volatile("prefetch.global.L1 [%0];" ::"l"(T + base + (nib_ahead >> 3) * 32 + t));
+        }
       }
       char next;
       if (cur == 'M') {
@@ -214,6 +220,17 @@ static int run_dp(Ctx* c, const DpInputs& in, const std::vector<uint32_t>& ids, 
     bytes[w] = (words * 4 + 255) & ~255ull;
     maxlb = std::max(maxlb, lb[p]);
   }
+  // Whole-CTA (pipelined) mode for problems with many strips.  A banded
+  // strip can only start once the previous one has passed the next strip's
+  // first column (about one strip height of drift plus the 64-column
+  // prefetch), so narrow bands would leave the pipeline nearly serial: they
+  // stay on one warp unless their strips are at least 8 strip heights wide.
+  std::vector<char> is_big(nwork);
+  for (int64_t w = 0; w < nwork; ++w) {
+    const int64_t a = la[ids[w]];
+    const bool many = (a + 32 * rows - 1) / (32 * rows) >= kCoopMinStrips;
+    is_big[w] = many && (!banded || cells[w] >= (uint64_t)a * 8 * 32 * rows);
+  }
   std::vector<uint32_t> idx(nwork);
   std::iota(idx.begin(), idx.end(), 0u);
   std::stable_sort(idx.begin(), idx.end(), [&](uint32_t x, uint32_t y) { return cells[x] > cells[y]; });
@@ -254,7 +271,7 @@ static int run_dp(Ctx* c, const DpInputs& in, const std::vector<uint32_t>& ids, 
       int64_t nb = 0;
       for (int pass = 0; pass < 2; ++pass)
         for (int64_t q = v; q < nwork; q += nwaves) {
-          const bool big = (la[ids[idx[q]]] + 32 * rows - 1) / (32 * rows) >= kCoopMinStrips;
+          const bool big = is_big[idx[q]];
           if (big != (pass == 0)) continue;
           order.push_back(ids[idx[q]]);
           tboff.push_back(acc);
@@ -410,15 +427,24 @@ int gapdp_banded_dev(Ctx* c, const uint8_t* d_sa, const uint64_t* d_oa, const ui
   if (!d_paths && (rc = scratch_paths(c, nprob, la, lb, in))) return rc;
   std::vector<int32_t> dv(h_delta, h_delta + nprob), hv(h_half, h_half + nprob);
   uint64_t bc = 0;
-  // a band covering at least half of its matrix saves little and may still
-  // fail its check: such problems go straight to the full DP
-  std::vector<uint32_t> ids;
-  ids.reserve(nprob);
+  // A band covering at least band_whole (default half) of its matrix saves
+  // little and may still fail its check: such problems are not banded.  They run in the same
+  // launch with a band that covers the whole matrix (no exit cells, so the
+  // check always passes and the result is the full DP's), which spares a
+  // second full-DP pass for them.
+  std::vector<uint32_t> ids(nprob);
+  std::vector<uint8_t> whole(nprob, 0);
   for (int64_t p = 0; p < nprob; ++p) {
     if (hv[p] < 0) return report_error(MVG_ERR_ARG, "negative band half-width");
+    ids[p] = (uint32_t)p;
+    const uint64_t full = (uint64_t)la[p] * (uint64_t)lb[p];
     const uint64_t cells = band_cells(make_band((int)la[p], (int)lb[p], dv[p], hv[p], 32 * c->band_rows));
-    if (2 * cells < (uint64_t)la[p] * (uint64_t)lb[p]) {
-      ids.push_back((uint32_t)p);
+    if ((double)cells >= c->band_whole * (double)full) {
+      whole[p] = 1;
+      dv[p] = 0;
+      hv[p] = (int32_t)std::max(la[p], lb[p]) + 2;
+      bc += full;
+    } else {
       bc += cells;
     }
   }
@@ -440,14 +466,15 @@ int gapdp_banded_dev(Ctx* c, const uint8_t* d_sa, const uint64_t* d_oa, const ui
   MVG_CUDA_TRY(cudaMemcpyAsync(acc.data(), d_accept, (size_t)nprob, cudaMemcpyDeviceToHost, c->stream));
   MVG_CUDA_TRY(cudaStreamSynchronize(c->stream));
   std::vector<uint32_t> fallback;
-  std::vector<uint8_t> tried(nprob, 0);
-  for (uint32_t p : ids) tried[p] = 1;
-  for (int64_t p = 0; p < nprob; ++p)
-    if (!acc[p]) {
+  for (int64_t p = 0; p < nprob; ++p) {
+    if (whole[p]) {
+      if (!acc[p]) return report_error(MVG_ERR_DEVICE, "whole-matrix band failed its check");
+      acc[p] = 2;  // not banded: the proposed band covered at least half the matrix
+    } else if (!acc[p]) {
       fallback.push_back((uint32_t)p);
       bc += (uint64_t)la[p] * (uint64_t)lb[p];
-      if (!tried[p]) acc[p] = 2;  // not tried: the band covered at least half the matrix
     }
+  }
   // rejected bands: the full DP is both the fallback and the judge
   rc = run_dp(c, in, fallback, la, lb, nullptr, nullptr, nullptr, nullptr, nullptr);
   if (rc) return rc;

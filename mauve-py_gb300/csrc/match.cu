@@ -175,21 +175,26 @@ __device__ __forceinline__ int64_t lower_bound_mhe(const Mhe* __restrict__ v, in
 }
 
 // ExtendMatch (LM/MatchFinder.h:218-374) for two genomes, executed by a full
-// warp in lockstep.  Phases 0/1 jump by the seed length until the first
-// mismatching window; phases 2/3 try the L single-base offsets and move to
-// the furthest matching one; any such move restarts the four phases.
+// warp.  The reference cycles through four phases (jump left and right by
+// the seed length until the first mismatching window, then try the L
+// single-base offsets left and right and move to the furthest matching one)
+// and restarts while a single-base phase moves.
 //
-// Every window pair the walk tests lies on the match's diagonal: in the
-// entry orientation S0, the pair tested at step size k from the current
-// left edge is the pair at displacement ML + k from the entry left edge (ML
-// = total moved in even phases), and in the inverted orientation the pair
-// at MR + k from the entry right edge (MR = total moved in odd phases);
-// positive starts move by exactly those amounts and negative starts stay.
-// So the walk reads match bits of the two sides, computed 1024 displacements
-// at a time into per-warp shared rings, instead of recomputing seed windows
-// in every phase.  For a same-strand pair a window pair matches iff the
-// pattern-selected bases are equal (equal canonical mers with equal strand
-// bits); other pairs use the canonical-mer test itself.
+// Every window pair a phase tests lies on the match's diagonal: in the entry
+// orientation S0, the pair tested at step size k from the current left edge
+// is the pair at displacement ML + k from the entry left edge (ML = total
+// moved in even phases), and in the inverted orientation the pair at MR + k
+// from the entry right edge (MR = total moved in odd phases); positive
+// starts move by exactly those amounts and negative starts stay.  The room
+// a phase has (the genome-end clamp) is likewise C - ML or C' - MR.  So the
+// two sides never interact: each side's total is the fixpoint of (jump,
+// single) on its own match bits, and the four-phase cycle only interleaves
+// the two fixpoint iterations.  Here the warp computes the two fixpoints one
+// after the other on match bits cached in per-warp shared rings (1024
+// displacements per fill); the walk itself is warp-uniform scalar work.
+// For a same-strand pair a window pair matches iff the pattern-selected
+// bases are equal (equal canonical mers with equal strand bits); other
+// pairs use the canonical-mer test itself.
 constexpr int kExtRing = 128;    // words per side: the last 4096 displacements
 constexpr int kExtChunk = 1024;  // displacements per fill (32 per lane)
 
@@ -243,102 +248,96 @@ __device__ void ext_fill(const MatchCtx& c, int64_t st0, int64_t st1, int64_t le
 }
 
 __device__ void warp_extend(const MatchCtx& c, Mhe& m, ExtRing& R) {
-  const int lane = threadIdx.x & 31;
   const int L = c.s.L;
   const uint64_t pmask = pattern_mask64(c.s);
   const int64_t e0 = m.s0, e1 = m.s1, elen = m.len;  // entry state S0
-  int64_t st0 = m.s0, st1 = m.s1, len = m.len;
-  int64_t moved_side[2] = {0, 0};   // ML, MR
-  int64_t filled[2] = {0, 0};       // displacements [0, filled) of each side are in the ring
-  // bit of side sd at displacement u (u >= filled - 4096 holds for every query)
-  auto ensure = [&](int sd, int64_t umax) {
-    while (filled[sd] <= umax) {
-      if (sd == 0)
-        ext_fill(c, e0, e1, elen, filled[0], pmask, R.w[0]);
-      else
-        ext_fill(c, -e0, -e1, elen, filled[1], pmask, R.w[1]);
-      filled[sd] += kExtChunk;
-    }
-  };
-  auto bit = [&](int sd, int64_t u) -> bool { return (R.w[sd][(u >> 5) & (kExtRing - 1)] >> (u & 31)) & 1u; };
-  bool extend_again = false;
-  for (int dir = 0; dir < 4; ++dir) {
-    const int sd = dir & 1;
-    int64_t maxlen = dir < 2 ? (int64_t)0xffffffffu : (int64_t)L;
-    if (st0 < 0) {
-      int64_t rc = c.n[0] - len + st0 + 1;
-      if (rc < maxlen) maxlen = rc;
-    } else if (st0 - 1 < maxlen) {
-      maxlen = st0 - 1;
-    }
-    if (st1 < 0) {
-      int64_t rc = c.n[1] - len + st1 + 1;
-      if (rc < maxlen) maxlen = rc;
-    } else if (st1 - 1 < maxlen) {
-      maxlen = st1 - 1;
-    }
-    const int64_t base = moved_side[sd];
-    int64_t moved = 0;
-    if (dir < 2) {
-      const int64_t nj = maxlen >= L ? maxlen / L : 0;
-      int64_t good = nj;
-      for (int64_t kb = 1; kb <= nj; kb += 32) {
-        const int64_t klast = kb + 31 < nj ? kb + 31 : nj;
-        ensure(sd, base + klast * L);
-        const int64_t k = kb + lane;
-        const bool bad = k <= nj && !bit(sd, base + k * L);
-        const unsigned mm = __ballot_sync(0xffffffffu, bad);
-        if (mm) {
-          good = kb - 1 + (__ffs(mm) - 1);
+  int64_t moved[2] = {0, 0};                          // ML, MR
+#pragma unroll 1
+  for (int sd = 0; sd < 2; ++sd) {
+    const int64_t sg = sd == 0 ? 1 : -1;
+    const int64_t s0 = sg * e0, s1 = sg * e1;
+    // room of this side: min over both genomes of the distance to the end
+    const int64_t r0 = s0 > 0 ? s0 - 1 : (s0 < 0 ? c.n[0] - elen + s0 + 1 : -1);
+    const int64_t r1 = s1 > 0 ? s1 - 1 : (s1 < 0 ? c.n[1] - elen + s1 + 1 : -1);
+    const int64_t room0 = r0 < r1 ? r0 : r1;
+    uint32_t* ring = R.w[sd];
+    int64_t filled = 0;
+    auto ensure = [&](int64_t umax) {
+      while (filled <= umax) {
+        ext_fill(c, s0, s1, elen, filled, pmask, ring);
+        filled += kExtChunk;
+      }
+    };
+    auto bit = [&](int64_t u) -> bool { return (ring[(u >> 5) & (kExtRing - 1)] >> (u & 31)) & 1u; };
+    int64_t u = 0;
+    for (;;) {
+      // jump phase: k-1 good jumps before the first mismatching window
+      int64_t room = room0 - u;
+      const int64_t nj = room >= L ? room / L : 0;
+      int64_t k = 1;
+      while (k <= nj) {
+        const int64_t d = u + k * L;
+        ensure(d);
+        if (!bit(d)) break;
+        ++k;
+      }
+      u += (k - 1) * L;
+      // single-base phase: the furthest matching offset in 1..min(room, L)
+      room = room0 - u;
+      const int64_t ms = room > 0 ? (room < L ? room : L) : 0;
+      if (ms <= 0) break;
+      ensure(u + ms);
+      int lim = 0;
+      for (int q = (int)ms; q >= 1; --q)
+        if (bit(u + q)) {
+          lim = q;
           break;
         }
-      }
-      moved = good * L;
-    } else {
-      const int64_t msteps = maxlen > 0 ? (maxlen < L ? maxlen : L) : 0;
-      if (msteps > 0) ensure(sd, base + msteps);
-      const int64_t k = lane + 1;
-      const bool ok = k <= msteps && bit(sd, base + k);
-      const unsigned mb = __ballot_sync(0xffffffffu, ok);
-      const int limit = mb ? 32 - __clz(mb) : 0;
-      if (msteps > 0 && limit > 0) extend_again = true;
-      moved = limit;
+      if (lim == 0) break;
+      u += lim;
     }
-    moved_side[sd] += moved;
-    len += moved;
-    if (st0 > 0) st0 -= moved;
-    if (st1 > 0) st1 -= moved;
-    st0 = -st0;  // Invert
-    st1 = -st1;
-    if (dir == 3 && extend_again) {
-      dir = -1;
-      extend_again = false;
-    }
+    moved[sd] = u;
   }
-  m.s0 = st0;
-  m.s1 = st1;
-  m.len = len;
+  m.len = elen + moved[0] + moved[1];
+  m.s0 = e0 > 0 ? e0 - moved[0] : e0 + moved[1];
+  m.s1 = e1 > 0 ? e1 - moved[0] : e1 + moved[1];
 }
 
-// Buckets with at least kBigBucket seeds get a whole CTA: 256 seeds are tested
-// per round against the bucket's entries held in shared memory (spilled to
-// the bucket's global region if they outgrow kCtaCap).  The first seed of the
-// round that is not contained is extended by its warp and inserted; later
-// seeds of the round are re-tested, exactly as in the sequential replay.
-// CTAs past the big buckets run the warp-per-bucket replay, 8 buckets each.
+// lower_bound_mhe over the sorted order given by a map (logical position ->
+// slot in E): the same probes on the same logical array.
+__device__ __forceinline__ int64_t lower_bound_mapped(const Mhe* __restrict__ E, const uint32_t* __restrict__ M,
+                                                      int64_t n, const Mhe& x, int L) {
+  int64_t first = 0, len = n;
+  while (len > 0) {
+    int64_t half = len >> 1, mid = first + half;
+    if (mhe_less(E[M[mid]], x, L)) {
+      first = mid + 1;
+      len = len - half - 1;
+    } else {
+      len = half;
+    }
+  }
+  return first;
+}
+
+// Buckets with at least kBigBucket seeds get a whole CTA: seeds are staged
+// kChunk at a time in shared memory and every open seed of the chunk is
+// tested at once against the bucket's entries; the first one not contained
+// is extended by warp 0 and inserted, and the test resumes right after it,
+// exactly as in the sequential replay.  CTAs past the big buckets run the
+// warp-per-bucket replay (32 seeds per test round), 8 buckets each.
 constexpr uint32_t kBigBucket = 512;
-constexpr int kCtaCap = 768;
+constexpr int kChunk = 1024;  // seeds staged per chunk (dynamic shared memory)
+extern __shared__ __align__(16) unsigned char replay_dyn_smem[];
 
 __global__ void __launch_bounds__(256) k_bucket_replay(MatchCtx c, const Mhe* __restrict__ mhe,
                                                        const uint32_t* __restrict__ sorted_pair,
                                                        const uint32_t* __restrict__ bstart,
                                                        const uint32_t* __restrict__ bcount,
                                                        const uint32_t* __restrict__ border, Mhe* ent,
-                                                       uint32_t* __restrict__ nent_out,
+                                                       uint32_t* emap, uint32_t* __restrict__ nent_out,
                                                        unsigned long long* __restrict__ coll) {
-  __shared__ Mhe sE[kCtaCap];
   __shared__ ExtRing s_ring[8];
-  __shared__ unsigned wmask[8];
   __shared__ Mhe s_x;
   __shared__ long long s_at;
   __shared__ int s_nbig;
@@ -407,6 +406,8 @@ __global__ void __launch_bounds__(256) k_bucket_replay(MatchCtx c, const Mhe* __
       }
       ncoll += __popc(pending);
     }
+    uint32_t* Mp = emap + bstart[b];  // warp mode keeps the entries in sorted order
+    for (int64_t k = lane; k < n; k += 32) Mp[k] = (uint32_t)k;
     if (lane == 0) {
       nent_out[b] = (uint32_t)n;
       atomicAdd(coll, ncoll);
@@ -414,81 +415,100 @@ __global__ void __launch_bounds__(256) k_bucket_replay(MatchCtx c, const Mhe* __
     return;
   }
   // ------------------------------------------------------- CTA per bucket
+  // Seeds are staged kChunk at a time in shared memory.  A round tests the
+  // chunk's open seeds (kChunk / 256 per thread) against the current
+  // entries; the first one not contained is extended and inserted, the ones
+  // before it are collisions, and the next round starts right after it -
+  // the reference's sequence of tests and inserts, seed by seed.
+  Mhe* s_chunk = reinterpret_cast<Mhe*>(replay_dyn_smem);
+  __shared__ uint32_t s_wmin[8];
   const uint32_t b = border[blockIdx.x];
   const uint32_t cnt = bcount[b];
+  // Entries are appended to the bucket's region G in insertion order; their
+  // sorted order is the map Mp (logical position -> slot), so an insert
+  // moves 4-byte map words in blocks of 2048 (two barriers per block)
+  // instead of 32-byte entries 256 at a time.
   Mhe* G = ent + bstart[b];
+  uint32_t* Mp = emap + bstart[b];
   const uint32_t* sp = sorted_pair + bstart[b];
-  Mhe* E = sE;
-  bool spilled = false;
   int64_t n = 0;
   unsigned long long ncoll = 0;
-  for (uint32_t base = 0; base < cnt; base += 256) {
-    const uint32_t i = base + tid;
-    Mhe m = {0, 0, 0, 0};
-    bool pending = i < cnt;
-    if (pending) m = mhe[sp[i]];
-    for (;;) {
-      bool fresh = false;
-      if (pending) {
-        const int64_t at = lower_bound_mhe(E, n, m, L);
-        fresh = !(at != n && !mhe_less(E[at], m, L) && !mhe_less(m, E[at], L));
+  // number of this thread's chunk slots (cbase + tid + 256 j) in [lo, hi)
+  auto mine_in = [&](uint32_t cbase, uint32_t lo, uint32_t hi) -> uint32_t {
+    const int64_t first = (int64_t)cbase + tid;
+    const int64_t j0 = lo > first ? ((int64_t)lo - first + 255) / 256 : 0;
+    const int64_t j1 = hi > first ? ((int64_t)hi - first + 255) / 256 : 0;
+    return j1 > j0 ? (uint32_t)(j1 - j0) : 0u;
+  };
+  for (uint32_t cbase = 0; cbase < cnt; cbase += kChunk) {
+    const uint32_t cend = min(cnt, cbase + (uint32_t)kChunk);
+    __syncthreads();  // the previous chunk is fully consumed
+    for (uint32_t i = cbase + tid; i < cend; i += 256) s_chunk[i - cbase] = mhe[sp[i]];
+    __syncthreads();
+    uint32_t pos = cbase;
+    while (pos < cend) {
+      uint32_t myf = 0xffffffffu;
+      {
+        const int64_t first = (int64_t)cbase + tid;
+        int64_t i = pos > first ? first + ((int64_t)pos - first + 255) / 256 * 256 : first;
+        for (; i < cend; i += 256) {
+          const Mhe m = s_chunk[i - cbase];
+          const int64_t at = lower_bound_mapped(G, Mp, n, m, L);
+          const bool contained = at != n && !mhe_less(G[Mp[at]], m, L) && !mhe_less(m, G[Mp[at]], L);
+          if (!contained) {
+            myf = (uint32_t)i;
+            break;
+          }
+        }
       }
-      const unsigned wm = __ballot_sync(0xffffffffu, fresh);
-      if (lane == 0) wmask[wid] = wm;
+      const uint32_t wmin = __reduce_min_sync(0xffffffffu, myf);
+      if (lane == 0) s_wmin[wid] = wmin;
       __syncthreads();
-      int f = -1;
+      uint32_t f = 0xffffffffu;
 #pragma unroll
-      for (int q = 0; q < 8; ++q) {
-        const unsigned v = wmask[q];
-        if (f < 0 && v) f = q * 32 + __ffs(v) - 1;
-      }
-      if (f < 0) {
-        if (pending) ++ncoll;
-        pending = false;
-        __syncthreads();  // every thread has read wmask before the next round rewrites it
+      for (int q = 0; q < 8; ++q) f = min(f, s_wmin[q]);
+      if (f == 0xffffffffu) {
+        ncoll += mine_in(cbase, pos, cend);
+        pos = cend;
         break;
       }
-      if (pending && tid < f) {
-        ++ncoll;
-        pending = false;
-      }
-      if (tid == f) {
-        s_x = m;
-        pending = false;
-      }
-      __syncthreads();
-      if (wid == (f >> 5)) {
-        Mhe x = s_x;
-        warp_extend(c, x, s_ring[wid]);
-        const int64_t at = lower_bound_mhe(E, n, x, L);
+      ncoll += mine_in(cbase, pos, f);
+      if (wid == 0) {
+        Mhe x = s_chunk[f - cbase];
+        warp_extend(c, x, s_ring[0]);
+        const int64_t at = lower_bound_mapped(G, Mp, n, x, L);
         if (lane == 0) {
           s_x = x;
           s_at = at;
         }
       }
       __syncthreads();
-      if (!spilled && n == kCtaCap) {  // move the entries to the bucket's global region
-        for (int k = tid; k < n; k += 256) G[k] = sE[k];
-        __syncthreads();
-        E = G;
-        spilled = true;
-      }
       const int64_t at = s_at;
-      for (int64_t hi = n - 1; hi >= at; hi -= 256) {
-        const int64_t k = hi - tid;
-        Mhe t;
-        if (k >= at) t = E[k];
+      for (int64_t hi = n; hi > at; hi -= 2048) {  // Mp[at, n) -> Mp[at + 1, n + 1)
+        const int64_t lo = hi - 2048 > at ? hi - 2048 : at;
+        uint32_t v[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          const int64_t k = lo + tid + 256 * q;
+          if (k < hi) v[q] = Mp[k];
+        }
         __syncthreads();
-        if (k >= at) E[k + 1] = t;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          const int64_t k = lo + tid + 256 * q;
+          if (k < hi) Mp[k + 1] = v[q];
+        }
         __syncthreads();
       }
-      if (tid == 0) E[at] = s_x;
+      if (tid == 0) {
+        G[n] = s_x;
+        Mp[at] = (uint32_t)n;
+      }
       ++n;
       __syncthreads();
+      pos = f + 1;
     }
   }
-  if (!spilled)
-    for (int k = tid; k < n; k += 256) G[k] = sE[k];
   if (tid == 0) nent_out[b] = (uint32_t)n;
   if (ncoll) atomicAdd(coll, ncoll);
 }
@@ -526,7 +546,8 @@ __global__ void k_lpt_keys(const uint32_t* __restrict__ cnt, uint32_t* __restric
 }
 
 // GetMatchList (LM/MemHash.h:182-203): bucket order, then vector order.
-__global__ void k_emit(const Mhe* __restrict__ ent, const uint32_t* __restrict__ bstart, const uint32_t* __restrict__ nent,
+__global__ void k_emit(const Mhe* __restrict__ ent, const uint32_t* __restrict__ emap, const uint32_t* __restrict__ bstart,
+                       const uint32_t* __restrict__ nent,
                        const uint32_t* __restrict__ ooff, int64_t* __restrict__ out, uint64_t cap) {
   const int lane = threadIdx.x & 31;
   const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -534,12 +555,14 @@ __global__ void k_emit(const Mhe* __restrict__ ent, const uint32_t* __restrict__
   for (int b = gw; b < kTableSize; b += nw) {
     const uint32_t n = nent[b];
     const Mhe* E = ent + bstart[b];
+    const uint32_t* M = emap + bstart[b];  // sorted order
     for (uint32_t k = lane; k < n; k += 32) {
       const uint64_t o = (uint64_t)ooff[b] + k;
       if (o < cap) {
-        out[3 * o + 0] = E[k].s0;
-        out[3 * o + 1] = E[k].s1;
-        out[3 * o + 2] = E[k].len;
+        const Mhe& e = E[M[k]];
+        out[3 * o + 0] = e.s0;
+        out[3 * o + 1] = e.s1;
+        out[3 * o + 2] = e.len;
       }
     }
   }
@@ -629,7 +652,8 @@ int pairwise_matches_dev(Ctx* c, const uint8_t* d_a, uint64_t na, const uint8_t*
   // per-bucket tables: count, start, nent, lpt key/id x2, out offsets, scan scratch, totals
   uint32_t* btab = (uint32_t*)ws.get(c, 44, (size_t)kTableSize * 4 * 10 + scan_scratch_words(kTableSize) * 4 + 256);
   Mhe* ent = (Mhe*)ws.get(c, 45, npairs * sizeof(Mhe));
-  if (!mhe || !bk0 || !bk1 || !or0 || !or1 || !sscr || !btab || !ent)
+  uint32_t* emap = (uint32_t*)ws.get(c, 48, npairs * sizeof(uint32_t));
+  if (!mhe || !bk0 || !bk1 || !or0 || !or1 || !sscr || !btab || !ent || !emap)
     return report_error(MVG_ERR_NOMEM, "workspace allocation failed");
   uint32_t* bcount = btab;
   uint32_t* bstart = btab + kTableSize;
@@ -666,11 +690,18 @@ int pairwise_matches_dev(Ctx* c, const uint8_t* d_a, uint64_t na, const uint8_t*
   mc.n[1] = (int64_t)nb;
   mc.s = s;
   stage_mark(c, "bucket_replay");
-  k_bucket_replay<<<kTableSize, 256, 0, c->stream>>>(mc, mhe, sorted_pair, bstart, bcount, border, ent, nent, d_coll);
+  static bool replay_attr = false;  // once per process: more than 48 KB of shared memory
+  if (!replay_attr) {
+    MVG_CUDA_TRY(cudaFuncSetAttribute(k_bucket_replay, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)(kChunk * sizeof(Mhe))));
+    replay_attr = true;
+  }
+  k_bucket_replay<<<kTableSize, 256, kChunk * sizeof(Mhe), c->stream>>>(mc, mhe, sorted_pair, bstart, bcount, border,
+                                                                        ent, emap, nent, d_coll);
   c->launches++;
   stage_mark(c, "emit");
   exclusive_scan(nent, ooff, kTableSize, bscr, tot + 1, c->stream, &c->launches);
-  k_emit<<<kTableSize / 8, 256, 0, c->stream>>>(ent, bstart, nent, ooff, d_out, cap);
+  k_emit<<<kTableSize / 8, 256, 0, c->stream>>>(ent, emap, bstart, nent, ooff, d_out, cap);
   c->launches++;
   stage_end(c);
   MVG_CUDA_TRY(cudaMemcpyAsync(c->h_scalars, tot + 1, 4, cudaMemcpyDeviceToHost, c->stream));

@@ -35,7 +35,8 @@ struct Ctx {
   uint64_t launches = 0;
   uint64_t tb_arena = ~0ull;  // capped per call at 60% of free device memory
   int dp_rows = 8;            // full gap-DP rows per lane (4 or 8)
-  int band_rows = 4;          // banded gap-DP rows per lane (2, 4 or 8)
+  int band_rows = 4;          // banded gap-DP rows per lane (1, 2, 4 or 8)
+  double band_whole = 0.5;    // bands covering at least this share of their matrix run whole
   Workspace ws;
   MatchStats stats;
   bool profiling = false;

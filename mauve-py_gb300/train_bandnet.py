@@ -204,18 +204,23 @@ def train(args):
     import synth  # noqa: F401
     vb = DeviceBatch(*subset_host_idx(tr, np.sort(val_idx)), dev)
     best = None
-    for alpha in (1.0, 1.25, 1.5, 2.0):
-        for beta in (0.0, 16.0, 48.0, 128.0):
-            d, h = net.propose_dev(*vb.ptrs(), vb.n, alpha, beta)
-            secs, used, cells, *_ = timed_banded(ctx, vb, d, h)
-            if best is None or secs < best[0]:
-                best = (secs, alpha, beta, float((used == 1).mean()), cells)
-    _, alpha, beta, acc_v, _ = best
-    print("calibrated alpha %.2f beta %.1f (validation accept %.3f)" % (alpha, beta, acc_v), flush=True)
+    for whole in (0.5, 0.3, 0.15):
+        ctx.set_band_whole_fraction(whole)
+        for alpha in (1.0, 1.25, 1.5, 2.0):
+            for beta in (0.0, 16.0, 48.0, 128.0):
+                d, h = net.propose_dev(*vb.ptrs(), vb.n, alpha, beta)
+                secs, used, cells, *_ = timed_banded(ctx, vb, d, h)
+                if best is None or secs < best[0]:
+                    best = (secs, alpha, beta, whole, float((used == 1).mean()), cells)
+    _, alpha, beta, whole, acc_v, _ = best
+    ctx.set_band_whole_fraction(whole)
+    print("calibrated alpha %.2f beta %.1f whole %.2f (validation accept %.3f)" % (alpha, beta, whole, acc_v),
+          flush=True)
     params = net.get_params()
     # held-out evaluation: full vs learned band vs band without the network
     res = {"train_gaps": tr.n, "eval_gaps": ev.n, "train_seconds": train_s, "steps": step,
-           "loss_curve": losses[-20:], "nonfinite_minibatches": skipped, "alpha": alpha, "beta": beta}
+           "loss_curve": losses[-20:], "nonfinite_minibatches": skipped, "alpha": alpha, "beta": beta,
+           "whole_fraction": whole}
     tf, sc_f, p_f, pl_f = timed_full(ctx, ev)
     tf, sc_f, p_f, pl_f = timed_full(ctx, ev)  # second run: warm
     t_prop0 = time.perf_counter()
@@ -262,7 +267,7 @@ def train(args):
     res["label_band"] = {"seconds": t_lab, **status_rates(used_lab), "cells": cells_lab,
                          "speedup_vs_full": tf / t_lab}
     print(json.dumps(res, indent=1), flush=True)
-    np.savez(args.out, params=params, alpha=np.float32(alpha), beta=np.float32(beta))
+    np.savez(args.out, params=params, alpha=np.float32(alpha), beta=np.float32(beta), whole=np.float32(whole))
     with open(os.path.splitext(args.out)[0] + "_eval.json", "w") as f:
         json.dump(res, f, indent=1)
     print("total %.1fs" % (time.time() - t_all))
