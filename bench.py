@@ -147,7 +147,7 @@ def cpu_gapdp_gcups(sa, oa, sb, ob, sample, threads):
 
 
 WEIGHTS = os.path.join(ROOT, "mauve-py_gb300", "bandnet_weights.npz")
-LB_NPROB = 20_000
+LB_NPROB = 200_000
 
 
 def learned_band_section(ctx, args, dev, stream, rank):

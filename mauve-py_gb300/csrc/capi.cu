@@ -126,6 +126,9 @@ int mvg_create(mvg_handle* out, int device) {
   mvg_context* c = new mvg_context();
   c->device = device;
   cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->aux, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->fork, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->join, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaMalloc(&c->d_err, 64);
   if (e == cudaSuccess) e = cudaMallocHost(&c->h_err, 64);
   if (e == cudaSuccess) e = cudaMallocHost(&c->h_scalars, 64);
@@ -153,6 +156,10 @@ int mvg_destroy(mvg_handle h) {
   if (h->d_err) cudaFree(h->d_err);
   if (h->h_err) cudaFreeHost(h->h_err);
   if (h->h_scalars) cudaFreeHost(h->h_scalars);
+  if (h->aux) cudaStreamSynchronize(h->aux);
+  if (h->fork) cudaEventDestroy(h->fork);
+  if (h->join) cudaEventDestroy(h->join);
+  if (h->aux) cudaStreamDestroy(h->aux);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
   return 0;

@@ -175,7 +175,7 @@ __device__ void dp_solve(const DpJob& J, DpShared& sh, int w, int kstart, int ks
   int32_t bound = kNeg;  // best score of any path leaving the band (this warp's part)
   // banded mode: totals and running prefixes of the per-base best scores
   int32_t totA = 0, totB = 0, pa = 0, pb_lo = 0, pb_hi = 0;
-  int pa_rows = 0, pb_lo_cols = 0, pb_hi_cols = 0;
+  int pa_rows = 0, pb_lo_cols = 0;
   if (BANDED) {
     totA = warp_best_sum(A, 0, LA, J.base_max);
     totB = warp_best_sum(B, 0, LB, J.base_max);
@@ -236,8 +236,10 @@ __device__ void dp_solve(const DpJob& J, DpShared& sh, int w, int kstart, int ks
     // banded mode: prefix of the row maxima up to each owned row, the
     // strip's bottom row, and the column prefix at jlo-1 for lane 31
     int32_t rowpre[R];
-    int32_t strip_pre = 0, run31 = 0;
+    int32_t strip_pre = 0, run31 = 0, pb_next = 0;
     if (BANDED) {
+      // prefixes carried from the previous strip of this warp cover the
+      // rows and columns up to it; only a gap (cooperative mode) is summed
       pa += warp_best_sum(A, pa_rows, row0, J.base_max);
       pa_rows = row0;
       int32_t lsum = 0;
@@ -259,6 +261,7 @@ __device__ void dp_solve(const DpJob& J, DpShared& sh, int w, int kstart, int ks
       pb_lo += warp_best_sum(B, pb_lo_cols, jlo - 1, J.base_max);
       pb_lo_cols = jlo - 1;
       run31 = pb_lo;
+      pb_next = pb_lo;  // prefix over B[0..next_lo-1), caught during the sweep
     }
     // Row above this strip at absolute column x: row 0 for the first strip,
     // else the previous strip's computed columns, its left boundary or -inf.
@@ -338,9 +341,10 @@ __device__ void dp_solve(const DpJob& J, DpShared& sh, int w, int kstart, int ks
         pubD = L.lD[R - 1];
         pubI = L.lI[R - 1];
         if (lane == 31 && writes_row) rb_out[j] = make_int4(pubM, pubD, pubI, 0);
-        if (BANDED && bottom_exit) {
+        if (BANDED && lane == 31) {
           run31 += best_of(J.base_max, bsel);  // prefix over B[0..j)
-          if (j < next_lo) {
+          if (j == next_lo - 1) pb_next = run31;
+          if (bottom_exit && j < next_lo) {
             const int32_t best = max(pubM, max(pubD, pubI));
             bound = max(bound, best + min(totA - strip_pre, totB - run31));
           }
@@ -396,9 +400,25 @@ __device__ void dp_solve(const DpJob& J, DpShared& sh, int w, int kstart, int ks
       J.scores[p] = sc;
       J.end_edge[p] = (uint8_t)e;
     }
+    if (BANDED) {
+      // lane 31 swept every column of the strip: its running sum is the
+      // prefix over B[0..jhi); carry the prefixes to this warp's next strip
+      pb_hi = __shfl_sync(0xffffffffu, run31, 31);
+      if (kstep == 1) {
+        pa = strip_pre;
+        pa_rows = row0 + SR;
+        if (k + 1 < nstrips) {
+          if (next_lo - 1 <= jhi) {  // lane 31 passed column next_lo-1 (or it is jlo-1)
+            pb_lo = __shfl_sync(0xffffffffu, pb_next, 31);
+            pb_lo_cols = next_lo - 1;
+          } else {  // the next strip starts right of this one: sum the rest there
+            pb_lo = pb_hi;
+            pb_lo_cols = jhi;
+          }
+        }
+      }
+    }
     if (BANDED && jhi < LB) {  // right-edge exits: an I step leaves the band
-      pb_hi += warp_best_sum(B, pb_hi_cols, jhi, J.base_max);
-      pb_hi_cols = jhi;
 #pragma unroll
       for (int r = 0; r < R; ++r) {
         const int i = row0 + lane * R + r + 1;

@@ -27,6 +27,8 @@
 //                                       the seeds after it are re-tested
 //   k_emit                               GetMatchList order: bucket 0..39999,
 //                                       then bucket vector order
+#include <cooperative_groups.h>
+
 #include "mvg_internal.h"
 #include "prim.cuh"
 
@@ -213,10 +215,28 @@ __device__ __forceinline__ uint64_t pattern_mask64(const SeedDesc& s) {
 // Window start (0-based) in genome q of the pair at displacement u from the
 // entry state's edge (st, len), or -1 outside the genome.
 __device__ __forceinline__ int64_t ext_start(int64_t st, int64_t len, int64_t u, int L, int64_t n) {
+  if (st > 0 && u >= st) return -1;  // a left step past the genome start (the phases never take it)
   const int64_t sq = st > 0 ? st - u : st;
   const int64_t get = sq < 0 ? -sq + len + u - L : sq;
   const int64_t x = get - 1;
   return (x >= 0 && x + L <= n) ? x : -1;
+}
+
+// 64 bases (128 bits, big-endian, base p in bits 127:126) from 2-bit words;
+// reads words p/16 .. p/16 + 4.
+__device__ __forceinline__ void window128(const uint32_t* __restrict__ g, uint64_t p, uint64_t& hi, uint64_t& lo) {
+  const uint64_t q = p >> 4;
+  const uint32_t sh = (uint32_t)(p & 15) * 2;
+  const uint64_t H = ((uint64_t)__ldg(g + q) << 32) | __ldg(g + q + 1);
+  const uint64_t M = ((uint64_t)__ldg(g + q + 2) << 32) | __ldg(g + q + 3);
+  const uint32_t T = __ldg(g + q + 4);
+  if (sh == 0) {
+    hi = H;
+    lo = M;
+  } else {
+    hi = (H << sh) | (M >> (64 - sh));
+    lo = (M << sh) | (uint64_t)(T >> (32 - sh));
+  }
 }
 
 __device__ void ext_fill(const MatchCtx& c, int64_t st0, int64_t st1, int64_t len, int64_t u0, uint64_t pmask,
@@ -225,7 +245,32 @@ __device__ void ext_fill(const MatchCtx& c, int64_t st0, int64_t st1, int64_t le
   const int L = c.s.L;
   const bool same = (st0 > 0) == (st1 > 0);
   uint32_t word = 0;
-  for (int t = 0; t < 32; ++t) {
+  bool done = false;
+  // Same-strand pairs: the lane's 32 windows lie in one 64-base stretch of
+  // each genome (both move the same way with u), so one XOR of the two
+  // stretches gives all 32 window tests.
+  if (same) {
+    const int64_t U = u0 + lane * 32;
+    const int64_t a0 = ext_start(st0, len, U, L, c.n[0]), a31 = ext_start(st0, len, U + 31, L, c.n[0]);
+    const int64_t b0 = ext_start(st1, len, U, L, c.n[1]), b31 = ext_start(st1, len, U + 31, L, c.n[1]);
+    const bool down = st0 > 0;  // window starts decrease with u
+    const int64_t amin = down ? a31 : a0, bmin = down ? b31 : b0;
+    if (a0 >= 0 && a31 >= 0 && b0 >= 0 && b31 >= 0 && amin + 80 <= c.n[0] && bmin + 80 <= c.n[1]) {
+      uint64_t ah, al, bh, bl;
+      window128(c.g[0], (uint64_t)amin, ah, al);
+      window128(c.g[1], (uint64_t)bmin, bh, bl);
+      const uint64_t dh = ah ^ bh, dl = al ^ bl;
+#pragma unroll 4
+      for (int t = 0; t < 32; ++t) {
+        const int j = down ? 31 - t : t;  // window start amin + j
+        const uint64_t w = j == 0 ? dh : ((dh << (2 * j)) | (dl >> (64 - 2 * j)));
+        word |= (uint32_t)((w & pmask) == 0) << t;
+      }
+      if (U == 0) word &= ~1u;  // displacement 0 is not a step
+      done = true;
+    }
+  }
+  for (int t = 0; t < 32 && !done; ++t) {
     const int64_t u = u0 + lane * 32 + t;
     const int64_t xa = ext_start(st0, len, u, L, c.n[0]);
     const int64_t xb = ext_start(st1, len, u, L, c.n[1]);
@@ -248,6 +293,7 @@ __device__ void ext_fill(const MatchCtx& c, int64_t st0, int64_t st1, int64_t le
 }
 
 __device__ void warp_extend(const MatchCtx& c, Mhe& m, ExtRing& R) {
+  const int lane = threadIdx.x & 31;
   const int L = c.s.L;
   const uint64_t pmask = pattern_mask64(c.s);
   const int64_t e0 = m.s0, e1 = m.s1, elen = m.len;  // entry state S0
@@ -274,27 +320,33 @@ __device__ void warp_extend(const MatchCtx& c, Mhe& m, ExtRing& R) {
       // jump phase: k-1 good jumps before the first mismatching window
       int64_t room = room0 - u;
       const int64_t nj = room >= L ? room / L : 0;
-      int64_t k = 1;
-      while (k <= nj) {
-        const int64_t d = u + k * L;
-        ensure(d);
-        if (!bit(d)) break;
-        ++k;
+      // 32 jumps per ballot: lane t tests jump kb + t
+      int64_t good = nj;
+      for (int64_t kb = 1; kb <= nj; kb += 32) {
+        const int64_t klast = kb + 31 < nj ? kb + 31 : nj;
+        ensure(u + klast * L);
+        const int64_t kk = kb + lane;
+        const bool miss = kk <= nj && !bit(u + kk * L);
+        const unsigned mm = __ballot_sync(0xffffffffu, miss);
+        if (mm) {
+          good = kb - 1 + (__ffs(mm) - 1);
+          break;
+        }
       }
-      u += (k - 1) * L;
+      u += good * L;
       // single-base phase: the furthest matching offset in 1..min(room, L)
       room = room0 - u;
       const int64_t ms = room > 0 ? (room < L ? room : L) : 0;
       if (ms <= 0) break;
       ensure(u + ms);
-      int lim = 0;
-      for (int q = (int)ms; q >= 1; --q)
-        if (bit(u + q)) {
-          lim = q;
-          break;
-        }
-      if (lim == 0) break;
-      u += lim;
+      // bits of displacements u+1 .. u+ms (ms <= 32): the highest set one
+      const int64_t b0 = u + 1;
+      const uint64_t two = ((uint64_t)ring[((b0 >> 5) + 1) & (kExtRing - 1)] << 32) |
+                           ring[(b0 >> 5) & (kExtRing - 1)];
+      uint64_t win = two >> (b0 & 31);
+      win &= ms >= 64 ? ~0ull : ((1ull << ms) - 1);
+      if (!win) break;
+      u += 64 - __clzll(win);
     }
     moved[sd] = u;
   }
@@ -328,6 +380,13 @@ __device__ __forceinline__ int64_t lower_bound_mapped(const Mhe* __restrict__ E,
 // warp-per-bucket replay (32 seeds per test round), 8 buckets each.
 constexpr uint32_t kBigBucket = 512;
 constexpr int kChunk = 1024;  // seeds staged per chunk (dynamic shared memory)
+// Buckets with at least kClusterBucket seeds are replayed by a cluster of
+// kClusterCtas CTAs (k_bucket_replay_cluster); one whose entries outgrow the
+// per-CTA copy is marked kRedo and replayed by k_bucket_replay instead.
+constexpr uint32_t kClusterBucket = 16384;
+constexpr int kClusterCtas = 8;
+constexpr int kLocalCap = 1536;
+constexpr uint32_t kRedo = 0xffffffffu;
 extern __shared__ __align__(16) unsigned char replay_dyn_smem[];
 
 __global__ void __launch_bounds__(256) k_bucket_replay(MatchCtx c, const Mhe* __restrict__ mhe,
@@ -336,7 +395,8 @@ __global__ void __launch_bounds__(256) k_bucket_replay(MatchCtx c, const Mhe* __
                                                        const uint32_t* __restrict__ bcount,
                                                        const uint32_t* __restrict__ border, Mhe* ent,
                                                        uint32_t* emap, uint32_t* __restrict__ nent_out,
-                                                       unsigned long long* __restrict__ coll) {
+                                                       unsigned long long* __restrict__ coll, int nclusters,
+                                                       int redo_pass) {
   __shared__ ExtRing s_ring[8];
   __shared__ Mhe s_x;
   __shared__ long long s_at;
@@ -358,6 +418,11 @@ __global__ void __launch_bounds__(256) k_bucket_replay(MatchCtx c, const Mhe* __
   }
   __syncthreads();
   const int nbig = s_nbig;
+  // the cluster pass owns the nclusters largest buckets (if big enough);
+  // the redo pass replays only those it handed back
+  const bool cluster_owned = (int)blockIdx.x < nclusters && bcount[border[blockIdx.x]] >= kClusterBucket;
+  if (redo_pass && !(cluster_owned && nent_out[border[blockIdx.x]] == kRedo)) return;
+  if (!redo_pass && cluster_owned) return;
   if ((int)blockIdx.x >= nbig) {
     // ------------------------------------------------ warp per bucket
     const int idx = nbig + ((int)blockIdx.x - nbig) * 8 + wid;
@@ -511,6 +576,158 @@ __global__ void __launch_bounds__(256) k_bucket_replay(MatchCtx c, const Mhe* __
   }
   if (tid == 0) nent_out[b] = (uint32_t)n;
   if (ncoll) atomicAdd(coll, ncoll);
+}
+
+// The largest buckets, one per cluster of kClusterCtas CTAs on as many SMs.
+// Every CTA keeps its own copy of the bucket's entries (appended, with a
+// uint16 sorted-order map) in shared memory and tests its 256 seeds of each
+// 2048-seed chunk against it; the CTAs' first fresh seeds meet in every
+// CTA's shared memory (distributed shared memory stores + cluster barrier),
+// the CTA owning the first one extends it and sends the new entry and its
+// sorted position to every CTA, and all insert it.  The result is the same
+// sequence of tests and inserts as the one-CTA replay.  A bucket that grows
+// past kLocalCap entries is left untouched and marked kRedo.
+constexpr int kClusterChunk = kClusterCtas * 256;
+
+__device__ __forceinline__ int64_t lower_bound_local(const Mhe* __restrict__ E, const uint16_t* __restrict__ M,
+                                                     int64_t n, const Mhe& x, int L) {
+  int64_t first = 0, len = n;
+  while (len > 0) {
+    int64_t half = len >> 1, mid = first + half;
+    if (mhe_less(E[M[mid]], x, L)) {
+      first = mid + 1;
+      len = len - half - 1;
+    } else {
+      len = half;
+    }
+  }
+  return first;
+}
+
+__global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(256, 1)
+    k_bucket_replay_cluster(MatchCtx c, const Mhe* __restrict__ mhe, const uint32_t* __restrict__ sorted_pair,
+                            const uint32_t* __restrict__ bstart, const uint32_t* __restrict__ bcount,
+                            const uint32_t* __restrict__ border, Mhe* ent, uint32_t* emap,
+                            uint32_t* __restrict__ nent_out, unsigned long long* __restrict__ coll) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cl = cg::this_cluster();
+  const unsigned rank = cl.block_rank();
+  Mhe* lent = reinterpret_cast<Mhe*>(replay_dyn_smem);                  // kLocalCap entries
+  uint16_t* lmap = reinterpret_cast<uint16_t*>(lent + kLocalCap);      // kLocalCap map words
+  __shared__ ExtRing s_ring;
+  __shared__ uint32_t s_wmin[8];
+  __shared__ uint32_t s_cmin[kClusterCtas];  // written by every CTA of the cluster
+  __shared__ Mhe s_seed;                     // the fresh seed, inside the owning CTA
+  __shared__ Mhe s_x;                        // the new entry, written by the owning CTA
+  __shared__ long long s_at;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const int L = c.s.L;
+  const int cid = (int)(blockIdx.x / kClusterCtas);
+  for (int idx = cid; idx == cid; ++idx) {  // the cid-th largest bucket
+    const uint32_t b = border[idx];
+    const uint32_t cnt = bcount[b];
+    if (cnt < kClusterBucket) break;
+    const uint32_t* sp = sorted_pair + bstart[b];
+    int64_t n = 0;
+    bool overflow = false;
+    unsigned long long ncoll = 0;
+    for (uint32_t cbase = 0; cbase < cnt && !overflow; cbase += kClusterChunk) {
+      const uint32_t cend = min(cnt, cbase + (uint32_t)kClusterChunk);
+      const uint32_t slot = cbase + rank * 256 + tid;
+      const bool have = slot < cend;
+      Mhe m = {0, 0, 0, 0};
+      if (have) m = mhe[sp[slot]];
+      uint32_t pos = cbase;
+      while (pos < cend) {
+        bool fresh = false;
+        if (have && slot >= pos) {
+          const int64_t at = lower_bound_local(lent, lmap, n, m, L);
+          fresh = !(at != n && !mhe_less(lent[lmap[at]], m, L) && !mhe_less(m, lent[lmap[at]], L));
+        }
+        const uint32_t wmin = __reduce_min_sync(0xffffffffu, fresh ? slot : kRedo);
+        if (lane == 0) s_wmin[wid] = wmin;
+        __syncthreads();
+        if (tid < kClusterCtas) {
+          uint32_t v = kRedo;
+#pragma unroll
+          for (int q = 0; q < 8; ++q) v = min(v, s_wmin[q]);
+          *cl.map_shared_rank(&s_cmin[rank], tid) = v;  // thread j tells CTA j
+        }
+        cl.sync();
+        uint32_t f = kRedo;
+#pragma unroll
+        for (int q = 0; q < kClusterCtas; ++q) f = min(f, s_cmin[q]);
+        if (f == kRedo) {
+          if (have && slot >= pos) ++ncoll;
+          pos = cend;
+          cl.sync();  // every CTA has read s_cmin before the next round writes it
+          break;
+        }
+        if (have && slot >= pos && slot < f) ++ncoll;
+        const unsigned owner = (f - cbase) / 256;
+        if (n == kLocalCap) {  // no room for the entry: hand the bucket to the one-CTA replay
+          overflow = true;
+          cl.sync();
+          break;
+        }
+        if (rank == owner) {
+          if (slot == f) s_seed = m;
+          __syncthreads();
+          if (wid == 0) {
+            Mhe x = s_seed;
+            warp_extend(c, x, s_ring);
+            const int64_t at = lower_bound_local(lent, lmap, n, x, L);
+            if (lane < kClusterCtas) {  // lane j sends the entry to CTA j
+              *cl.map_shared_rank(&s_x, lane) = x;
+              *cl.map_shared_rank(&s_at, lane) = at;
+            }
+          }
+        }
+        cl.sync();
+        const int64_t at = s_at;
+        for (int64_t hi = n; hi > at; hi -= 2048) {  // lmap[at, n) -> lmap[at + 1, n + 1)
+          const int64_t lo = hi - 2048 > at ? hi - 2048 : at;
+          uint16_t v[8];
+#pragma unroll
+          for (int q = 0; q < 8; ++q) {
+            const int64_t k = lo + tid + 256 * q;
+            if (k < hi) v[q] = lmap[k];
+          }
+          __syncthreads();
+#pragma unroll
+          for (int q = 0; q < 8; ++q) {
+            const int64_t k = lo + tid + 256 * q;
+            if (k < hi) lmap[k + 1] = v[q];
+          }
+          __syncthreads();
+        }
+        if (tid == 0) {
+          lent[n] = s_x;
+          lmap[at] = (uint16_t)n;
+        }
+        ++n;
+        __syncthreads();
+        pos = f + 1;
+      }
+    }
+    // ncoll of the CTAs that finished: summed per CTA
+    if (overflow) {
+      if (rank == 0 && tid == 0) nent_out[b] = kRedo;
+    } else {
+      if (rank == 0) {
+        Mhe* G = ent + bstart[b];
+        uint32_t* Mp = emap + bstart[b];
+        for (int64_t k = tid; k < n; k += 256) {
+          G[k] = lent[lmap[k]];
+          Mp[k] = (uint32_t)k;
+        }
+        if (tid == 0) nent_out[b] = (uint32_t)n;
+      }
+      for (int d = 16; d > 0; d >>= 1) ncoll += __shfl_xor_sync(0xffffffffu, ncoll, d);
+      if (lane == 0 && ncoll) atomicAdd(coll, ncoll);
+    }
+    cl.sync();  // the shared copies are reset for the next bucket
+  }
 }
 
 // Segment of each bucket in the bucket-sorted pair list: two lower_bounds.
@@ -691,13 +908,31 @@ int pairwise_matches_dev(Ctx* c, const uint8_t* d_a, uint64_t na, const uint8_t*
   mc.s = s;
   stage_mark(c, "bucket_replay");
   static bool replay_attr = false;  // once per process: more than 48 KB of shared memory
+  const size_t cl_smem = (size_t)kLocalCap * (sizeof(Mhe) + sizeof(uint16_t));
   if (!replay_attr) {
     MVG_CUDA_TRY(cudaFuncSetAttribute(k_bucket_replay, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)(kChunk * sizeof(Mhe))));
+    MVG_CUDA_TRY(cudaFuncSetAttribute(k_bucket_replay_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)cl_smem));
     replay_attr = true;
   }
+  int sms = 0;
+  MVG_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device));
+  const int nclusters = sms / kClusterCtas > 0 ? sms / kClusterCtas : 1;
+  // the largest buckets on clusters (aux stream) beside everything else
+  MVG_CUDA_TRY(cudaEventRecord(c->fork, c->stream));
+  MVG_CUDA_TRY(cudaStreamWaitEvent(c->aux, c->fork, 0));
+  k_bucket_replay_cluster<<<nclusters * kClusterCtas, 256, cl_smem, c->aux>>>(mc, mhe, sorted_pair, bstart, bcount,
+                                                                            border, ent, emap, nent, d_coll);
+  MVG_CUDA_TRY(cudaEventRecord(c->join, c->aux));
+  c->launches++;
   k_bucket_replay<<<kTableSize, 256, kChunk * sizeof(Mhe), c->stream>>>(mc, mhe, sorted_pair, bstart, bcount, border,
-                                                                        ent, emap, nent, d_coll);
+                                                                        ent, emap, nent, d_coll, nclusters, 0);
+  MVG_CUDA_TRY(cudaStreamWaitEvent(c->stream, c->join, 0));
+  // buckets the cluster pass handed back (more entries than a CTA's copy holds)
+  k_bucket_replay<<<nclusters, 256, kChunk * sizeof(Mhe), c->stream>>>(mc, mhe, sorted_pair, bstart, bcount, border,
+                                                                       ent, emap, nent, d_coll, nclusters, 1);
+  c->launches++;
   c->launches++;
   stage_mark(c, "emit");
   exclusive_scan(nent, ooff, kTableSize, bscr, tot + 1, c->stream, &c->launches);

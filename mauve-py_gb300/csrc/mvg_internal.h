@@ -29,6 +29,8 @@ constexpr int kMaxStages = 24;
 struct Ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
+  cudaStream_t aux = nullptr;       // second stream for work that runs beside the main stream's
+  cudaEvent_t fork = nullptr, join = nullptr;
   uint32_t* d_err = nullptr;     // device error word
   uint32_t* h_err = nullptr;     // pinned mirror
   uint64_t* h_scalars = nullptr; // pinned scalars for small device->host reads

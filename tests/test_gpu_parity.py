@@ -113,6 +113,21 @@ def test_matches_reference_mds42_pair(ctx):
     np.testing.assert_array_equal(out[:3 * n].cpu().numpy().reshape(-1, 3), want)
 
 
+@pytest.mark.parametrize("n,sub", [(300000, 0.01), (300000, 0.05), (600000, 0.10)])
+def test_matches_single_diagonal_buckets(ctx, n, sub):
+    """Substitutions only: nearly every seed pair lands in one bucket (the
+    cluster replay), with few or with more entries than a CTA's shared copy
+    holds (the hand-back to the one-CTA replay)."""
+    rng = np.random.default_rng(int(n * sub))
+    acgt = np.frombuffer(b"ACGT", np.uint8)
+    a = rng.choice(acgt, n)
+    b = a.copy()
+    m = rng.random(n) < sub
+    b[m] = acgt[(np.searchsorted(acgt, b[m]) + rng.integers(1, 4, int(m.sum()))) % 4]
+    seed = O.get_seed(O.default_seed_weight(n), 3)
+    np.testing.assert_array_equal(ctx.pairwise_matches(a, b, seed), O.pairwise_matches(a, b, seed))
+
+
 def test_matches_degenerate_inputs(ctx):
     seed = mvg.get_seed(15, 3)
     assert ctx.pairwise_matches(b"ACGT", b"ACGTACGT", seed).shape == (0, 3)
