@@ -553,7 +553,7 @@ def run_gb300(args, world, rank, local):
         }
         if args.only == "gapdp":
             line.update({"value": round(gcups, 2), "unit": "GCUPS", "ms_per_step": round(dp_ms, 3)})
-        lb_section = learned_band_section(ctx, args, dev, stream, rank)
+        lb_section = None if args.no_learned_band else learned_band_section(ctx, args, dev, stream, rank)
         if lb_section:
             line["gap_dp"]["learned_band"] = lb_section
 
@@ -609,6 +609,7 @@ def main():
     ap.add_argument("--pair", choices=["recoded", "small"], default="recoded",
                     help="genome pair: recoded 4.6 Mbp (default) or the 1 Mbp plain-method pair")
     ap.add_argument("--gap-nprob", type=int, default=GAP_NPROB)
+    ap.add_argument("--no-learned-band", action="store_true", help="skip the learned-band section (profiling)")
     args = ap.parse_args()
     world, rank, local = dist_setup(args.gpus)
     if args.impl == "reference":

@@ -241,88 +241,102 @@ __global__ void __launch_bounds__(os::kThreads) k_os_pass(const K* __restrict__ 
   using namespace os;
   __shared__ K skey[kTile];
   __shared__ uint32_t sval[kTile];
-  __shared__ uint32_t wcnt[8][256];
-  __shared__ uint32_t cnt[256];
-  __shared__ uint32_t run[256];
+  __shared__ uint32_t whist[8][256];  // per-warp digit counts, then per-warp offsets
   __shared__ uint32_t lstart[256];
   __shared__ uint32_t gbase[256];
   __shared__ uint32_t s_tile;
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   if (tid == 0) s_tile = atomicAdd(tile_ctr, 1u);
-  cnt[tid] = 0;
-  run[tid] = 0;
 #pragma unroll
-  for (int w = 0; w < 8; ++w) wcnt[w][tid] = 0;
+  for (int w = 0; w < 8; ++w) whist[w][tid] = 0;
   __syncthreads();
   const int64_t tile = s_tile;
   const int64_t base = tile * kTile;
   const int tile_n = (int)min((int64_t)kTile, n - base);
+  // warp w owns tile items [256 w, 256 w + 256): item 256 w + 32 k + lane
   K key[kItems];
-  uint32_t val[kItems], dig[kItems];
+  uint32_t val[kItems], dig[kItems], rank[kItems];
+  const uint32_t lt_mask = (1u << lane) - 1u;
 #pragma unroll
-  for (int c = 0; c < kItems; ++c) {
-    const int li = c * kThreads + tid;
+  for (int k = 0; k < kItems; ++k) {
+    const int li = wid * 256 + 32 * k + lane;
     if (li < tile_n) {
-      key[c] = kin[base + li];
-      val[c] = vin[base + li];
-      dig[c] = (uint32_t)(key[c] >> shift) & 255u;
-      atomicAdd(&cnt[dig[c]], 1u);
+      key[k] = kin[base + li];
+      val[k] = vin[base + li];
+      dig[k] = (uint32_t)(key[k] >> shift) & 255u;
     } else {
-      key[c] = 0;
-      val[c] = 0;
-      dig[c] = 256u + (uint32_t)lane;  // private digit: never shares a rank
+      key[k] = 0;
+      val[k] = 0;
+      dig[k] = 256u + (uint32_t)lane;  // private digit: never shares a rank
     }
   }
+  // stable rank inside the warp: earlier rounds, then lower lanes
+#pragma unroll
+  for (int k = 0; k < kItems; ++k) {
+    const uint32_t d = dig[k];
+    const uint32_t peers = __match_any_sync(0xffffffffu, d);
+    const uint32_t before = d < 256u ? whist[wid][d] : 0u;
+    rank[k] = before + __popc(peers & lt_mask);
+    __syncwarp();
+    if (d < 256u && (peers & lt_mask) == 0) whist[wid][d] = before + __popc(peers);
+    __syncwarp();
+  }
   __syncthreads();
-  // publish this tile's counts, then look back over earlier tiles
-  const uint32_t mine = cnt[tid];
+  // per digit: the tile count and each warp's offset inside the digit's run
+  uint32_t mine = 0;
+#pragma unroll
+  for (int w = 0; w < 8; ++w) {
+    const uint32_t c = whist[w][tid];
+    whist[w][tid] = mine;
+    mine += c;
+  }
+  // publish this tile's counts, then look back over earlier tiles, kWin
+  // tiles per step (independent loads issued together; a tile not yet
+  // published is re-read, bounded)
   uint32_t* st = state + tile * 256 + tid;
   *(volatile uint32_t*)st = (tile == 0 ? kPre : kAgg) | mine;
+  constexpr int kWin = 16;
   uint32_t excl = 0;
-  for (int64_t t = tile - 1; t >= 0; --t) {
-    const volatile uint32_t* p = state + t * 256 + tid;
-    uint32_t v = *p;
-    long long spins = 0;
-    while ((v & ~kVal) == 0 && ++spins < kSpin) v = *p;
-    if ((v & ~kVal) == 0) {
-      set_error(err, kDevWatchdog);
-      break;
+  for (int64_t t = tile - 1; t >= 0; t -= kWin) {
+    uint32_t v[kWin];
+#pragma unroll
+    for (int q = 0; q < kWin; ++q) v[q] = t - q >= 0 ? *(const volatile uint32_t*)(state + (t - q) * 256 + tid) : kPre;
+    bool done = false;
+#pragma unroll
+    for (int q = 0; q < kWin; ++q) {
+      if (done) break;
+      if (t - q < 0) {
+        done = true;
+        break;
+      }
+      uint32_t x = v[q];
+      const volatile uint32_t* p = state + (t - q) * 256 + tid;
+      long long spins = 0;
+      while ((x & ~kVal) == 0 && ++spins < kSpin) x = *p;
+      if ((x & ~kVal) == 0) {
+        set_error(err, kDevWatchdog);
+        done = true;
+        break;
+      }
+      excl += x & kVal;
+      if (x & kPre) done = true;
     }
-    excl += v & kVal;
-    if (v & kPre) break;
+    if (done) break;
   }
   if (tile > 0) *(volatile uint32_t*)st = kPre | (excl + mine);
   gbase[tid] = gstart[tid] + excl;
   lstart[tid] = block_excl_scan256(mine, nullptr);
   __syncthreads();
-  // stable rank inside the tile: chunks of 256 in order, warps in order
-  const uint32_t lt_mask = (1u << lane) - 1u;
 #pragma unroll
-  for (int c = 0; c < kItems; ++c) {
-    const uint32_t d = dig[c];
-    const uint32_t peers = __match_any_sync(0xffffffffu, d);
-    const uint32_t lrank = __popc(peers & lt_mask);
-    if (d < 256u && lrank == 0) wcnt[wid][d] = __popc(peers);
-    __syncthreads();
+  for (int k = 0; k < kItems; ++k) {
+    const uint32_t d = dig[k];
     if (d < 256u) {
-      uint32_t r = run[d] + lrank;
-      for (int w = 0; w < wid; ++w) r += wcnt[w][d];
-      const uint32_t lp = lstart[d] + r;
-      skey[lp] = key[c];
-      sval[lp] = val[c];
+      const uint32_t lp = lstart[d] + whist[wid][d] + rank[k];
+      skey[lp] = key[k];
+      sval[lp] = val[k];
     }
-    __syncthreads();
-    {
-      uint32_t s = 0;
-#pragma unroll
-      for (int w = 0; w < 8; ++w) {
-        s += wcnt[w][tid];
-        wcnt[w][tid] = 0;
-      }
-      run[tid] += s;
-    }
-    __syncthreads();
   }
+  __syncthreads();
   for (int i = tid; i < tile_n; i += kThreads) {
     const K k = skey[i];
     const uint32_t d = (uint32_t)(k >> shift) & 255u;
