@@ -148,6 +148,10 @@ def cpu_gapdp_gcups(sa, oa, sb, ob, sample, threads):
 
 WEIGHTS = os.path.join(ROOT, "mauve-py_gb300", "bandnet_weights.npz")
 LB_NPROB = 200_000
+# DRAM bytes of the seed-path kernels per match-finding call on the recoded
+# pair, from one ncu capture (profiles/anchoring_launch_list_recoded_pair.md);
+# below the algorithmic bytes because the sort passes' outputs stay in L2
+SEED_PATH_TRAFFIC = 0.61e9
 
 
 def learned_band_section(ctx, args, dev, stream, rank):
@@ -165,7 +169,7 @@ def learned_band_section(ctx, args, dev, stream, rank):
     alpha, beta = float(w["alpha"]), float(w["beta"])
     whole = float(w["whole"]) if "whole" in w.files else 0.5
     ctx.set_band_whole_fraction(whole)
-    sa, oa, sb, ob = synth.gap_batch_recoded(seed=1000 + rank, nprob=LB_NPROB)
+    sa, oa, sb, ob = synth.gap_batch_recoded(seed=1000 + rank, nprob=args.lb_nprob)
     n = len(oa) - 1
     la, lb = np.diff(oa), np.diff(ob)
     cells = float(np.sum(la * lb))
@@ -483,7 +487,10 @@ def run_gb300(args, world, rank, local):
                 "achieved": round(seed_bytes / (seed_ms / 1e3) / 1e9, 2) if seed_ms else None,
                 "peak": hbm_peak, "unit": "GB/s", "peak_kind": peak_kind,
                 "frac": round(seed_bytes / (seed_ms / 1e3) / 1e9 / hbm_peak, 4) if seed_ms else None,
-                "traffic": None, "algorithmic_bytes": seed_bytes, "bytes_per_base": per_base,
+                "traffic": SEED_PATH_TRAFFIC if args.pair == "recoded" else None,
+                "traffic_source": "ncu dram__bytes_read+write of the seed-path kernels per call "
+                                  "(profiles/anchoring_launch_list_recoded_pair.md)",
+                "algorithmic_bytes": seed_bytes, "bytes_per_base": per_base,
                 "stage_ms": stages, "dominant_stage": max(stages, key=stages.get) if stages else None},
             "e2e": {"value": round(e2e_value, 3), "unit": "Mbp/s", "h2d_bytes_per_step": na + nb,
                     "d2h_bytes_per_step": int(nmatch) * 24 + 12},
@@ -610,6 +617,7 @@ def main():
                     help="genome pair: recoded 4.6 Mbp (default) or the 1 Mbp plain-method pair")
     ap.add_argument("--gap-nprob", type=int, default=GAP_NPROB)
     ap.add_argument("--no-learned-band", action="store_true", help="skip the learned-band section (profiling)")
+    ap.add_argument("--lb-nprob", type=int, default=LB_NPROB, help="gaps in the learned-band section")
     args = ap.parse_args()
     world, rank, local = dist_setup(args.gpus)
     if args.impl == "reference":

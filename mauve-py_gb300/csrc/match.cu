@@ -586,8 +586,7 @@ __global__ void __launch_bounds__(256) k_bucket_replay(MatchCtx c, const Mhe* __
 // the CTA owning the first one extends it and sends the new entry and its
 // sorted position to every CTA, and all insert it.  The result is the same
 // sequence of tests and inserts as the one-CTA replay.  A bucket that grows
-// past kLocalCap entries is left untouched and marked kRedo.  While the
-// owner extends, the other CTAs extend their own first fresh seeds ahead.
+// past kLocalCap entries is left untouched and marked kRedo.
 constexpr int kClusterChunk = kClusterCtas * 256;
 
 __device__ __forceinline__ int64_t lower_bound_local(const Mhe* __restrict__ E, const uint16_t* __restrict__ M,
@@ -618,9 +617,7 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(256, 1)
   __shared__ ExtRing s_ring;
   __shared__ uint32_t s_wmin[8];
   __shared__ uint32_t s_cmin[kClusterCtas];  // written by every CTA of the cluster
-  __shared__ Mhe s_seed;                     // this CTA's candidate seed
-  __shared__ Mhe s_spec;                     // its extension, computed ahead (see below)
-  __shared__ uint32_t s_spec_slot;           // the slot s_spec belongs to
+  __shared__ Mhe s_seed;                     // the fresh seed, inside the owning CTA
   __shared__ Mhe s_x;                        // the new entry, written by the owning CTA
   __shared__ long long s_at;
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
@@ -634,8 +631,6 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(256, 1)
     int64_t n = 0;
     bool overflow = false;
     unsigned long long ncoll = 0;
-    if (tid == 0) s_spec_slot = kRedo;
-    __syncthreads();
     for (uint32_t cbase = 0; cbase < cnt && !overflow; cbase += kClusterChunk) {
       const uint32_t cend = min(cnt, cbase + (uint32_t)kClusterChunk);
       const uint32_t slot = cbase + rank * 256 + tid;
@@ -652,25 +647,16 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(256, 1)
         const uint32_t wmin = __reduce_min_sync(0xffffffffu, fresh ? slot : kRedo);
         if (lane == 0) s_wmin[wid] = wmin;
         __syncthreads();
-        // this CTA's candidate (its first fresh seed) and whether its
-        // extension is already known; bit 31 marks a known one
-        uint32_t cand = kRedo;
+        if (tid < kClusterCtas) {
+          uint32_t v = kRedo;
 #pragma unroll
-        for (int q = 0; q < 8; ++q) cand = min(cand, s_wmin[q]);
-        const bool known = cand != kRedo && cand == s_spec_slot;
-        if (tid < kClusterCtas) *cl.map_shared_rank(&s_cmin[rank], tid) = cand | (known ? 0x80000000u : 0u);
+          for (int q = 0; q < 8; ++q) v = min(v, s_wmin[q]);
+          *cl.map_shared_rank(&s_cmin[rank], tid) = v;  // thread j tells CTA j
+        }
         cl.sync();
         uint32_t f = kRedo;
-        bool f_known = false;
 #pragma unroll
-        for (int q = 0; q < kClusterCtas; ++q) {
-          const uint32_t v = s_cmin[q] & 0x7fffffffu;
-          if (s_cmin[q] != kRedo && v < f) {
-            f = v;
-            f_known = (s_cmin[q] & 0x80000000u) != 0;
-          }
-        }
-        if (f == (kRedo & 0x7fffffffu)) f = kRedo;
+        for (int q = 0; q < kClusterCtas; ++q) f = min(f, s_cmin[q]);
         if (f == kRedo) {
           if (have && slot >= pos) ++ncoll;
           pos = cend;
@@ -684,29 +670,17 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(256, 1)
           cl.sync();
           break;
         }
-        // Extensions depend only on the seed, so when the first fresh seed's
-        // extension is not known yet, every CTA extends its own candidate in
-        // the same wait (they usually become the first fresh seed of later
-        // rounds); a known one is reused without waiting.
-        if (!f_known && cand != kRedo && !known) {
-          if (slot == cand) s_seed = m;
+        if (rank == owner) {
+          if (slot == f) s_seed = m;
           __syncthreads();
           if (wid == 0) {
             Mhe x = s_seed;
             warp_extend(c, x, s_ring);
-            if (lane == 0) {
-              s_spec = x;
-              s_spec_slot = cand;
+            const int64_t at = lower_bound_local(lent, lmap, n, x, L);
+            if (lane < kClusterCtas) {  // lane j sends the entry to CTA j
+              *cl.map_shared_rank(&s_x, lane) = x;
+              *cl.map_shared_rank(&s_at, lane) = at;
             }
-          }
-          __syncthreads();
-        }
-        if (rank == owner && wid == 0) {
-          const Mhe x = s_spec;  // s_spec_slot == f here
-          const int64_t at = lower_bound_local(lent, lmap, n, x, L);
-          if (lane < kClusterCtas) {  // lane j sends the entry to CTA j
-            *cl.map_shared_rank(&s_x, lane) = x;
-            *cl.map_shared_rank(&s_at, lane) = at;
           }
         }
         cl.sync();
