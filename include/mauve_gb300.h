@@ -268,10 +268,19 @@ int mvg_set_tb_arena(mvg_handle h, uint64_t bytes);
  * the tuned choice committed in mauve-py_gb300/dp_tuning.json. */
 int mvg_set_dp_rows(mvg_handle h, int full_rows, int band_rows);
 
-/* Banded passes: a proposed band whose strips cover at least `fraction` of
- * its matrix (0 < fraction <= 1, default 0.5) is not banded; the problem
- * runs over the whole matrix in the same launch (status 2). */
+/* Banded passes: a proposed band that covers at least `fraction` of its
+ * matrix (0 < fraction <= 1, default 0.5) is not banded; the problem runs
+ * over the whole matrix in the strip kernel's launch (status 2).  With the
+ * ring schedule on, the share is that of the columns a row keeps
+ * (2*half + 2 + ceil(LB/LA)) in LB; otherwise that of the strips' cells. */
 int mvg_set_band_whole_fraction(mvg_handle h, double fraction);
+
+/* Banded passes on the ring schedule (on = 1, the default): one warp per
+ * problem, groups of 4, 8, 16 or 32 rows per lane chained lane to lane along
+ * the band, the smallest group height whose schedule is valid for the band;
+ * bands no height fits run in the strip kernel.  on = 0 runs every band in
+ * the strip kernel.  Results are identical either way. */
+int mvg_set_band_ring(mvg_handle h, int on);
 
 /* Per-stage timing with CUDA events on the handle's stream (off by default;
  * no extra synchronisation).  After a call, mvg_stage_times gives the stage

@@ -90,4 +90,77 @@ MVG_HD uint64_t band_cells(const Band& b) {
   return cells;
 }
 
+// Ring-schedule geometry of the banded kernel (gapdp_ring.cuh).
+//
+// Rows are cut into groups of R; group g (rows gR+1 .. gR+R) keeps columns
+// [lo_g, lo_g + W) with lo_g = floor((gR+1)*LB/LA) + delta - half and the
+// same width W for every group, W = 2*half + 2 + ceil((R-1)*LB/LA): the
+// columns within `half` of the band centre of each of its rows, like Band.
+// lo_g is not clamped: column 0 is the matrix's left boundary, columns below
+// it and above LB lie outside the matrix.  Lane g mod 32 of a warp runs group
+// g on wavefront steps [start_g, start_g + W) with start_g = g + lo_g - lo_0,
+// so group g reaches column j (step j + g - lo_0) exactly one step after
+// group g-1 did, and the cell above comes from the previous lane of the ring.
+struct RingBand {
+  int LA, LB, R, G, delta, half, W, lo0, lo_last;
+  int64_t steps;  // wavefront steps of the whole problem
+};
+
+MVG_HD int ring_lo(const RingBand& b, int g) {
+  return (int)(((int64_t)g * b.R + 1) * b.LB / b.LA + b.delta - b.half);
+}
+
+MVG_HD RingBand make_ring_band(int LA, int LB, int delta, int half, int R) {
+  RingBand b;
+  b.LA = LA;
+  b.LB = LB;
+  b.R = R;
+  b.delta = delta;
+  b.half = half < 0 ? 0 : half;
+  b.G = (LA + R - 1) / R;
+  const int64_t span = ((int64_t)(R - 1) * LB + LA - 1) / LA;
+  const int64_t W = 2 * (int64_t)b.half + 2 + span;
+  b.W = W > (1 << 30) ? (1 << 30) : (int)W;
+  b.lo0 = ring_lo(b, 0);
+  b.lo_last = ring_lo(b, b.G - 1);
+  b.steps = (int64_t)(b.G - 1) + b.lo_last - b.lo0 + b.W;
+  return b;
+}
+
+// Whether the ring schedule is valid for this band: group 0 reaches column 1
+// and the last group column LB (the path's end cells); lo_g <= LB and
+// lo_g + W > 1 for every group (lo is non-decreasing); each group's first
+// column lies inside its predecessor's range (lo_g - lo_{g-1} <=
+// ceil(R*LB/LA) <= W - 1); and a lane finishes group g before it starts
+// group g+32: W <= 32 + lo_{g+32} - lo_g, where lo_{g+32} - lo_g >=
+// floor(32*R*LB/LA).
+MVG_HD bool ring_eligible(const RingBand& b) {
+  if (b.half > (1 << 20) || b.delta > (1 << 24) || b.delta < -(1 << 24)) return false;
+  if (b.lo0 > 1 || b.lo0 + b.W - 1 < 1) return false;
+  if (b.lo_last > b.LB || b.lo_last + b.W - 1 < b.LB) return false;
+  const int64_t step = ((int64_t)b.R * b.LB + b.LA - 1) / b.LA;
+  if (step > b.W - 1) return false;
+  if (b.G > 32 && (int64_t)b.W > 32 + (int64_t)32 * b.R * b.LB / b.LA) return false;
+  return true;
+}
+
+// Traceback words of a ring-scheduled problem: each lane stores its R
+// nibbles per step as one stream, nibble s*R + r in word (s*R + r) / 8 of
+// the lane; word x of lane t sits at x*32 + t.
+MVG_HD uint64_t ring_tb_words(const RingBand& b) { return (uint64_t)((b.steps * b.R + 7) / 8) * 32; }
+
+// Matrix cells inside the kept region (rows 1..LA, columns 1..LB).
+MVG_HD uint64_t ring_cells(const RingBand& b) {
+  uint64_t cells = 0;
+  for (int g = 0; g < b.G; ++g) {
+    int rows = b.LA - g * b.R;
+    if (rows > b.R) rows = b.R;
+    int lo = ring_lo(b, g), hi = lo + b.W - 1;
+    if (lo < 1) lo = 1;
+    if (hi > b.LB) hi = b.LB;
+    if (hi >= lo) cells += (uint64_t)rows * (uint64_t)(hi - lo + 1);
+  }
+  return cells;
+}
+
 }  // namespace mvg

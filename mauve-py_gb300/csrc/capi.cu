@@ -407,6 +407,12 @@ int mvg_set_band_whole_fraction(mvg_handle h, double fraction) {
   return 0;
 }
 
+int mvg_set_band_ring(mvg_handle h, int on) {
+  if (!h || (on != 0 && on != 1)) return report_error(MVG_ERR_ARG, "on must be 0 or 1");
+  h->band_ring = on;
+  return 0;
+}
+
 int mvg_set_profiling(mvg_handle h, int on) {
   if (!h) return report_error(MVG_ERR_ARG, "null handle");
   h->profiling = on != 0;

@@ -17,10 +17,12 @@
 // k_traceback walks each problem's bits from (LA, LB) like BitTraceBack
 // (MU/bittraceback.cpp:138-210); k_path_compact moves paths to slot heads.
 #include <algorithm>
+#include <cmath>
 #include <numeric>
 #include <vector>
 
 #include "gapdp_kernel.cuh"
+#include "gapdp_ring.cuh"
 #include "mvg_internal.h"
 
 namespace mvg {
@@ -64,6 +66,10 @@ template __global__ void k_gapdp_t<false, 8>(DpJob);
 template __global__ void k_gapdp_t<true, 8>(DpJob);
 template __global__ void k_gapdp_t<true, 2>(DpJob);
 template __global__ void k_gapdp_t<true, 1>(DpJob);
+template __global__ void k_gapdp_ring<4>(RingJob);
+template __global__ void k_gapdp_ring<8>(RingJob);
+template __global__ void k_gapdp_ring<16>(RingJob);
+template __global__ void k_gapdp_ring<32>(RingJob);
 
 // BitTraceBack from (LA, LB); writes the path reversed at the end of the
 // problem's path slot and its length.  Banded problems index their strips
@@ -348,6 +354,119 @@ static int run_dp(Ctx* c, const DpInputs& in, const std::vector<uint32_t>& ids, 
   return 0;
 }
 
+// Ring-scheduled banded problems (gapdp_ring.cuh): rsel[w] is the group
+// height R of ids[w].  Slots are ordered by R, each class most expensive
+// first, and cut into waves that fit the traceback arena; per wave one
+// k_gapdp_ring<R> launch per class, then traceback and path compaction.
+static int run_ring(Ctx* c, const DpInputs& in, const std::vector<uint32_t>& ids, const std::vector<uint8_t>& rsel,
+                    const std::vector<int64_t>& la, const std::vector<int64_t>& lb, const std::vector<int32_t>& dv,
+                    const std::vector<int32_t>& hv, const int32_t* d_delta, const int32_t* d_half, uint8_t* d_accept,
+                    unsigned long long* d_cells) {
+  const int64_t nwork = (int64_t)ids.size();
+  if (nwork == 0) return 0;
+  std::vector<uint64_t> bytes(nwork), cost(nwork);
+  for (int64_t w = 0; w < nwork; ++w) {
+    const uint32_t p = ids[w];
+    const RingBand b = make_ring_band((int)la[p], (int)lb[p], dv[p], hv[p], rsel[w]);
+    bytes[w] = (ring_tb_words(b) * 4 + 255) & ~255ull;
+    cost[w] = (uint64_t)b.steps * (uint64_t)(rsel[w] * 18 + 50);
+  }
+  std::vector<uint32_t> idx(nwork);
+  std::iota(idx.begin(), idx.end(), 0u);
+  std::sort(idx.begin(), idx.end(), [&](uint32_t x, uint32_t y) {
+    return rsel[x] != rsel[y] ? rsel[x] < rsel[y] : (cost[x] != cost[y] ? cost[x] > cost[y] : x < y);
+  });
+  uint64_t arena = c->tb_arena;
+  {
+    size_t free_b = 0, total_b = 0;
+    if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess) {
+      const uint64_t cap = (uint64_t)((c->ws.size[18] + free_b) * 0.6);
+      if (arena > cap) arena = cap;
+    }
+  }
+  std::vector<uint32_t> order(nwork);
+  std::vector<uint8_t> rows_of(nwork);
+  std::vector<uint64_t> tboff(nwork);
+  std::vector<int64_t> wave_begin;
+  uint64_t acc = 0, arena_need = 0;
+  for (int64_t q = 0; q < nwork; ++q) {
+    const uint32_t w = idx[q];
+    if (bytes[w] > arena) return report_error(MVG_ERR_CAPACITY, "one gap-DP problem exceeds the traceback arena");
+    if (q == 0 || acc + bytes[w] > arena) {
+      wave_begin.push_back(q);
+      acc = 0;
+    }
+    order[q] = ids[w];
+    rows_of[q] = rsel[w];
+    tboff[q] = acc;
+    acc += bytes[w];
+    arena_need = std::max(arena_need, acc);
+  }
+  wave_begin.push_back(nwork);
+  Workspace& ws = c->ws;
+  uint32_t* d_order = (uint32_t*)ws.get(c, 11, (size_t)nwork * 4);
+  uint64_t* d_tboff = (uint64_t*)ws.get(c, 12, (size_t)nwork * 8);
+  uint8_t* d_edge = (uint8_t*)ws.get(c, 13, la.size() + 16);
+  unsigned* d_counter = (unsigned*)ws.get(c, 14, 64);
+  uint8_t* d_rows = (uint8_t*)ws.get(c, 60, (size_t)nwork + 16);
+  uint32_t* tb = (uint32_t*)ws.get(c, 18, arena_need);
+  if (!d_order || !d_tboff || !d_edge || !d_counter || !d_rows || !tb)
+    return report_error(MVG_ERR_NOMEM, "workspace allocation failed");
+  MVG_CUDA_TRY(cudaMemcpyAsync(d_order, order.data(), (size_t)nwork * 4, cudaMemcpyHostToDevice, c->stream));
+  MVG_CUDA_TRY(cudaMemcpyAsync(d_tboff, tboff.data(), (size_t)nwork * 8, cudaMemcpyHostToDevice, c->stream));
+  MVG_CUDA_TRY(cudaMemcpyAsync(d_rows, rows_of.data(), (size_t)nwork, cudaMemcpyHostToDevice, c->stream));
+  int dev_sms = 0;
+  MVG_CUDA_TRY(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, c->device));
+  for (size_t wv = 0; wv + 1 < wave_begin.size(); ++wv) {
+    const int64_t w0 = wave_begin[wv], w1 = wave_begin[wv + 1];
+    stage_mark(c, "dp_ring");
+    for (int64_t a = w0; a < w1;) {
+      int64_t e = a;
+      while (e < w1 && rows_of[e] == rows_of[a]) ++e;
+      const int R = rows_of[a];
+      void (*kern)(RingJob) = R == 4 ? k_gapdp_ring<4> : R == 8 ? k_gapdp_ring<8> : R == 16 ? k_gapdp_ring<16>
+                                                                                              : k_gapdp_ring<32>;
+      int bps = 0;
+      MVG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kern, kRingThreads, 0));
+      if (bps < 1) bps = 1;
+      const int64_t need_blocks = (e - a + kRingThreads / 32 - 1) / (kRingThreads / 32);
+      const int grid = (int)std::min<int64_t>((int64_t)dev_sms * bps, need_blocks);
+      RingJob J;
+      J.sa = in.sa;
+      J.oa = in.oa;
+      J.sb = in.sb;
+      J.ob = in.ob;
+      J.order = d_order + a;
+      J.tb_off = d_tboff + a;
+      J.nwork = (int)(e - a);
+      J.tb = tb;
+      J.scores = in.scores;
+      J.end_edge = d_edge;
+      J.band_delta = d_delta;
+      J.band_half = d_half;
+      J.accept = d_accept;
+      J.base_max = g_base_max;
+      J.counter = d_counter;
+      J.cells = d_cells;
+      MVG_CUDA_TRY(cudaMemsetAsync(d_counter, 0, 4, c->stream));
+      kern<<<grid, kRingThreads, 0, c->stream>>>(J);
+      c->launches++;
+      a = e;
+    }
+    stage_mark(c, "traceback");
+    const int nw = (int)(w1 - w0);
+    k_traceback_ring<<<grid_for(nw, 128), 128, 0, c->stream>>>(
+        in.oa, in.ob, d_order + w0, d_rows + w0, d_tboff + w0, nw, tb, d_edge, d_delta, d_half, d_accept,
+        in.path_off, in.paths, in.path_len, c->d_err);
+    stage_mark(c, "path_compact");
+    k_path_compact<<<grid_for((int64_t)nw * 32, 256), 256, 0, c->stream>>>(in.oa, in.ob, d_order + w0, nw, d_accept,
+                                                                            in.path_off, in.paths, in.path_len);
+    c->launches += 2;
+    MVG_CUDA_TRY(cudaGetLastError());
+  }
+  return 0;
+}
+
 // Every base code must be 0..3 (the kernels mask to 2 bits; this reports it).
 static int check_codes(Ctx* c, const uint8_t* d_sa, uint64_t na, const uint8_t* d_sb, uint64_t nb) {
   k_check_codes<<<grid_for(na / 16 + 1, 256), 256, 0, c->stream>>>(d_sa, na, c->d_err);
@@ -428,33 +547,60 @@ int gapdp_banded_dev(Ctx* c, const uint8_t* d_sa, const uint64_t* d_oa, const ui
   std::vector<int32_t> dv(h_delta, h_delta + nprob), hv(h_half, h_half + nprob);
   uint64_t bc = 0;
   // A band covering at least band_whole (default half) of its matrix saves
-  // little and may still fail its check: such problems are not banded.  They run in the same
-  // launch with a band that covers the whole matrix (no exit cells, so the
-  // check always passes and the result is the full DP's), which spares a
-  // second full-DP pass for them.
-  std::vector<uint32_t> ids(nprob);
+  // little and may still fail its check: such problems are not banded.  They
+  // run in the strip kernel's launch with a band that covers the whole matrix
+  // (no exit cells, so the check always passes and the result is the full
+  // DP's), which spares a second full-DP pass for them.  Other bands run on
+  // the ring schedule with the smallest valid group height, or in the strip
+  // kernel when no height is valid (or the ring kernel is switched off).
+  static const int kRingRows[4] = {4, 8, 16, 32};
+  std::vector<uint32_t> ids, rids;
+  std::vector<uint8_t> rsel;
   std::vector<uint8_t> whole(nprob, 0);
   for (int64_t p = 0; p < nprob; ++p) {
     if (hv[p] < 0) return report_error(MVG_ERR_ARG, "negative band half-width");
-    ids[p] = (uint32_t)p;
     const uint64_t full = (uint64_t)la[p] * (uint64_t)lb[p];
-    const uint64_t cells = band_cells(make_band((int)la[p], (int)lb[p], dv[p], hv[p], 32 * c->band_rows));
-    if ((double)cells >= c->band_whole * (double)full) {
+    bool is_whole;
+    uint64_t cells = 0;
+    if (c->band_ring) {
+      // columns a row keeps: both half-widths, the row's own cells and the
+      // diagonal's drift over one row
+      const double cols = 2.0 * hv[p] + 2.0 + std::ceil((double)lb[p] / (double)la[p]);
+      is_whole = cols >= c->band_whole * (double)lb[p];
+    } else {
+      cells = band_cells(make_band((int)la[p], (int)lb[p], dv[p], hv[p], 32 * c->band_rows));
+      is_whole = (double)cells >= c->band_whole * (double)full;
+    }
+    if (is_whole) {
       whole[p] = 1;
       dv[p] = 0;
       hv[p] = (int32_t)std::max(la[p], lb[p]) + 2;
       bc += full;
+      ids.push_back((uint32_t)p);
+      continue;
+    }
+    int rr = 0;
+    if (c->band_ring)
+      for (int q = 0; q < 4 && !rr; ++q)
+        if (ring_eligible(make_ring_band((int)la[p], (int)lb[p], dv[p], hv[p], kRingRows[q]))) rr = kRingRows[q];
+    if (rr) {
+      rids.push_back((uint32_t)p);
+      rsel.push_back((uint8_t)rr);
     } else {
+      if (c->band_ring) cells = band_cells(make_band((int)la[p], (int)lb[p], dv[p], hv[p], 32 * c->band_rows));
       bc += cells;
+      ids.push_back((uint32_t)p);
     }
   }
   int32_t* d_delta = (int32_t*)c->ws.get(c, 23, (size_t)nprob * 4);
   int32_t* d_half = (int32_t*)c->ws.get(c, 25, (size_t)nprob * 4);
   uint8_t* d_accept = (uint8_t*)c->ws.get(c, 26, (size_t)nprob + 16);
-  if (!d_delta || !d_half || !d_accept) return report_error(MVG_ERR_NOMEM, "workspace allocation failed");
+  unsigned long long* d_cells = (unsigned long long*)c->ws.get(c, 61, 64);
+  if (!d_delta || !d_half || !d_accept || !d_cells) return report_error(MVG_ERR_NOMEM, "workspace allocation failed");
   MVG_CUDA_TRY(cudaMemcpyAsync(d_delta, dv.data(), (size_t)nprob * 4, cudaMemcpyHostToDevice, c->stream));
   MVG_CUDA_TRY(cudaMemcpyAsync(d_half, hv.data(), (size_t)nprob * 4, cudaMemcpyHostToDevice, c->stream));
   MVG_CUDA_TRY(cudaMemsetAsync(d_accept, 0, (size_t)nprob, c->stream));
+  MVG_CUDA_TRY(cudaMemsetAsync(d_cells, 0, 8, c->stream));
   MVG_CUDA_TRY(cudaMemsetAsync(c->d_err, 0, 4, c->stream));
   if ((rc = check_codes(c, d_sa, h_oa[nprob], d_sb, h_ob[nprob]))) return rc;
   stage_begin_call(c);
@@ -462,9 +608,15 @@ int gapdp_banded_dev(Ctx* c, const uint8_t* d_sa, const uint64_t* d_oa, const ui
     rc = run_dp(c, in, ids, la, lb, d_delta, d_half, &dv, &hv, d_accept);
     if (rc) return rc;
   }
+  if (!rids.empty()) {
+    rc = run_ring(c, in, rids, rsel, la, lb, dv, hv, d_delta, d_half, d_accept, d_cells);
+    if (rc) return rc;
+  }
   std::vector<uint8_t> acc(nprob);
   MVG_CUDA_TRY(cudaMemcpyAsync(acc.data(), d_accept, (size_t)nprob, cudaMemcpyDeviceToHost, c->stream));
+  MVG_CUDA_TRY(cudaMemcpyAsync(c->h_scalars, d_cells, 8, cudaMemcpyDeviceToHost, c->stream));
   MVG_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  bc += c->h_scalars[0];
   std::vector<uint32_t> fallback;
   for (int64_t p = 0; p < nprob; ++p) {
     if (whole[p]) {

@@ -39,6 +39,7 @@ struct Ctx {
   int dp_rows = 8;            // full gap-DP rows per lane (4 or 8)
   int band_rows = 4;          // banded gap-DP rows per lane (1, 2, 4 or 8)
   double band_whole = 0.5;    // bands covering at least this share of their matrix run whole
+  int band_ring = 1;          // banded problems on the ring schedule where it is valid
   Workspace ws;
   MatchStats stats;
   bool profiling = false;

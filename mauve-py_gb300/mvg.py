@@ -43,7 +43,7 @@ EXPORTS = ["mvg_create", "mvg_destroy", "mvg_last_error", "mvg_stream", "mvg_ker
            "mvg_lut_fix_zero_idx_dev", "mvg_lut_fill_gaps", "mvg_lut_fill_gaps_dev", "mvg_lut_smooth_edges",
            "mvg_lut_smooth_edges_dev", "mvg_lut_find_gaps", "mvg_lut_find_gaps_dev", "mvg_lut_find_edges",
            "mvg_lut_find_mismatches", "mvg_lut_find_duplicate_mappings", "mvg_build_index_lut",
-           "mvg_build_index_lut_dev", "mvg_set_band_whole_fraction"]
+           "mvg_build_index_lut_dev", "mvg_set_band_whole_fraction", "mvg_set_band_ring"]
 
 TUNING_PATH = os.path.join(HERE, "dp_tuning.json")
 
@@ -80,6 +80,7 @@ def load_library(path=LIB_PATH):
         "mvg_gapdp_banded_dev": (ci, [vp, vp, vp, vp, vp, i64, vp, vp, vp, vp, vp, vp, vp, ctypes.POINTER(u64)]),
         "mvg_set_dp_rows": (ci, [vp, ci, ci]),
         "mvg_set_band_whole_fraction": (ci, [vp, ctypes.c_double]),
+        "mvg_set_band_ring": (ci, [vp, ci]),
         "mvg_gapdp_envelope_dev": (ci, [vp, vp, vp, vp, vp, i64, vp, vp]),
         "mvg_mlp_num_params": (i64, []),
         "mvg_mlp_set_params": (ci, [vp, vp]),
@@ -179,6 +180,10 @@ class Context:
     def set_band_whole_fraction(self, fraction):
         """Bands covering at least this share of their matrix run whole (default 0.5)."""
         _check(load_library().mvg_set_band_whole_fraction(self._h, float(fraction)))
+
+    def set_band_ring(self, on=True):
+        """Banded passes on the ring schedule (default) or all in the strip kernel."""
+        _check(load_library().mvg_set_band_ring(self._h, 1 if on else 0))
 
     def set_dp_rows(self, full_rows, band_rows=None):
         band_rows = self.band_rows if band_rows is None else band_rows

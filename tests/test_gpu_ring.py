@@ -1,0 +1,177 @@
+"""GPU tests of the ring-scheduled banded gap DP (csrc/gapdp_ring.cuh).
+
+Every banded result must equal the full DP's (scores and paths), whichever
+group height the schedule picks; the tests build bands that land in each
+height class and at the edges of the schedule's validity."""
+import numpy as np
+import pytest
+
+import bandnet
+import mvg
+import oracle as O
+import synth
+
+pytestmark = pytest.mark.gpu
+
+RING_ROWS = (4, 8, 16, 32)
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    import build as pkg_build
+    pkg_build.build()
+    c = mvg.Context(0)
+    yield c
+    c.close()
+
+
+def ring_lo(LA, LB, delta, half, R, g):
+    return (g * R + 1) * LB // LA + delta - half
+
+
+def ring_rows(LA, LB, delta, half):
+    """The group height the host picks (band.h ring_eligible), 0 if none."""
+    half = max(half, 0)
+    for R in RING_ROWS:
+        G = (LA + R - 1) // R
+        W = 2 * half + 2 + ((R - 1) * LB + LA - 1) // LA
+        lo0, lol = ring_lo(LA, LB, delta, half, R, 0), ring_lo(LA, LB, delta, half, R, G - 1)
+        if half > (1 << 20) or abs(delta) > (1 << 24):
+            continue
+        if lo0 > 1 or lo0 + W - 1 < 1 or lol > LB or lol + W - 1 < LB:
+            continue
+        if (R * LB + LA - 1) // LA > W - 1:
+            continue
+        if G > 32 and W > 32 + 32 * R * LB // LA:
+            continue
+        return R
+    return 0
+
+
+def whole_band(LA, LB, half, frac=0.5):
+    return 2.0 * half + 2.0 + np.ceil(LB / LA) >= frac * LB
+
+
+def batch_from_pairs(pairs):
+    sa = np.concatenate([a for a, _ in pairs]).astype(np.uint8)
+    sb = np.concatenate([b for _, b in pairs]).astype(np.uint8)
+    oa = np.zeros(len(pairs) + 1, np.uint64)
+    ob = np.zeros(len(pairs) + 1, np.uint64)
+    oa[1:] = np.cumsum([len(a) for a, _ in pairs])
+    ob[1:] = np.cumsum([len(b) for _, b in pairs])
+    return sa, oa, sb, ob
+
+
+def related_pair(rng, la, sub=0.02, indels=2):
+    a = rng.integers(0, 4, la).astype(np.uint8)
+    b = a.copy()
+    m = rng.random(la) < sub
+    b[m] = (b[m] + rng.integers(1, 4, int(m.sum()))) % 4
+    for _ in range(indels):
+        if len(b) < 4:
+            break
+        k = int(rng.integers(1, len(b) - 1))
+        if rng.random() < 0.5:
+            b = np.concatenate([b[:k], b[k + int(rng.integers(1, 5)):]])
+        else:
+            b = np.concatenate([b[:k], rng.integers(0, 4, int(rng.integers(1, 5))).astype(np.uint8), b[k:]])
+    if len(b) == 0:
+        b = rng.integers(0, 4, 1).astype(np.uint8)
+    return a, b
+
+
+def check_identical(ctx, sa, oa, sb, ob, delta, half):
+    s_full, p_full = ctx.gap_align_batch(sa, oa, sb, ob)
+    s, p, used, cells = ctx.gap_align_banded(sa, oa, sb, ob, np.asarray(delta, np.int32), np.asarray(half, np.int32))
+    np.testing.assert_array_equal(s, s_full)
+    assert p == p_full
+    return used, cells, s_full
+
+
+@pytest.mark.parametrize("R", RING_ROWS)
+def test_each_group_height_matches_full_dp(ctx, R):
+    """Bands sized so the schedule picks group height R; accepted ones must
+    exist and every output equals the full DP's."""
+    rng = np.random.default_rng(100 + R)
+    pairs, deltas, halves = [], [], []
+    target_half = {4: 40, 8: 110, 16: 230, 32: 470}[R]
+    while len(pairs) < 48:
+        la = int(rng.integers(2 * target_half + 200, 6000))
+        # divergence low enough for the band's exactness bound to pass:
+        # each substitution costs about 210 against the best-base sum,
+        # a band of half-width h absorbs about 155 h
+        sub = float(rng.uniform(0.0005, 0.5 * 155 * target_half / (210 * la)))
+        a, b = related_pair(rng, la, sub=sub, indels=int(rng.integers(0, 3)))
+        half = int(target_half + rng.integers(-5, 6))
+        delta = int(rng.integers(-8, 9))
+        if ring_rows(len(a), len(b), delta, half) != R or whole_band(len(a), len(b), half):
+            continue
+        pairs.append((a, b))
+        deltas.append(delta)
+        halves.append(half)
+    sa, oa, sb, ob = batch_from_pairs(pairs)
+    used, cells, _ = check_identical(ctx, sa, oa, sb, ob, deltas, halves)
+    assert (used == 1).sum() >= 24, used
+    la, lb = np.diff(oa.astype(np.int64)), np.diff(ob.astype(np.int64))
+    assert 0 < cells < float(np.sum(la * lb))
+
+
+def test_ring_and_strip_kernels_agree_on_mixed_batch(ctx):
+    sa, oa, sb, ob = synth.gap_batch_recoded(seed=31, nprob=600, lmin=1, lmax=3000)
+    la, lb = np.diff(oa), np.diff(ob)
+    rng = np.random.default_rng(5)
+    n = len(la)
+    for delta, half in [bandnet.heuristic_band(la, lb),
+                        (rng.integers(-60, 60, n).astype(np.int32), rng.integers(0, 400, n).astype(np.int32)),
+                        (np.zeros(n, np.int32), np.zeros(n, np.int32))]:
+        used_ring, _, _ = check_identical(ctx, sa, oa, sb, ob, delta, half)
+        ctx.set_band_ring(False)
+        try:
+            used_strip, _, _ = check_identical(ctx, sa, oa, sb, ob, delta, half)
+        finally:
+            ctx.set_band_ring(True)
+        assert set(np.unique(used_ring)) <= {0, 1, 2}
+        assert set(np.unique(used_strip)) <= {0, 1, 2}
+
+
+def test_edge_shapes(ctx):
+    """Tiny problems, one-row and one-column matrices, steep and flat
+    diagonals, bands pushed off the diagonal, zero and huge half-widths."""
+    rng = np.random.default_rng(9)
+    pairs, deltas, halves = [], [], []
+    shapes = [(1, 1), (1, 7), (7, 1), (2, 2), (3, 40), (40, 3), (33, 33), (64, 65), (200, 900), (900, 200),
+              (1500, 1500), (2048, 2050), (4000, 3990), (1, 300), (300, 1)]
+    for la, lb in shapes:
+        for delta, half in [(0, 0), (0, 3), (5, 20), (-5, 20), (0, 90), (40, 10), (-40, 10), (0, 5000)]:
+            a = rng.integers(0, 4, la).astype(np.uint8)
+            b = a[:lb].copy() if lb <= la else np.concatenate([a, rng.integers(0, 4, lb - la).astype(np.uint8)])
+            m = rng.random(len(b)) < 0.03
+            b[m] = (b[m] + 1) % 4
+            pairs.append((a, b))
+            deltas.append(delta)
+            halves.append(half)
+    sa, oa, sb, ob = batch_from_pairs(pairs)
+    used, _, s_full = check_identical(ctx, sa, oa, sb, ob, deltas, halves)
+    oscores, _, _, _ = O.nw_batch(sa, oa, sb, ob, with_paths=False)
+    np.testing.assert_array_equal(s_full, oscores)
+    classes = {ring_rows(len(a), len(b), d, h) for (a, b), d, h in zip(pairs, deltas, halves)}
+    assert {4, 8}.issubset(classes)
+
+
+def test_label_bands_are_accepted(ctx):
+    """Bands as wide as the training labels pass the exactness check on the
+    ring schedule as they do on strips."""
+    sa, oa, sb, ob = synth.gap_batch_recoded(seed=12, nprob=400, lmin=50, lmax=3000, unrelated=0.0)
+    la, lb = np.diff(oa), np.diff(ob)
+    scores, _ = ctx.gap_align_batch(sa, oa, sb, ob, with_paths=False)
+    import torch
+    t = [torch.from_numpy(np.ascontiguousarray(x)).cuda() for x in (sa, oa.astype(np.int64), sb, ob.astype(np.int64))]
+    _, env = bandnet.full_dp_labels_dev(ctx, *[x.data_ptr() for x in t], len(la), torch_device=t[0].device)
+    totals = (bandnet.best_totals(sa, oa), bandnet.best_totals(sb, ob))
+    _, delta, half = bandnet.labels_from_full_dp(la, lb, scores, env, margin=16, totals=totals)
+    s, p, used, cells = ctx.gap_align_banded(sa, oa, sb, ob, delta, half, with_paths=False)
+    np.testing.assert_array_equal(s, scores)
+    ring = np.array([ring_rows(int(x), int(y), int(d), int(h)) for x, y, d, h in zip(la, lb, delta, half)])
+    tried = (used != 2) & (ring > 0)
+    assert tried.sum() > 100
+    assert (used[tried] == 1).mean() > 0.9
