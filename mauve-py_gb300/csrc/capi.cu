@@ -129,6 +129,12 @@ int mvg_create(mvg_handle* out, int device) {
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->aux, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->fork, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->join, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->aux2, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->aux3, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->fork2, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->join2, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->fork3, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->join3, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaMalloc(&c->d_err, 64);
   if (e == cudaSuccess) e = cudaMallocHost(&c->h_err, 64);
   if (e == cudaSuccess) e = cudaMallocHost(&c->h_scalars, 64);
@@ -150,17 +156,17 @@ int mvg_create(mvg_handle* out, int device) {
 int mvg_destroy(mvg_handle h) {
   if (!h) return 0;
   cudaSetDevice(h->device);
-  if (h->stream) cudaStreamSynchronize(h->stream);
+  for (cudaStream_t st : {h->stream, h->aux, h->aux2, h->aux3})
+    if (st) cudaStreamSynchronize(st);
   mlp_release(h);
   h->ws.release();
   if (h->d_err) cudaFree(h->d_err);
   if (h->h_err) cudaFreeHost(h->h_err);
   if (h->h_scalars) cudaFreeHost(h->h_scalars);
-  if (h->aux) cudaStreamSynchronize(h->aux);
-  if (h->fork) cudaEventDestroy(h->fork);
-  if (h->join) cudaEventDestroy(h->join);
-  if (h->aux) cudaStreamDestroy(h->aux);
-  if (h->stream) cudaStreamDestroy(h->stream);
+  for (cudaEvent_t ev : {h->fork, h->join, h->fork2, h->join2, h->fork3, h->join3})
+    if (ev) cudaEventDestroy(ev);
+  for (cudaStream_t st : {h->aux3, h->aux2, h->aux, h->stream})
+    if (st) cudaStreamDestroy(st);
   delete h;
   return 0;
 }

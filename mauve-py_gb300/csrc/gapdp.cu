@@ -16,12 +16,16 @@
 // Kernels: k_gapdp_t (gapdp_kernel.cuh) fills the traceback arena;
 // k_traceback walks each problem's bits from (LA, LB) like BitTraceBack
 // (MU/bittraceback.cpp:138-210); k_path_compact moves paths to slot heads.
+#include <limits.h>
+
 #include <algorithm>
 #include <cmath>
+#include <functional>
 #include <numeric>
 #include <vector>
 
 #include "gapdp_kernel.cuh"
+#include "traceback_win.cuh"
 #include "gapdp_ring.cuh"
 #include "mvg_internal.h"
 
@@ -80,12 +84,13 @@ __global__ void k_traceback(const uint64_t* __restrict__ oa, const uint64_t* __r
                             const int32_t* __restrict__ band_delta, const int32_t* __restrict__ band_half,
                             const uint8_t* __restrict__ accept, const uint64_t* __restrict__ path_off,
                             char* __restrict__ paths, int64_t* __restrict__ path_len, uint32_t* err,
-                            int rows, int32_t* __restrict__ env) {
+                            int rows, int32_t* __restrict__ env, int long_path) {
   const int srows = 32 * rows;
   for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < nwork; w += gridDim.x * blockDim.x) {
     const uint32_t p = order[w];
     if (accept && !accept[p]) continue;
     const int LA = (int)(oa[p + 1] - oa[p]), LB = (int)(ob[p + 1] - ob[p]);
+    if (LA + LB >= long_path) continue;  // k_traceback_win walks it
     const uint32_t* T = tb + tb_off[w] / 4;
     const bool banded = band_delta != nullptr;
     const Band band = banded ? make_band(LA, LB, band_delta[p], band_half[p], srows) : make_full(LA, LB, srows);
@@ -203,12 +208,89 @@ struct DpInputs {
   int32_t* env = nullptr;  // optional path envelope output [2 * nprob]
 };
 
+// Starts the long-path walker for one wave on the aux stream (joined by
+// tb_long_join), beside the thread walker on the main stream.  A warp walks
+// a path about ten times faster than a thread but far fewer warps than
+// threads run at once, so warps take the longest paths only: those with
+// LA + LB >= kTbLongPath, at most one round of the walker's warps, longest
+// first.  *long_path receives the length from which paths go to warps.
+// The streams one DP pass runs on: its own, and the side stream its
+// long-path walker forks to, with the events and workspace slots for that.
+struct TbLanes {
+  cudaStream_t st, side;
+  cudaEvent_t fork, join;
+  int slot_list, slot_ctr;
+};
+
+static TbLanes main_lanes(Ctx* c) { return TbLanes{c->stream, c->aux, c->fork, c->join, 62, 63}; }
+
+static int tb_long_fork(Ctx* c, const TbLanes& L, const DpInputs& in, const std::vector<uint32_t>& slot_len,
+                        const uint32_t* d_order, const uint64_t* d_tboff, const uint32_t* tb, const uint8_t* d_edge,
+                        const int32_t* d_delta, const int32_t* d_half, const uint8_t* d_accept, int rows,
+                        const uint8_t* d_rows, int* long_path, bool* forked) {
+  *forked = false;
+  *long_path = INT_MAX;
+  static bool attr = false;  // once per process: more than 48 KB of shared memory
+  static int cap = 0;
+  int sms = 0;
+  MVG_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device));
+  if (!attr) {
+    MVG_CUDA_TRY(cudaFuncSetAttribute(k_traceback_win, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTbSmem));
+    int bps = 0;
+    MVG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_traceback_win, kTbWarps * 32, kTbSmem));
+    cap = std::max(1, bps) * kTbWarps;
+    attr = true;
+  }
+  const size_t round = (size_t)cap * (size_t)sms;
+  std::vector<uint32_t> lens;
+  for (uint32_t L : slot_len)
+    if (L >= (uint32_t)kTbLongPath) lens.push_back(L);
+  if (lens.empty()) return 0;
+  uint32_t thr = kTbLongPath;
+  if (lens.size() > round) {
+    std::nth_element(lens.begin(), lens.begin() + (round - 1), lens.end(), std::greater<uint32_t>());
+    thr = std::max<uint32_t>(thr, lens[round - 1]);
+  }
+  std::vector<std::pair<uint32_t, uint32_t>> sel;  // (length, slot)
+  for (size_t q = 0; q < slot_len.size(); ++q)
+    if (slot_len[q] >= thr) sel.push_back({slot_len[q], (uint32_t)q});
+  std::sort(sel.begin(), sel.end(), [](const std::pair<uint32_t, uint32_t>& a, const std::pair<uint32_t, uint32_t>& b) {
+    return a.first != b.first ? a.first > b.first : a.second < b.second;
+  });
+  std::vector<uint32_t> long_slots(sel.size());
+  for (size_t q = 0; q < sel.size(); ++q) long_slots[q] = sel[q].second;
+  const int n = (int)long_slots.size();
+  uint32_t* d_slots = (uint32_t*)c->ws.get(c, L.slot_list, (size_t)n * 4 + 16);
+  unsigned* d_ctr = (unsigned*)c->ws.get(c, L.slot_ctr, 64);
+  if (!d_slots || !d_ctr) return report_error(MVG_ERR_NOMEM, "workspace allocation failed");
+  MVG_CUDA_TRY(cudaMemcpyAsync(d_slots, long_slots.data(), (size_t)n * 4, cudaMemcpyHostToDevice, L.st));
+  MVG_CUDA_TRY(cudaMemsetAsync(d_ctr, 0, 4, L.st));
+  MVG_CUDA_TRY(cudaEventRecord(L.fork, L.st));
+  MVG_CUDA_TRY(cudaStreamWaitEvent(L.side, L.fork, 0));
+  const int grid = std::min(sms * (cap / kTbWarps), (n + kTbWarps - 1) / kTbWarps);
+  k_traceback_win<<<grid, kTbWarps * 32, kTbSmem, L.side>>>(in.oa, in.ob, d_order, d_tboff, d_slots, n, tb, d_edge,
+                                                            d_delta, d_half, d_accept, in.path_off, in.paths,
+                                                            in.path_len, c->d_err, rows, d_rows, in.env, d_ctr);
+  MVG_CUDA_TRY(cudaEventRecord(L.join, L.side));
+  c->launches++;
+  *long_path = (int)thr;
+  *forked = true;
+  return 0;
+}
+
+static int tb_long_join(const TbLanes& L, bool forked) {
+  if (forked) MVG_CUDA_TRY(cudaStreamWaitEvent(L.st, L.join, 0));
+  return 0;
+}
+
 // Runs the DP for the problems in `ids` (full, or banded with per-problem
 // delta/half on the device): LPT order, size-mixed waves that fit the
 // traceback arena, then traceback and path compaction per wave.
 static int run_dp(Ctx* c, const DpInputs& in, const std::vector<uint32_t>& ids, const std::vector<int64_t>& la,
                   const std::vector<int64_t>& lb, const int32_t* d_delta, const int32_t* d_half,
-                  const std::vector<int32_t>* h_delta, const std::vector<int32_t>* h_half, uint8_t* d_accept) {
+                  const std::vector<int32_t>* h_delta, const std::vector<int32_t>* h_half, uint8_t* d_accept,
+                  const TbLanes* lanes = nullptr) {
+  const TbLanes L = lanes ? *lanes : main_lanes(c);
   const int64_t nwork = (int64_t)ids.size();
   if (nwork == 0) return 0;
   const bool banded = d_delta != nullptr;
@@ -237,9 +319,14 @@ static int run_dp(Ctx* c, const DpInputs& in, const std::vector<uint32_t>& ids, 
     const bool many = (a + 32 * rows - 1) / (32 * rows) >= kCoopMinStrips;
     is_big[w] = many && (!banded || cells[w] >= (uint64_t)a * 8 * 32 * rows);
   }
+  // largest first, ties in input order: one sort of packed (cells, index) keys
   std::vector<uint32_t> idx(nwork);
-  std::iota(idx.begin(), idx.end(), 0u);
-  std::stable_sort(idx.begin(), idx.end(), [&](uint32_t x, uint32_t y) { return cells[x] > cells[y]; });
+  {
+    std::vector<std::pair<uint64_t, uint32_t>> key(nwork);
+    for (int64_t w = 0; w < nwork; ++w) key[w] = {~cells[w], (uint32_t)w};
+    std::sort(key.begin(), key.end());
+    for (int64_t w = 0; w < nwork; ++w) idx[w] = key[w].second;
+  }
 
   uint64_t arena = c->tb_arena;
   {
@@ -314,8 +401,8 @@ static int run_dp(Ctx* c, const DpInputs& in, const std::vector<uint32_t>& ids, 
   uint32_t* tb = (uint32_t*)ws.get(c, 18, arena_need);
   if (!rowbuf || !d_order || !d_tboff || !d_edge || !d_counter || !tb)
     return report_error(MVG_ERR_NOMEM, "workspace allocation failed");
-  MVG_CUDA_TRY(cudaMemcpyAsync(d_order, order.data(), (size_t)nwork * 4, cudaMemcpyHostToDevice, c->stream));
-  MVG_CUDA_TRY(cudaMemcpyAsync(d_tboff, tboff.data(), (size_t)nwork * 8, cudaMemcpyHostToDevice, c->stream));
+  MVG_CUDA_TRY(cudaMemcpyAsync(d_order, order.data(), (size_t)nwork * 4, cudaMemcpyHostToDevice, L.st));
+  MVG_CUDA_TRY(cudaMemcpyAsync(d_tboff, tboff.data(), (size_t)nwork * 8, cudaMemcpyHostToDevice, L.st));
   for (size_t wv = 0; wv + 1 < wave_begin.size(); ++wv) {
     const int64_t w0 = wave_begin[wv], w1 = wave_begin[wv + 1];
     DpJob J;
@@ -338,15 +425,24 @@ static int run_dp(Ctx* c, const DpInputs& in, const std::vector<uint32_t>& ids, 
     J.base_max = g_base_max;
     J.counter = d_counter;
     J.err = c->d_err;
-    MVG_CUDA_TRY(cudaMemsetAsync(d_counter, 0, 8, c->stream));
+    MVG_CUDA_TRY(cudaMemsetAsync(d_counter, 0, 8, L.st));
     stage_mark(c, banded ? "dp_banded" : "dp");
-    kern<<<grid, kDpThreads, 0, c->stream>>>(J);
+    kern<<<grid, kDpThreads, 0, L.st>>>(J);
     stage_mark(c, "traceback");
-    k_traceback<<<grid_for(J.nwork, 128), 128, 0, c->stream>>>(in.oa, in.ob, J.order, J.tb_off, J.nwork, tb, d_edge,
+    std::vector<uint32_t> slot_len(w1 - w0);
+    for (int64_t q = w0; q < w1; ++q)
+      slot_len[q - w0] = (uint32_t)(la[order[q]] + lb[order[q]]);
+    bool forked = false;
+    int long_path = INT_MAX;
+    int trc = tb_long_fork(c, L, in, slot_len, J.order, J.tb_off, tb, d_edge, d_delta, d_half, d_accept, rows,
+                           nullptr, &long_path, &forked);
+    if (trc) return trc;
+    k_traceback<<<grid_for(J.nwork, 128), 128, 0, L.st>>>(in.oa, in.ob, J.order, J.tb_off, J.nwork, tb, d_edge,
                                                                 d_delta, d_half, d_accept, in.path_off, in.paths,
-                                                                in.path_len, c->d_err, rows, in.env);
+                                                                in.path_len, c->d_err, rows, in.env, long_path);
+    if ((trc = tb_long_join(L, forked))) return trc;
     stage_mark(c, "path_compact");
-    k_path_compact<<<grid_for((int64_t)J.nwork * 32, 256), 256, 0, c->stream>>>(
+    k_path_compact<<<grid_for((int64_t)J.nwork * 32, 256), 256, 0, L.st>>>(
         in.oa, in.ob, J.order, J.nwork, d_accept, in.path_off, in.paths, in.path_len);
     c->launches += 3;
     MVG_CUDA_TRY(cudaGetLastError());
@@ -358,10 +454,10 @@ static int run_dp(Ctx* c, const DpInputs& in, const std::vector<uint32_t>& ids, 
 // height R of ids[w].  Slots are ordered by R, each class most expensive
 // first, and cut into waves that fit the traceback arena; per wave one
 // k_gapdp_ring<R> launch per class, then traceback and path compaction.
-static int run_ring(Ctx* c, const DpInputs& in, const std::vector<uint32_t>& ids, const std::vector<uint8_t>& rsel,
-                    const std::vector<int64_t>& la, const std::vector<int64_t>& lb, const std::vector<int32_t>& dv,
-                    const std::vector<int32_t>& hv, const int32_t* d_delta, const int32_t* d_half, uint8_t* d_accept,
-                    unsigned long long* d_cells) {
+static int run_ring(Ctx* c, const TbLanes& L, const DpInputs& in, const std::vector<uint32_t>& ids,
+                    const std::vector<uint8_t>& rsel, const std::vector<int64_t>& la, const std::vector<int64_t>& lb,
+                    const std::vector<int32_t>& dv, const std::vector<int32_t>& hv, const int32_t* d_delta,
+                    const int32_t* d_half, uint8_t* d_accept, unsigned long long* d_cells) {
   const int64_t nwork = (int64_t)ids.size();
   if (nwork == 0) return 0;
   std::vector<uint64_t> bytes(nwork), cost(nwork);
@@ -371,16 +467,20 @@ static int run_ring(Ctx* c, const DpInputs& in, const std::vector<uint32_t>& ids
     bytes[w] = (ring_tb_words(b) * 4 + 255) & ~255ull;
     cost[w] = (uint64_t)b.steps * (uint64_t)(rsel[w] * 18 + 50);
   }
+  // by group height, each class most expensive first, ties in input order
   std::vector<uint32_t> idx(nwork);
-  std::iota(idx.begin(), idx.end(), 0u);
-  std::sort(idx.begin(), idx.end(), [&](uint32_t x, uint32_t y) {
-    return rsel[x] != rsel[y] ? rsel[x] < rsel[y] : (cost[x] != cost[y] ? cost[x] > cost[y] : x < y);
-  });
+  {
+    std::vector<std::pair<uint64_t, uint32_t>> key(nwork);
+    for (int64_t w = 0; w < nwork; ++w)
+      key[w] = {((uint64_t)rsel[w] << 56) | ((~cost[w]) & ((1ull << 56) - 1)), (uint32_t)w};
+    std::sort(key.begin(), key.end());
+    for (int64_t w = 0; w < nwork; ++w) idx[w] = key[w].second;
+  }
   uint64_t arena = c->tb_arena;
   {
     size_t free_b = 0, total_b = 0;
     if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess) {
-      const uint64_t cap = (uint64_t)((c->ws.size[18] + free_b) * 0.6);
+      const uint64_t cap = (uint64_t)((c->ws.size[67] + free_b) * 0.6);
       if (arena > cap) arena = cap;
     }
   }
@@ -404,22 +504,21 @@ static int run_ring(Ctx* c, const DpInputs& in, const std::vector<uint32_t>& ids
   }
   wave_begin.push_back(nwork);
   Workspace& ws = c->ws;
-  uint32_t* d_order = (uint32_t*)ws.get(c, 11, (size_t)nwork * 4);
-  uint64_t* d_tboff = (uint64_t*)ws.get(c, 12, (size_t)nwork * 8);
+  uint32_t* d_order = (uint32_t*)ws.get(c, 64, (size_t)nwork * 4);
+  uint64_t* d_tboff = (uint64_t*)ws.get(c, 65, (size_t)nwork * 8);
   uint8_t* d_edge = (uint8_t*)ws.get(c, 13, la.size() + 16);
-  unsigned* d_counter = (unsigned*)ws.get(c, 14, 64);
+  unsigned* d_counter = (unsigned*)ws.get(c, 66, 64);
   uint8_t* d_rows = (uint8_t*)ws.get(c, 60, (size_t)nwork + 16);
-  uint32_t* tb = (uint32_t*)ws.get(c, 18, arena_need);
+  uint32_t* tb = (uint32_t*)ws.get(c, 67, arena_need);
   if (!d_order || !d_tboff || !d_edge || !d_counter || !d_rows || !tb)
     return report_error(MVG_ERR_NOMEM, "workspace allocation failed");
-  MVG_CUDA_TRY(cudaMemcpyAsync(d_order, order.data(), (size_t)nwork * 4, cudaMemcpyHostToDevice, c->stream));
-  MVG_CUDA_TRY(cudaMemcpyAsync(d_tboff, tboff.data(), (size_t)nwork * 8, cudaMemcpyHostToDevice, c->stream));
-  MVG_CUDA_TRY(cudaMemcpyAsync(d_rows, rows_of.data(), (size_t)nwork, cudaMemcpyHostToDevice, c->stream));
+  MVG_CUDA_TRY(cudaMemcpyAsync(d_order, order.data(), (size_t)nwork * 4, cudaMemcpyHostToDevice, L.st));
+  MVG_CUDA_TRY(cudaMemcpyAsync(d_tboff, tboff.data(), (size_t)nwork * 8, cudaMemcpyHostToDevice, L.st));
+  MVG_CUDA_TRY(cudaMemcpyAsync(d_rows, rows_of.data(), (size_t)nwork, cudaMemcpyHostToDevice, L.st));
   int dev_sms = 0;
   MVG_CUDA_TRY(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, c->device));
   for (size_t wv = 0; wv + 1 < wave_begin.size(); ++wv) {
     const int64_t w0 = wave_begin[wv], w1 = wave_begin[wv + 1];
-    stage_mark(c, "dp_ring");
     for (int64_t a = w0; a < w1;) {
       int64_t e = a;
       while (e < w1 && rows_of[e] == rows_of[a]) ++e;
@@ -448,18 +547,24 @@ static int run_ring(Ctx* c, const DpInputs& in, const std::vector<uint32_t>& ids
       J.base_max = g_base_max;
       J.counter = d_counter;
       J.cells = d_cells;
-      MVG_CUDA_TRY(cudaMemsetAsync(d_counter, 0, 4, c->stream));
-      kern<<<grid, kRingThreads, 0, c->stream>>>(J);
+      MVG_CUDA_TRY(cudaMemsetAsync(d_counter, 0, 4, L.st));
+      kern<<<grid, kRingThreads, 0, L.st>>>(J);
       c->launches++;
       a = e;
     }
-    stage_mark(c, "traceback");
     const int nw = (int)(w1 - w0);
-    k_traceback_ring<<<grid_for(nw, 128), 128, 0, c->stream>>>(
+    std::vector<uint32_t> slot_len(w1 - w0);
+    for (int64_t q = w0; q < w1; ++q) slot_len[q - w0] = (uint32_t)(la[order[q]] + lb[order[q]]);
+    bool forked = false;
+    int long_path = INT_MAX;
+    int trc = tb_long_fork(c, L, in, slot_len, d_order + w0, d_tboff + w0, tb, d_edge, d_delta, d_half, d_accept, 0,
+                           d_rows + w0, &long_path, &forked);
+    if (trc) return trc;
+    k_traceback_ring<<<grid_for(nw, 128), 128, 0, L.st>>>(
         in.oa, in.ob, d_order + w0, d_rows + w0, d_tboff + w0, nw, tb, d_edge, d_delta, d_half, d_accept,
-        in.path_off, in.paths, in.path_len, c->d_err);
-    stage_mark(c, "path_compact");
-    k_path_compact<<<grid_for((int64_t)nw * 32, 256), 256, 0, c->stream>>>(in.oa, in.ob, d_order + w0, nw, d_accept,
+        in.path_off, in.paths, in.path_len, c->d_err, long_path);
+    if ((trc = tb_long_join(L, forked))) return trc;
+    k_path_compact<<<grid_for((int64_t)nw * 32, 256), 256, 0, L.st>>>(in.oa, in.ob, d_order + w0, nw, d_accept,
                                                                             in.path_off, in.paths, in.path_len);
     c->launches += 2;
     MVG_CUDA_TRY(cudaGetLastError());
@@ -550,10 +655,11 @@ int gapdp_banded_dev(Ctx* c, const uint8_t* d_sa, const uint64_t* d_oa, const ui
   // little and may still fail its check: such problems are not banded.  They
   // run in the strip kernel's launch with a band that covers the whole matrix
   // (no exit cells, so the check always passes and the result is the full
-  // DP's), which spares a second full-DP pass for them.  Other bands run on
-  // the ring schedule with the smallest valid group height, or in the strip
-  // kernel when no height is valid (or the ring kernel is switched off).
-  static const int kRingRows[4] = {4, 8, 16, 32};
+  // DP's; short strips suit these mostly small problems better than the full
+  // DP's), which spares a second pass for them (status 2).  Other bands run
+  // on the ring schedule with the smallest valid group height, or in the
+  // strip kernel when no height is valid (or the ring kernel is switched off).
+  static const int kRingRows[4] = {4, 8, 16, 32};  // smallest first
   std::vector<uint32_t> ids, rids;
   std::vector<uint8_t> rsel;
   std::vector<uint8_t> whole(nprob, 0);
@@ -580,9 +686,17 @@ int gapdp_banded_dev(Ctx* c, const uint8_t* d_sa, const uint64_t* d_oa, const ui
       continue;
     }
     int rr = 0;
-    if (c->band_ring)
-      for (int q = 0; q < 4 && !rr; ++q)
-        if (ring_eligible(make_ring_band((int)la[p], (int)lb[p], dv[p], hv[p], kRingRows[q]))) rr = kRingRows[q];
+    if (c->band_ring) {
+      // the lane-reuse condition W <= 32 + 32*R*LB/LA decides most heights;
+      // only heights that pass it (with a column of slack) get the exact test
+      const double slope = (double)lb[p] / (double)la[p];
+      for (int q = 0; q < 4 && !rr; ++q) {
+        const int R = kRingRows[q];
+        const bool many = (la[p] + R - 1) / R > 32;
+        if (many && 2.0 * hv[p] + 2.0 + (R - 1) * slope > 32.0 + 32.0 * R * slope + 2.0) continue;
+        if (ring_eligible(make_ring_band((int)la[p], (int)lb[p], dv[p], hv[p], R))) rr = R;
+      }
+    }
     if (rr) {
       rids.push_back((uint32_t)p);
       rsel.push_back((uint8_t)rr);
@@ -604,14 +718,23 @@ int gapdp_banded_dev(Ctx* c, const uint8_t* d_sa, const uint64_t* d_oa, const ui
   MVG_CUDA_TRY(cudaMemsetAsync(c->d_err, 0, 4, c->stream));
   if ((rc = check_codes(c, d_sa, h_oa[nprob], d_sb, h_ob[nprob]))) return rc;
   stage_begin_call(c);
-  if (!ids.empty()) {
-    rc = run_dp(c, in, ids, la, lb, d_delta, d_half, &dv, &hv, d_accept);
-    if (rc) return rc;
-  }
+  // the ring-scheduled bands on the aux stream beside the strip kernel's
+  // problems on the main stream (their launches have separate tails)
+  const TbLanes ring_lanes{c->aux, c->aux2, c->fork2, c->join2, 68, 69};
+  const TbLanes strip_lanes{c->stream, c->aux3, c->fork3, c->join3, 57, 58};
   if (!rids.empty()) {
-    rc = run_ring(c, in, rids, rsel, la, lb, dv, hv, d_delta, d_half, d_accept, d_cells);
+    MVG_CUDA_TRY(cudaEventRecord(c->fork, c->stream));
+    MVG_CUDA_TRY(cudaStreamWaitEvent(c->aux, c->fork, 0));
+    rc = run_ring(c, ring_lanes, in, rids, rsel, la, lb, dv, hv, d_delta, d_half, d_accept, d_cells);
+    if (rc) return rc;
+    MVG_CUDA_TRY(cudaEventRecord(c->join, c->aux));
+  }
+  if (!ids.empty()) {
+    rc = run_dp(c, in, ids, la, lb, d_delta, d_half, &dv, &hv, d_accept, &strip_lanes);
     if (rc) return rc;
   }
+  if (!rids.empty()) MVG_CUDA_TRY(cudaStreamWaitEvent(c->stream, c->join, 0));
+  stage_mark(c, "banded_done");
   std::vector<uint8_t> acc(nprob);
   MVG_CUDA_TRY(cudaMemcpyAsync(acc.data(), d_accept, (size_t)nprob, cudaMemcpyDeviceToHost, c->stream));
   MVG_CUDA_TRY(cudaMemcpyAsync(c->h_scalars, d_cells, 8, cudaMemcpyDeviceToHost, c->stream));
@@ -621,7 +744,7 @@ int gapdp_banded_dev(Ctx* c, const uint8_t* d_sa, const uint64_t* d_oa, const ui
   for (int64_t p = 0; p < nprob; ++p) {
     if (whole[p]) {
       if (!acc[p]) return report_error(MVG_ERR_DEVICE, "whole-matrix band failed its check");
-      acc[p] = 2;  // not banded: the proposed band covered at least half the matrix
+      acc[p] = 2;  // not banded: the proposed band covered most of the matrix
     } else if (!acc[p]) {
       fallback.push_back((uint32_t)p);
       bc += (uint64_t)la[p] * (uint64_t)lb[p];

@@ -52,6 +52,7 @@ struct RingJob {
 };
 
 constexpr int kRingThreads = 128;
+constexpr int kRingA = 256;  // rows of A staged per warp (codes of the next groups to start)
 
 // One column segment of R rows, as dp_column, with the R traceback nibbles
 // returned in (R + 7) / 8 words (nibble r in word r / 8).
@@ -88,7 +89,7 @@ __device__ __forceinline__ void ring_column(DpLane<R>& L, int32_t upM, int32_t u
 }
 
 template <int R>
-__device__ void ring_solve(const RingJob& J, uint8_t* ringB, int w) {
+__device__ void ring_solve(const RingJob& J, uint8_t* ringB, uint8_t* ringA, int w) {
   constexpr int NW = (R + 7) / 8;
   const int lane = threadIdx.x & 31;
   const int src = (lane + 31) & 31;  // the ring's previous lane
@@ -100,7 +101,6 @@ __device__ void ring_solve(const RingJob& J, uint8_t* ringB, int w) {
   const RingBand b = make_ring_band(LA, LB, J.band_delta[p], J.band_half[p], R);
   const int G = b.G, W = b.W, lo0 = b.lo0;
   const int S = (int)b.steps;
-  uint32_t* tbs = J.tb + J.tb_off[w] / 4;
   const int32_t totA = warp_best_sum(A, 0, LA, J.base_max);
   const int32_t totB = warp_best_sum(B, 0, LB, J.base_max);
 
@@ -113,10 +113,11 @@ __device__ void ring_solve(const RingJob& J, uint8_t* ringB, int w) {
   int lo_next = f + shift;  // == lo0
   int lo_started = lo0;     // first column of the last group started
   int filled = lo0 - 1;     // ringB holds the B codes of columns (filled-128, filled]
+  int filledA = 0;          // ringA holds rows [filledA - kRingA, filledA) of A
 
   // this lane's group
-  int my_g = -1, my_lo = 0, my_end = INT_MIN, prev_hi = INT_MIN, next_lo = INT_MIN;
-  int32_t goA0 = kGap, pa_start = 0, pa_end = 0, pb = 0;
+  int my_g = -1, my_end = INT_MIN, prev_hi = INT_MIN, next_lo = INT_MIN, end_col = INT_MIN, rexit_col = INT_MIN;
+  int32_t goA0 = kGap, topI = kNeg, pa_end = 0, pb = 0;
   DpLane<R> L;
 #pragma unroll
   for (int r = 0; r < R; ++r) {
@@ -130,14 +131,26 @@ __device__ void ring_solve(const RingJob& J, uint8_t* ringB, int w) {
   int32_t rawM = kNeg, rawD = kNeg, rawI = kNeg;     // what the previous lane published one step ago
   int32_t bound = kNeg, endsc = kNeg;
   int end_lane_edge = 0;
-  unsigned long long kept = 0;
+  uint32_t kept = 0;
   uint32_t acc = 0;
+  uint32_t* tbp = J.tb + J.tb_off[w] / 4 + lane;
 
   for (int s = 0; s < S; ++s) {
     const int32_t rM = __shfl_sync(0xffffffffu, pubM, src);
     const int32_t rD = __shfl_sync(0xffffffffu, pubD, src);
     const int32_t rI = __shfl_sync(0xffffffffu, pubI, src);
     if (gnext < G && s - gnext == lo_next - lo0) {
+      // A codes of the rows about to start, staged 128 rows at a time
+      if (filledA < (gnext + 1) * R) {
+        __syncwarp();
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const int i = filledA + k * 32 + lane;
+          ringA[i & (kRingA - 1)] = i < LA ? A[i] : 0;
+        }
+        __syncwarp();
+        filledA += 128;
+      }
       // group gnext starts on lane gnext % 32; its predecessor (previous
       // lane) passes the prefix sums it carries
       const int32_t chain_pb = __shfl_sync(0xffffffffu, pb, src);
@@ -152,25 +165,36 @@ __device__ void ring_solve(const RingJob& J, uint8_t* ringB, int w) {
       }
       const int lo_after = f + shift;
       if (lane == (g & 31)) {
+        const int my_lo = lo_next;
         my_g = g;
-        my_lo = lo_next;
-        my_end = lo_next + W - 1;
+        my_end = my_lo + W - 1;
         prev_hi = g == 0 ? INT_MIN : lo_prev + W - 1;
         next_lo = g + 1 < G ? lo_after : INT_MIN;
+        end_col = g == G - 1 ? LB : INT_MIN;
+        rexit_col = my_end < LB ? my_end : INT_MIN;
+        const int rows_here = LA - g * R < R ? LA - g * R : R;
+        // cells of this group inside the matrix
+        const int c0 = my_lo < 1 ? 1 : my_lo, c1 = my_end < LB ? my_end : LB;
+        if (c1 >= c0) kept += (uint32_t)rows_here * (uint32_t)(c1 - c0 + 1);
         goA0 = g == 0 ? 0 : kGap;
-        pa_start = g == 0 ? 0 : chain_pa;
-        int32_t pa = pa_start;
+        topI = g == 0 ? 0 : kNeg;
+        int32_t pa = g == 0 ? 0 : chain_pa;
+        const uint32_t* ra = reinterpret_cast<const uint32_t*>(ringA);
 #pragma unroll
-        for (int r = 0; r < R; ++r) {
-          const int i = g * R + r + 1;
-          const uint32_t code = i <= LA ? A[i - 1] : 0u;
-          L.arow[r] = c_score_rows[code & 3u];
-          if (i <= LA) pa += best_of(J.base_max, code);
+        for (int q = 0; q < R / 4; ++q) {
+          const uint32_t c4 = ra[((g * R) >> 2) + q & (kRingA / 4 - 1)];
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
+            const int r = 4 * q + k;
+            const uint32_t code = (c4 >> (8 * k)) & 3u;
+            L.arow[r] = c_score_rows[code];
+            if (r < rows_here) pa += best_of(J.base_max, code);
+          }
         }
         pa_end = pa;
         // prefix of B's best scores before column my_lo: the predecessor
         // has just added column my_lo
-        pb = (g == 0 || my_lo <= 0) ? 0 : chain_pb - best_of(J.base_max, B[my_lo - 1]);
+        pb = (g == 0 || my_lo <= 0) ? 0 : chain_pb - best_of(J.base_max, ringB[my_lo & 127]);
         const int32_t leftD = my_lo - 1 == 0 ? 0 : kNeg;  // column 0 is (-inf, 0, -inf) below row 0
 #pragma unroll
         for (int r = 0; r < R; ++r) {
@@ -203,8 +227,7 @@ __device__ void ring_solve(const RingJob& J, uint8_t* ringB, int w) {
       ++gnext;
     }
     // B codes of the running groups' columns: up to s - (gnext - 32) + lo0
-    const int jmax = s + 32 - gnext + lo0;
-    if (filled < jmax) {
+    if (filled < s + 32 - gnext + lo0) {
       const int x = filled + 1 + lane;
       __syncwarp();
       ringB[x & 127] = (x >= 1 && x <= LB) ? B[x - 1] : 0;
@@ -212,18 +235,16 @@ __device__ void ring_solve(const RingJob& J, uint8_t* ringB, int w) {
       filled += 32;
     }
     const int j = s - my_g + lo0;
-    const bool active = my_g >= 0 && j <= my_end;
-    // the cell above: the predecessor's bottom row while inside its range,
-    // row 0 for group 0
+    // the cell above: the predecessor's bottom row while inside its range;
+    // for group 0 row 0 (I = 0 right of column 0; M(0,0) is set below)
     const bool from_ring = j <= prev_hi;
-    const bool top = my_g == 0;
-    const int32_t aM = from_ring ? rM : (top && j == 0 ? 0 : kNeg);
+    int32_t aM = from_ring ? rM : kNeg;
     const int32_t aD = from_ring ? rD : kNeg;
-    const int32_t aI = from_ring ? rI : (top && j >= 1 ? 0 : kNeg);
+    int32_t aI = from_ring ? rI : topI;
     uint32_t nw[NW];
 #pragma unroll
     for (int q = 0; q < NW; ++q) nw[q] = 0;
-    if (active && j >= 1 && j <= LB) {
+    if (j <= my_end && j >= 1 && j <= LB && my_g >= 0) {
       const uint32_t bsel = (uint32_t)ringB[j & 127] | 0x4440u;
       ring_column<R>(L, aM, aD, dgM, dgD, dgI, bsel, j == 1 ? 0 : kGap, goA0, nw);
       if (LA == 1 && j == 1) {
@@ -235,14 +256,12 @@ __device__ void ring_solve(const RingJob& J, uint8_t* ringB, int w) {
       pubM = L.lM[R - 1];
       pubD = L.lD[R - 1];
       pubI = L.lI[R - 1];
-      pb += best_of(J.base_max, bsel);  // prefix over B[0..j)
-      const int rows = LA - my_g * R;
-      kept += (unsigned long long)(rows < R ? rows : R);
+      pb += (int32_t)__byte_perm(J.base_max, 0u, bsel) - kScoreBias;  // prefix over B[0..j)
       if (j < next_lo) {  // bottom-row exit
         const int32_t best = max(pubM, max(pubD, pubI));
         bound = max(bound, best + min(totA - pa_end, totB - pb));
       }
-      if (my_g == G - 1 && j == LB) {  // the end cell (LA, LB)
+      if (j == end_col) {  // the end cell (LA, LB)
         const int er = LA - 1 - my_g * R;
         int32_t eM = kNeg, eD = kNeg, eI = kNeg;
 #pragma unroll
@@ -265,19 +284,27 @@ __device__ void ring_solve(const RingJob& J, uint8_t* ringB, int w) {
         endsc = sc;
         end_lane_edge = e;
       }
-      if (j == my_end && j < LB) {  // right-edge exits of every row
-        int32_t run = pa_start;
+      if (j == rexit_col) {  // right-edge exits of every row
+        // the rows' best scores are the largest bytes of their score rows;
+        // A's prefix before the group is pa_end minus their sum
+        const int rows_here = LA - my_g * R < R ? LA - my_g * R : R;
+        int32_t run = pa_end;
 #pragma unroll
         for (int r = 0; r < R; ++r) {
-          const int i = my_g * R + r + 1;
-          if (i <= LA) {
-            run += best_of(J.base_max, A[i - 1]);
+          const uint32_t h = __vmaxu4(L.arow[r], L.arow[r] >> 16);
+          if (r < rows_here) run -= (int32_t)max(h & 0xffu, (h >> 8) & 0xffu) - kScoreBias;
+        }
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+          if (r < rows_here) {
+            const uint32_t h = __vmaxu4(L.arow[r], L.arow[r] >> 16);
+            run += (int32_t)max(h & 0xffu, (h >> 8) & 0xffu) - kScoreBias;
             const int32_t best = max(L.lM[r], max(L.lD[r], L.lI[r]));
             bound = max(bound, best + min(totA - run, totB - pb));
           }
         }
       }
-    } else if (active && j <= 0) {
+    } else if (j <= my_end && j <= 0 && my_g >= 0) {
       // the left boundary column (D = 0 below row 0) or outside the matrix
       const int32_t d0 = j == 0 ? 0 : kNeg;
 #pragma unroll
@@ -289,6 +316,10 @@ __device__ void ring_solve(const RingJob& J, uint8_t* ringB, int w) {
       pubM = kNeg;
       pubD = d0;
       pubI = kNeg;
+      if (my_g == 0 && j == 0) {  // cell (0, 0)
+        aM = 0;
+        aI = kNeg;
+      }
     } else {
       pubM = kNeg;
       pubD = kNeg;
@@ -298,12 +329,14 @@ __device__ void ring_solve(const RingJob& J, uint8_t* ringB, int w) {
       constexpr int kPer = 8 / R;
       acc |= nw[0] << (4 * R * (s % kPer));
       if ((s % kPer) == kPer - 1 || s == S - 1) {
-        tbs[(int64_t)(s / kPer) * 32 + lane] = acc;
+        *tbp = acc;
+        tbp += 32;
         acc = 0;
       }
     } else {
 #pragma unroll
-      for (int q = 0; q < NW; ++q) tbs[((int64_t)s * NW + q) * 32 + lane] = nw[q];
+      for (int q = 0; q < NW; ++q) tbp[q * 32] = nw[q];
+      tbp += NW * 32;
     }
     dgM = aM;
     dgD = aD;
@@ -324,10 +357,11 @@ __device__ void ring_solve(const RingJob& J, uint8_t* ringB, int w) {
     if (hi0 < LB) bound = max(bound, min(totA, totB - pb0));
     if (last_col0 < LA) bound = max(bound, min(totA - pa0, totB));
   }
+  unsigned long long kept64 = kept;
 #pragma unroll
   for (int d = 16; d > 0; d >>= 1) {
     bound = max(bound, __shfl_xor_sync(0xffffffffu, bound, d));
-    kept += __shfl_xor_sync(0xffffffffu, kept, d);
+    kept64 += __shfl_xor_sync(0xffffffffu, kept64, d);
   }
   const int end_lane = (G - 1) & 31;
   const int32_t sc = __shfl_sync(0xffffffffu, endsc, end_lane);
@@ -337,13 +371,14 @@ __device__ void ring_solve(const RingJob& J, uint8_t* ringB, int w) {
   }
   if (lane == 0) {
     J.accept[p] = sc > bound ? 1 : 0;
-    if (J.cells) atomicAdd(J.cells, kept);
+    if (J.cells) atomicAdd(J.cells, kept64);
   }
 }
 
 template <int R>
 __global__ void __launch_bounds__(kRingThreads) k_gapdp_ring(RingJob J) {
   __shared__ uint8_t ringB[kRingThreads / 32][128];
+  __shared__ __align__(16) uint8_t ringA[kRingThreads / 32][kRingA];
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
   for (;;) {
@@ -351,7 +386,7 @@ __global__ void __launch_bounds__(kRingThreads) k_gapdp_ring(RingJob J) {
     if (lane == 0) w = (int)atomicAdd(J.counter, 1u);
     w = __shfl_sync(0xffffffffu, w, 0);
     if (w >= J.nwork) break;
-    ring_solve<R>(J, ringB[wib], w);
+    ring_solve<R>(J, ringB[wib], ringA[wib], w);
   }
 }
 
@@ -364,11 +399,12 @@ __global__ void k_traceback_ring(const uint64_t* __restrict__ oa, const uint64_t
                                  const uint8_t* __restrict__ end_edge, const int32_t* __restrict__ band_delta,
                                  const int32_t* __restrict__ band_half, const uint8_t* __restrict__ accept,
                                  const uint64_t* __restrict__ path_off, char* __restrict__ paths,
-                                 int64_t* __restrict__ path_len, uint32_t* err) {
+                                 int64_t* __restrict__ path_len, uint32_t* err, int long_path) {
   for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < nwork; w += gridDim.x * blockDim.x) {
     const uint32_t p = order[w];
     if (!accept[p]) continue;
     const int LA = (int)(oa[p + 1] - oa[p]), LB = (int)(ob[p + 1] - ob[p]);
+    if (LA + LB >= long_path) continue;  // k_traceback_win walks it
     const int R = rows_of[w];
     const RingBand b = make_ring_band(LA, LB, band_delta[p], band_half[p], R);
     const uint32_t* T = tb + tb_off[w] / 4;

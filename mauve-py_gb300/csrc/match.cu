@@ -7,11 +7,13 @@
 // maximal spaced-seed match and inserts it in sorted position.  Only seeds
 // in the same bucket ever interact, so on the GPU:
 //
-//   k_unique_flags / k_compact_unique   per genome: keys unique under the
-//                                       seed mask (strand bit ignored)
-//   k_join                               merge-join of the two unique lists:
-//                                       the seed pairs, in ascending key
-//                                       order = the reference's hash order
+//   pair_sort (seeds.cu)                 both genomes' seed keys in one
+//                                       stable radix sort, a genome bit
+//                                       below the SML key
+//   k_pair_flags                         seeds unique in each genome (strand
+//                                       ignored): runs of two, one per
+//                                       genome, in ascending seed order =
+//                                       the reference's hash order
 //   k_hash_pairs                         SetDirection + CalculateOffset +
 //                                       bucket id per pair
 //   stable radix sort by bucket          keeps key order inside a bucket
@@ -48,77 +50,43 @@ struct MatchCtx {
 
 // ------------------------------------------------------------------ join
 
+// Both genomes' seeds sorted in one array by (seed bits, strand, genome).  A
+// seed unique in each genome (counted once in each, strand ignored:
+// LM/PairwiseMatchFinder.cpp:37-71 over LM/MatchFinder.cpp:172-340) is a run
+// of equal seed bits with exactly two members, one per genome; runs come in
+// ascending seed order, the reference's enumeration order.
 template <typename K>
-__global__ void k_unique_flags(const K* __restrict__ keys, int64_t n, uint32_t* __restrict__ flag) {
+__global__ void k_pair_flags(const K* __restrict__ keys, int64_t n, uint32_t* __restrict__ flag) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    uint64_t cur = (uint64_t)keys[i] >> 1;
-    bool u = true;
-    if (i > 0 && ((uint64_t)keys[i - 1] >> 1) == cur) u = false;
-    if (i + 1 < n && ((uint64_t)keys[i + 1] >> 1) == cur) u = false;
-    flag[i] = u;
+    const uint64_t k0 = (uint64_t)keys[i], cur = k0 >> 2;
+    bool f = false;
+    if ((i == 0 || ((uint64_t)keys[i - 1] >> 2) != cur) && i + 1 < n) {
+      const uint64_t k1 = (uint64_t)keys[i + 1];
+      f = (k1 >> 2) == cur && ((k0 ^ k1) & 1ull) && (i + 2 == n || ((uint64_t)keys[i + 2] >> 2) != cur);
+    }
+    flag[i] = f;
   }
 }
 
+// One pair per flagged run: HashMatch (LM/MemHash.cpp:167-187) ->
+// SetDirection (:189-207) -> CalculateOffset (LM/MatchHashEntry.cpp:141-162)
+// -> bucket.
 template <typename K>
-__global__ void k_compact_unique(const K* __restrict__ keys, const uint32_t* __restrict__ pos, int64_t n,
-                                 const uint32_t* __restrict__ flag, const uint32_t* __restrict__ idx,
-                                 uint64_t* __restrict__ ukey, uint32_t* __restrict__ upos) {
+__global__ void k_hash_pairs(const K* __restrict__ keys, const uint32_t* __restrict__ pos, int64_t n,
+                             const uint32_t* __restrict__ flag, const uint32_t* __restrict__ idx, int L,
+                             Mhe* __restrict__ mhe, uint32_t* __restrict__ bucket, uint32_t* __restrict__ order) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    if (flag[i]) {
-      uint32_t j = idx[i];
-      ukey[j] = (uint64_t)keys[i];  // seed bits << 1 | strand
-      upos[j] = pos[i];
-    }
-  }
-}
-
-// For each unique key of A, binary search the unique keys of B.
-__global__ void k_join(const uint64_t* __restrict__ ka, const uint32_t* __restrict__ nua_p, const uint64_t* __restrict__ kb,
-                       const uint32_t* __restrict__ nub_p, uint32_t* __restrict__ hit, int64_t cap_a) {
-  const int64_t na = *nua_p, nb = *nub_p;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < cap_a; i += (int64_t)gridDim.x * blockDim.x) {
-    uint32_t h = 0xffffffffu;
-    if (i < na) {
-      uint64_t key = ka[i] >> 1;
-      int64_t lo = 0, len = nb;
-      while (len > 0) {
-        int64_t half = len >> 1;
-        if ((kb[lo + half] >> 1) < key) {
-          lo = lo + half + 1;
-          len -= half + 1;
-        } else {
-          len = half;
-        }
-      }
-      if (lo < nb && (kb[lo] >> 1) == key) h = (uint32_t)lo;
-    }
-    hit[i] = h;
-  }
-}
-
-__global__ void k_hit_flags(const uint32_t* __restrict__ hit, int64_t n, uint32_t* __restrict__ flag) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    flag[i] = hit[i] != 0xffffffffu;
-}
-
-// One pair per hit: HashMatch (LM/MemHash.cpp:167-187) -> SetDirection
-// (:189-207) -> CalculateOffset (LM/MatchHashEntry.cpp:141-162) -> bucket.
-__global__ void k_hash_pairs(const uint64_t* __restrict__ ka, const uint32_t* __restrict__ pa, const uint64_t* __restrict__ kb,
-                             const uint32_t* __restrict__ pb, const uint32_t* __restrict__ hit,
-                             const uint32_t* __restrict__ flag, const uint32_t* __restrict__ idx, int64_t cap_a,
-                             const uint32_t* __restrict__ nua_p, int L, Mhe* __restrict__ mhe,
-                             uint32_t* __restrict__ bucket, uint32_t* __restrict__ order) {
-  const int64_t na = *nua_p;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < na && i < cap_a;
-       i += (int64_t)gridDim.x * blockDim.x) {
     if (!flag[i]) continue;
-    const uint32_t j = idx[i], h = hit[i];
+    const uint64_t k0 = (uint64_t)keys[i], k1 = (uint64_t)keys[i + 1];
+    const bool a_first = (k0 & 1ull) == 0;
+    const uint64_t ka = a_first ? k0 : k1, kb = a_first ? k1 : k0;
+    const uint32_t j = idx[i];
     Mhe m;
-    m.s0 = (int64_t)pa[i] + 1;
-    m.s1 = (int64_t)pb[h] + 1;
+    m.s0 = (int64_t)(a_first ? pos[i] : pos[i + 1]) + 1;
+    m.s1 = (int64_t)(a_first ? pos[i + 1] : pos[i]) + 1;
     m.len = L;
-    const bool ref_forward = !(ka[i] & 1ull);
-    if (ref_forward == (bool)(kb[h] & 1ull)) m.s1 = -m.s1;
+    const bool ref_forward = !((ka >> 1) & 1ull);
+    if (ref_forward == (bool)((kb >> 1) & 1ull)) m.s1 = -m.s1;
     m.off = m.s1 - m.s0;
     if (m.s1 < 0) m.off -= m.len;
     const int64_t t = kTableSize;
@@ -785,28 +753,6 @@ __global__ void k_emit(const Mhe* __restrict__ ent, const uint32_t* __restrict__
   }
 }
 
-template <typename K>
-static int unique_list(Ctx* c, const SmlKeys& sk, int slot, uint64_t** ukey, uint32_t** upos, uint32_t** d_count) {
-  const int64_t n = (int64_t)sk.count;
-  Workspace& ws = c->ws;
-  uint32_t* flag = (uint32_t*)ws.get(c, slot + 0, (n + 1) * sizeof(uint32_t));
-  uint32_t* idx = (uint32_t*)ws.get(c, slot + 1, (n + 1) * sizeof(uint32_t));
-  uint32_t* scr = (uint32_t*)ws.get(c, slot + 2, scan_scratch_words(n + 1) * sizeof(uint32_t) + 64);
-  *ukey = (uint64_t*)ws.get(c, slot + 3, (n + 1) * sizeof(uint64_t));
-  *upos = (uint32_t*)ws.get(c, slot + 4, (n + 1) * sizeof(uint32_t));
-  if (!flag || !idx || !scr || !*ukey || !*upos) return report_error(MVG_ERR_NOMEM, "workspace allocation failed");
-  *d_count = scr + scan_scratch_words(n + 1);
-  if (n == 0) {
-    MVG_CUDA_TRY(cudaMemsetAsync(*d_count, 0, sizeof(uint32_t), c->stream));
-    return 0;
-  }
-  k_unique_flags<K><<<grid_for(n, 256), 256, 0, c->stream>>>((const K*)sk.keys, n, flag);
-  exclusive_scan(flag, idx, n, scr, *d_count, c->stream, &c->launches);
-  k_compact_unique<K><<<grid_for(n, 256), 256, 0, c->stream>>>((const K*)sk.keys, sk.pos, n, flag, idx, *ukey, *upos);
-  c->launches += 2;
-  return 0;
-}
-
 int pairwise_matches_dev(Ctx* c, const uint8_t* d_a, uint64_t na, const uint8_t* d_b, uint64_t nb, uint64_t seed,
                          int64_t* d_out, uint64_t cap, uint64_t* count) {
   const SeedDesc s = make_seed_desc(seed);
@@ -827,32 +773,22 @@ int pairwise_matches_dev(Ctx* c, const uint8_t* d_a, uint64_t na, const uint8_t*
   const uint64_t ca = na >= (uint64_t)s.L ? na - s.L + 1 : 0;
   const uint64_t cb = nb >= (uint64_t)s.L ? nb - s.L + 1 : 0;
   if (ca == 0 || cb == 0) return check_device_error(c);
-  SmlKeys ska, skb;
+  SmlKeys sk;
   stage_mark(c, "sml_sort");
-  if ((rc = sml_sort(c, ga, ca, s, nullptr, nullptr, &ska, 0))) return rc;
-  if ((rc = sml_sort(c, gb, cb, s, nullptr, nullptr, &skb, 52))) return rc;
+  if ((rc = pair_sort(c, ga, ca, gb, cb, s, &sk))) return rc;
   stage_mark(c, "unique_join");
-  uint64_t *uka, *ukb;
-  uint32_t *upa, *upb, *nua, *nub;
-  if (ska.wide) {
-    if ((rc = unique_list<uint64_t>(c, ska, 24, &uka, &upa, &nua))) return rc;
-    if ((rc = unique_list<uint64_t>(c, skb, 29, &ukb, &upb, &nub))) return rc;
-  } else {
-    if ((rc = unique_list<uint32_t>(c, ska, 24, &uka, &upa, &nua))) return rc;
-    if ((rc = unique_list<uint32_t>(c, skb, 29, &ukb, &upb, &nub))) return rc;
-  }
-  // join: capacity = unique count of A <= ca
-  const int64_t capa = (int64_t)ca;
-  uint32_t* hit = (uint32_t*)ws.get(c, 34, (capa + 1) * 4);
-  uint32_t* hflag = (uint32_t*)ws.get(c, 35, (capa + 1) * 4);
-  uint32_t* hidx = (uint32_t*)ws.get(c, 36, (capa + 1) * 4);
-  uint32_t* hscr = (uint32_t*)ws.get(c, 37, scan_scratch_words(capa + 1) * 4 + 64);
-  if (!hit || !hflag || !hidx || !hscr) return report_error(MVG_ERR_NOMEM, "workspace allocation failed");
-  uint32_t* d_npairs = hscr + scan_scratch_words(capa + 1);
-  k_join<<<grid_for(capa, 256), 256, 0, c->stream>>>(uka, nua, ukb, nub, hit, capa);
-  k_hit_flags<<<grid_for(capa, 256), 256, 0, c->stream>>>(hit, capa, hflag);
-  c->launches += 2;
-  exclusive_scan(hflag, hidx, capa, hscr, d_npairs, c->stream, &c->launches);
+  const int64_t nk = (int64_t)sk.count;
+  uint32_t* pflag = (uint32_t*)ws.get(c, 35, (nk + 1) * 4);
+  uint32_t* pidx = (uint32_t*)ws.get(c, 36, (nk + 1) * 4);
+  uint32_t* pscr = (uint32_t*)ws.get(c, 37, scan_scratch_words(nk + 1) * 4 + 64);
+  if (!pflag || !pidx || !pscr) return report_error(MVG_ERR_NOMEM, "workspace allocation failed");
+  uint32_t* d_npairs = pscr + scan_scratch_words(nk + 1);
+  if (sk.wide)
+    k_pair_flags<uint64_t><<<grid_for(nk, 256), 256, 0, c->stream>>>((const uint64_t*)sk.keys, nk, pflag);
+  else
+    k_pair_flags<uint32_t><<<grid_for(nk, 256), 256, 0, c->stream>>>((const uint32_t*)sk.keys, nk, pflag);
+  c->launches++;
+  exclusive_scan(pflag, pidx, nk, pscr, d_npairs, c->stream, &c->launches);
   MVG_CUDA_TRY(cudaMemcpyAsync(c->h_scalars, d_npairs, 4, cudaMemcpyDeviceToHost, c->stream));
   MVG_CUDA_TRY(cudaStreamSynchronize(c->stream));
   const int64_t npairs = (int64_t)(uint32_t)c->h_scalars[0];
@@ -886,8 +822,12 @@ int pairwise_matches_dev(Ctx* c, const uint8_t* d_a, uint64_t na, const uint8_t*
   unsigned long long* d_coll = (unsigned long long*)(((uintptr_t)(tot + 4) + 7) & ~(uintptr_t)7);
 
   stage_mark(c, "hash_bucket_sort");
-  k_hash_pairs<<<grid_for(capa, 256), 256, 0, c->stream>>>(uka, upa, ukb, upb, hit, hflag, hidx, capa, nua, s.L, mhe,
-                                                            bk0, or0);
+  if (sk.wide)
+    k_hash_pairs<uint64_t><<<grid_for(nk, 256), 256, 0, c->stream>>>((const uint64_t*)sk.keys, sk.pos, nk, pflag,
+                                                                      pidx, s.L, mhe, bk0, or0);
+  else
+    k_hash_pairs<uint32_t><<<grid_for(nk, 256), 256, 0, c->stream>>>((const uint32_t*)sk.keys, sk.pos, nk, pflag,
+                                                                      pidx, s.L, mhe, bk0, or0);
   c->launches++;
   int which = sort_pairs<uint32_t>(bk0, or0, bk1, or1, npairs, 16, sscr, c->stream, &c->launches, c->d_err);
   uint32_t* sorted_pair = which ? or1 : or0;

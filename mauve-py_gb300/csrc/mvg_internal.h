@@ -31,6 +31,8 @@ struct Ctx {
   cudaStream_t stream = nullptr;
   cudaStream_t aux = nullptr;       // second stream for work that runs beside the main stream's
   cudaEvent_t fork = nullptr, join = nullptr;
+  cudaStream_t aux2 = nullptr, aux3 = nullptr;  // side streams of work already on two streams
+  cudaEvent_t fork2 = nullptr, join2 = nullptr, fork3 = nullptr, join3 = nullptr;
   uint32_t* d_err = nullptr;     // device error word
   uint32_t* h_err = nullptr;     // pinned mirror
   uint64_t* h_scalars = nullptr; // pinned scalars for small device->host reads
@@ -61,9 +63,9 @@ inline void stage_mark(Ctx* c, const char* name) {
 inline void stage_begin_call(Ctx* c) { c->nstage = -1; }
 inline void stage_end(Ctx* c) { stage_mark(c, "end"); }
 
-// Sorted keys of one genome kept on the device for the join.
+// Sorted keys kept on the device for the join.
 struct SmlKeys {
-  const void* keys = nullptr;  // uint32 or uint64 compact keys: (seed bits << 1) | strand
+  const void* keys = nullptr;  // uint32 or uint64 compact keys: (seed bits << 1) | strand [, genome bit]
   const uint32_t* pos = nullptr;
   bool wide = false;
   uint64_t count = 0;
@@ -76,6 +78,9 @@ int grid_for(uint64_t n, int threads);
 int pack_sequence(Ctx* c, const uint8_t* d_seq, uint64_t n, uint32_t* d_packed);
 int sml_sort(Ctx* c, const uint32_t* d_packed, uint64_t count, const SeedDesc& s, uint32_t* d_pos_out,
              uint64_t* d_mer_out, SmlKeys* keep, int slot_base);
+// Both genomes' keys ((seed bits, strand, genome) with A = 0) sorted in one array.
+int pair_sort(Ctx* c, const uint32_t* ga, uint64_t ca, const uint32_t* gb, uint64_t cb, const SeedDesc& s,
+              SmlKeys* out);
 int check_device_error(Ctx* c);
 size_t sml_key_bytes(const SeedDesc& s);
 int sml_build_into(const uint8_t* d_seq, uint64_t n, uint64_t count, const SeedDesc& s, uint32_t* packed, void* k0,

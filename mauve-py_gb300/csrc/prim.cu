@@ -77,4 +77,30 @@ __global__ void __launch_bounds__(256) k_os_scan(uint32_t* __restrict__ ghist) {
   g[threadIdx.x] = ex;
 }
 
+// Block d: offsets[d][t] = gstart[d] + counts[d][0] + ... + counts[d][t-1].
+__global__ void __launch_bounds__(256) k_rts_rowscan(uint32_t* __restrict__ counts, int64_t ntiles,
+                                                     const uint32_t* __restrict__ gstart) {
+  uint32_t* row = counts + (int64_t)blockIdx.x * ntiles;
+  __shared__ uint32_t tot;
+  uint32_t carry = gstart[blockIdx.x];
+  for (int64_t c = 0; c < ntiles; c += 256 * 8) {
+    const int64_t i0 = c + (int64_t)threadIdx.x * 8;
+    uint32_t v[8];
+    uint32_t sum = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      v[k] = i0 + k < ntiles ? row[i0 + k] : 0u;
+      sum += v[k];
+    }
+    uint32_t run = carry + block_excl_scan256(sum, &tot);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      if (i0 + k < ntiles) row[i0 + k] = run;
+      run += v[k];
+    }
+    carry += tot;
+    __syncthreads();
+  }
+}
+
 }  // namespace mvg

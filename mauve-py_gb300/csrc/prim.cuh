@@ -234,7 +234,7 @@ __global__ void __launch_bounds__(256) k_os_hist(const K* __restrict__ keys, int
 __global__ void k_os_scan(uint32_t* __restrict__ ghist);
 
 template <typename K>
-__global__ void __launch_bounds__(os::kThreads) k_os_pass(const K* __restrict__ kin, const uint32_t* __restrict__ vin,
+__global__ void __launch_bounds__(os::kThreads, sizeof(K) == 4 ? 4 : 3) k_os_pass(const K* __restrict__ kin, const uint32_t* __restrict__ vin,
                                                          K* __restrict__ kout, uint32_t* __restrict__ vout, int64_t n,
                                                          int shift, const uint32_t* __restrict__ gstart,
                                                          uint32_t* state, uint32_t* tile_ctr, uint32_t* err) {
@@ -295,9 +295,18 @@ __global__ void __launch_bounds__(os::kThreads) k_os_pass(const K* __restrict__ 
   // published is re-read, bounded)
   uint32_t* st = state + tile * 256 + tid;
   *(volatile uint32_t*)st = (tile == 0 ? kPre : kAgg) | mine;
-  constexpr int kWin = 16;
+  constexpr int kWin = 8;
   uint32_t excl = 0;
-  for (int64_t t = tile - 1; t >= 0; t -= kWin) {
+  int64_t t0 = tile - 1;
+  if (t0 >= 0) {
+    // usually the previous tile has its inclusive prefix out already
+    const uint32_t x = *(const volatile uint32_t*)(state + t0 * 256 + tid);
+    if (x & kPre) {
+      excl = x & kVal;
+      t0 = -1;
+    }
+  }
+  for (int64_t t = t0; t >= 0; t -= kWin) {
     uint32_t v[kWin];
 #pragma unroll
     for (int q = 0; q < kWin; ++q) v[q] = t - q >= 0 ? *(const volatile uint32_t*)(state + (t - q) * 256 + tid) : kPre;
@@ -383,18 +392,173 @@ int onesweep_sort_pairs(K* keys, uint32_t* vals, K* keys_alt, uint32_t* vals_alt
   return which;
 }
 
-// The sort the workspace paths use: one-sweep below 2^30 elements, the
-// three-kernel passes above.  scratch: sort_scratch_words(n, nbits) words.
+// ------------------------------------- reduce-then-scan radix sort
+//
+// The same stable LSD result again, three kernels per 8-bit digit and no
+// waits between tiles: every tile's digit counts first (k_rts_count, one
+// read of the keys), then one block per digit turns its row of tile counts
+// into output offsets (k_rts_rowscan, starting at the digit's global start
+// from k_os_hist), then each tile ranks its keys stably in shared memory
+// and writes them out digit run by digit run (k_rts_scatter).  Compared with
+// one sweep it reads the keys once more per pass but never serialises
+// tiles on their predecessors' prefixes, which with thousands of tiles in
+// flight is the one-sweep pass's critical path.
+template <typename K>
+__global__ void __launch_bounds__(os::kThreads) k_rts_count(const K* __restrict__ keys, int64_t n, int shift,
+                                                            uint32_t* __restrict__ counts, int64_t ntiles) {
+  __shared__ uint32_t h[8][256];
+  const int tid = threadIdx.x, wid = tid >> 5;
+#pragma unroll
+  for (int w = 0; w < 8; ++w) h[w][tid] = 0;
+  __syncthreads();
+  const int64_t base = (int64_t)blockIdx.x * os::kTile;
+  uint32_t d[os::kItems];
+#pragma unroll
+  for (int k = 0; k < os::kItems; ++k) {
+    const int64_t i = base + k * os::kThreads + tid;
+    d[k] = i < n ? ((uint32_t)(keys[i] >> shift) & 255u) : 256u;
+  }
+#pragma unroll
+  for (int k = 0; k < os::kItems; ++k)
+    if (d[k] < 256u) atomicAdd(&h[wid][d[k]], 1u);
+  __syncthreads();
+  uint32_t s = 0;
+#pragma unroll
+  for (int w = 0; w < 8; ++w) s += h[w][tid];
+  counts[(int64_t)tid * ntiles + blockIdx.x] = s;
+}
+
+// Row d of the digit-major count table -> offsets, in place.
+__global__ void k_rts_rowscan(uint32_t* __restrict__ counts, int64_t ntiles, const uint32_t* __restrict__ gstart);
+
+template <typename K>
+__global__ void __launch_bounds__(os::kThreads, sizeof(K) == 4 ? 4 : 3)
+    k_rts_scatter(const K* __restrict__ kin, const uint32_t* __restrict__ vin, K* __restrict__ kout,
+                  uint32_t* __restrict__ vout, int64_t n, int shift, const uint32_t* __restrict__ offsets,
+                  int64_t ntiles) {
+  using namespace os;
+  __shared__ K skey[kTile];
+  __shared__ uint32_t sval[kTile];
+  __shared__ uint32_t whist[8][256];  // per-warp digit counts, then per-warp offsets
+  __shared__ uint32_t lstart[256];
+  __shared__ uint32_t gbase[256];
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+#pragma unroll
+  for (int w = 0; w < 8; ++w) whist[w][tid] = 0;
+  gbase[tid] = offsets[(int64_t)tid * ntiles + blockIdx.x];
+  __syncthreads();
+  const int64_t base = (int64_t)blockIdx.x * kTile;
+  const int tile_n = (int)min((int64_t)kTile, n - base);
+  // warp w owns tile items [256 w, 256 w + 256): item 256 w + 32 k + lane
+  K key[kItems];
+  uint32_t val[kItems], dig[kItems], rank[kItems];
+  const uint32_t lt_mask = (1u << lane) - 1u;
+#pragma unroll
+  for (int k = 0; k < kItems; ++k) {
+    const int li = wid * 256 + 32 * k + lane;
+    if (li < tile_n) {
+      key[k] = kin[base + li];
+      val[k] = vin[base + li];
+      dig[k] = (uint32_t)(key[k] >> shift) & 255u;
+    } else {
+      key[k] = 0;
+      val[k] = 0;
+      dig[k] = 256u + (uint32_t)lane;  // private digit: never shares a rank
+    }
+  }
+  // stable rank inside the warp: earlier rounds, then lower lanes
+#pragma unroll
+  for (int k = 0; k < kItems; ++k) {
+    const uint32_t d = dig[k];
+    const uint32_t peers = __match_any_sync(0xffffffffu, d);
+    const uint32_t before = d < 256u ? whist[wid][d] : 0u;
+    rank[k] = before + __popc(peers & lt_mask);
+    __syncwarp();
+    if (d < 256u && (peers & lt_mask) == 0) whist[wid][d] = before + __popc(peers);
+    __syncwarp();
+  }
+  __syncthreads();
+  uint32_t mine = 0;
+#pragma unroll
+  for (int w = 0; w < 8; ++w) {
+    const uint32_t c = whist[w][tid];
+    whist[w][tid] = mine;
+    mine += c;
+  }
+  lstart[tid] = block_excl_scan256(mine, nullptr);
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < kItems; ++k) {
+    const uint32_t d = dig[k];
+    if (d < 256u) {
+      const uint32_t lp = lstart[d] + whist[wid][d] + rank[k];
+      skey[lp] = key[k];
+      sval[lp] = val[k];
+    }
+  }
+  __syncthreads();
+  for (int i = tid; i < tile_n; i += kThreads) {
+    const K k = skey[i];
+    const uint32_t d = (uint32_t)(k >> shift) & 255u;
+    const int64_t o = (int64_t)gbase[d] + (i - (int)lstart[d]);
+    kout[o] = k;
+    vout[o] = sval[i];
+  }
+}
+
+inline int64_t rts_scratch_words(int64_t n, int nbits) {
+  const int64_t npass = (nbits + 7) / 8;
+  const int64_t ntiles = (n + os::kTile - 1) / os::kTile;
+  return ntiles * 256 + npass * 256 + 16;
+}
+
+template <typename K>
+int rts_sort_pairs(K* keys, uint32_t* vals, K* keys_alt, uint32_t* vals_alt, int64_t n, int nbits,
+                   uint32_t* scratch, cudaStream_t st, uint64_t* launches) {
+  if (n <= 0) return 0;
+  const int npass = (nbits + 7) / 8;
+  const int64_t ntiles = (n + os::kTile - 1) / os::kTile;
+  uint32_t* counts = scratch;
+  uint32_t* ghist = counts + ntiles * 256;
+  cudaMemsetAsync(ghist, 0, (size_t)npass * 256 * 4, st);
+  int hb = (int)((n + 255) / 256);
+  if (hb > 152 * 8) hb = 152 * 8;
+  k_os_hist<K><<<hb, 256, 0, st>>>(keys, n, npass, ghist);
+  k_os_scan<<<npass, 256, 0, st>>>(ghist);
+  K* ka = keys;
+  K* kb = keys_alt;
+  uint32_t* va = vals;
+  uint32_t* vb = vals_alt;
+  int which = 0;
+  for (int p = 0; p < npass; ++p) {
+    k_rts_count<K><<<(unsigned)ntiles, os::kThreads, 0, st>>>(ka, n, 8 * p, counts, ntiles);
+    k_rts_rowscan<<<256, 256, 0, st>>>(counts, ntiles, ghist + p * 256);
+    k_rts_scatter<K><<<(unsigned)ntiles, os::kThreads, 0, st>>>(ka, va, kb, vb, n, 8 * p, counts, ntiles);
+    K* tk = ka;
+    ka = kb;
+    kb = tk;
+    uint32_t* tv = va;
+    va = vb;
+    vb = tv;
+    which ^= 1;
+  }
+  if (launches) *launches += 2 + 3 * npass;
+  return which;
+}
+
+// The sort the workspace paths use: reduce-then-scan passes below 2^31
+// elements, the older three-kernel passes above.  scratch:
+// sort_scratch_words(n, nbits) words.
 inline int64_t sort_scratch_words(int64_t n, int nbits) {
-  const int64_t a = radix_scratch_words(n), b = onesweep_scratch_words(n, nbits);
+  const int64_t a = radix_scratch_words(n), b = rts_scratch_words(n, nbits);
   return a > b ? a : b;
 }
 
 template <typename K>
 int sort_pairs(K* keys, uint32_t* vals, K* keys_alt, uint32_t* vals_alt, int64_t n, int nbits, uint32_t* scratch,
                cudaStream_t st, uint64_t* launches, uint32_t* err) {
-  if (n < (int64_t)os::kVal)
-    return onesweep_sort_pairs<K>(keys, vals, keys_alt, vals_alt, n, nbits, scratch, st, launches, err);
+  (void)err;
+  if (n < (1ll << 31)) return rts_sort_pairs<K>(keys, vals, keys_alt, vals_alt, n, nbits, scratch, st, launches);
   return radix_sort_pairs<K>(keys, vals, keys_alt, vals_alt, n, nbits, scratch, st, launches);
 }
 

@@ -10,6 +10,8 @@
 //                   strand bit, (2w+1) bits in all, which orders exactly like
 //                   the reference's 64-bit bmer.mer.
 //   radix sort      stable LSD over those 2w+1 bits (prim.cuh).
+//   k_seed_keys_pair  the pairwise matcher's keys: both genomes in one array,
+//                   a genome bit below the SML key, sorted once.
 #include <string.h>
 
 #include "mvg_internal.h"
@@ -111,6 +113,24 @@ __global__ void k_seed_keys(const uint32_t* __restrict__ g, uint64_t count, Seed
   }
 }
 
+// Both genomes' keys in one array for the pairwise matcher: the SML key
+// (seed bits, strand bit) followed by a genome bit (A = 0, B = 1); values are
+// positions.  Sorted stably, every seed's occurrences in the two genomes are
+// adjacent, each genome's in position order.
+template <typename K>
+__global__ void k_seed_keys_pair(const uint32_t* __restrict__ ga, uint64_t ca, const uint32_t* __restrict__ gb,
+                                 uint64_t cb, SeedDesc s, K* __restrict__ keys, uint32_t* __restrict__ pos) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  const int shift = 64 - 2 * s.w;
+  for (uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < ca + cb; p += stride) {
+    const bool in_b = p >= ca;
+    const uint64_t q = in_b ? p - ca : p;
+    const uint64_t m = canonical_mer(in_b ? gb : ga, q, s);
+    keys[p] = (K)(((((m >> shift) << 1) | (m & 1ull)) << 1) | (in_b ? 1ull : 0ull));
+    pos[p] = (uint32_t)q;
+  }
+}
+
 template <typename K>
 __global__ void k_key_to_mer(const K* __restrict__ keys, uint64_t count, int w, uint64_t* __restrict__ mer) {
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
@@ -202,6 +222,35 @@ int sml_build_into(const uint8_t* d_seq, uint64_t n, uint64_t count, const SeedD
                                          d_err, launches);
   return sml_build_into_impl<uint64_t>(d_seq, n, count, s, packed, k0, k1, v0, v1, scr, d_pos_out, d_mer_out, st,
                                        d_err, launches);
+}
+
+template <typename K>
+static int pair_sort_impl(Ctx* c, const uint32_t* ga, uint64_t ca, const uint32_t* gb, uint64_t cb,
+                          const SeedDesc& s, SmlKeys* out) {
+  const uint64_t count = ca + cb;
+  const int nbits = 2 * s.w + 2;
+  Workspace& ws = c->ws;
+  K* k0 = (K*)ws.get(c, 0, count * sizeof(K));
+  K* k1 = (K*)ws.get(c, 1, count * sizeof(K));
+  uint32_t* v0 = (uint32_t*)ws.get(c, 2, count * sizeof(uint32_t));
+  uint32_t* v1 = (uint32_t*)ws.get(c, 3, count * sizeof(uint32_t));
+  uint32_t* scr = (uint32_t*)ws.get(c, 4, sort_scratch_words(count, nbits) * sizeof(uint32_t));
+  if (!k0 || !k1 || !v0 || !v1 || !scr) return report_error(MVG_ERR_NOMEM, "workspace allocation failed");
+  k_seed_keys_pair<K><<<grid_for(count, 256), 256, 0, c->stream>>>(ga, ca, gb, cb, s, k0, v0);
+  c->launches++;
+  const int which = sort_pairs<K>(k0, v0, k1, v1, (int64_t)count, nbits, scr, c->stream, &c->launches, c->d_err);
+  out->keys = which ? k1 : k0;
+  out->pos = which ? v1 : v0;
+  out->wide = sizeof(K) == 8;
+  out->count = count;
+  MVG_CUDA_TRY(cudaGetLastError());
+  return 0;
+}
+
+int pair_sort(Ctx* c, const uint32_t* ga, uint64_t ca, const uint32_t* gb, uint64_t cb, const SeedDesc& s,
+              SmlKeys* out) {
+  if (2 * s.w + 2 <= 32) return pair_sort_impl<uint32_t>(c, ga, ca, gb, cb, s, out);
+  return pair_sort_impl<uint64_t>(c, ga, ca, gb, cb, s, out);
 }
 
 int sml_sort(Ctx* c, const uint32_t* d_packed, uint64_t count, const SeedDesc& s, uint32_t* d_pos_out,

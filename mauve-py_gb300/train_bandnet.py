@@ -176,7 +176,7 @@ def train(args):
     t0 = time.time()
     sc_tr, env_tr = label(ctx, tr)
     print("labels %.1fs (%.3g cells)" % (time.time() - t0, tr.cells), flush=True)
-    T, d_lab_tr, h_lab_tr = bandnet.labels_from_full_dp(tr.la, tr.lb, sc_tr, env_tr,
+    T, d_lab_tr, h_lab_tr = bandnet.labels_from_full_dp(tr.la, tr.lb, sc_tr, env_tr, margin=args.margin,
                                                          totals=(tot_a[:n_tr], tot_b[:n_tr]))
     # gaps whose label band the exactness check still rejects are labelled
     # "whole matrix": proposing their band would only add a rerun
@@ -197,13 +197,19 @@ def train(args):
     perm = np.random.default_rng(args.seed).permutation(tr.n)
     val_idx, fit_idx = perm[:nval], perm[nval:]
     fit_idx_t = torch.from_numpy(fit_idx).to(dev)
+    # minibatches drawn with probability ~ cells^w: the gaps that carry the
+    # DP's cells weigh more in the fit (w = 0: uniform)
+    wts = torch.from_numpy((tr.la[fit_idx].astype(np.float64) * tr.lb[fit_idx]) ** args.cell_weight).to(dev)
     t0 = time.time()
     losses = []
     step = 0
     skipped = 0
     for ep in range(args.epochs):
-        order = fit_idx_t[torch.randperm(len(fit_idx_t), device=dev)]
-        lr = args.lr * (0.5 ** ep)
+        if args.cell_weight > 0:
+            order = fit_idx_t[torch.multinomial(wts, len(fit_idx_t), replacement=True)]
+        else:
+            order = fit_idx_t[torch.randperm(len(fit_idx_t), device=dev)]
+        lr = args.lr * (args.lr_decay ** ep)
         for s in range(0, len(order), args.batch):
             idx = order[s:s + args.batch]
             xb = X.index_select(0, idx).contiguous()
@@ -231,10 +237,10 @@ def train(args):
     import synth  # noqa: F401
     vb = DeviceBatch(*subset_host_idx(tr, np.sort(val_idx)), dev)
     best = None
-    for whole in (0.5, 0.3, 0.15):
+    for whole in (0.35, 0.5, 0.7, 0.9):
         ctx.set_band_whole_fraction(whole)
-        for alpha in (1.0, 1.25, 1.5, 2.0):
-            for beta in (0.0, 16.0, 48.0, 128.0):
+        for alpha in (0.9, 1.0, 1.15, 1.3, 1.5):
+            for beta in (0.0, 16.0, 48.0):
                 d, h = net.propose_dev(*vb.ptrs(), vb.n, alpha, beta)
                 secs, used, cells, *_ = timed_banded(ctx, vb, d, h)
                 if best is None or secs < best[0]:
@@ -289,7 +295,8 @@ def train(args):
                          "fallback_seconds_at_full_gcups": fb_cells / gcups_full / 1e9})
         del sub
     env = bandnet.full_dp_labels_dev(ctx, *ev.ptrs(), ev.n, torch_device=dev)
-    _, d_lab, h_lab = bandnet.labels_from_full_dp(ev.la, ev.lb, *env, totals=(tot_a[n_tr:], tot_b[n_tr:]))
+    _, d_lab, h_lab = bandnet.labels_from_full_dp(ev.la, ev.lb, *env, margin=args.margin,
+                                                  totals=(tot_a[n_tr:], tot_b[n_tr:]))
     t_lab, used_lab, cells_lab, *_ = timed_banded(ctx, ev, d_lab, h_lab)
     res["label_band"] = {"seconds": t_lab, **status_rates(used_lab), "cells": cells_lab,
                          "speedup_vs_full": tf / t_lab}
@@ -305,7 +312,11 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--train", type=int, default=1_000_000)
     ap.add_argument("--eval", type=int, default=200_000)
-    ap.add_argument("--epochs", type=int, default=4)
+    ap.add_argument("--epochs", type=int, default=12)
+    ap.add_argument("--lr-decay", type=float, default=0.75, help="learning-rate factor per epoch")
+    ap.add_argument("--margin", type=int, default=24, help="columns added to each label half-width")
+    ap.add_argument("--cell-weight", type=float, default=0.5,
+                    help="minibatch sampling probability ~ (LA*LB)^w")
     ap.add_argument("--batch", type=int, default=4096)
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--seed", type=int, default=4)
