@@ -168,7 +168,9 @@ def learned_band_section(ctx, args, dev, stream, rank):
     net = bandnet.BandNet(ctx, params=w["params"])
     alpha, beta = float(w["alpha"]), float(w["beta"])
     whole = float(w["whole"]) if "whole" in w.files else 0.5
+    gate = int(w["gate"]) if "gate" in w.files else 0
     ctx.set_band_whole_fraction(whole)
+    ctx.set_band_gate(gate)
     sa, oa, sb, ob = synth.gap_batch_recoded(seed=1000 + rank, nprob=args.lb_nprob)
     n = len(oa) - 1
     la, lb = np.diff(oa), np.diff(ob)
@@ -220,7 +222,7 @@ def learned_band_section(ctx, args, dev, stream, rank):
                            "not_tried": round(float((used == 2).mean()), 4)},
         "cells_computed": band_cells,
         "identical_to_full": identical, "weights": "mauve-py_gb300/bandnet_weights.npz",
-        "margins": {"alpha": alpha, "beta": beta, "whole_fraction": whole},
+        "margins": {"alpha": alpha, "beta": beta, "whole_fraction": whole, "divergence_gate": gate},
     }
 
 

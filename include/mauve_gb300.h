@@ -193,6 +193,13 @@ int mvg_mlp_train_step_dev(mvg_handle h, const void* d_x_bf16, const float* d_ta
 int mvg_band_propose_dev(mvg_handle h, const uint8_t* d_seq_a, const uint64_t* d_off_a, const uint8_t* d_seq_b,
                          const uint64_t* d_off_b, int64_t nprob, float alpha, float beta, int32_t* band_delta,
                          int32_t* band_half);
+/* Divergence gate for mvg_band_propose_dev (min_match = 0, the default,
+ * turns it off): up to 8 windows of 32 bases of A along the diagonal
+ * j = i*LB/LA are matched against B at diagonal offsets -8..8; a gap where
+ * fewer than half of its windows reach min_match matching bases (of 32) at
+ * their best offset is proposed the whole matrix, since no narrow band can
+ * pass the exactness check there.  Gaps shorter than 32 are not gated. */
+int mvg_set_band_gate(mvg_handle h, int min_match);
 
 /* ------------------------------------------------------------ index LUT */
 

@@ -52,6 +52,8 @@ def run(args):
         net = bandnet.BandNet(ctx, params=w["params"])
         if "whole" in w.files:
             ctx.set_band_whole_fraction(float(w["whole"]))
+        if "gate" in w.files:
+            ctx.set_band_gate(int(w["gate"]))
         d, h = net.propose_dev(*band.ptrs(), band.n, float(w["alpha"]), float(w["beta"]))
         src = "network"
     else:

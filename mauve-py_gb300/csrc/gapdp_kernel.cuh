@@ -172,11 +172,13 @@ __device__ void dp_solve(const DpJob& J, DpShared& sh, int w, int kstart, int ks
   const int end_lane = ((LA - 1) % SR) / R;
   const int end_r = (LA - 1) % R;
   const Band band = BANDED ? make_band(LA, LB, J.band_delta[p], J.band_half[p], SR) : make_full(LA, LB, SR);
+  // a band at least as wide as the matrix has no exits: nothing to bound
+  const bool track = BANDED && J.band_half[p] <= (LA > LB ? LA : LB);
   int32_t bound = kNeg;  // best score of any path leaving the band (this warp's part)
   // banded mode: totals and running prefixes of the per-base best scores
   int32_t totA = 0, totB = 0, pa = 0, pb_lo = 0, pb_hi = 0;
   int pa_rows = 0, pb_lo_cols = 0;
-  if (BANDED) {
+  if (track) {
     totA = warp_best_sum(A, 0, LA, J.base_max);
     totB = warp_best_sum(B, 0, LB, J.base_max);
   }
@@ -237,7 +239,7 @@ __device__ void dp_solve(const DpJob& J, DpShared& sh, int w, int kstart, int ks
     // strip's bottom row, and the column prefix at jlo-1 for lane 31
     int32_t rowpre[R];
     int32_t strip_pre = 0, run31 = 0, pb_next = 0;
-    if (BANDED) {
+    if (track) {
       // prefixes carried from the previous strip of this warp cover the
       // rows and columns up to it; only a gap (cooperative mode) is summed
       pa += warp_best_sum(A, pa_rows, row0, J.base_max);
@@ -291,7 +293,7 @@ __device__ void dp_solve(const DpJob& J, DpShared& sh, int w, int kstart, int ks
     int32_t pubM = kNeg, pubD = leftD, pubI = kNeg;  // bottom row, last computed column
     int32_t upM = kNeg, upD = kNeg, upI = kNeg;      // row above, current column
     uint32_t acc = 0;
-    const bool bottom_exit = BANDED && lane == 31 && row0 + SR < LA;
+    const bool bottom_exit = track && lane == 31 && row0 + SR < LA;
     const bool writes_row = k + 1 < nstrips;
     bool alive = true;
 
@@ -341,7 +343,7 @@ __device__ void dp_solve(const DpJob& J, DpShared& sh, int w, int kstart, int ks
         pubD = L.lD[R - 1];
         pubI = L.lI[R - 1];
         if (lane == 31 && writes_row) rb_out[j] = make_int4(pubM, pubD, pubI, 0);
-        if (BANDED && lane == 31) {
+        if (track && lane == 31) {
           run31 += best_of(J.base_max, bsel);  // prefix over B[0..j)
           if (j == next_lo - 1) pb_next = run31;
           if (bottom_exit && j < next_lo) {
@@ -400,7 +402,7 @@ __device__ void dp_solve(const DpJob& J, DpShared& sh, int w, int kstart, int ks
       J.scores[p] = sc;
       J.end_edge[p] = (uint8_t)e;
     }
-    if (BANDED) {
+    if (track) {
       // lane 31 swept every column of the strip: its running sum is the
       // prefix over B[0..jhi); carry the prefixes to this warp's next strip
       pb_hi = __shfl_sync(0xffffffffu, run31, 31);
@@ -418,7 +420,7 @@ __device__ void dp_solve(const DpJob& J, DpShared& sh, int w, int kstart, int ks
         }
       }
     }
-    if (BANDED && jhi < LB) {  // right-edge exits: an I step leaves the band
+    if (track && jhi < LB) {  // right-edge exits: an I step leaves the band
 #pragma unroll
       for (int r = 0; r < R; ++r) {
         const int i = row0 + lane * R + r + 1;
@@ -434,7 +436,7 @@ __device__ void dp_solve(const DpJob& J, DpShared& sh, int w, int kstart, int ks
   }
   if (BANDED) {
     // paths along row 0 past the band, or down column 0 past it (added once)
-    if (kstart == 0) {
+    if (track && kstart == 0) {
       const int hi0 = band_hi(band, 0);
       const int last_col0 = band_last_row_at_col1(band, LA);
       const int32_t pb0 = hi0 < LB ? warp_best_sum(B, 0, hi0, J.base_max) : 0;

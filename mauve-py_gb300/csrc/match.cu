@@ -10,12 +10,13 @@
 //   pair_sort (seeds.cu)                 both genomes' seed keys in one
 //                                       stable radix sort, a genome bit
 //                                       below the SML key
-//   k_pair_flags                         seeds unique in each genome (strand
+//   k_pair_count / k_pair_emit           seeds unique in each genome (strand
 //                                       ignored): runs of two, one per
 //                                       genome, in ascending seed order =
-//                                       the reference's hash order
-//   k_hash_pairs                         SetDirection + CalculateOffset +
-//                                       bucket id per pair
+//                                       the reference's hash order; counted
+//                                       per tile, then each pair's
+//                                       SetDirection + CalculateOffset +
+//                                       bucket id written in that order
 //   stable radix sort by bucket          keeps key order inside a bucket
 //   k_bucket_replay                      per bucket (a CTA for big buckets,
 //                                       a warp for the rest) replays the
@@ -54,33 +55,64 @@ struct MatchCtx {
 // seed unique in each genome (counted once in each, strand ignored:
 // LM/PairwiseMatchFinder.cpp:37-71 over LM/MatchFinder.cpp:172-340) is a run
 // of equal seed bits with exactly two members, one per genome; runs come in
-// ascending seed order, the reference's enumeration order.
+// ascending seed order, the reference's enumeration order.  Key i opens such
+// a run when pair_flag(i).
 template <typename K>
-__global__ void k_pair_flags(const K* __restrict__ keys, int64_t n, uint32_t* __restrict__ flag) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const uint64_t k0 = (uint64_t)keys[i], cur = k0 >> 2;
-    bool f = false;
-    if ((i == 0 || ((uint64_t)keys[i - 1] >> 2) != cur) && i + 1 < n) {
-      const uint64_t k1 = (uint64_t)keys[i + 1];
-      f = (k1 >> 2) == cur && ((k0 ^ k1) & 1ull) && (i + 2 == n || ((uint64_t)keys[i + 2] >> 2) != cur);
-    }
-    flag[i] = f;
+__device__ __forceinline__ bool pair_flag(const K* __restrict__ keys, int64_t n, int64_t i) {
+  const uint64_t k0 = (uint64_t)keys[i], cur = k0 >> 2;
+  if (i + 1 >= n || (i > 0 && ((uint64_t)keys[i - 1] >> 2) == cur)) return false;
+  const uint64_t k1 = (uint64_t)keys[i + 1];
+  return (k1 >> 2) == cur && ((k0 ^ k1) & 1ull) && (i + 2 == n || ((uint64_t)keys[i + 2] >> 2) != cur);
+}
+
+constexpr int kPairItems = 8;  // consecutive keys per thread
+constexpr int kPairTile = 256 * kPairItems;
+
+// Pass 1: the number of pairs opened in each tile of kPairTile keys.
+template <typename K>
+__global__ void __launch_bounds__(256) k_pair_count(const K* __restrict__ keys, int64_t n, uint32_t* __restrict__ bsum) {
+  const int64_t i0 = (int64_t)blockIdx.x * kPairTile + (int64_t)threadIdx.x * kPairItems;
+  uint32_t c = 0;
+#pragma unroll 4
+  for (int k = 0; k < kPairItems; ++k)
+    if (i0 + k < n) c += pair_flag(keys, n, i0 + k);
+  for (int d = 16; d > 0; d >>= 1) c += __shfl_xor_sync(0xffffffffu, c, d);
+  __shared__ uint32_t ws[8];
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = c;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t t = 0;
+    for (int w = 0; w < 8; ++w) t += ws[w];
+    bsum[blockIdx.x] = t;
   }
 }
 
-// One pair per flagged run: HashMatch (LM/MemHash.cpp:167-187) ->
-// SetDirection (:189-207) -> CalculateOffset (LM/MatchHashEntry.cpp:141-162)
-// -> bucket.
+// Pass 2 (after the tile counts are scanned): each pair's slot and its hash
+// entry: HashMatch (LM/MemHash.cpp:167-187) -> SetDirection (:189-207) ->
+// CalculateOffset (LM/MatchHashEntry.cpp:141-162) -> bucket.  A tile's
+// entries (at most one per two keys) are staged in shared memory and
+// written out contiguously.
 template <typename K>
-__global__ void k_hash_pairs(const K* __restrict__ keys, const uint32_t* __restrict__ pos, int64_t n,
-                             const uint32_t* __restrict__ flag, const uint32_t* __restrict__ idx, int L,
-                             Mhe* __restrict__ mhe, uint32_t* __restrict__ bucket, uint32_t* __restrict__ order) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    if (!flag[i]) continue;
+__global__ void __launch_bounds__(256) k_pair_emit(const K* __restrict__ keys, const uint32_t* __restrict__ pos,
+                                                   int64_t n, const uint32_t* __restrict__ bstart, int L,
+                                                   Mhe* __restrict__ mhe, uint32_t* __restrict__ bucket,
+                                                   uint32_t* __restrict__ order) {
+  __shared__ Mhe sm[kPairTile / 2];
+  __shared__ uint32_t sbk[kPairTile / 2];
+  __shared__ uint32_t tile_pairs;
+  const int64_t i0 = (int64_t)blockIdx.x * kPairTile + (int64_t)threadIdx.x * kPairItems;
+  uint32_t flags = 0;
+#pragma unroll
+  for (int k = 0; k < kPairItems; ++k)
+    if (i0 + k < n && pair_flag(keys, n, i0 + k)) flags |= 1u << k;
+  uint32_t li = block_excl_scan256(__popc(flags), &tile_pairs);
+  while (flags) {
+    const int k = __ffs(flags) - 1;
+    flags &= flags - 1;
+    const int64_t i = i0 + k;
     const uint64_t k0 = (uint64_t)keys[i], k1 = (uint64_t)keys[i + 1];
     const bool a_first = (k0 & 1ull) == 0;
     const uint64_t ka = a_first ? k0 : k1, kb = a_first ? k1 : k0;
-    const uint32_t j = idx[i];
     Mhe m;
     m.s0 = (int64_t)(a_first ? pos[i] : pos[i + 1]) + 1;
     m.s1 = (int64_t)(a_first ? pos[i + 1] : pos[i]) + 1;
@@ -90,9 +122,16 @@ __global__ void k_hash_pairs(const K* __restrict__ keys, const uint32_t* __restr
     m.off = m.s1 - m.s0;
     if (m.s1 < 0) m.off -= m.len;
     const int64_t t = kTableSize;
-    bucket[j] = (uint32_t)(((m.off % t) + t) % t);
-    order[j] = j;
-    mhe[j] = m;
+    sbk[li] = (uint32_t)(((m.off % t) + t) % t);
+    sm[li] = m;
+    ++li;
+  }
+  __syncthreads();
+  const uint32_t j0 = bstart[blockIdx.x], np = tile_pairs;
+  for (uint32_t q = threadIdx.x; q < np; q += blockDim.x) {
+    mhe[j0 + q] = sm[q];
+    bucket[j0 + q] = sbk[q];
+    order[j0 + q] = j0 + q;
   }
 }
 
@@ -778,17 +817,16 @@ int pairwise_matches_dev(Ctx* c, const uint8_t* d_a, uint64_t na, const uint8_t*
   if ((rc = pair_sort(c, ga, ca, gb, cb, s, &sk))) return rc;
   stage_mark(c, "unique_join");
   const int64_t nk = (int64_t)sk.count;
-  uint32_t* pflag = (uint32_t*)ws.get(c, 35, (nk + 1) * 4);
-  uint32_t* pidx = (uint32_t*)ws.get(c, 36, (nk + 1) * 4);
-  uint32_t* pscr = (uint32_t*)ws.get(c, 37, scan_scratch_words(nk + 1) * 4 + 64);
-  if (!pflag || !pidx || !pscr) return report_error(MVG_ERR_NOMEM, "workspace allocation failed");
-  uint32_t* d_npairs = pscr + scan_scratch_words(nk + 1);
+  const int64_t ptiles = (nk + kPairTile - 1) / kPairTile;
+  uint32_t* pbs = (uint32_t*)ws.get(c, 37, (ptiles + 4) * 4 + 64);
+  if (!pbs) return report_error(MVG_ERR_NOMEM, "workspace allocation failed");
+  uint32_t* d_npairs = pbs + ptiles + 2;
   if (sk.wide)
-    k_pair_flags<uint64_t><<<grid_for(nk, 256), 256, 0, c->stream>>>((const uint64_t*)sk.keys, nk, pflag);
+    k_pair_count<uint64_t><<<(unsigned)ptiles, 256, 0, c->stream>>>((const uint64_t*)sk.keys, nk, pbs);
   else
-    k_pair_flags<uint32_t><<<grid_for(nk, 256), 256, 0, c->stream>>>((const uint32_t*)sk.keys, nk, pflag);
-  c->launches++;
-  exclusive_scan(pflag, pidx, nk, pscr, d_npairs, c->stream, &c->launches);
+    k_pair_count<uint32_t><<<(unsigned)ptiles, 256, 0, c->stream>>>((const uint32_t*)sk.keys, nk, pbs);
+  k_scan_bsums<<<1, 256, 0, c->stream>>>(pbs, ptiles, d_npairs);
+  c->launches += 2;
   MVG_CUDA_TRY(cudaMemcpyAsync(c->h_scalars, d_npairs, 4, cudaMemcpyDeviceToHost, c->stream));
   MVG_CUDA_TRY(cudaStreamSynchronize(c->stream));
   const int64_t npairs = (int64_t)(uint32_t)c->h_scalars[0];
@@ -823,11 +861,11 @@ int pairwise_matches_dev(Ctx* c, const uint8_t* d_a, uint64_t na, const uint8_t*
 
   stage_mark(c, "hash_bucket_sort");
   if (sk.wide)
-    k_hash_pairs<uint64_t><<<grid_for(nk, 256), 256, 0, c->stream>>>((const uint64_t*)sk.keys, sk.pos, nk, pflag,
-                                                                      pidx, s.L, mhe, bk0, or0);
+    k_pair_emit<uint64_t><<<(unsigned)ptiles, 256, 0, c->stream>>>((const uint64_t*)sk.keys, sk.pos, nk, pbs, s.L,
+                                                                   mhe, bk0, or0);
   else
-    k_hash_pairs<uint32_t><<<grid_for(nk, 256), 256, 0, c->stream>>>((const uint32_t*)sk.keys, sk.pos, nk, pflag,
-                                                                      pidx, s.L, mhe, bk0, or0);
+    k_pair_emit<uint32_t><<<(unsigned)ptiles, 256, 0, c->stream>>>((const uint32_t*)sk.keys, sk.pos, nk, pbs, s.L,
+                                                                   mhe, bk0, or0);
   c->launches++;
   int which = sort_pairs<uint32_t>(bk0, or0, bk1, or1, npairs, 16, sscr, c->stream, &c->launches, c->d_err);
   uint32_t* sorted_pair = which ? or1 : or0;

@@ -286,11 +286,48 @@ __global__ void __launch_bounds__(256) k_band_features(const uint8_t* __restrict
 
 // Maps outputs to integer bands: delta = round(o0 * kDeltaScale),
 // half = ceil(alpha * (exp(o1) - 1) + beta), clamped to [0, 1e6].
+// Divergence gate: the share of up to 8 windows of 32 bases of A, spread
+// along the diagonal j = i*LB/LA, whose best match count with B over the
+// diagonal offsets -8..8 reaches `min_match` (one warp per gap; gaps
+// shorter than one window score 1).  Closely related gaps keep nearly every
+// window; gaps a band cannot help (divergent throughout) keep few.
+constexpr int kGateWin = 8, kGateReach = 8;
+__global__ void __launch_bounds__(256) k_band_gate(const uint8_t* __restrict__ sa, const uint64_t* __restrict__ oa,
+                                                   const uint8_t* __restrict__ sb, const uint64_t* __restrict__ ob,
+                                                   int64_t nprob, int min_match, float* __restrict__ share) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t p = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; p < nprob;
+       p += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+    const int64_t la = (int64_t)(oa[p + 1] - oa[p]), lb = (int64_t)(ob[p + 1] - ob[p]);
+    const uint8_t* A = sa + oa[p];
+    const uint8_t* B = sb + ob[p];
+    const int nwin = la < 32 ? 0 : (la / 32 < kGateWin ? (int)(la / 32) : kGateWin);
+    int good = 0;
+    for (int k = 0; k < nwin; ++k) {
+      const int64_t i0 = nwin == 1 ? 0 : (int64_t)k * (la - 32) / (nwin - 1);
+      const int64_t i = i0 + lane;
+      const int64_t j = i * lb / la;
+      const uint8_t a = A[i] & 3u;
+      int best = 0;
+#pragma unroll
+      for (int o = -kGateReach; o <= kGateReach; ++o) {
+        const int64_t jj = j + o;
+        const bool m = jj >= 0 && jj < lb && (B[jj] & 3u) == a;
+        best = max(best, __popc(__ballot_sync(0xffffffffu, m)));
+      }
+      good += best >= min_match;
+    }
+    if (lane == 0) share[p] = nwin ? (float)good / (float)nwin : 1.f;
+  }
+}
+
 __global__ void k_to_band(const float* __restrict__ o, int64_t n, float alpha, float beta, int32_t* __restrict__ delta,
-                          int32_t* __restrict__ half) {
+                          int32_t* __restrict__ half, const float* __restrict__ gate_share) {
   for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
-    // a non-finite output proposes the whole matrix (centred, half 1e6)
-    const bool ok = isfinite(o[p * kOut]) && isfinite(o[p * kOut + 1]);
+    // a non-finite output proposes the whole matrix (centred, half 1e6), and
+    // so does a gap the divergence gate turns away (under half its windows
+    // matched)
+    const bool ok = isfinite(o[p * kOut]) && isfinite(o[p * kOut + 1]) && !(gate_share && gate_share[p] < 0.5f);
     const float d = ok ? rintf(o[p * kOut] * kDeltaScale) : 0.f;
     float h = ok ? ceilf(alpha * (expf(fminf(o[p * kOut + 1], 13.f)) - 1.f) + beta) : 1e6f;
     h = fminf(fmaxf(h, 0.f), 1e6f);
@@ -540,6 +577,12 @@ int mvg_mlp_train_step_dev(mvg_handle h, const void* d_x_bf16, const float* d_ta
   return 0;
 }
 
+int mvg_set_band_gate(mvg_handle h, int min_match) {
+  if (!h || min_match < 0 || min_match > 32) return report_error(MVG_ERR_ARG, "min_match must be in 0..32");
+  reinterpret_cast<Ctx*>(h)->band_gate = min_match;
+  return 0;
+}
+
 int mvg_band_propose_dev(mvg_handle h, const uint8_t* d_sa, const uint64_t* d_oa, const uint8_t* d_sb,
                          const uint64_t* d_ob, int64_t nprob, float alpha, float beta, int32_t* h_delta,
                          int32_t* h_half) {
@@ -559,7 +602,15 @@ int mvg_band_propose_dev(mvg_handle h, const uint8_t* d_sa, const uint64_t* d_oa
   c->launches++;
   stage_mark(c, "mlp_forward");
   mlp_forward(c, s, X, nprob);
-  k_to_band<<<grid_for(nprob, 256), 256, 0, c->stream>>>(s.out, nprob, alpha, beta, dd, dd + nprob);
+  float* gate = nullptr;
+  if (c->band_gate > 0) {
+    gate = (float*)c->ws.get(c, 59, (size_t)nprob * 4 + 16);
+    if (!gate) return report_error(MVG_ERR_NOMEM, "workspace allocation failed");
+    k_band_gate<<<grid_for((uint64_t)nprob * 32, 256), 256, 0, c->stream>>>(d_sa, d_oa, d_sb, d_ob, nprob,
+                                                                            c->band_gate, gate);
+    c->launches++;
+  }
+  k_to_band<<<grid_for(nprob, 256), 256, 0, c->stream>>>(s.out, nprob, alpha, beta, dd, dd + nprob, gate);
   c->launches++;
   MVG_CUDA_TRY(cudaMemcpyAsync(h_delta, dd, nprob * 4, cudaMemcpyDeviceToHost, c->stream));
   MVG_CUDA_TRY(cudaMemcpyAsync(h_half, dd + nprob, nprob * 4, cudaMemcpyDeviceToHost, c->stream));

@@ -78,6 +78,40 @@ __device__ __forceinline__ uint64_t canonical_mer(const uint32_t* __restrict__ g
   return f < r ? f : r;
 }
 
+// The seed gather as a table: window byte c (bases 4c .. 4c+3) maps to its
+// selected bases already at their place in the left-aligned mer, so a mer is
+// the OR of one lookup per window byte.  Built by the whole block in shared
+// memory (8 x 256 entries); seed_bytes(s) = ceil(L / 4) bytes are used.
+__device__ __forceinline__ int seed_bytes(const SeedDesc& s) { return (s.L + 3) >> 2; }
+
+__device__ __forceinline__ void seed_lut_build(const SeedDesc& s, uint64_t (*lut)[256]) {
+  const int nb = seed_bytes(s);
+  for (int e = threadIdx.x; e < nb * 256; e += blockDim.x) {
+    const int c = e >> 8, b = e & 255;
+    uint64_t v = 0;
+#pragma unroll
+    for (int kk = 0; kk < 4; ++kk) {
+      const int k = 4 * c + kk;  // window base
+      if (k < s.L && ((s.pattern >> (s.L - 1 - k)) & 1ull)) {
+        const int o = k == 0 ? 0 : __popcll(s.pattern >> (s.L - k));  // selected bases before k
+        v |= (uint64_t)((b >> (6 - 2 * kk)) & 3) << (62 - 2 * o);
+      }
+    }
+    lut[c][b] = v;
+  }
+}
+
+__device__ __forceinline__ uint64_t canonical_mer_lut(const uint32_t* __restrict__ g, uint64_t pos,
+                                                      const uint64_t (*lut)[256], int nb, int w) {
+  const uint64_t win = window64(g, pos);
+  uint64_t f = 0;
+#pragma unroll
+  for (int c = 0; c < 8; ++c)
+    if (c < nb) f |= lut[c][(uint32_t)(win >> (56 - 8 * c)) & 255u];
+  const uint64_t r = revcomp_mer(f, w);
+  return f < r ? f : r;
+}
+
 inline int div_up(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
 
 }  // namespace mvg

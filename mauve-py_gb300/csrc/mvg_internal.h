@@ -42,6 +42,7 @@ struct Ctx {
   int band_rows = 4;          // banded gap-DP rows per lane (1, 2, 4 or 8)
   double band_whole = 0.5;    // bands covering at least this share of their matrix run whole
   int band_ring = 1;          // banded problems on the ring schedule where it is valid
+  int band_gate = 0;          // band proposals: divergence gate window threshold (0 = off)
   Workspace ws;
   MatchStats stats;
   bool profiling = false;

@@ -512,18 +512,31 @@ inline int64_t rts_scratch_words(int64_t n, int nbits) {
   return ntiles * 256 + npass * 256 + 16;
 }
 
+// Scratch layout: the digit-major tile count table (ntiles * 256 words),
+// then each pass's 256 global digit counts.
+inline uint32_t* rts_counts(uint32_t* scratch) { return scratch; }
+inline uint32_t* rts_ghist(uint32_t* scratch, int64_t n) {
+  return scratch + ((n + os::kTile - 1) / os::kTile) * 256;
+}
+
+// counted: the producer of the keys already wrote every pass's global digit
+// counts (rts_ghist, zeroed before) and the first pass's tile counts
+// (rts_counts) while writing the keys in tiles of os::kTile.
 template <typename K>
 int rts_sort_pairs(K* keys, uint32_t* vals, K* keys_alt, uint32_t* vals_alt, int64_t n, int nbits,
-                   uint32_t* scratch, cudaStream_t st, uint64_t* launches) {
+                   uint32_t* scratch, cudaStream_t st, uint64_t* launches, bool counted = false) {
   if (n <= 0) return 0;
   const int npass = (nbits + 7) / 8;
   const int64_t ntiles = (n + os::kTile - 1) / os::kTile;
-  uint32_t* counts = scratch;
-  uint32_t* ghist = counts + ntiles * 256;
-  cudaMemsetAsync(ghist, 0, (size_t)npass * 256 * 4, st);
-  int hb = (int)((n + 255) / 256);
-  if (hb > 152 * 8) hb = 152 * 8;
-  k_os_hist<K><<<hb, 256, 0, st>>>(keys, n, npass, ghist);
+  uint32_t* counts = rts_counts(scratch);
+  uint32_t* ghist = rts_ghist(scratch, n);
+  if (!counted) {
+    cudaMemsetAsync(ghist, 0, (size_t)npass * 256 * 4, st);
+    int hb = (int)((n + 255) / 256);
+    if (hb > 152 * 8) hb = 152 * 8;
+    k_os_hist<K><<<hb, 256, 0, st>>>(keys, n, npass, ghist);
+    if (launches) *launches += 1;
+  }
   k_os_scan<<<npass, 256, 0, st>>>(ghist);
   K* ka = keys;
   K* kb = keys_alt;
@@ -531,7 +544,10 @@ int rts_sort_pairs(K* keys, uint32_t* vals, K* keys_alt, uint32_t* vals_alt, int
   uint32_t* vb = vals_alt;
   int which = 0;
   for (int p = 0; p < npass; ++p) {
-    k_rts_count<K><<<(unsigned)ntiles, os::kThreads, 0, st>>>(ka, n, 8 * p, counts, ntiles);
+    if (p > 0 || !counted) {
+      k_rts_count<K><<<(unsigned)ntiles, os::kThreads, 0, st>>>(ka, n, 8 * p, counts, ntiles);
+      if (launches) *launches += 1;
+    }
     k_rts_rowscan<<<256, 256, 0, st>>>(counts, ntiles, ghist + p * 256);
     k_rts_scatter<K><<<(unsigned)ntiles, os::kThreads, 0, st>>>(ka, va, kb, vb, n, 8 * p, counts, ntiles);
     K* tk = ka;
@@ -542,7 +558,7 @@ int rts_sort_pairs(K* keys, uint32_t* vals, K* keys_alt, uint32_t* vals_alt, int
     vb = tv;
     which ^= 1;
   }
-  if (launches) *launches += 2 + 3 * npass;
+  if (launches) *launches += 1 + 2 * npass;
   return which;
 }
 

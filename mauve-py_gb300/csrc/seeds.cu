@@ -104,10 +104,14 @@ __global__ void k_pack(const uint8_t* __restrict__ seq, uint64_t n, uint32_t* __
 template <typename K>
 __global__ void k_seed_keys(const uint32_t* __restrict__ g, uint64_t count, SeedDesc s, K* __restrict__ keys,
                             uint32_t* __restrict__ pos) {
+  __shared__ uint64_t lut[8][256];
+  seed_lut_build(s, lut);
+  __syncthreads();
+  const int nb = seed_bytes(s);
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   const int shift = 64 - 2 * s.w;
   for (uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < count; p += stride) {
-    uint64_t m = canonical_mer(g, p, s);
+    uint64_t m = canonical_mer_lut(g, p, lut, nb, s.w);
     keys[p] = (K)(((m >> shift) << 1) | (m & 1ull));
     pos[p] = (uint32_t)p;
   }
@@ -116,18 +120,46 @@ __global__ void k_seed_keys(const uint32_t* __restrict__ g, uint64_t count, Seed
 // Both genomes' keys in one array for the pairwise matcher: the SML key
 // (seed bits, strand bit) followed by a genome bit (A = 0, B = 1); values are
 // positions.  Sorted stably, every seed's occurrences in the two genomes are
-// adjacent, each genome's in position order.
+// adjacent, each genome's in position order.  One block writes one sort tile
+// and also counts its digits for the sort: every pass's global digit counts
+// (ghist, added atomically) and the first pass's tile counts (counts0,
+// digit-major); both may be null.
 template <typename K>
-__global__ void k_seed_keys_pair(const uint32_t* __restrict__ ga, uint64_t ca, const uint32_t* __restrict__ gb,
-                                 uint64_t cb, SeedDesc s, K* __restrict__ keys, uint32_t* __restrict__ pos) {
-  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+__global__ void __launch_bounds__(256) k_seed_keys_pair(const uint32_t* __restrict__ ga, uint64_t ca,
+                                                        const uint32_t* __restrict__ gb, uint64_t cb, SeedDesc s,
+                                                        K* __restrict__ keys, uint32_t* __restrict__ pos, int npass,
+                                                        uint32_t* __restrict__ counts0, int64_t ntiles,
+                                                        uint32_t* __restrict__ ghist) {
+  __shared__ uint32_t h[8][256];
+  __shared__ uint64_t lut[8][256];
+  const int tid = threadIdx.x;
+  const bool hist = ghist != nullptr;
+  if (hist)
+    for (int q = 0; q < npass; ++q) h[q][tid] = 0;
+  seed_lut_build(s, lut);
+  __syncthreads();
+  const int nb = seed_bytes(s);
   const int shift = 64 - 2 * s.w;
-  for (uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < ca + cb; p += stride) {
+  const uint64_t n = ca + cb;
+  const uint64_t base = (uint64_t)blockIdx.x * os::kTile;
+#pragma unroll 2
+  for (int k = 0; k < os::kItems; ++k) {
+    const uint64_t p = base + (uint64_t)k * 256 + tid;
+    if (p >= n) break;
     const bool in_b = p >= ca;
     const uint64_t q = in_b ? p - ca : p;
-    const uint64_t m = canonical_mer(in_b ? gb : ga, q, s);
-    keys[p] = (K)(((((m >> shift) << 1) | (m & 1ull)) << 1) | (in_b ? 1ull : 0ull));
+    const uint64_t m = canonical_mer_lut(in_b ? gb : ga, q, lut, nb, s.w);
+    const K key = (K)(((((m >> shift) << 1) | (m & 1ull)) << 1) | (in_b ? 1ull : 0ull));
+    keys[p] = key;
     pos[p] = (uint32_t)q;
+    if (hist)
+      for (int d = 0; d < npass; ++d) atomicAdd(&h[d][(uint32_t)(key >> (8 * d)) & 255u], 1u);
+  }
+  if (hist) {
+    __syncthreads();
+    counts0[(int64_t)tid * ntiles + blockIdx.x] = h[0][tid];
+    for (int d = 0; d < npass; ++d)
+      if (h[d][tid]) atomicAdd(&ghist[d * 256 + tid], h[d][tid]);
   }
 }
 
@@ -236,9 +268,22 @@ static int pair_sort_impl(Ctx* c, const uint32_t* ga, uint64_t ca, const uint32_
   uint32_t* v1 = (uint32_t*)ws.get(c, 3, count * sizeof(uint32_t));
   uint32_t* scr = (uint32_t*)ws.get(c, 4, sort_scratch_words(count, nbits) * sizeof(uint32_t));
   if (!k0 || !k1 || !v0 || !v1 || !scr) return report_error(MVG_ERR_NOMEM, "workspace allocation failed");
-  k_seed_keys_pair<K><<<grid_for(count, 256), 256, 0, c->stream>>>(ga, ca, gb, cb, s, k0, v0);
-  c->launches++;
-  const int which = sort_pairs<K>(k0, v0, k1, v1, (int64_t)count, nbits, scr, c->stream, &c->launches, c->d_err);
+  const int64_t ntiles = ((int64_t)count + os::kTile - 1) / os::kTile;
+  int which;
+  if ((int64_t)count < (1ll << 31)) {  // the sort_pairs range of the reduce-then-scan sort
+    const int npass = (nbits + 7) / 8;
+    uint32_t* ghist = rts_ghist(scr, (int64_t)count);
+    MVG_CUDA_TRY(cudaMemsetAsync(ghist, 0, (size_t)npass * 256 * 4, c->stream));
+    k_seed_keys_pair<K><<<(unsigned)ntiles, 256, 0, c->stream>>>(ga, ca, gb, cb, s, k0, v0, npass, rts_counts(scr),
+                                                                 ntiles, ghist);
+    c->launches++;
+    which = rts_sort_pairs<K>(k0, v0, k1, v1, (int64_t)count, nbits, scr, c->stream, &c->launches, true);
+  } else {
+    k_seed_keys_pair<K><<<(unsigned)ntiles, 256, 0, c->stream>>>(ga, ca, gb, cb, s, k0, v0, 0, nullptr, ntiles,
+                                                                 nullptr);
+    c->launches++;
+    which = sort_pairs<K>(k0, v0, k1, v1, (int64_t)count, nbits, scr, c->stream, &c->launches, c->d_err);
+  }
   out->keys = which ? k1 : k0;
   out->pos = which ? v1 : v0;
   out->wide = sizeof(K) == 8;

@@ -43,7 +43,8 @@ EXPORTS = ["mvg_create", "mvg_destroy", "mvg_last_error", "mvg_stream", "mvg_ker
            "mvg_lut_fix_zero_idx_dev", "mvg_lut_fill_gaps", "mvg_lut_fill_gaps_dev", "mvg_lut_smooth_edges",
            "mvg_lut_smooth_edges_dev", "mvg_lut_find_gaps", "mvg_lut_find_gaps_dev", "mvg_lut_find_edges",
            "mvg_lut_find_mismatches", "mvg_lut_find_duplicate_mappings", "mvg_build_index_lut",
-           "mvg_build_index_lut_dev", "mvg_set_band_whole_fraction", "mvg_set_band_ring"]
+           "mvg_build_index_lut_dev", "mvg_set_band_whole_fraction", "mvg_set_band_ring",
+           "mvg_set_band_gate"]
 
 TUNING_PATH = os.path.join(HERE, "dp_tuning.json")
 
@@ -81,6 +82,7 @@ def load_library(path=LIB_PATH):
         "mvg_set_dp_rows": (ci, [vp, ci, ci]),
         "mvg_set_band_whole_fraction": (ci, [vp, ctypes.c_double]),
         "mvg_set_band_ring": (ci, [vp, ci]),
+        "mvg_set_band_gate": (ci, [vp, ci]),
         "mvg_gapdp_envelope_dev": (ci, [vp, vp, vp, vp, vp, i64, vp, vp]),
         "mvg_mlp_num_params": (i64, []),
         "mvg_mlp_set_params": (ci, [vp, vp]),
@@ -180,6 +182,10 @@ class Context:
     def set_band_whole_fraction(self, fraction):
         """Bands covering at least this share of their matrix run whole (default 0.5)."""
         _check(load_library().mvg_set_band_whole_fraction(self._h, float(fraction)))
+
+    def set_band_gate(self, min_match):
+        """Divergence gate of the band proposal (0 = off); see mvg_set_band_gate."""
+        _check(load_library().mvg_set_band_gate(self._h, int(min_match)))
 
     def set_band_ring(self, on=True):
         """Banded passes on the ring schedule (default) or all in the strip kernel."""

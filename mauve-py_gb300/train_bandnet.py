@@ -237,23 +237,26 @@ def train(args):
     import synth  # noqa: F401
     vb = DeviceBatch(*subset_host_idx(tr, np.sort(val_idx)), dev)
     best = None
-    for whole in (0.35, 0.5, 0.7, 0.9):
-        ctx.set_band_whole_fraction(whole)
-        for alpha in (0.9, 1.0, 1.15, 1.3, 1.5):
-            for beta in (0.0, 16.0, 48.0):
-                d, h = net.propose_dev(*vb.ptrs(), vb.n, alpha, beta)
-                secs, used, cells, *_ = timed_banded(ctx, vb, d, h)
-                if best is None or secs < best[0]:
-                    best = (secs, alpha, beta, whole, float((used == 1).mean()), cells)
-    _, alpha, beta, whole, acc_v, _ = best
+    for gate in (0, 24, 26):
+        ctx.set_band_gate(gate)
+        for whole in (0.35, 0.5, 0.7, 0.9):
+            ctx.set_band_whole_fraction(whole)
+            for alpha in (0.9, 1.0, 1.15, 1.3, 1.5):
+                for beta in (0.0, 16.0, 48.0):
+                    d, h = net.propose_dev(*vb.ptrs(), vb.n, alpha, beta)
+                    secs, used, cells, *_ = timed_banded(ctx, vb, d, h)
+                    if best is None or secs < best[0]:
+                        best = (secs, alpha, beta, whole, gate, float((used == 1).mean()), cells)
+    _, alpha, beta, whole, gate, acc_v, _ = best
     ctx.set_band_whole_fraction(whole)
-    print("calibrated alpha %.2f beta %.1f whole %.2f (validation accept %.3f)" % (alpha, beta, whole, acc_v),
-          flush=True)
+    ctx.set_band_gate(gate)
+    print("calibrated alpha %.2f beta %.1f whole %.2f gate %d (validation accept %.3f)" % (alpha, beta, whole, gate,
+                                                                                           acc_v), flush=True)
     params = net.get_params()
     # held-out evaluation: full vs learned band vs band without the network
     res = {"train_gaps": tr.n, "eval_gaps": ev.n, "train_seconds": train_s, "steps": step,
            "loss_curve": losses[-20:], "nonfinite_minibatches": skipped, "alpha": alpha, "beta": beta,
-           "whole_fraction": whole}
+           "whole_fraction": whole, "divergence_gate": gate}
     tf, sc_f, p_f, pl_f = timed_full(ctx, ev)
     tf, sc_f, p_f, pl_f = timed_full(ctx, ev)  # second run: warm
     t_prop0 = time.perf_counter()
@@ -301,7 +304,8 @@ def train(args):
     res["label_band"] = {"seconds": t_lab, **status_rates(used_lab), "cells": cells_lab,
                          "speedup_vs_full": tf / t_lab}
     print(json.dumps(res, indent=1), flush=True)
-    np.savez(args.out, params=params, alpha=np.float32(alpha), beta=np.float32(beta), whole=np.float32(whole))
+    np.savez(args.out, params=params, alpha=np.float32(alpha), beta=np.float32(beta), whole=np.float32(whole),
+             gate=np.int32(gate))
     with open(os.path.splitext(args.out)[0] + "_eval.json", "w") as f:
         json.dump(res, f, indent=1)
     print("total %.1fs" % (time.time() - t_all))

@@ -140,3 +140,60 @@ def test_training_reduces_loss(ctx):
     for _ in range(150):
         last = net.train_step_dev(X.data_ptr(), Tg.data_ptr(), n, 1e-3)
     assert last < 0.5 * first
+
+
+def gate_share_ref(sa, oa, sb, ob, min_match):
+    """numpy mirror of the proposal's divergence gate (k_band_gate)."""
+    out = np.ones(len(oa) - 1)
+    for p in range(len(oa) - 1):
+        A = sa[oa[p]:oa[p + 1]].astype(np.int64) & 3
+        B = sb[ob[p]:ob[p + 1]].astype(np.int64) & 3
+        la, lb = len(A), len(B)
+        nwin = 0 if la < 32 else min(8, la // 32)
+        if nwin == 0:
+            continue
+        good = 0
+        for k in range(nwin):
+            i0 = 0 if nwin == 1 else k * (la - 32) // (nwin - 1)
+            i = np.arange(i0, i0 + 32)
+            j = i * lb // la
+            best = 0
+            for o in range(-8, 9):
+                jj = j + o
+                ok = (jj >= 0) & (jj < lb)
+                m = np.zeros(32, bool)
+                m[ok] = B[jj[ok]] == A[i[ok]]
+                best = max(best, int(m.sum()))
+            good += best >= min_match
+        out[p] = good / nwin
+    return out
+
+
+def test_divergence_gate_matches_reference_and_sends_divergent_gaps_whole(ctx):
+    import os
+    weights = os.path.join(os.path.dirname(bandnet.__file__), "bandnet_weights.npz")
+    w = np.load(weights)
+    net = bandnet.BandNet(ctx, params=w["params"])
+    sa, oa, sb, ob = synth.gap_batch_recoded(seed=41, nprob=400, lmin=10, lmax=3000, unrelated=0.5)
+    t, ptrs = _batch_ptrs(sa, oa, sb, ob)
+    n = len(oa) - 1
+    ctx.set_band_gate(0)
+    _, h_off = net.propose_dev(*ptrs, n, 1.0, 0.0)
+    ctx.set_band_gate(26)
+    try:
+        _, h_on = net.propose_dev(*ptrs, n, 1.0, 0.0)
+    finally:
+        ctx.set_band_gate(0)
+    share = gate_share_ref(sa, oa, sb, ob, 26)
+    gated = share < 0.5
+    np.testing.assert_array_equal(h_on[gated], 1000000)
+    np.testing.assert_array_equal(h_on[~gated], h_off[~gated])
+    # the gate picks out the divergent gaps: score deficit per base far above
+    # that of the closely related ones
+    scores, _ = ctx.gap_align_batch(sa, oa, sb, ob, with_paths=False)
+    la, lb = np.diff(oa), np.diff(ob)
+    best = np.minimum(bandnet.best_totals(sa, oa), bandnet.best_totals(sb, ob))
+    rate = (best - scores) / np.minimum(la, lb)
+    big = la >= 256
+    assert gated[big & (rate > 40)].mean() > 0.9
+    assert gated[big & (rate < 10)].mean() < 0.05
