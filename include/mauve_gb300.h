@@ -201,6 +201,32 @@ int mvg_band_propose_dev(mvg_handle h, const uint8_t* d_seq_a, const uint64_t* d
  * pass the exactness check there.  Gaps shorter than 32 are not gated. */
 int mvg_set_band_gate(mvg_handle h, int min_match);
 
+/* ------------------------------------------------------ .sslist cache file */
+
+/* The sorted mer list file progressiveMauve caches next to each FASTA
+ * (FileSML::Create / LoadFile2, libMems/FileSML.cpp:401-459, 120-195):
+ * the SMLHeader struct (libMems/SortedMerList.h:48-63, 2352 bytes, format
+ * version 5), the 2-bit packed sequence (binary_seq_len uint32 words: the
+ * sequence's words plus two pad words), then one uint32 position per SML
+ * entry in sorted order.  mvg_sslist_write builds the SML on the GPU and
+ * writes the file; entries with equal mers are in position order.
+ * mvg_sslist_read parses a file (no GPU needed): with words / pos NULL it
+ * only fills info; status gets LoadFile2's failure code (1 cannot open, 2
+ * short header, 3 other format version, 4 truncated sequence, 5 positions
+ * unreadable; 0 otherwise). */
+typedef struct {
+  uint64_t seed;
+  uint32_t seed_length, seed_weight;
+  uint64_t length;   /* bases */
+  uint64_t words;    /* packed sequence words, pad words included */
+  uint64_t entries;  /* positions after the sequence */
+  int circular;
+  int status;
+} mvg_sslist_info;
+int mvg_sslist_write(mvg_handle h, const uint8_t* seq, uint64_t n, uint64_t seed, const char* path);
+int mvg_sslist_read(const char* path, mvg_sslist_info* info, uint32_t* words, uint64_t cap_words, uint32_t* pos,
+                    uint64_t cap_pos);
+
 /* ------------------------------------------------------------ index LUT */
 
 /* Genome -> reference index LUT (int32, -1 = unmapped) as mauve.buildIndex

@@ -44,7 +44,7 @@ EXPORTS = ["mvg_create", "mvg_destroy", "mvg_last_error", "mvg_stream", "mvg_ker
            "mvg_lut_smooth_edges_dev", "mvg_lut_find_gaps", "mvg_lut_find_gaps_dev", "mvg_lut_find_edges",
            "mvg_lut_find_mismatches", "mvg_lut_find_duplicate_mappings", "mvg_build_index_lut",
            "mvg_build_index_lut_dev", "mvg_set_band_whole_fraction", "mvg_set_band_ring",
-           "mvg_set_band_gate"]
+           "mvg_set_band_gate", "mvg_sslist_write", "mvg_sslist_read"]
 
 TUNING_PATH = os.path.join(HERE, "dp_tuning.json")
 
@@ -83,6 +83,8 @@ def load_library(path=LIB_PATH):
         "mvg_set_band_whole_fraction": (ci, [vp, ctypes.c_double]),
         "mvg_set_band_ring": (ci, [vp, ci]),
         "mvg_set_band_gate": (ci, [vp, ci]),
+        "mvg_sslist_write": (ci, [vp, vp, u64, u64, ctypes.c_char_p]),
+        "mvg_sslist_read": (ci, [ctypes.c_char_p, vp, vp, u64, vp, u64]),
         "mvg_gapdp_envelope_dev": (ci, [vp, vp, vp, vp, vp, i64, vp, vp]),
         "mvg_mlp_num_params": (i64, []),
         "mvg_mlp_set_params": (ci, [vp, vp]),
@@ -163,6 +165,26 @@ def seed_weight(seed):
     return int(load_library().mvg_seed_weight(seed))
 
 
+class SslistInfo(ctypes.Structure):
+    _fields_ = [("seed", ctypes.c_uint64), ("seed_length", ctypes.c_uint32), ("seed_weight", ctypes.c_uint32),
+                ("length", ctypes.c_uint64), ("words", ctypes.c_uint64), ("entries", ctypes.c_uint64),
+                ("circular", ctypes.c_int), ("status", ctypes.c_int)]
+
+
+def sslist_read(path):
+    """(info, packed words, positions) of a .sslist file (no GPU needed)."""
+    L = load_library()
+    info = SslistInfo()
+    p = os.fsencode(path)
+    rc = L.mvg_sslist_read(p, ctypes.byref(info), None, 0, None, 0)
+    if rc:
+        raise RuntimeError("mvg error %d (status %d): %s" % (rc, info.status, L.mvg_last_error().decode()))
+    words = np.zeros(max(int(info.words), 1), np.uint32)
+    pos = np.zeros(max(int(info.entries), 1), np.uint32)
+    _check(L.mvg_sslist_read(p, ctypes.byref(info), _ptr(words), int(info.words), _ptr(pos), int(info.entries)))
+    return info, words[:info.words], pos[:info.entries]
+
+
 class Context:
     """A CUDA device, a stream and the device workspaces (opaque handle)."""
 
@@ -230,6 +252,11 @@ class Context:
         _check(load_library().mvg_sml_build(self._h, _ptr(s), len(s), seed, _ptr(pos), _ptr(mer), cnt,
                                             ctypes.byref(out)))
         return pos[:cnt], (mer[:cnt] if with_mers else None)
+
+    def sslist_write(self, seq, seed, path):
+        """Builds the SML of seq and writes it as a .sslist file."""
+        a = _u8(seq)
+        _check(load_library().mvg_sslist_write(self._h, _ptr(a), len(a), int(seed), os.fsencode(path)))
 
     def sml_build_dev(self, d_seq_ptr, n, seed, d_pos_ptr, d_mer_ptr, cap):
         wait_producers()

@@ -12,6 +12,12 @@
 //   ref_profile_align    -> muscle::ProfileProfile with the DNA settings that
 //                           MuscleInterface::ProfileAlignFast installs
 //                           (libMems/MuscleInterface.cpp:1053-1112)
+//   ref_sml_header_layout, ref_sml_file_image
+//                        -> the SMLHeader struct (libMems/SortedMerList.h:48-63)
+//                           and the header and packed sequence an SML holds
+//                           after Create, which FileSML::Create writes
+//                           (libMems/FileSML.cpp:401-459)
+#include <cstddef>
 #include <cstdint>
 #include <cstring>
 #include <string>
@@ -69,6 +75,63 @@ int64_t ref_sml_build(const char* seq, uint64_t len, uint64_t seed,
     if (buf.empty()) break;
   }
   return (int64_t)n;
+}
+
+// sizeof(SMLHeader) then the offset of each member in declaration order
+// (15 values).
+int ref_sml_header_layout(int64_t* out) {
+  out[0] = (int64_t)sizeof(SMLHeader);
+  out[1] = (int64_t)offsetof(SMLHeader, version);
+  out[2] = (int64_t)offsetof(SMLHeader, alphabet_bits);
+  out[3] = (int64_t)offsetof(SMLHeader, seed);
+  out[4] = (int64_t)offsetof(SMLHeader, seed_length);
+  out[5] = (int64_t)offsetof(SMLHeader, seed_weight);
+  out[6] = (int64_t)offsetof(SMLHeader, length);
+  out[7] = (int64_t)offsetof(SMLHeader, unique_mers);
+  out[8] = (int64_t)offsetof(SMLHeader, word_size);
+  out[9] = (int64_t)offsetof(SMLHeader, little_endian);
+  out[10] = (int64_t)offsetof(SMLHeader, id);
+  out[11] = (int64_t)offsetof(SMLHeader, circular);
+  out[12] = (int64_t)offsetof(SMLHeader, translation_table);
+  out[13] = (int64_t)offsetof(SMLHeader, description);
+  out[14] = (int64_t)(sizeof(((SMLHeader*)0)->translation_table));
+  return 0;
+}
+
+namespace {
+// Exposes the header and packed words an SML holds after Create.
+struct SmlImage : public DNAMemorySML {
+  const SMLHeader& hdr() const { return header; }
+  const uint32* words() const { return sequence; }
+  uint64_t nwords() const { return binary_seq_len; }
+};
+}  // namespace
+
+// After DNAMemorySML::Create: the header (sizeof(SMLHeader) bytes; members
+// the reference never sets are zeroed here) and the packed sequence words.
+// Returns the number of words, or -1 if cap_words is too small.
+int64_t ref_sml_file_image(const char* seq, uint64_t len, uint64_t seed, uint8_t* header_out, uint32_t* words_out,
+                           uint64_t cap_words) {
+  gnSequence gs(std::string(seq, len));
+  SmlImage sml;
+  sml.Create(gs, seed);
+  SMLHeader h;
+  memset(&h, 0, sizeof(h));
+  const SMLHeader& r = sml.hdr();
+  h.alphabet_bits = r.alphabet_bits;
+  h.seed = r.seed;
+  h.seed_length = r.seed_length;
+  h.seed_weight = r.seed_weight;
+  h.length = r.length;
+  h.unique_mers = r.unique_mers;
+  h.id = r.id;
+  h.circular = r.circular;
+  memcpy(h.translation_table, r.translation_table, sizeof(h.translation_table));
+  h.description[0] = r.description[0];
+  memcpy(header_out, &h, sizeof(h));
+  if (sml.nwords() > cap_words) return -1;
+  memcpy(words_out, sml.words(), sml.nwords() * 4);
+  return (int64_t)sml.nwords();
 }
 
 // Canonical seed mer at every position, in position order (the unsorted fill).
