@@ -572,6 +572,11 @@ static int run_ring(Ctx* c, const TbLanes& L, const DpInputs& in, const std::vec
   return 0;
 }
 
+// Whole-matrix problems with at least this many rows run in the full DP's
+// launch (strips of 32 * dp_rows rows), shorter ones in the banded strip
+// launch (32 * band_rows rows).
+constexpr int64_t kWholeFullRows = 1024;
+
 // Every base code must be 0..3 (the kernels mask to 2 bits; this reports it).
 static int check_codes(Ctx* c, const uint8_t* d_sa, uint64_t na, const uint8_t* d_sb, uint64_t nb) {
   k_check_codes<<<grid_for(na / 16 + 1, 256), 256, 0, c->stream>>>(d_sa, na, c->d_err);
@@ -660,7 +665,7 @@ int gapdp_banded_dev(Ctx* c, const uint8_t* d_sa, const uint64_t* d_oa, const ui
   // on the ring schedule with the smallest valid group height, or in the
   // strip kernel when no height is valid (or the ring kernel is switched off).
   static const int kRingRows[4] = {4, 8, 16, 32};  // smallest first
-  std::vector<uint32_t> ids, rids;
+  std::vector<uint32_t> ids, rids, wids;
   std::vector<uint8_t> rsel;
   std::vector<uint8_t> whole(nprob, 0);
   for (int64_t p = 0; p < nprob; ++p) {
@@ -682,7 +687,9 @@ int gapdp_banded_dev(Ctx* c, const uint8_t* d_sa, const uint64_t* d_oa, const ui
       dv[p] = 0;
       hv[p] = (int32_t)std::max(la[p], lb[p]) + 2;
       bc += full;
-      ids.push_back((uint32_t)p);
+      // long ones through the full DP's taller strips, short ones beside
+      // the strip kernel's bands
+      (la[p] >= kWholeFullRows ? wids : ids).push_back((uint32_t)p);
       continue;
     }
     int rr = 0;
@@ -729,6 +736,10 @@ int gapdp_banded_dev(Ctx* c, const uint8_t* d_sa, const uint64_t* d_oa, const ui
     if (rc) return rc;
     MVG_CUDA_TRY(cudaEventRecord(c->join, c->aux));
   }
+  if (!wids.empty()) {
+    rc = run_dp(c, in, wids, la, lb, nullptr, nullptr, nullptr, nullptr, nullptr, &strip_lanes);
+    if (rc) return rc;
+  }
   if (!ids.empty()) {
     rc = run_dp(c, in, ids, la, lb, d_delta, d_half, &dv, &hv, d_accept, &strip_lanes);
     if (rc) return rc;
@@ -743,7 +754,7 @@ int gapdp_banded_dev(Ctx* c, const uint8_t* d_sa, const uint64_t* d_oa, const ui
   std::vector<uint32_t> fallback;
   for (int64_t p = 0; p < nprob; ++p) {
     if (whole[p]) {
-      if (!acc[p]) return report_error(MVG_ERR_DEVICE, "whole-matrix band failed its check");
+      if (!acc[p] && la[p] < kWholeFullRows) return report_error(MVG_ERR_DEVICE, "whole-matrix band failed its check");
       acc[p] = 2;  // not banded: the proposed band covered most of the matrix
     } else if (!acc[p]) {
       fallback.push_back((uint32_t)p);

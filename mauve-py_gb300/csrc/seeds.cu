@@ -14,6 +14,8 @@
 //                   a genome bit below the SML key, sorted once.
 #include <string.h>
 
+#include <algorithm>
+
 #include "mvg_internal.h"
 #include "prim.cuh"
 
@@ -120,10 +122,11 @@ __global__ void k_seed_keys(const uint32_t* __restrict__ g, uint64_t count, Seed
 // Both genomes' keys in one array for the pairwise matcher: the SML key
 // (seed bits, strand bit) followed by a genome bit (A = 0, B = 1); values are
 // positions.  Sorted stably, every seed's occurrences in the two genomes are
-// adjacent, each genome's in position order.  One block writes one sort tile
-// and also counts its digits for the sort: every pass's global digit counts
-// (ghist, added atomically) and the first pass's tile counts (counts0,
-// digit-major); both may be null.
+// adjacent, each genome's in position order.  Blocks build the seed's gather
+// table once and then take sort tiles of os::kTile positions in turn; for
+// each tile they also count its digits for the sort: every pass's global
+// digit counts (ghist, added atomically) and the first pass's tile counts
+// (counts0, digit-major); both may be null.
 template <typename K>
 __global__ void __launch_bounds__(256) k_seed_keys_pair(const uint32_t* __restrict__ ga, uint64_t ca,
                                                         const uint32_t* __restrict__ gb, uint64_t cb, SeedDesc s,
@@ -134,32 +137,43 @@ __global__ void __launch_bounds__(256) k_seed_keys_pair(const uint32_t* __restri
   __shared__ uint64_t lut[8][256];
   const int tid = threadIdx.x;
   const bool hist = ghist != nullptr;
-  if (hist)
-    for (int q = 0; q < npass; ++q) h[q][tid] = 0;
   seed_lut_build(s, lut);
-  __syncthreads();
   const int nb = seed_bytes(s);
   const int shift = 64 - 2 * s.w;
   const uint64_t n = ca + cb;
-  const uint64_t base = (uint64_t)blockIdx.x * os::kTile;
-#pragma unroll 2
-  for (int k = 0; k < os::kItems; ++k) {
-    const uint64_t p = base + (uint64_t)k * 256 + tid;
-    if (p >= n) break;
-    const bool in_b = p >= ca;
-    const uint64_t q = in_b ? p - ca : p;
-    const uint64_t m = canonical_mer_lut(in_b ? gb : ga, q, lut, nb, s.w);
-    const K key = (K)(((((m >> shift) << 1) | (m & 1ull)) << 1) | (in_b ? 1ull : 0ull));
-    keys[p] = key;
-    pos[p] = (uint32_t)q;
+  uint32_t gsum[8];
+#pragma unroll
+  for (int d = 0; d < 8; ++d) gsum[d] = 0;
+  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     if (hist)
-      for (int d = 0; d < npass; ++d) atomicAdd(&h[d][(uint32_t)(key >> (8 * d)) & 255u], 1u);
+      for (int q = 0; q < npass; ++q) h[q][tid] = 0;
+    __syncthreads();
+    const uint64_t base = (uint64_t)tile * os::kTile;
+#pragma unroll 2
+    for (int k = 0; k < os::kItems; ++k) {
+      const uint64_t p = base + (uint64_t)k * 256 + tid;
+      if (p >= n) break;
+      const bool in_b = p >= ca;
+      const uint64_t q = in_b ? p - ca : p;
+      const uint64_t m = canonical_mer_lut(in_b ? gb : ga, q, lut, nb, s.w);
+      const K key = (K)(((((m >> shift) << 1) | (m & 1ull)) << 1) | (in_b ? 1ull : 0ull));
+      keys[p] = key;
+      pos[p] = (uint32_t)q;
+      if (hist)
+        for (int d = 0; d < npass; ++d) atomicAdd(&h[d][(uint32_t)(key >> (8 * d)) & 255u], 1u);
+    }
+    if (hist) {
+      __syncthreads();
+      counts0[(int64_t)tid * ntiles + tile] = h[0][tid];
+#pragma unroll
+      for (int d = 0; d < 8; ++d)
+        if (d < npass) gsum[d] += h[d][tid];
+    }
   }
   if (hist) {
-    __syncthreads();
-    counts0[(int64_t)tid * ntiles + blockIdx.x] = h[0][tid];
-    for (int d = 0; d < npass; ++d)
-      if (h[d][tid]) atomicAdd(&ghist[d * 256 + tid], h[d][tid]);
+#pragma unroll
+    for (int d = 0; d < 8; ++d)
+      if (d < npass && gsum[d]) atomicAdd(&ghist[d * 256 + tid], gsum[d]);
   }
 }
 
@@ -274,13 +288,13 @@ static int pair_sort_impl(Ctx* c, const uint32_t* ga, uint64_t ca, const uint32_
     const int npass = (nbits + 7) / 8;
     uint32_t* ghist = rts_ghist(scr, (int64_t)count);
     MVG_CUDA_TRY(cudaMemsetAsync(ghist, 0, (size_t)npass * 256 * 4, c->stream));
-    k_seed_keys_pair<K><<<(unsigned)ntiles, 256, 0, c->stream>>>(ga, ca, gb, cb, s, k0, v0, npass, rts_counts(scr),
-                                                                 ntiles, ghist);
+    k_seed_keys_pair<K><<<(unsigned)std::min<int64_t>(ntiles, 152 * 4), 256, 0, c->stream>>>(
+        ga, ca, gb, cb, s, k0, v0, npass, rts_counts(scr), ntiles, ghist);
     c->launches++;
     which = rts_sort_pairs<K>(k0, v0, k1, v1, (int64_t)count, nbits, scr, c->stream, &c->launches, true);
   } else {
-    k_seed_keys_pair<K><<<(unsigned)ntiles, 256, 0, c->stream>>>(ga, ca, gb, cb, s, k0, v0, 0, nullptr, ntiles,
-                                                                 nullptr);
+    k_seed_keys_pair<K><<<(unsigned)std::min<int64_t>(ntiles, 152 * 4), 256, 0, c->stream>>>(
+        ga, ca, gb, cb, s, k0, v0, 0, nullptr, ntiles, nullptr);
     c->launches++;
     which = sort_pairs<K>(k0, v0, k1, v1, (int64_t)count, nbits, scr, c->stream, &c->launches, c->d_err);
   }

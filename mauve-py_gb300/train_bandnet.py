@@ -237,11 +237,11 @@ def train(args):
     import synth  # noqa: F401
     vb = DeviceBatch(*subset_host_idx(tr, np.sort(val_idx)), dev)
     best = None
-    for gate in (0, 24, 26):
+    for gate in (0, 22, 24):
         ctx.set_band_gate(gate)
-        for whole in (0.35, 0.5, 0.7, 0.9):
+        for whole in (0.35, 0.5, 0.7):
             ctx.set_band_whole_fraction(whole)
-            for alpha in (0.9, 1.0, 1.15, 1.3, 1.5):
+            for alpha in (0.9, 1.0, 1.15, 1.3):
                 for beta in (0.0, 16.0, 48.0):
                     d, h = net.propose_dev(*vb.ptrs(), vb.n, alpha, beta)
                     secs, used, cells, *_ = timed_banded(ctx, vb, d, h)
