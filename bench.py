@@ -152,6 +152,8 @@ LB_NPROB = 200_000
 # pair, from one ncu capture (profiles/anchoring_launch_list_recoded_pair.md);
 # below the algorithmic bytes because the sort passes' outputs stay in L2
 SEED_PATH_TRAFFIC = 0.61e9
+# stages of the seed path (pack, seed keys, bucket or radix sort, unique-pair join)
+SEED_STAGES = ("pack", "sml_sort", "seed_scatter", "seed_local", "unique_join")
 
 
 def learned_band_section(ctx, args, dev, stream, rank):
@@ -476,7 +478,7 @@ def run_gb300(args, world, rank, local):
         hbm_peak, peak_kind = peaks()
         P = (2 * w + 1 + 7) // 8
         per_base = 24.25 + 24 * P  # seed path bytes per base per genome
-        seed_ms = sum(stage_tot.get(k, 0.0) for k in ("pack", "sml_sort", "unique_join")) / args.steps
+        seed_ms = sum(stage_tot.get(k, 0.0) for k in SEED_STAGES) / args.steps
         seed_bytes = per_base * (na + nb)
         stages = {k: round(v / args.steps, 4) for k, v in stage_tot.items()}
         line.update({

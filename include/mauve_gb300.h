@@ -108,6 +108,12 @@ int mvg_pairwise_matches_dev(mvg_handle h, const uint8_t* d_seq_a, uint64_t na, 
  * [2] = matches, [3] = non-empty hash buckets. */
 int mvg_pairwise_stats(mvg_handle h, uint64_t stats[4]);
 
+/* The seed join groups both genomes' seeds into buckets by the mer's top
+ * bits and sorts each bucket in shared memory when it holds at most cap
+ * seeds, else in chunks through global memory.  cap in 32..3072 (default
+ * 3072); the matches do not depend on it. */
+int mvg_set_pair_bucket_cap(mvg_handle h, int cap);
+
 /* ---------------------------------------------------------------- gap DP */
 
 /* Batched global gap alignment: for each problem p, muscle NWSmall

@@ -144,10 +144,28 @@ MVG_HD bool ring_eligible(const RingBand& b) {
   return true;
 }
 
-// Traceback words of a ring-scheduled problem: each lane stores its R
-// nibbles per step as one stream, nibble s*R + r in word (s*R + r) / 8 of
-// the lane; word x of lane t sits at x*32 + t.
-MVG_HD uint64_t ring_tb_words(const RingBand& b) { return (uint64_t)((b.steps * b.R + 7) / 8) * 32; }
+// Traceback layout of a ring-scheduled problem: each lane stores its R
+// nibbles per step as one stream.  When R divides 8, 8 / R steps share a
+// word (nibble r of step s at nibble R*(s mod 8/R) + r of word s / (8/R));
+// otherwise a step takes ceil(R / 8) words (nibble r in word s*NW + r/8 at
+// nibble r mod 8).  Word x of lane t sits at x*32 + t.
+MVG_HD int ring_steps_per_word(int R) { return (R < 8 && 8 % R == 0) ? 8 / R : 1; }
+MVG_HD int ring_words_per_step(int R) { return (R + 7) / 8; }
+MVG_HD void ring_tb_at(int R, int64_t s, int r, int64_t& word, int& shift) {
+  const int per = ring_steps_per_word(R);
+  if (per > 1) {
+    word = s / per;
+    shift = 4 * (R * (int)(s % per) + r);
+  } else {
+    word = s * ring_words_per_step(R) + (r >> 3);
+    shift = 4 * (r & 7);
+  }
+}
+MVG_HD uint64_t ring_tb_words(const RingBand& b) {
+  const int per = ring_steps_per_word(b.R);
+  const uint64_t w = per > 1 ? (uint64_t)((b.steps + per - 1) / per) : (uint64_t)b.steps * ring_words_per_step(b.R);
+  return w * 32;
+}
 
 // Matrix cells inside the kept region (rows 1..LA, columns 1..LB).
 MVG_HD uint64_t ring_cells(const RingBand& b) {

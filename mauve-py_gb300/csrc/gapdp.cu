@@ -71,9 +71,28 @@ template __global__ void k_gapdp_t<true, 8>(DpJob);
 template __global__ void k_gapdp_t<true, 2>(DpJob);
 template __global__ void k_gapdp_t<true, 1>(DpJob);
 template __global__ void k_gapdp_ring<4>(RingJob);
+template __global__ void k_gapdp_ring<6>(RingJob);
 template __global__ void k_gapdp_ring<8>(RingJob);
+template __global__ void k_gapdp_ring<12>(RingJob);
 template __global__ void k_gapdp_ring<16>(RingJob);
+template __global__ void k_gapdp_ring<24>(RingJob);
 template __global__ void k_gapdp_ring<32>(RingJob);
+
+// The group heights the ring schedule offers, smallest first.
+static const int kRingRows[] = {4, 6, 8, 12, 16, 24, 32};
+constexpr int kRingHeights = (int)(sizeof(kRingRows) / sizeof(kRingRows[0]));
+
+static void (*ring_kernel(int R))(RingJob) {
+  switch (R) {
+    case 4: return k_gapdp_ring<4>;
+    case 6: return k_gapdp_ring<6>;
+    case 8: return k_gapdp_ring<8>;
+    case 12: return k_gapdp_ring<12>;
+    case 16: return k_gapdp_ring<16>;
+    case 24: return k_gapdp_ring<24>;
+    default: return k_gapdp_ring<32>;
+  }
+}
 
 // BitTraceBack from (LA, LB); writes the path reversed at the end of the
 // problem's path slot and its length.  Banded problems index their strips
@@ -523,8 +542,7 @@ static int run_ring(Ctx* c, const TbLanes& L, const DpInputs& in, const std::vec
       int64_t e = a;
       while (e < w1 && rows_of[e] == rows_of[a]) ++e;
       const int R = rows_of[a];
-      void (*kern)(RingJob) = R == 4 ? k_gapdp_ring<4> : R == 8 ? k_gapdp_ring<8> : R == 16 ? k_gapdp_ring<16>
-                                                                                              : k_gapdp_ring<32>;
+      void (*kern)(RingJob) = ring_kernel(R);
       int bps = 0;
       MVG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kern, kRingThreads, 0));
       if (bps < 1) bps = 1;
@@ -664,7 +682,6 @@ int gapdp_banded_dev(Ctx* c, const uint8_t* d_sa, const uint64_t* d_oa, const ui
   // DP's), which spares a second pass for them (status 2).  Other bands run
   // on the ring schedule with the smallest valid group height, or in the
   // strip kernel when no height is valid (or the ring kernel is switched off).
-  static const int kRingRows[4] = {4, 8, 16, 32};  // smallest first
   std::vector<uint32_t> ids, rids, wids;
   std::vector<uint8_t> rsel;
   std::vector<uint8_t> whole(nprob, 0);
@@ -697,7 +714,7 @@ int gapdp_banded_dev(Ctx* c, const uint8_t* d_sa, const uint64_t* d_oa, const ui
       // the lane-reuse condition W <= 32 + 32*R*LB/LA decides most heights;
       // only heights that pass it (with a column of slack) get the exact test
       const double slope = (double)lb[p] / (double)la[p];
-      for (int q = 0; q < 4 && !rr; ++q) {
+      for (int q = 0; q < kRingHeights && !rr; ++q) {
         const int R = kRingRows[q];
         const bool many = (la[p] + R - 1) / R > 32;
         if (many && 2.0 * hv[p] + 2.0 + (R - 1) * slope > 32.0 + 32.0 * R * slope + 2.0) continue;

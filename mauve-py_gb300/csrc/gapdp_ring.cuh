@@ -179,14 +179,23 @@ __device__ void ring_solve(const RingJob& J, uint8_t* ringB, uint8_t* ringA, int
         goA0 = g == 0 ? 0 : kGap;
         topI = g == 0 ? 0 : kNeg;
         int32_t pa = g == 0 ? 0 : chain_pa;
-        const uint32_t* ra = reinterpret_cast<const uint32_t*>(ringA);
+        if constexpr (R % 4 == 0) {  // the group's codes as whole words
+          const uint32_t* ra = reinterpret_cast<const uint32_t*>(ringA);
 #pragma unroll
-        for (int q = 0; q < R / 4; ++q) {
-          const uint32_t c4 = ra[((g * R) >> 2) + q & (kRingA / 4 - 1)];
+          for (int q = 0; q < R / 4; ++q) {
+            const uint32_t c4 = ra[((g * R) >> 2) + q & (kRingA / 4 - 1)];
 #pragma unroll
-          for (int k = 0; k < 4; ++k) {
-            const int r = 4 * q + k;
-            const uint32_t code = (c4 >> (8 * k)) & 3u;
+            for (int k = 0; k < 4; ++k) {
+              const int r = 4 * q + k;
+              const uint32_t code = (c4 >> (8 * k)) & 3u;
+              L.arow[r] = c_score_rows[code];
+              if (r < rows_here) pa += best_of(J.base_max, code);
+            }
+          }
+        } else {
+#pragma unroll
+          for (int r = 0; r < R; ++r) {
+            const uint32_t code = ringA[(g * R + r) & (kRingA - 1)] & 3u;
             L.arow[r] = c_score_rows[code];
             if (r < rows_here) pa += best_of(J.base_max, code);
           }
@@ -325,7 +334,7 @@ __device__ void ring_solve(const RingJob& J, uint8_t* ringB, uint8_t* ringA, int
       pubD = kNeg;
       pubI = kNeg;
     }
-    if constexpr (R < 8) {
+    if constexpr (R < 8 && 8 % R == 0) {
       constexpr int kPer = 8 / R;
       acc |= nw[0] << (4 * R * (s % kPer));
       if ((s % kPer) == kPer - 1 || s == S - 1) {
@@ -428,8 +437,10 @@ __global__ void k_traceback_ring(const uint64_t* __restrict__ oa, const uint64_t
           set_error(err, kDevCapacity);
           break;
         }
-        const int64_t nib = (int64_t)(pb + g - b.lo0) * R + r;
-        bits = (T[(nib >> 3) * 32 + (g & 31)] >> (4 * (nib & 7))) & 15u;
+        int64_t word;
+        int sh;
+        ring_tb_at(R, (int64_t)(pb + g - b.lo0), r, word, sh);
+        bits = (T[word * 32 + (g & 31)] >> sh) & 15u;
       }
       char next;
       if (cur == 'M') {

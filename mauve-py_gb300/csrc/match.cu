@@ -135,6 +135,30 @@ __global__ void __launch_bounds__(256) k_pair_emit(const K* __restrict__ keys, c
   }
 }
 
+// The same hash entries from pairs staged per seed-join bucket
+// (pair_buckets.cu): bucket b's pairs go to slots pbase[b] .. in order.
+__global__ void __launch_bounds__(256) k_stage_emit(const uint2* __restrict__ stage, const uint32_t* __restrict__ bstart,
+                                                    const uint32_t* __restrict__ pcount,
+                                                    const uint32_t* __restrict__ pbase, int L, Mhe* __restrict__ mhe,
+                                                    uint32_t* __restrict__ bucket, uint32_t* __restrict__ order) {
+  const int b = blockIdx.x;
+  const uint32_t np = pcount[b], s0 = bstart[b], j0 = pbase[b];
+  for (uint32_t q = threadIdx.x; q < np; q += blockDim.x) {
+    const uint2 e = stage[s0 + q];
+    Mhe m;
+    m.s0 = (int64_t)e.x + 1;
+    m.s1 = (int64_t)(e.y & 0x7fffffffu) + 1;
+    m.len = L;
+    if (e.y >> 31) m.s1 = -m.s1;
+    m.off = m.s1 - m.s0;
+    if (m.s1 < 0) m.off -= m.len;
+    const int64_t t = kTableSize;
+    mhe[j0 + q] = m;
+    bucket[j0 + q] = (uint32_t)(((m.off % t) + t) % t);
+    order[j0 + q] = j0 + q;
+  }
+}
+
 // ------------------------------------------------------- bucket replay
 
 // LM/MatchHashEntry.cpp:164-200 (Contains), two genomes, both present.
@@ -812,21 +836,37 @@ int pairwise_matches_dev(Ctx* c, const uint8_t* d_a, uint64_t na, const uint8_t*
   const uint64_t ca = na >= (uint64_t)s.L ? na - s.L + 1 : 0;
   const uint64_t cb = nb >= (uint64_t)s.L ? nb - s.L + 1 : 0;
   if (ca == 0 || cb == 0) return check_device_error(c);
+  // 32-bit keys up to 2^25 of them: the bucketed join; otherwise one sort
+  // of both genomes' keys and a join over its runs
+  const bool bucketed = 2 * s.w + 2 <= 32 && ca + cb <= kPairBucketMaxKeys;
   SmlKeys sk;
+  PairStage ps;
+  int64_t nk = 0, ptiles = 0;
+  uint32_t* pbs = nullptr;
+  uint32_t* d_npairs = nullptr;
   stage_mark(c, "sml_sort");
-  if ((rc = pair_sort(c, ga, ca, gb, cb, s, &sk))) return rc;
-  stage_mark(c, "unique_join");
-  const int64_t nk = (int64_t)sk.count;
-  const int64_t ptiles = (nk + kPairTile - 1) / kPairTile;
-  uint32_t* pbs = (uint32_t*)ws.get(c, 37, (ptiles + 4) * 4 + 64);
-  if (!pbs) return report_error(MVG_ERR_NOMEM, "workspace allocation failed");
-  uint32_t* d_npairs = pbs + ptiles + 2;
-  if (sk.wide)
-    k_pair_count<uint64_t><<<(unsigned)ptiles, 256, 0, c->stream>>>((const uint64_t*)sk.keys, nk, pbs);
-  else
-    k_pair_count<uint32_t><<<(unsigned)ptiles, 256, 0, c->stream>>>((const uint32_t*)sk.keys, nk, pbs);
-  k_scan_bsums<<<1, 256, 0, c->stream>>>(pbs, ptiles, d_npairs);
-  c->launches += 2;
+  if (bucketed) {
+    if ((rc = pair_buckets(c, ga, ca, gb, cb, s, &ps))) return rc;
+    stage_mark(c, "unique_join");
+    uint32_t* sscr = (uint32_t*)ws.get(c, 34, (scan_scratch_words(ps.nbuckets) + 8) * 4);
+    if (!sscr) return report_error(MVG_ERR_NOMEM, "workspace allocation failed");
+    d_npairs = sscr + scan_scratch_words(ps.nbuckets) + 1;
+    exclusive_scan(ps.pcount, ps.pbase, ps.nbuckets, sscr, d_npairs, c->stream, &c->launches);
+  } else {
+    if ((rc = pair_sort(c, ga, ca, gb, cb, s, &sk))) return rc;
+    stage_mark(c, "unique_join");
+    nk = (int64_t)sk.count;
+    ptiles = (nk + kPairTile - 1) / kPairTile;
+    pbs = (uint32_t*)ws.get(c, 37, (ptiles + 4) * 4 + 64);
+    if (!pbs) return report_error(MVG_ERR_NOMEM, "workspace allocation failed");
+    d_npairs = pbs + ptiles + 2;
+    if (sk.wide)
+      k_pair_count<uint64_t><<<(unsigned)ptiles, 256, 0, c->stream>>>((const uint64_t*)sk.keys, nk, pbs);
+    else
+      k_pair_count<uint32_t><<<(unsigned)ptiles, 256, 0, c->stream>>>((const uint32_t*)sk.keys, nk, pbs);
+    k_scan_bsums<<<1, 256, 0, c->stream>>>(pbs, ptiles, d_npairs);
+    c->launches += 2;
+  }
   MVG_CUDA_TRY(cudaMemcpyAsync(c->h_scalars, d_npairs, 4, cudaMemcpyDeviceToHost, c->stream));
   MVG_CUDA_TRY(cudaStreamSynchronize(c->stream));
   const int64_t npairs = (int64_t)(uint32_t)c->h_scalars[0];
@@ -860,7 +900,10 @@ int pairwise_matches_dev(Ctx* c, const uint8_t* d_a, uint64_t na, const uint8_t*
   unsigned long long* d_coll = (unsigned long long*)(((uintptr_t)(tot + 4) + 7) & ~(uintptr_t)7);
 
   stage_mark(c, "hash_bucket_sort");
-  if (sk.wide)
+  if (bucketed)
+    k_stage_emit<<<(unsigned)ps.nbuckets, 256, 0, c->stream>>>(ps.stage, ps.bstart, ps.pcount, ps.pbase, s.L, mhe,
+                                                               bk0, or0);
+  else if (sk.wide)
     k_pair_emit<uint64_t><<<(unsigned)ptiles, 256, 0, c->stream>>>((const uint64_t*)sk.keys, sk.pos, nk, pbs, s.L,
                                                                    mhe, bk0, or0);
   else

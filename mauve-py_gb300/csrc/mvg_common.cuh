@@ -112,6 +112,43 @@ __device__ __forceinline__ uint64_t canonical_mer_lut(const uint32_t* __restrict
   return f < r ? f : r;
 }
 
+// The same table for seeds of weight w <= 15: the mer left-aligned in 32
+// bits (the top 2w bits), so a lookup is one 4-byte word.
+__device__ __forceinline__ void seed_lut_build32(const SeedDesc& s, uint32_t (*lut)[256]) {
+  const int nb = seed_bytes(s);
+  for (int e = threadIdx.x; e < nb * 256; e += blockDim.x) {
+    const int c = e >> 8, b = e & 255;
+    uint32_t v = 0;
+#pragma unroll
+    for (int kk = 0; kk < 4; ++kk) {
+      const int k = 4 * c + kk;
+      if (k < s.L && ((s.pattern >> (s.L - 1 - k)) & 1ull)) {
+        const int o = k == 0 ? 0 : __popcll(s.pattern >> (s.L - k));
+        v |= (uint32_t)((b >> (6 - 2 * kk)) & 3) << (30 - 2 * o);
+      }
+    }
+    lut[c][b] = v;
+  }
+}
+
+// revcomp_mer in 32 bits (w <= 15): the reverse complement left-aligned,
+// bit 0 set as the reverse-strand flag; min(f, revcomp32(f)) orders exactly
+// as the 64-bit pair does.
+__device__ __forceinline__ uint32_t revcomp_mer32(uint32_t mer, int w) {
+  uint32_t r = __brev(~mer);
+  r = ((r >> 1) & 0x55555555u) | ((r & 0x55555555u) << 1);
+  return (r << (32 - 2 * w)) | 1u;
+}
+
+// The forward mer of the position u bases into a 64-bit window (u + L <= 32).
+__device__ __forceinline__ uint32_t gather_mer32(uint64_t win, int u, const uint32_t (*lut)[256], int nb) {
+  uint32_t f = 0;
+#pragma unroll
+  for (int c = 0; c < 8; ++c)
+    if (c < nb) f |= lut[c][(uint32_t)(win >> (56 - 8 * c - 2 * u)) & 255u];
+  return f;
+}
+
 inline int div_up(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
 
 }  // namespace mvg

@@ -43,6 +43,7 @@ struct Ctx {
   double band_whole = 0.5;    // bands covering at least this share of their matrix run whole
   int band_ring = 1;          // banded problems on the ring schedule where it is valid
   int band_gate = 0;          // band proposals: divergence gate window threshold (0 = off)
+  int pair_bucket_cap = 3072;  // seed-join buckets sorted in shared memory up to this size
   Workspace ws;
   MatchStats stats;
   bool profiling = false;
@@ -80,6 +81,23 @@ int pack_sequence(Ctx* c, const uint8_t* d_seq, uint64_t n, uint32_t* d_packed);
 int sml_sort(Ctx* c, const uint32_t* d_packed, uint64_t count, const SeedDesc& s, uint32_t* d_pos_out,
              uint64_t* d_mer_out, SmlKeys* keep, int slot_base);
 // Both genomes' keys ((seed bits, strand, genome) with A = 0) sorted in one array.
+// The bucketed seed join (pair_buckets.cu) for 32-bit keys and at most
+// kPairBucketMaxKeys keys: pairs staged per bucket in mer order.
+constexpr uint64_t kPairBucketMaxKeys = 1ull << 25;
+struct PairBucketGeom {
+  int bbits, nbuckets, npass, dbits, lbits, spass, sbits;
+  int64_t tile, ntiles, nchunks;
+};
+PairBucketGeom pair_bucket_geom(uint64_t n, int w);
+struct PairStage {
+  const uint2* stage = nullptr;   // bucket b's pairs at stage[bstart[b] ..]: (pos A, pos B | reverse << 31)
+  const uint32_t* bstart = nullptr;
+  uint32_t* pcount = nullptr;     // pairs per bucket
+  uint32_t* pbase = nullptr;      // room for their exclusive scan
+  int nbuckets = 0;
+};
+int pair_buckets(Ctx* c, const uint32_t* ga, uint64_t ca, const uint32_t* gb, uint64_t cb, const SeedDesc& s,
+                 PairStage* out);
 int pair_sort(Ctx* c, const uint32_t* ga, uint64_t ca, const uint32_t* gb, uint64_t cb, const SeedDesc& s,
               SmlKeys* out);
 int check_device_error(Ctx* c);

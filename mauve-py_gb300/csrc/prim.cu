@@ -22,19 +22,23 @@ __global__ void k_scan_reduce(const uint32_t* __restrict__ in, int64_t n, uint32
 }
 
 __global__ void k_scan_bsums(uint32_t* __restrict__ bsum, int64_t nb, uint32_t* __restrict__ total) {
-  __shared__ uint32_t carry;
-  if (threadIdx.x == 0) carry = 0;
-  __syncthreads();
-  for (int64_t c = 0; c < nb; c += 256) {
-    int64_t i = c + threadIdx.x;
-    uint32_t v = i < nb ? bsum[i] : 0;
-    uint32_t tot;
-    __shared__ uint32_t ctot;
-    uint32_t ex = block_excl_scan256(v, &ctot);
-    (void)tot;
-    if (i < nb) bsum[i] = carry + ex;
-    __syncthreads();
-    if (threadIdx.x == 0) carry += ctot;
+  __shared__ uint32_t ctot;
+  uint32_t carry = 0;
+  for (int64_t c = 0; c < nb; c += 256 * 8) {  // 8 consecutive sums per thread
+    const int64_t i0 = c + (int64_t)threadIdx.x * 8;
+    uint32_t v[8], sum = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      v[k] = i0 + k < nb ? bsum[i0 + k] : 0u;
+      sum += v[k];
+    }
+    uint32_t run = carry + block_excl_scan256(sum, &ctot);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      if (i0 + k < nb) bsum[i0 + k] = run;
+      run += v[k];
+    }
+    carry += ctot;
     __syncthreads();
   }
   if (threadIdx.x == 0 && total) *total = carry;
@@ -70,36 +74,57 @@ void exclusive_scan(const uint32_t* in, uint32_t* out, int64_t n, uint32_t* scra
   if (launches) *launches += 3;
 }
 
-__global__ void __launch_bounds__(256) k_os_scan(uint32_t* __restrict__ ghist) {
-  uint32_t* g = ghist + blockIdx.x * 256;
-  const uint32_t v = g[threadIdx.x];
-  const uint32_t ex = block_excl_scan256(v, nullptr);
-  g[threadIdx.x] = ex;
-}
-
-// Block d: offsets[d][t] = gstart[d] + counts[d][0] + ... + counts[d][t-1].
-__global__ void __launch_bounds__(256) k_rts_rowscan(uint32_t* __restrict__ counts, int64_t ntiles,
-                                                     const uint32_t* __restrict__ gstart) {
-  uint32_t* row = counts + (int64_t)blockIdx.x * ntiles;
-  __shared__ uint32_t tot;
-  uint32_t carry = gstart[blockIdx.x];
-  for (int64_t c = 0; c < ntiles; c += 256 * 8) {
-    const int64_t i0 = c + (int64_t)threadIdx.x * 8;
-    uint32_t v[8];
-    uint32_t sum = 0;
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {
-      v[k] = i0 + k < ntiles ? row[i0 + k] : 0u;
-      sum += v[k];
-    }
-    uint32_t run = carry + block_excl_scan256(sum, &tot);
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {
-      if (i0 + k < ntiles) row[i0 + k] = run;
-      run += v[k];
-    }
-    carry += tot;
-    __syncthreads();
+// Block c of nchunks, 1024 threads: thread (q, d) takes digit d over every
+// fourth chunk sum (from q) and over quarter q of chunk c's tiles.
+//   offset(t, d) = start(d) + sum of d's counts in chunks before c
+//                + sum of d's counts in tiles of chunk c before t
+// where start(d) is the number of keys with a smaller digit.
+__global__ void __launch_bounds__(1024) k_rts_offsets(uint32_t* __restrict__ counts, int64_t ntiles,
+                                                      const uint32_t* __restrict__ csum, int64_t ctiles,
+                                                      int64_t nchunks) {
+  const int d = threadIdx.x & 255, q = threadIdx.x >> 8;
+  const int64_t c = blockIdx.x;
+  __shared__ uint32_t s_before[4][256], s_tot[4][256], s_part[4][256];
+  __shared__ uint32_t wtot[8];
+  uint32_t tot = 0, before = 0;
+#pragma unroll 8
+  for (int64_t cc = q; cc < nchunks; cc += 4) {
+    const uint32_t v = csum[cc * 256 + d];
+    tot += v;
+    before += cc < c ? v : 0u;
+  }
+  const int64_t per = (ctiles + 3) / 4;
+  const int64_t t0 = c * ctiles + q * per;
+  const int64_t t1 = min(ntiles, min(c * ctiles + ctiles, t0 + per));
+  uint32_t part = 0;
+#pragma unroll 8
+  for (int64_t t = t0; t < t1; ++t) part += counts[t * 256 + d];
+  s_before[q][d] = before;
+  s_tot[q][d] = tot;
+  s_part[q][d] = part;
+  __syncthreads();
+  uint32_t T = 0, inc = 0;
+  if (q == 0) {
+    T = s_tot[0][d] + s_tot[1][d] + s_tot[2][d] + s_tot[3][d];
+    inc = warp_incl_scan(T);
+    if ((d & 31) == 31) wtot[d >> 5] = inc;
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    const uint32_t x = threadIdx.x < 8 ? wtot[threadIdx.x] : 0u;
+    const uint32_t y = warp_incl_scan(x);
+    if (threadIdx.x < 8) wtot[threadIdx.x] = y - x;
+  }
+  __syncthreads();
+  if (q == 0) s_tot[0][d] = wtot[d >> 5] + inc - T;  // start(d)
+  __syncthreads();
+  uint32_t run = s_tot[0][d] + s_before[0][d] + s_before[1][d] + s_before[2][d] + s_before[3][d];
+  for (int k = 0; k < q; ++k) run += s_part[k][d];
+#pragma unroll 8
+  for (int64_t t = t0; t < t1; ++t) {
+    const uint32_t x = counts[t * 256 + d];
+    counts[t * 256 + d] = run;
+    run += x;
   }
 }
 

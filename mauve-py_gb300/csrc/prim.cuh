@@ -187,225 +187,61 @@ int radix_sort_pairs(K* keys, uint32_t* vals, K* keys_alt, uint32_t* vals_alt, i
   return which;
 }
 
-// ------------------------------------------------- one-sweep radix sort
+// ------------------------------------- reduce-then-scan radix sort
 //
-// Same stable LSD result as radix_sort_pairs, one kernel per 8-bit digit:
-//   k_os_hist   all passes' digit histograms in one read of the keys
-//   k_os_scan   exclusive scan of each pass's 256 counts
-//   k_os_pass   per tile (claimed in order through an atomic counter): keys
-//               and values held in registers, the tile's digit counts
-//               published at once, the counts of all earlier tiles gathered
-//               by decoupled look-back (each state word carries a flag and
-//               a 30-bit count in one 32-bit store), the tile ranked stably
-//               in shared memory and written out digit run by digit run.
-// A tile only waits for tiles claimed before it, which are already running,
-// so the look-back always finishes; each wait is still bounded and a give-up
-// raises kDevWatchdog.  n must stay below 2^30.
+// Stable LSD sort by 8-bit digits, three kernels per pass and no waits
+// between tiles:
+//   k_rts_count    per tile of kTile keys: its 256 digit counts, stored
+//                  tile-major (one coalesced 1 KB row per tile), and added
+//                  into the counts of the tile's chunk (ctiles tiles)
+//   k_rts_offsets  one block per chunk: every digit's global start (from
+//                  all chunks' sums) plus the chunks before this one, then
+//                  the chunk's tiles' rows turned into output offsets in
+//                  place
+//   k_rts_scatter  per tile: keys ranked stably in shared memory and
+//                  written out digit run by digit run
+// Rows are read and written whole, so every count access is coalesced; the
+// chunk sums make the offsets kernel a two-level scan with no serial walk
+// over thousands of tiles.
 namespace os {
 constexpr int kThreads = 256;
 constexpr int kItems = 8;
 constexpr int kTile = kThreads * kItems;
-constexpr uint32_t kAgg = 1u << 30, kPre = 2u << 30, kVal = (1u << 30) - 1;
-constexpr long long kSpin = 1ll << 22;
 }  // namespace os
 
-inline int64_t onesweep_scratch_words(int64_t n, int nbits) {
-  const int64_t npass = (nbits + 7) / 8;
-  const int64_t ntiles = (n + os::kTile - 1) / os::kTile;
-  return npass * ntiles * 256 + npass * 256 + npass + 16;
+struct RtsGeom {
+  int64_t ntiles, ctiles, nchunks;
+  int npass;
+};
+
+// Chunks of at least 64 tiles and at most about 128 chunks.
+inline RtsGeom rts_geom(int64_t n, int nbits) {
+  RtsGeom g;
+  g.npass = (nbits + 7) / 8;
+  g.ntiles = (n + os::kTile - 1) / os::kTile;
+  int64_t ct = (g.ntiles + 127) / 128;
+  ct = (ct + 3) & ~3ll;
+  g.ctiles = ct < 64 ? 64 : ct;
+  g.nchunks = (g.ntiles + g.ctiles - 1) / g.ctiles;
+  return g;
 }
 
-template <typename K>
-__global__ void __launch_bounds__(256) k_os_hist(const K* __restrict__ keys, int64_t n, int npass,
-                                                 uint32_t* __restrict__ ghist) {
-  __shared__ uint32_t h[8][256];
-  for (int p = 0; p < 8; ++p) h[p][threadIdx.x] = 0;
-  __syncthreads();
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const K k = keys[i];
-    for (int p = 0; p < npass; ++p) atomicAdd(&h[p][(uint32_t)(k >> (8 * p)) & 255u], 1u);
-  }
-  __syncthreads();
-  for (int p = 0; p < npass; ++p)
-    if (h[p][threadIdx.x]) atomicAdd(&ghist[p * 256 + threadIdx.x], h[p][threadIdx.x]);
+// Scratch layout: the tile count rows (ntiles x 256 words, reused by every
+// pass), then each pass's chunk sums (nchunks x 256 words per pass, zeroed
+// before the sort).  nchunks <= min(ntiles, 128), so sizing by that bound
+// makes a scratch sized for n and nbits fit every smaller sort.
+inline int64_t rts_scratch_words(int64_t n, int nbits) {
+  const RtsGeom g = rts_geom(n, nbits);
+  const int64_t cap = g.ntiles < 128 ? g.ntiles : 128;
+  return g.ntiles * 256 + (int64_t)g.npass * cap * 256 + 16;
 }
+inline uint32_t* rts_counts(uint32_t* scratch) { return scratch; }
+inline uint32_t* rts_csum(uint32_t* scratch, const RtsGeom& g) { return scratch + g.ntiles * 256; }
 
-// Exclusive scan of each pass's 256 digit counts (one block per pass).
-__global__ void k_os_scan(uint32_t* __restrict__ ghist);
-
-template <typename K>
-__global__ void __launch_bounds__(os::kThreads, sizeof(K) == 4 ? 4 : 3) k_os_pass(const K* __restrict__ kin, const uint32_t* __restrict__ vin,
-                                                         K* __restrict__ kout, uint32_t* __restrict__ vout, int64_t n,
-                                                         int shift, const uint32_t* __restrict__ gstart,
-                                                         uint32_t* state, uint32_t* tile_ctr, uint32_t* err) {
-  using namespace os;
-  __shared__ K skey[kTile];
-  __shared__ uint32_t sval[kTile];
-  __shared__ uint32_t whist[8][256];  // per-warp digit counts, then per-warp offsets
-  __shared__ uint32_t lstart[256];
-  __shared__ uint32_t gbase[256];
-  __shared__ uint32_t s_tile;
-  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-  if (tid == 0) s_tile = atomicAdd(tile_ctr, 1u);
-#pragma unroll
-  for (int w = 0; w < 8; ++w) whist[w][tid] = 0;
-  __syncthreads();
-  const int64_t tile = s_tile;
-  const int64_t base = tile * kTile;
-  const int tile_n = (int)min((int64_t)kTile, n - base);
-  // warp w owns tile items [256 w, 256 w + 256): item 256 w + 32 k + lane
-  K key[kItems];
-  uint32_t val[kItems], dig[kItems], rank[kItems];
-  const uint32_t lt_mask = (1u << lane) - 1u;
-#pragma unroll
-  for (int k = 0; k < kItems; ++k) {
-    const int li = wid * 256 + 32 * k + lane;
-    if (li < tile_n) {
-      key[k] = kin[base + li];
-      val[k] = vin[base + li];
-      dig[k] = (uint32_t)(key[k] >> shift) & 255u;
-    } else {
-      key[k] = 0;
-      val[k] = 0;
-      dig[k] = 256u + (uint32_t)lane;  // private digit: never shares a rank
-    }
-  }
-  // stable rank inside the warp: earlier rounds, then lower lanes
-#pragma unroll
-  for (int k = 0; k < kItems; ++k) {
-    const uint32_t d = dig[k];
-    const uint32_t peers = __match_any_sync(0xffffffffu, d);
-    const uint32_t before = d < 256u ? whist[wid][d] : 0u;
-    rank[k] = before + __popc(peers & lt_mask);
-    __syncwarp();
-    if (d < 256u && (peers & lt_mask) == 0) whist[wid][d] = before + __popc(peers);
-    __syncwarp();
-  }
-  __syncthreads();
-  // per digit: the tile count and each warp's offset inside the digit's run
-  uint32_t mine = 0;
-#pragma unroll
-  for (int w = 0; w < 8; ++w) {
-    const uint32_t c = whist[w][tid];
-    whist[w][tid] = mine;
-    mine += c;
-  }
-  // publish this tile's counts, then look back over earlier tiles, kWin
-  // tiles per step (independent loads issued together; a tile not yet
-  // published is re-read, bounded)
-  uint32_t* st = state + tile * 256 + tid;
-  *(volatile uint32_t*)st = (tile == 0 ? kPre : kAgg) | mine;
-  constexpr int kWin = 8;
-  uint32_t excl = 0;
-  int64_t t0 = tile - 1;
-  if (t0 >= 0) {
-    // usually the previous tile has its inclusive prefix out already
-    const uint32_t x = *(const volatile uint32_t*)(state + t0 * 256 + tid);
-    if (x & kPre) {
-      excl = x & kVal;
-      t0 = -1;
-    }
-  }
-  for (int64_t t = t0; t >= 0; t -= kWin) {
-    uint32_t v[kWin];
-#pragma unroll
-    for (int q = 0; q < kWin; ++q) v[q] = t - q >= 0 ? *(const volatile uint32_t*)(state + (t - q) * 256 + tid) : kPre;
-    bool done = false;
-#pragma unroll
-    for (int q = 0; q < kWin; ++q) {
-      if (done) break;
-      if (t - q < 0) {
-        done = true;
-        break;
-      }
-      uint32_t x = v[q];
-      const volatile uint32_t* p = state + (t - q) * 256 + tid;
-      long long spins = 0;
-      while ((x & ~kVal) == 0 && ++spins < kSpin) x = *p;
-      if ((x & ~kVal) == 0) {
-        set_error(err, kDevWatchdog);
-        done = true;
-        break;
-      }
-      excl += x & kVal;
-      if (x & kPre) done = true;
-    }
-    if (done) break;
-  }
-  if (tile > 0) *(volatile uint32_t*)st = kPre | (excl + mine);
-  gbase[tid] = gstart[tid] + excl;
-  lstart[tid] = block_excl_scan256(mine, nullptr);
-  __syncthreads();
-#pragma unroll
-  for (int k = 0; k < kItems; ++k) {
-    const uint32_t d = dig[k];
-    if (d < 256u) {
-      const uint32_t lp = lstart[d] + whist[wid][d] + rank[k];
-      skey[lp] = key[k];
-      sval[lp] = val[k];
-    }
-  }
-  __syncthreads();
-  for (int i = tid; i < tile_n; i += kThreads) {
-    const K k = skey[i];
-    const uint32_t d = (uint32_t)(k >> shift) & 255u;
-    const int64_t o = (int64_t)gbase[d] + (i - (int)lstart[d]);
-    kout[o] = k;
-    vout[o] = sval[i];
-  }
-}
-
-// Stable LSD sort of (keys, vals) on bits [0, nbits); returns which buffer
-// holds the result (0 = keys/vals, 1 = alt).  scratch:
-// onesweep_scratch_words(n, nbits) words.  n < 2^30.
-template <typename K>
-int onesweep_sort_pairs(K* keys, uint32_t* vals, K* keys_alt, uint32_t* vals_alt, int64_t n, int nbits,
-                        uint32_t* scratch, cudaStream_t st, uint64_t* launches, uint32_t* err) {
-  if (n <= 0) return 0;
-  const int npass = (nbits + 7) / 8;
-  const int64_t ntiles = (n + os::kTile - 1) / os::kTile;
-  uint32_t* state = scratch;
-  uint32_t* ghist = state + (int64_t)npass * ntiles * 256;
-  uint32_t* ctr = ghist + npass * 256;
-  cudaMemsetAsync(scratch, 0, (size_t)onesweep_scratch_words(n, nbits) * 4, st);
-  int hb = (int)((n + 255) / 256);
-  if (hb > 152 * 8) hb = 152 * 8;
-  k_os_hist<K><<<hb, 256, 0, st>>>(keys, n, npass, ghist);
-  k_os_scan<<<npass, 256, 0, st>>>(ghist);
-  K* ka = keys;
-  K* kb = keys_alt;
-  uint32_t* va = vals;
-  uint32_t* vb = vals_alt;
-  int which = 0;
-  for (int p = 0; p < npass; ++p) {
-    k_os_pass<K><<<(unsigned)ntiles, os::kThreads, 0, st>>>(ka, va, kb, vb, n, 8 * p, ghist + p * 256,
-                                                            state + (int64_t)p * ntiles * 256, ctr + p, err);
-    K* tk = ka;
-    ka = kb;
-    kb = tk;
-    uint32_t* tv = va;
-    va = vb;
-    vb = tv;
-    which ^= 1;
-  }
-  if (launches) *launches += 2 + npass;
-  return which;
-}
-
-// ------------------------------------- reduce-then-scan radix sort
-//
-// The same stable LSD result again, three kernels per 8-bit digit and no
-// waits between tiles: every tile's digit counts first (k_rts_count, one
-// read of the keys), then one block per digit turns its row of tile counts
-// into output offsets (k_rts_rowscan, starting at the digit's global start
-// from k_os_hist), then each tile ranks its keys stably in shared memory
-// and writes them out digit run by digit run (k_rts_scatter).  Compared with
-// one sweep it reads the keys once more per pass but never serialises
-// tiles on their predecessors' prefixes, which with thousands of tiles in
-// flight is the one-sweep pass's critical path.
 template <typename K>
 __global__ void __launch_bounds__(os::kThreads) k_rts_count(const K* __restrict__ keys, int64_t n, int shift,
-                                                            uint32_t* __restrict__ counts, int64_t ntiles) {
+                                                            uint32_t* __restrict__ counts, uint32_t* __restrict__ csum,
+                                                            int64_t ctiles) {
   __shared__ uint32_t h[8][256];
   const int tid = threadIdx.x, wid = tid >> 5;
 #pragma unroll
@@ -425,27 +261,31 @@ __global__ void __launch_bounds__(os::kThreads) k_rts_count(const K* __restrict_
   uint32_t s = 0;
 #pragma unroll
   for (int w = 0; w < 8; ++w) s += h[w][tid];
-  counts[(int64_t)tid * ntiles + blockIdx.x] = s;
+  counts[(int64_t)blockIdx.x * 256 + tid] = s;
+  if (s) atomicAdd(&csum[((int64_t)blockIdx.x / ctiles) * 256 + tid], s);
 }
 
-// Row d of the digit-major count table -> offsets, in place.
-__global__ void k_rts_rowscan(uint32_t* __restrict__ counts, int64_t ntiles, const uint32_t* __restrict__ gstart);
+// Block c, 1024 threads: thread (q, d) handles digit d for a quarter q of
+// the chunk sums and a quarter of chunk c's tiles.
+__global__ void k_rts_offsets(uint32_t* __restrict__ counts, int64_t ntiles, const uint32_t* __restrict__ csum,
+                              int64_t ctiles, int64_t nchunks);
 
 template <typename K>
 __global__ void __launch_bounds__(os::kThreads, sizeof(K) == 4 ? 4 : 3)
     k_rts_scatter(const K* __restrict__ kin, const uint32_t* __restrict__ vin, K* __restrict__ kout,
-                  uint32_t* __restrict__ vout, int64_t n, int shift, const uint32_t* __restrict__ offsets,
-                  int64_t ntiles) {
+                  uint32_t* __restrict__ vout, int64_t n, int shift, const uint32_t* __restrict__ offsets) {
   using namespace os;
-  __shared__ K skey[kTile];
-  __shared__ uint32_t sval[kTile];
-  __shared__ uint32_t whist[8][256];  // per-warp digit counts, then per-warp offsets
-  __shared__ uint32_t lstart[256];
-  __shared__ uint32_t gbase[256];
+  constexpr bool kPacked = sizeof(K) == 4;  // (key, value) as one 8-byte word in shared memory
+  __shared__ __align__(16) uint32_t sbuf[kPacked ? 2 * kTile : kTile * (sizeof(K) / 4 + 1)];
+  __shared__ uint32_t wofs[8][256];  // per-warp digit counts, then each warp's first slot per digit
+  __shared__ uint32_t gofs[256];     // output index of the tile's slot 0 for each digit
+  uint2* skv = reinterpret_cast<uint2*>(sbuf);
+  K* skey = reinterpret_cast<K*>(sbuf);
+  uint32_t* sval = sbuf + kTile * (sizeof(K) / 4);
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
 #pragma unroll
-  for (int w = 0; w < 8; ++w) whist[w][tid] = 0;
-  gbase[tid] = offsets[(int64_t)tid * ntiles + blockIdx.x];
+  for (int w = 0; w < 8; ++w) wofs[w][tid] = 0;
+  const uint32_t gbase = offsets[(int64_t)blockIdx.x * 256 + tid];
   __syncthreads();
   const int64_t base = (int64_t)blockIdx.x * kTile;
   const int tile_n = (int)min((int64_t)kTile, n - base);
@@ -471,85 +311,80 @@ __global__ void __launch_bounds__(os::kThreads, sizeof(K) == 4 ? 4 : 3)
   for (int k = 0; k < kItems; ++k) {
     const uint32_t d = dig[k];
     const uint32_t peers = __match_any_sync(0xffffffffu, d);
-    const uint32_t before = d < 256u ? whist[wid][d] : 0u;
+    const uint32_t before = d < 256u ? wofs[wid][d] : 0u;
     rank[k] = before + __popc(peers & lt_mask);
     __syncwarp();
-    if (d < 256u && (peers & lt_mask) == 0) whist[wid][d] = before + __popc(peers);
+    if (d < 256u && (peers & lt_mask) == 0) wofs[wid][d] = before + __popc(peers);
     __syncwarp();
   }
   __syncthreads();
-  uint32_t mine = 0;
+  uint32_t wpre[8], mine = 0;
 #pragma unroll
   for (int w = 0; w < 8; ++w) {
-    const uint32_t c = whist[w][tid];
-    whist[w][tid] = mine;
-    mine += c;
+    wpre[w] = mine;
+    mine += wofs[w][tid];
   }
-  lstart[tid] = block_excl_scan256(mine, nullptr);
+  const uint32_t lstart = block_excl_scan256(mine, nullptr);
+#pragma unroll
+  for (int w = 0; w < 8; ++w) wofs[w][tid] = lstart + wpre[w];
+  gofs[tid] = gbase - lstart;  // gbase >= lstart: earlier digits of this tile precede it
   __syncthreads();
 #pragma unroll
   for (int k = 0; k < kItems; ++k) {
     const uint32_t d = dig[k];
     if (d < 256u) {
-      const uint32_t lp = lstart[d] + whist[wid][d] + rank[k];
-      skey[lp] = key[k];
-      sval[lp] = val[k];
+      const uint32_t lp = wofs[wid][d] + rank[k];
+      if constexpr (kPacked) {
+        skv[lp] = make_uint2((uint32_t)key[k], val[k]);
+      } else {
+        skey[lp] = key[k];
+        sval[lp] = val[k];
+      }
     }
   }
   __syncthreads();
   for (int i = tid; i < tile_n; i += kThreads) {
-    const K k = skey[i];
+    K k;
+    uint32_t v;
+    if constexpr (kPacked) {
+      const uint2 kv = skv[i];
+      k = (K)kv.x;
+      v = kv.y;
+    } else {
+      k = skey[i];
+      v = sval[i];
+    }
     const uint32_t d = (uint32_t)(k >> shift) & 255u;
-    const int64_t o = (int64_t)gbase[d] + (i - (int)lstart[d]);
+    const int64_t o = (int64_t)gofs[d] + i;
     kout[o] = k;
-    vout[o] = sval[i];
+    vout[o] = v;
   }
 }
 
-inline int64_t rts_scratch_words(int64_t n, int nbits) {
-  const int64_t npass = (nbits + 7) / 8;
-  const int64_t ntiles = (n + os::kTile - 1) / os::kTile;
-  return ntiles * 256 + npass * 256 + 16;
-}
-
-// Scratch layout: the digit-major tile count table (ntiles * 256 words),
-// then each pass's 256 global digit counts.
-inline uint32_t* rts_counts(uint32_t* scratch) { return scratch; }
-inline uint32_t* rts_ghist(uint32_t* scratch, int64_t n) {
-  return scratch + ((n + os::kTile - 1) / os::kTile) * 256;
-}
-
-// counted: the producer of the keys already wrote every pass's global digit
-// counts (rts_ghist, zeroed before) and the first pass's tile counts
-// (rts_counts) while writing the keys in tiles of os::kTile.
+// counted: the producer of the keys already wrote the first pass's tile
+// count rows and chunk sums (rts_counts, rts_csum) for tiles of os::kTile,
+// and zeroed the other passes' chunk sums.
 template <typename K>
 int rts_sort_pairs(K* keys, uint32_t* vals, K* keys_alt, uint32_t* vals_alt, int64_t n, int nbits,
                    uint32_t* scratch, cudaStream_t st, uint64_t* launches, bool counted = false) {
   if (n <= 0) return 0;
-  const int npass = (nbits + 7) / 8;
-  const int64_t ntiles = (n + os::kTile - 1) / os::kTile;
+  const RtsGeom g = rts_geom(n, nbits);
   uint32_t* counts = rts_counts(scratch);
-  uint32_t* ghist = rts_ghist(scratch, n);
-  if (!counted) {
-    cudaMemsetAsync(ghist, 0, (size_t)npass * 256 * 4, st);
-    int hb = (int)((n + 255) / 256);
-    if (hb > 152 * 8) hb = 152 * 8;
-    k_os_hist<K><<<hb, 256, 0, st>>>(keys, n, npass, ghist);
-    if (launches) *launches += 1;
-  }
-  k_os_scan<<<npass, 256, 0, st>>>(ghist);
+  uint32_t* csum = rts_csum(scratch, g);
+  if (!counted) cudaMemsetAsync(csum, 0, (size_t)g.npass * g.nchunks * 256 * 4, st);
   K* ka = keys;
   K* kb = keys_alt;
   uint32_t* va = vals;
   uint32_t* vb = vals_alt;
   int which = 0;
-  for (int p = 0; p < npass; ++p) {
+  for (int p = 0; p < g.npass; ++p) {
+    uint32_t* cs = csum + (int64_t)p * g.nchunks * 256;
     if (p > 0 || !counted) {
-      k_rts_count<K><<<(unsigned)ntiles, os::kThreads, 0, st>>>(ka, n, 8 * p, counts, ntiles);
+      k_rts_count<K><<<(unsigned)g.ntiles, os::kThreads, 0, st>>>(ka, n, 8 * p, counts, cs, g.ctiles);
       if (launches) *launches += 1;
     }
-    k_rts_rowscan<<<256, 256, 0, st>>>(counts, ntiles, ghist + p * 256);
-    k_rts_scatter<K><<<(unsigned)ntiles, os::kThreads, 0, st>>>(ka, va, kb, vb, n, 8 * p, counts, ntiles);
+    k_rts_offsets<<<(unsigned)g.nchunks, 1024, 0, st>>>(counts, g.ntiles, cs, g.ctiles, g.nchunks);
+    k_rts_scatter<K><<<(unsigned)g.ntiles, os::kThreads, 0, st>>>(ka, va, kb, vb, n, 8 * p, counts);
     K* tk = ka;
     ka = kb;
     kb = tk;
@@ -558,7 +393,7 @@ int rts_sort_pairs(K* keys, uint32_t* vals, K* keys_alt, uint32_t* vals_alt, int
     vb = tv;
     which ^= 1;
   }
-  if (launches) *launches += 1 + 2 * npass;
+  if (launches) *launches += 2 * g.npass;
   return which;
 }
 

@@ -123,57 +123,107 @@ __global__ void k_seed_keys(const uint32_t* __restrict__ g, uint64_t count, Seed
 // (seed bits, strand bit) followed by a genome bit (A = 0, B = 1); values are
 // positions.  Sorted stably, every seed's occurrences in the two genomes are
 // adjacent, each genome's in position order.  Blocks build the seed's gather
-// table once and then take sort tiles of os::kTile positions in turn; for
-// each tile they also count its digits for the sort: every pass's global
-// digit counts (ghist, added atomically) and the first pass's tile counts
-// (counts0, digit-major); both may be null.
+// table once and then take sort tiles of os::kTile positions in turn.  With
+// 32-bit keys (weight <= 15) a thread makes the keys of 4 consecutive
+// positions from one window and stores them as one 16-byte word.  Unless
+// counts0 is null, each tile's first-pass digit counts are written as its
+// count row (counts0) and added into its chunk's sums (csum0), the layout
+// rts_sort_pairs reads when told the keys come counted.
 template <typename K>
 __global__ void __launch_bounds__(256) k_seed_keys_pair(const uint32_t* __restrict__ ga, uint64_t ca,
                                                         const uint32_t* __restrict__ gb, uint64_t cb, SeedDesc s,
-                                                        K* __restrict__ keys, uint32_t* __restrict__ pos, int npass,
-                                                        uint32_t* __restrict__ counts0, int64_t ntiles,
-                                                        uint32_t* __restrict__ ghist) {
+                                                        K* __restrict__ keys, uint32_t* __restrict__ pos,
+                                                        uint32_t* __restrict__ counts0, uint32_t* __restrict__ csum0,
+                                                        int64_t ntiles, int64_t ctiles) {
+  constexpr bool k32 = sizeof(K) == 4;
   __shared__ uint32_t h[8][256];
-  __shared__ uint64_t lut[8][256];
-  const int tid = threadIdx.x;
-  const bool hist = ghist != nullptr;
-  seed_lut_build(s, lut);
+  __shared__ __align__(8) uint32_t lutw[k32 ? 8 * 256 : 2 * 8 * 256];
+  const int tid = threadIdx.x, wid = tid >> 5;
+  const bool count = counts0 != nullptr;
+  auto lut32 = reinterpret_cast<uint32_t(*)[256]>(lutw);
+  auto lut64 = reinterpret_cast<uint64_t(*)[256]>(lutw);
+  if constexpr (k32)
+    seed_lut_build32(s, lut32);
+  else
+    seed_lut_build(s, lut64);
+#pragma unroll
+  for (int w = 0; w < 8; ++w) h[w][tid] = 0;
+  __syncthreads();
   const int nb = seed_bytes(s);
-  const int shift = 64 - 2 * s.w;
   const uint64_t n = ca + cb;
-  uint32_t gsum[8];
-#pragma unroll
-  for (int d = 0; d < 8; ++d) gsum[d] = 0;
+  // four positions from one 32-base window: u + L <= 32 and no byte shift
+  // below zero (8 nb + 6 <= 64)
+  const bool quad = nb <= 7;
   for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    if (hist)
-      for (int q = 0; q < npass; ++q) h[q][tid] = 0;
-    __syncthreads();
     const uint64_t base = (uint64_t)tile * os::kTile;
+    if constexpr (k32) {
+      const int sh = 32 - 2 * s.w;
+#pragma unroll
+      for (int j = 0; j < os::kTile / 1024; ++j) {
+        const uint64_t p0 = base + (uint64_t)j * 1024 + 4 * tid;
+        if (p0 >= n) break;
+        if (quad && p0 + 4 <= n && (p0 + 4 <= ca || p0 >= ca)) {
+          const bool in_b = p0 >= ca;
+          const uint64_t q0 = in_b ? p0 - ca : p0;
+          const uint64_t win = window64(in_b ? gb : ga, q0);
+          uint32_t kk[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            const uint32_t f = gather_mer32(win, u, lut32, nb);
+            const uint32_t r = revcomp_mer32(f, s.w);
+            const uint32_t m = f < r ? f : r;
+            kk[u] = ((((m >> sh) << 1) | (m & 1u)) << 1) | (in_b ? 1u : 0u);
+          }
+          *reinterpret_cast<uint4*>(keys + p0) = make_uint4(kk[0], kk[1], kk[2], kk[3]);
+          *reinterpret_cast<uint4*>(pos + p0) =
+              make_uint4((uint32_t)q0, (uint32_t)q0 + 1, (uint32_t)q0 + 2, (uint32_t)q0 + 3);
+          if (count) {
+#pragma unroll
+            for (int u = 0; u < 4; ++u) atomicAdd(&h[wid][kk[u] & 255u], 1u);
+          }
+        } else {
+          for (int u = 0; u < 4; ++u) {
+            const uint64_t p = p0 + u;
+            if (p >= n) break;
+            const bool in_b = p >= ca;
+            const uint64_t q = in_b ? p - ca : p;
+            const uint32_t f = gather_mer32(window64(in_b ? gb : ga, q), 0, lut32, nb);
+            const uint32_t r = revcomp_mer32(f, s.w);
+            const uint32_t m = f < r ? f : r;
+            const uint32_t key = ((((m >> sh) << 1) | (m & 1u)) << 1) | (in_b ? 1u : 0u);
+            keys[p] = (K)key;
+            pos[p] = (uint32_t)q;
+            if (count) atomicAdd(&h[wid][key & 255u], 1u);
+          }
+        }
+      }
+    } else {
+      const int shift = 64 - 2 * s.w;
 #pragma unroll 2
-    for (int k = 0; k < os::kItems; ++k) {
-      const uint64_t p = base + (uint64_t)k * 256 + tid;
-      if (p >= n) break;
-      const bool in_b = p >= ca;
-      const uint64_t q = in_b ? p - ca : p;
-      const uint64_t m = canonical_mer_lut(in_b ? gb : ga, q, lut, nb, s.w);
-      const K key = (K)(((((m >> shift) << 1) | (m & 1ull)) << 1) | (in_b ? 1ull : 0ull));
-      keys[p] = key;
-      pos[p] = (uint32_t)q;
-      if (hist)
-        for (int d = 0; d < npass; ++d) atomicAdd(&h[d][(uint32_t)(key >> (8 * d)) & 255u], 1u);
+      for (int k = 0; k < os::kItems; ++k) {
+        const uint64_t p = base + (uint64_t)k * 256 + tid;
+        if (p >= n) break;
+        const bool in_b = p >= ca;
+        const uint64_t q = in_b ? p - ca : p;
+        const uint64_t m = canonical_mer_lut(in_b ? gb : ga, q, lut64, nb, s.w);
+        const K key = (K)(((((m >> shift) << 1) | (m & 1ull)) << 1) | (in_b ? 1ull : 0ull));
+        keys[p] = key;
+        pos[p] = (uint32_t)q;
+        if (count) atomicAdd(&h[wid][(uint32_t)key & 255u], 1u);
+      }
     }
-    if (hist) {
+    if (count) {
       __syncthreads();
-      counts0[(int64_t)tid * ntiles + tile] = h[0][tid];
+      uint32_t sum = 0;
 #pragma unroll
-      for (int d = 0; d < 8; ++d)
-        if (d < npass) gsum[d] += h[d][tid];
+      for (int w = 0; w < 8; ++w) {
+        sum += h[w][tid];
+        h[w][tid] = 0;
+      }
+      counts0[tile * 256 + tid] = sum;
+      if (sum) atomicAdd(&csum0[(tile / ctiles) * 256 + tid], sum);
+      __syncthreads();
     }
-  }
-  if (hist) {
-#pragma unroll
-    for (int d = 0; d < 8; ++d)
-      if (d < npass && gsum[d]) atomicAdd(&ghist[d * 256 + tid], gsum[d]);
   }
 }
 
@@ -282,19 +332,18 @@ static int pair_sort_impl(Ctx* c, const uint32_t* ga, uint64_t ca, const uint32_
   uint32_t* v1 = (uint32_t*)ws.get(c, 3, count * sizeof(uint32_t));
   uint32_t* scr = (uint32_t*)ws.get(c, 4, sort_scratch_words(count, nbits) * sizeof(uint32_t));
   if (!k0 || !k1 || !v0 || !v1 || !scr) return report_error(MVG_ERR_NOMEM, "workspace allocation failed");
-  const int64_t ntiles = ((int64_t)count + os::kTile - 1) / os::kTile;
+  const RtsGeom g = rts_geom((int64_t)count, nbits);
+  const unsigned grid = (unsigned)std::min<int64_t>(g.ntiles, 152 * 4);
   int which;
   if ((int64_t)count < (1ll << 31)) {  // the sort_pairs range of the reduce-then-scan sort
-    const int npass = (nbits + 7) / 8;
-    uint32_t* ghist = rts_ghist(scr, (int64_t)count);
-    MVG_CUDA_TRY(cudaMemsetAsync(ghist, 0, (size_t)npass * 256 * 4, c->stream));
-    k_seed_keys_pair<K><<<(unsigned)std::min<int64_t>(ntiles, 152 * 4), 256, 0, c->stream>>>(
-        ga, ca, gb, cb, s, k0, v0, npass, rts_counts(scr), ntiles, ghist);
+    uint32_t* csum = rts_csum(scr, g);
+    MVG_CUDA_TRY(cudaMemsetAsync(csum, 0, (size_t)g.npass * g.nchunks * 256 * 4, c->stream));
+    k_seed_keys_pair<K><<<grid, 256, 0, c->stream>>>(ga, ca, gb, cb, s, k0, v0, rts_counts(scr), csum, g.ntiles,
+                                                      g.ctiles);
     c->launches++;
     which = rts_sort_pairs<K>(k0, v0, k1, v1, (int64_t)count, nbits, scr, c->stream, &c->launches, true);
   } else {
-    k_seed_keys_pair<K><<<(unsigned)std::min<int64_t>(ntiles, 152 * 4), 256, 0, c->stream>>>(
-        ga, ca, gb, cb, s, k0, v0, 0, nullptr, ntiles, nullptr);
+    k_seed_keys_pair<K><<<grid, 256, 0, c->stream>>>(ga, ca, gb, cb, s, k0, v0, nullptr, nullptr, g.ntiles, 1);
     c->launches++;
     which = sort_pairs<K>(k0, v0, k1, v1, (int64_t)count, nbits, scr, c->stream, &c->launches, c->d_err);
   }

@@ -56,7 +56,7 @@ struct StripMap {
 };
 
 // Ring layout: group g = (i-1)/R computes column j at step j + g - lo_0;
-// nibble step*R + r of lane g mod 32.
+// row r of the group is nibble r of that step in lane g mod 32 (ring_tb_at).
 struct RingMap {
   RingBand b;
   int gc, loc;
@@ -66,16 +66,14 @@ struct RingMap {
     loc = 0;
   }
   __device__ bool map(int pa, int pb, int64_t& X, int& t, int& sh) {
-    const int g = (pa - 1) >> (__ffs(b.R) - 1), r = (pa - 1) & (b.R - 1);  // R is 4, 8, 16 or 32
+    const int g = (pa - 1) / b.R, r = (pa - 1) - g * b.R;
     if (g != gc) {
       gc = g;
       loc = ring_lo(b, g);
     }
     if (pb < loc || pb > loc + b.W - 1) return false;
-    const int64_t nib = (int64_t)(pb + g - b.lo0) * b.R + r;
-    X = nib >> 3;
+    ring_tb_at(b.R, (int64_t)(pb + g - b.lo0), r, X, sh);
     t = g & 31;
-    sh = 4 * (int)(nib & 7);
     return true;
   }
 };

@@ -128,6 +128,34 @@ def test_matches_single_diagonal_buckets(ctx, n, sub):
     np.testing.assert_array_equal(ctx.pairwise_matches(a, b, seed), O.pairwise_matches(a, b, seed))
 
 
+@pytest.mark.parametrize("cap", [32, 300])
+def test_matches_bucket_sort_in_chunks(ctx, cap):
+    """Seed-join buckets above the shared-memory capacity are sorted in
+    chunks through global memory: forcing that for most buckets changes no
+    match."""
+    rng = np.random.default_rng(cap)
+    b = synth.insert_repeats(rng, synth.random_bases(rng, 150_000), 500, 20)
+    a = synth.mutate(rng, b, 0.03, 40, 4.0, 3, (200, 5000))
+    seed = mvg.get_seed(15, 3)
+    want = O.pairwise_matches(a, b, seed)
+    ctx.set_pair_bucket_cap(cap)
+    try:
+        np.testing.assert_array_equal(ctx.pairwise_matches(a, b, seed), want)
+    finally:
+        ctx.set_pair_bucket_cap(3072)
+    np.testing.assert_array_equal(ctx.pairwise_matches(a, b, seed), want)
+
+
+@pytest.mark.parametrize("weight,rank", [(16, 0), (17, 3)])
+def test_matches_wide_seed_keys(ctx, weight, rank):
+    """Seeds of weight above 15 take 64-bit keys and the one-sort join."""
+    rng = np.random.default_rng(weight)
+    b = synth.random_bases(rng, 80_000)
+    a = synth.mutate(rng, b, 0.04, 30, 4.0, 2, (200, 3000))
+    seed = mvg.get_seed(weight, rank)
+    np.testing.assert_array_equal(ctx.pairwise_matches(a, b, seed), O.pairwise_matches(a, b, seed))
+
+
 def test_matches_degenerate_inputs(ctx):
     seed = mvg.get_seed(15, 3)
     assert ctx.pairwise_matches(b"ACGT", b"ACGTACGT", seed).shape == (0, 3)
