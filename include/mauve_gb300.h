@@ -315,7 +315,7 @@ int mvg_set_dp_rows(mvg_handle h, int full_rows, int band_rows);
 int mvg_set_band_whole_fraction(mvg_handle h, double fraction);
 
 /* Banded passes on the ring schedule (on = 1, the default): one warp per
- * problem, groups of 4, 8, 16 or 32 rows per lane chained lane to lane along
+ * problem, groups of 4, 6, 8, 12, 16, 24 or 32 rows per lane chained lane to lane along
  * the band, the smallest group height whose schedule is valid for the band;
  * bands no height fits run in the strip kernel.  on = 0 runs every band in
  * the strip kernel.  Results are identical either way. */
@@ -324,8 +324,9 @@ int mvg_set_band_ring(mvg_handle h, int on);
 /* Per-stage timing with CUDA events on the handle's stream (off by default;
  * no extra synchronisation).  After a call, mvg_stage_times gives the stage
  * names (comma separated into names, of capacity names_cap) and each stage's
- * milliseconds in ms[0..*n).  No counterpart in the reference (it prints
- * progress only). */
+ * milliseconds in ms[0..*n); the device stages come first, then the call's
+ * host-side planning sections as "host_<name>" (wall time, summed per
+ * name).  No counterpart in the reference (it prints progress only). */
 int mvg_set_profiling(mvg_handle h, int on);
 int mvg_stage_times(mvg_handle h, char* names, size_t names_cap, double* ms, int cap, int* n);
 

@@ -115,6 +115,41 @@ static const uint64_t kSeedTable[29][6] = {
     {0x7fffffff, 0x7fffffff, 0x7fffffff, 0x7fffffff, 0x7fffffff, 0x7fffffff},
 };
 
+namespace mvg {
+
+int stage_reserve(Ctx* c, size_t need) {
+  for (cudaStream_t st : {c->stream, c->aux, c->aux2, c->aux3})
+    if (st) MVG_CUDA_TRY(cudaStreamSynchronize(st));
+  c->h_stage_used = 0;
+  if (c->h_stage_cap >= need) return 0;
+  if (c->h_stage) cudaFreeHost(c->h_stage);
+  c->h_stage = nullptr;
+  c->h_stage_cap = 0;
+  const size_t want = need + need / 4 + (1 << 20);
+  if (cudaMallocHost(&c->h_stage, want) != cudaSuccess) {
+    cudaGetLastError();
+    c->h_stage = nullptr;
+    return 0;  // copies fall back to pageable sources
+  }
+  c->h_stage_cap = want;
+  return 0;
+}
+
+int h2d_async(Ctx* c, void* dst, const void* src, size_t bytes, cudaStream_t st) {
+  if (bytes == 0) return 0;
+  const size_t off = (c->h_stage_used + 255) & ~(size_t)255;
+  if (c->h_stage && off + bytes <= c->h_stage_cap) {
+    memcpy(c->h_stage + off, src, bytes);
+    c->h_stage_used = off + bytes;
+    MVG_CUDA_TRY(cudaMemcpyAsync(dst, c->h_stage + off, bytes, cudaMemcpyHostToDevice, st));
+    return 0;
+  }
+  MVG_CUDA_TRY(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st));
+  return 0;
+}
+
+}  // namespace mvg
+
 extern "C" {
 
 const char* mvg_last_error(void) { return g_last_error; }
@@ -163,6 +198,7 @@ int mvg_destroy(mvg_handle h) {
   if (h->d_err) cudaFree(h->d_err);
   if (h->h_err) cudaFreeHost(h->h_err);
   if (h->h_scalars) cudaFreeHost(h->h_scalars);
+  if (h->h_stage) cudaFreeHost(h->h_stage);
   for (cudaEvent_t ev : {h->fork, h->join, h->fork2, h->join2, h->fork3, h->join3})
     if (ev) cudaEventDestroy(ev);
   for (cudaStream_t st : {h->aux3, h->aux2, h->aux, h->stream})
@@ -429,22 +465,30 @@ int mvg_stage_times(mvg_handle h, char* names, size_t names_cap, double* ms, int
   if (!h || !n || (cap && !ms) || (names_cap && !names)) return report_error(MVG_ERR_ARG, "null argument");
   *n = 0;
   if (names_cap) names[0] = 0;
-  if (h->nstage < 2) return 0;
-  MVG_CUDA_TRY(cudaEventSynchronize(h->ev[h->nstage - 1]));
   size_t used = 0;
-  for (int k = 0; k + 1 < h->nstage && k < cap; ++k) {
-    float t = 0;
-    MVG_CUDA_TRY(cudaEventElapsedTime(&t, h->ev[k], h->ev[k + 1]));
-    ms[k] = t;
-    const size_t len = strlen(h->stage_name[k]);
-    if (names_cap && used + len + 2 < names_cap) {
+  auto add = [&](const char* prefix, const char* name, double t) {
+    if (*n >= cap) return;
+    ms[*n] = t;
+    const size_t lp = strlen(prefix), len = strlen(name);
+    if (names_cap && used + lp + len + 2 < names_cap) {
       if (used) names[used++] = ',';
-      memcpy(names + used, h->stage_name[k], len);
-      used += len;
+      memcpy(names + used, prefix, lp);
+      memcpy(names + used + lp, name, len);
+      used += lp + len;
       names[used] = 0;
     }
-    *n = k + 1;
+    *n += 1;
+  };
+  if (h->nstage >= 2) {
+    MVG_CUDA_TRY(cudaEventSynchronize(h->ev[h->nstage - 1]));
+    for (int k = 0; k + 1 < h->nstage; ++k) {
+      float t = 0;
+      MVG_CUDA_TRY(cudaEventElapsedTime(&t, h->ev[k], h->ev[k + 1]));
+      add("", h->stage_name[k], t);
+    }
   }
+  // host planning sections, after the device stages
+  for (int k = 0; k < h->nhost; ++k) add("host_", h->host_name[k], h->host_ms[k]);
   return 0;
 }
 

@@ -19,6 +19,7 @@
 #include <limits.h>
 
 #include <algorithm>
+#include <memory>
 #include <cmath>
 #include <functional>
 #include <numeric>
@@ -282,7 +283,7 @@ static int tb_long_fork(Ctx* c, const TbLanes& L, const DpInputs& in, const std:
   uint32_t* d_slots = (uint32_t*)c->ws.get(c, L.slot_list, (size_t)n * 4 + 16);
   unsigned* d_ctr = (unsigned*)c->ws.get(c, L.slot_ctr, 64);
   if (!d_slots || !d_ctr) return report_error(MVG_ERR_NOMEM, "workspace allocation failed");
-  MVG_CUDA_TRY(cudaMemcpyAsync(d_slots, long_slots.data(), (size_t)n * 4, cudaMemcpyHostToDevice, L.st));
+  if (int e = h2d_async(c, d_slots, long_slots.data(), (size_t)n * 4, L.st)) return e;
   MVG_CUDA_TRY(cudaMemsetAsync(d_ctr, 0, 4, L.st));
   MVG_CUDA_TRY(cudaEventRecord(L.fork, L.st));
   MVG_CUDA_TRY(cudaStreamWaitEvent(L.side, L.fork, 0));
@@ -312,6 +313,7 @@ static int run_dp(Ctx* c, const DpInputs& in, const std::vector<uint32_t>& ids, 
   const TbLanes L = lanes ? *lanes : main_lanes(c);
   const int64_t nwork = (int64_t)ids.size();
   if (nwork == 0) return 0;
+  std::unique_ptr<HostSpan> span(new HostSpan(c, "dp_plan"));
   const bool banded = d_delta != nullptr;
   // banded passes may use shorter strips: the staircase of a narrow band
   // widens by the diagonal's drift over one strip
@@ -420,8 +422,9 @@ static int run_dp(Ctx* c, const DpInputs& in, const std::vector<uint32_t>& ids, 
   uint32_t* tb = (uint32_t*)ws.get(c, 18, arena_need);
   if (!rowbuf || !d_order || !d_tboff || !d_edge || !d_counter || !tb)
     return report_error(MVG_ERR_NOMEM, "workspace allocation failed");
-  MVG_CUDA_TRY(cudaMemcpyAsync(d_order, order.data(), (size_t)nwork * 4, cudaMemcpyHostToDevice, L.st));
-  MVG_CUDA_TRY(cudaMemcpyAsync(d_tboff, tboff.data(), (size_t)nwork * 8, cudaMemcpyHostToDevice, L.st));
+  if (int e = h2d_async(c, d_order, order.data(), (size_t)nwork * 4, L.st)) return e;
+  if (int e = h2d_async(c, d_tboff, tboff.data(), (size_t)nwork * 8, L.st)) return e;
+  span.reset();
   for (size_t wv = 0; wv + 1 < wave_begin.size(); ++wv) {
     const int64_t w0 = wave_begin[wv], w1 = wave_begin[wv + 1];
     DpJob J;
@@ -479,6 +482,7 @@ static int run_ring(Ctx* c, const TbLanes& L, const DpInputs& in, const std::vec
                     const int32_t* d_half, uint8_t* d_accept, unsigned long long* d_cells) {
   const int64_t nwork = (int64_t)ids.size();
   if (nwork == 0) return 0;
+  std::unique_ptr<HostSpan> span(new HostSpan(c, "ring_plan"));
   std::vector<uint64_t> bytes(nwork), cost(nwork);
   for (int64_t w = 0; w < nwork; ++w) {
     const uint32_t p = ids[w];
@@ -531,11 +535,12 @@ static int run_ring(Ctx* c, const TbLanes& L, const DpInputs& in, const std::vec
   uint32_t* tb = (uint32_t*)ws.get(c, 67, arena_need);
   if (!d_order || !d_tboff || !d_edge || !d_counter || !d_rows || !tb)
     return report_error(MVG_ERR_NOMEM, "workspace allocation failed");
-  MVG_CUDA_TRY(cudaMemcpyAsync(d_order, order.data(), (size_t)nwork * 4, cudaMemcpyHostToDevice, L.st));
-  MVG_CUDA_TRY(cudaMemcpyAsync(d_tboff, tboff.data(), (size_t)nwork * 8, cudaMemcpyHostToDevice, L.st));
-  MVG_CUDA_TRY(cudaMemcpyAsync(d_rows, rows_of.data(), (size_t)nwork, cudaMemcpyHostToDevice, L.st));
+  if (int e = h2d_async(c, d_order, order.data(), (size_t)nwork * 4, L.st)) return e;
+  if (int e = h2d_async(c, d_tboff, tboff.data(), (size_t)nwork * 8, L.st)) return e;
+  if (int e = h2d_async(c, d_rows, rows_of.data(), (size_t)nwork, L.st)) return e;
   int dev_sms = 0;
   MVG_CUDA_TRY(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, c->device));
+  span.reset();
   for (size_t wv = 0; wv + 1 < wave_begin.size(); ++wv) {
     const int64_t w0 = wave_begin[wv], w1 = wave_begin[wv + 1];
     for (int64_t a = w0; a < w1;) {
@@ -633,7 +638,7 @@ static int scratch_paths(Ctx* c, int64_t nprob, const std::vector<int64_t>& la, 
   uint64_t* d_tmp_poff = (uint64_t*)c->ws.get(c, 16, (nprob + 1) * 8);
   int64_t* d_tmp_plen = (int64_t*)c->ws.get(c, 17, nprob * 8);
   if (!d_tmp_paths || !d_tmp_poff || !d_tmp_plen) return report_error(MVG_ERR_NOMEM, "workspace allocation failed");
-  MVG_CUDA_TRY(cudaMemcpyAsync(d_tmp_poff, po.data(), (nprob + 1) * 8, cudaMemcpyHostToDevice, c->stream));
+  if (int e = h2d_async(c, d_tmp_poff, po.data(), (nprob + 1) * 8, c->stream)) return e;
   MVG_CUDA_TRY(cudaStreamSynchronize(c->stream));
   in.paths = d_tmp_paths;
   in.path_off = d_tmp_poff;
@@ -648,6 +653,7 @@ int gapdp_batch_dev(Ctx* c, const uint8_t* d_sa, const uint64_t* d_oa, const uin
   std::vector<int64_t> la, lb;
   int rc = check_lengths(nprob, h_oa, h_ob, la, lb);
   if (rc) return rc;
+  if ((rc = stage_reserve(c, (size_t)nprob * 40 + (1 << 20)))) return rc;
   DpInputs in{d_sa, d_oa, d_sb, d_ob, d_scores, d_paths, d_path_off, d_path_len, d_env};
   if (!d_paths && (rc = scratch_paths(c, nprob, la, lb, in))) return rc;
   std::vector<uint32_t> ids(nprob);
@@ -667,9 +673,13 @@ int gapdp_banded_dev(Ctx* c, const uint8_t* d_sa, const uint64_t* d_oa, const ui
                      const uint64_t* d_path_off, int64_t* d_path_len, uint8_t* h_used_band, const uint64_t* h_oa,
                      const uint64_t* h_ob, uint64_t* banded_cells) {
   if (nprob <= 0) return 0;
+  stage_begin_call(c);
+  std::unique_ptr<HostSpan> plan(new HostSpan(c, "plan"));
   std::vector<int64_t> la, lb;
   int rc = check_lengths(nprob, h_oa, h_ob, la, lb);
   if (rc) return rc;
+  // staging: bands, and per launch group its order, offsets, heights and long-path lists
+  if ((rc = stage_reserve(c, (size_t)nprob * 96 + (1 << 20)))) return rc;
   DpInputs in{d_sa, d_oa, d_sb, d_ob, d_scores, d_paths, d_path_off, d_path_len};
   if (!d_paths && (rc = scratch_paths(c, nprob, la, lb, in))) return rc;
   std::vector<int32_t> dv(h_delta, h_delta + nprob), hv(h_half, h_half + nprob);
@@ -735,13 +745,13 @@ int gapdp_banded_dev(Ctx* c, const uint8_t* d_sa, const uint64_t* d_oa, const ui
   uint8_t* d_accept = (uint8_t*)c->ws.get(c, 26, (size_t)nprob + 16);
   unsigned long long* d_cells = (unsigned long long*)c->ws.get(c, 61, 64);
   if (!d_delta || !d_half || !d_accept || !d_cells) return report_error(MVG_ERR_NOMEM, "workspace allocation failed");
-  MVG_CUDA_TRY(cudaMemcpyAsync(d_delta, dv.data(), (size_t)nprob * 4, cudaMemcpyHostToDevice, c->stream));
-  MVG_CUDA_TRY(cudaMemcpyAsync(d_half, hv.data(), (size_t)nprob * 4, cudaMemcpyHostToDevice, c->stream));
+  if ((rc = h2d_async(c, d_delta, dv.data(), (size_t)nprob * 4, c->stream))) return rc;
+  if ((rc = h2d_async(c, d_half, hv.data(), (size_t)nprob * 4, c->stream))) return rc;
   MVG_CUDA_TRY(cudaMemsetAsync(d_accept, 0, (size_t)nprob, c->stream));
   MVG_CUDA_TRY(cudaMemsetAsync(d_cells, 0, 8, c->stream));
   MVG_CUDA_TRY(cudaMemsetAsync(c->d_err, 0, 4, c->stream));
   if ((rc = check_codes(c, d_sa, h_oa[nprob], d_sb, h_ob[nprob]))) return rc;
-  stage_begin_call(c);
+  plan.reset();
   // the ring-scheduled bands on the aux stream beside the strip kernel's
   // problems on the main stream (their launches have separate tails)
   const TbLanes ring_lanes{c->aux, c->aux2, c->fork2, c->join2, 68, 69};
@@ -767,6 +777,7 @@ int gapdp_banded_dev(Ctx* c, const uint8_t* d_sa, const uint64_t* d_oa, const ui
   MVG_CUDA_TRY(cudaMemcpyAsync(acc.data(), d_accept, (size_t)nprob, cudaMemcpyDeviceToHost, c->stream));
   MVG_CUDA_TRY(cudaMemcpyAsync(c->h_scalars, d_cells, 8, cudaMemcpyDeviceToHost, c->stream));
   MVG_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  std::unique_ptr<HostSpan> tail(new HostSpan(c, "fallback_list"));
   bc += c->h_scalars[0];
   std::vector<uint32_t> fallback;
   for (int64_t p = 0; p < nprob; ++p) {
@@ -778,6 +789,7 @@ int gapdp_banded_dev(Ctx* c, const uint8_t* d_sa, const uint64_t* d_oa, const ui
       bc += (uint64_t)la[p] * (uint64_t)lb[p];
     }
   }
+  tail.reset();
   // rejected bands: the full DP is both the fallback and the judge
   rc = run_dp(c, in, fallback, la, lb, nullptr, nullptr, nullptr, nullptr, nullptr);
   if (rc) return rc;

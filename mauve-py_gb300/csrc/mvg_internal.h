@@ -3,6 +3,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <chrono>
+
 #include "mvg_common.cuh"
 
 namespace mvg {
@@ -36,6 +38,8 @@ struct Ctx {
   uint32_t* d_err = nullptr;     // device error word
   uint32_t* h_err = nullptr;     // pinned mirror
   uint64_t* h_scalars = nullptr; // pinned scalars for small device->host reads
+  uint8_t* h_stage = nullptr;    // pinned staging of one call's host->device copies (bump allocated)
+  size_t h_stage_cap = 0, h_stage_used = 0;
   uint64_t launches = 0;
   uint64_t tb_arena = ~0ull;  // capped per call at 60% of free device memory
   int dp_rows = 8;            // full gap-DP rows per lane (4 or 8)
@@ -50,6 +54,11 @@ struct Ctx {
   cudaEvent_t ev[kMaxStages + 1] = {};
   const char* stage_name[kMaxStages] = {};
   int nstage = -1;  // -1: no stage recorded yet in this call
+  // host-side planning time of the call, by name (summed), when profiling
+  static constexpr int kMaxHost = 8;
+  double host_ms[kMaxHost] = {};
+  const char* host_name[kMaxHost] = {};
+  int nhost = 0;
 };
 
 // Marks the start of a named stage (and the end of the previous one).
@@ -62,7 +71,31 @@ inline void stage_mark(Ctx* c, const char* name) {
   c->stage_name[c->nstage] = name;
   c->nstage++;
 }
-inline void stage_begin_call(Ctx* c) { c->nstage = -1; }
+inline void stage_begin_call(Ctx* c) {
+  c->nstage = -1;
+  c->nhost = 0;
+}
+
+// Wall time of a host-side section, added to the call's host stage `name`.
+struct HostSpan {
+  Ctx* c;
+  const char* name;
+  std::chrono::steady_clock::time_point t0;
+  HostSpan(Ctx* c_, const char* n) : c(c_), name(n), t0(std::chrono::steady_clock::now()) {}
+  ~HostSpan() {
+    if (!c->profiling) return;
+    const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    for (int k = 0; k < c->nhost; ++k)
+      if (c->host_name[k] == name) {
+        c->host_ms[k] += ms;
+        return;
+      }
+    if (c->nhost < Ctx::kMaxHost) {
+      c->host_name[c->nhost] = name;
+      c->host_ms[c->nhost++] = ms;
+    }
+  }
+};
 inline void stage_end(Ctx* c) { stage_mark(c, "end"); }
 
 // Sorted keys kept on the device for the join.
@@ -101,6 +134,13 @@ int pair_buckets(Ctx* c, const uint32_t* ga, uint64_t ca, const uint32_t* gb, ui
 int pair_sort(Ctx* c, const uint32_t* ga, uint64_t ca, const uint32_t* gb, uint64_t cb, const SeedDesc& s,
               SmlKeys* out);
 int check_device_error(Ctx* c);
+// Pinned staging for a call's host->device copies: stage_reserve waits for
+// the handle's streams, makes room for `need` bytes and starts the call's
+// allocation over; h2d_async copies through it (a truly asynchronous copy,
+// so the host goes on planning while the stream is busy), or straight from
+// the pageable source when the staging is full.
+int stage_reserve(Ctx* c, size_t need);
+int h2d_async(Ctx* c, void* dst, const void* src, size_t bytes, cudaStream_t st);
 size_t sml_key_bytes(const SeedDesc& s);
 int sml_build_into(const uint8_t* d_seq, uint64_t n, uint64_t count, const SeedDesc& s, uint32_t* packed, void* k0,
                    void* k1, uint32_t* v0, uint32_t* v1, uint32_t* scr, uint32_t* d_pos_out, uint64_t* d_mer_out,

@@ -41,6 +41,9 @@ constexpr int kCap = 3072;      // bucket elements sorted in shared memory
 constexpr int kLocItems = kCap / kLocThreads;
 constexpr int kMaxDigit = 64;   // chunked in-bucket passes: digits of at most 6 bits
 constexpr int kSmemDigit = 512; // shared-memory in-bucket passes: digits of at most 9 bits
+constexpr int kGroups = 512;    // groups of a bucket split by its top 9 in-bucket bits
+constexpr int kGroupSmall = 24; // groups up to this size: insertion sort by one thread
+constexpr int kGroupMax = 1024; // larger groups: radix passes for the bucket instead
 constexpr int kChunkTiles = 32;
 }  // namespace pb
 
@@ -439,11 +442,42 @@ __device__ uint32_t pb_pairs(const uint2* v, int n, uint2* stage, LocalSmem& S) 
   return total;
 }
 
-// Block b sorts bucket b.  Buckets of at most cap (<= kCap) elements are
-// loaded into shared memory (two buffers) and sorted in passes of up to 9
-// bits; larger ones are sorted in chunks between their region of `buf` and
-// the same region of `alt` in an odd number of passes of up to 6 bits, which
-// leaves them in `alt`.  The staged pairs go to the bucket's region of
+// A group of the bucket (one value of the top in-bucket bits), s[beg, end),
+// sorted by in-bucket key with insertion sort; returns its pairs (runs of
+// exactly two, one per genome), counted only (out == nullptr) or written.
+__device__ __forceinline__ uint32_t pb_group_pairs(const uint2* s, int beg, int end, uint2* out) {
+  uint32_t np = 0;
+  int i = beg;
+  while (i < end) {
+    const uint32_t m = s[i].x >> 2;
+    int e = i + 1;
+    while (e < end && (s[e].x >> 2) == m) ++e;
+    if (e - i == 2 && ((s[i].x ^ s[i + 1].x) & 1u)) {
+      if (out) {
+        const bool a_first = (s[i].x & 1u) == 0;
+        const uint2 ea = a_first ? s[i] : s[i + 1], eb = a_first ? s[i + 1] : s[i];
+        // SetDirection (LM/MemHash.cpp:189-207): B is reversed relative to
+        // A when the two occurrences have different strand bits
+        const uint32_t rev = ((ea.x >> 1) ^ (eb.x >> 1)) & 1u;
+        out[np] = make_uint2(ea.y, eb.y | (rev << 31));
+      }
+      ++np;
+    }
+    i = e;
+  }
+  return np;
+}
+
+// Block b sorts bucket b.  A bucket of at most cap (<= kCap) elements is
+// loaded into shared memory and split by its top in-bucket bits (up to 9:
+// at most 512 groups of a few elements each, placed by shared-memory
+// atomics in any order inside a group); each thread then sorts two groups
+// with insertion sort and finds their pairs, and one scan over the groups
+// places the pairs in mer order.  If a group has more than kGroupMax
+// elements the bucket is instead sorted by stable radix passes of up to 9
+// bits.  Larger buckets are sorted in chunks between their region of `buf`
+// and the same region of `alt` in an odd number of passes of up to 6 bits,
+// which leaves them in `alt`.  The staged pairs go to the bucket's region of
 // `buf`, which the sorted data no longer occupies.
 __global__ void __launch_bounds__(pb::kLocThreads) k_pb_local(uint2* __restrict__ buf, uint2* __restrict__ alt,
                                                               const uint32_t* __restrict__ bstart,
@@ -452,24 +486,97 @@ __global__ void __launch_bounds__(pb::kLocThreads) k_pb_local(uint2* __restrict_
                                                               uint32_t* __restrict__ pcount) {
   extern __shared__ __align__(16) uint2 sbuf[];  // 2 * kCap elements
   __shared__ LocalSmem S;
+  __shared__ uint32_t gcnt[pb::kGroups], gend[pb::kGroups];
+  const int tid = threadIdx.x;
   const int b = blockIdx.x;
   const int n = (int)bsize[b];
   uint2* g = buf + bstart[b];
   uint2* h = alt + bstart[b];
   uint32_t np;
   if (n <= cap) {
-    const uint32_t mask = (1u << sbits) - 1u;
+    const int hbits = lbits < 9 ? lbits : 9, lo = lbits - hbits, ng = 1 << hbits;
     uint2* s0 = sbuf;
     uint2* s1 = sbuf + pb::kCap;
-    for (int i = threadIdx.x; i < n; i += pb::kLocThreads) s0[i] = g[i];
+    for (int d = tid; d < pb::kGroups; d += pb::kLocThreads) gcnt[d] = 0;
     __syncthreads();
-    for (int p = 0; p < spass; ++p) {
-      pb_pass_smem(s0, s1, n, p * sbits, mask, lbits, S);
-      uint2* t = s0;
-      s0 = s1;
-      s1 = t;
+    for (int i = tid; i < n; i += pb::kLocThreads) {
+      const uint2 it = g[i];
+      s0[i] = it;
+      atomicAdd(&gcnt[pb_lkey(it.x, lbits) >> lo], 1u);
     }
-    np = pb_pairs(s0, n, g, S);
+    __syncthreads();
+    // thread t: groups 2t and 2t + 1
+    const int d0 = 2 * tid;
+    const uint32_t c0 = d0 < ng ? gcnt[d0] : 0u, c1 = d0 + 1 < ng ? gcnt[d0 + 1] : 0u;
+    const uint32_t st = block_excl_scan256(c0 + c1, nullptr);
+    if (d0 < ng) gend[d0] = st;
+    if (d0 + 1 < ng) gend[d0 + 1] = st + c0;
+    __syncthreads();
+    for (int i = tid; i < n; i += pb::kLocThreads) {
+      const uint2 it = s0[i];
+      s1[atomicAdd(&gend[pb_lkey(it.x, lbits) >> lo], 1u)] = it;
+    }
+    __syncthreads();
+    const int b0 = (int)st, e0 = b0 + (int)c0, e1 = e0 + (int)c1;
+    const bool big = __syncthreads_or(c0 > (uint32_t)pb::kGroupMax || c1 > (uint32_t)pb::kGroupMax);
+    if (!big) {
+      if (tid == 0) S.total = 0;
+      __syncthreads();
+      for (int k = 0; k < 2; ++k) {
+        const int beg = k ? e0 : b0, end = k ? e1 : e0;
+        if (end - beg > pb::kGroupSmall) {  // sorted by a warp below
+          S.whist[0][atomicAdd(&S.total, 1u)] = (uint32_t)(d0 + k);
+          continue;
+        }
+        for (int i = beg + 1; i < end; ++i) {  // insertion sort by in-bucket key
+          const uint2 x = s1[i];
+          const uint32_t kx = pb_lkey(x.x, lbits);
+          int j = i - 1;
+          while (j >= beg && pb_lkey(s1[j].x, lbits) > kx) {
+            s1[j + 1] = s1[j];
+            --j;
+          }
+          s1[j + 1] = x;
+        }
+      }
+      __syncthreads();
+      // larger groups, a warp each: every element's rank is the number of
+      // smaller keys (ties by index), written to the group's range of s0
+      // (free since the split) and copied back
+      const int nbig = (int)S.total, lane = tid & 31, wid = tid >> 5;
+      for (int q = wid; q < nbig; q += pb::kLocWarps) {
+        const int d = (int)S.whist[0][q];
+        const int end = (int)gend[d], beg = end - (int)gcnt[d];
+        for (int i = beg + lane; i < end; i += 32) {
+          const uint2 x = s1[i];
+          const uint32_t kx = pb_lkey(x.x, lbits);
+          int r = 0;
+          for (int j = beg; j < end; ++j) {
+            const uint32_t kj = pb_lkey(s1[j].x, lbits);
+            r += (kj < kx) || (kj == kx && j < i);
+          }
+          s0[beg + r] = x;
+        }
+        __syncwarp();
+        for (int i = beg + lane; i < end; i += 32) s1[i] = s0[i];
+        __syncwarp();
+      }
+      __syncthreads();
+      const uint32_t p0 = pb_group_pairs(s1, b0, e0, nullptr), p1 = pb_group_pairs(s1, e0, e1, nullptr);
+      const uint32_t pst = block_excl_scan256(p0 + p1, &S.total);
+      pb_group_pairs(s1, b0, e0, g + pst);
+      pb_group_pairs(s1, e0, e1, g + pst + p0);
+      np = S.total;
+    } else {
+      const uint32_t mask = (1u << sbits) - 1u;
+      for (int p = 0; p < spass; ++p) {
+        pb_pass_smem(s0, s1, n, p * sbits, mask, lbits, S);
+        uint2* t = s0;
+        s0 = s1;
+        s1 = t;
+      }
+      np = pb_pairs(s0, n, g, S);
+    }
   } else {
     const uint32_t mask = (1u << dbits) - 1u;
     const uint2* src = g;
@@ -482,7 +589,7 @@ __global__ void __launch_bounds__(pb::kLocThreads) k_pb_local(uint2* __restrict_
     }
     np = pb_pairs(src, n, g, S);  // npass is odd: the sorted bucket is in alt
   }
-  if (threadIdx.x == 0) pcount[b] = np;
+  if (tid == 0) pcount[b] = np;
 }
 
 // ------------------------------------------------------------------ host
