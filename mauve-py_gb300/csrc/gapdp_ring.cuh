@@ -439,8 +439,17 @@ __global__ void k_traceback_ring(const uint64_t* __restrict__ oa, const uint64_t
         }
         int64_t word;
         int sh;
-        ring_tb_at(R, (int64_t)(pb + g - b.lo0), r, word, sh);
+        const int64_t st = (int64_t)(pb + g - b.lo0);
+        ring_tb_at(R, st, r, word, sh);
         bits = (T[word * 32 + (g & 31)] >> sh) & 15u;
+        // the path runs right to left along the group: start fetching the
+        // word 8 steps back (each step's word is otherwise a dependent miss)
+        if (st >= 8) {
+          int64_t w8;
+          int sh8;
+          ring_tb_at(R, st - 8, r, w8, sh8);
+          asm volatile("prefetch.global.L1 [%0];" ::"l"(T + w8 * 32 + (g & 31)));
+        }
       }
       char next;
       if (cur == 'M') {

@@ -42,8 +42,7 @@ constexpr int kLocItems = kCap / kLocThreads;
 constexpr int kMaxDigit = 64;   // chunked in-bucket passes: digits of at most 6 bits
 constexpr int kSmemDigit = 512; // shared-memory in-bucket passes: digits of at most 9 bits
 constexpr int kGroups = 512;    // groups of a bucket split by its top 9 in-bucket bits
-constexpr int kGroupSmall = 24; // groups up to this size: insertion sort by one thread
-constexpr int kGroupMax = 1024; // larger groups: radix passes for the bucket instead
+constexpr int kGroupMax = 256;  // larger groups: radix passes for the bucket instead
 constexpr int kChunkTiles = 32;
 }  // namespace pb
 
@@ -442,43 +441,20 @@ __device__ uint32_t pb_pairs(const uint2* v, int n, uint2* stage, LocalSmem& S) 
   return total;
 }
 
-// A group of the bucket (one value of the top in-bucket bits), s[beg, end),
-// sorted by in-bucket key with insertion sort; returns its pairs (runs of
-// exactly two, one per genome), counted only (out == nullptr) or written.
-__device__ __forceinline__ uint32_t pb_group_pairs(const uint2* s, int beg, int end, uint2* out) {
-  uint32_t np = 0;
-  int i = beg;
-  while (i < end) {
-    const uint32_t m = s[i].x >> 2;
-    int e = i + 1;
-    while (e < end && (s[e].x >> 2) == m) ++e;
-    if (e - i == 2 && ((s[i].x ^ s[i + 1].x) & 1u)) {
-      if (out) {
-        const bool a_first = (s[i].x & 1u) == 0;
-        const uint2 ea = a_first ? s[i] : s[i + 1], eb = a_first ? s[i + 1] : s[i];
-        // SetDirection (LM/MemHash.cpp:189-207): B is reversed relative to
-        // A when the two occurrences have different strand bits
-        const uint32_t rev = ((ea.x >> 1) ^ (eb.x >> 1)) & 1u;
-        out[np] = make_uint2(ea.y, eb.y | (rev << 31));
-      }
-      ++np;
-    }
-    i = e;
-  }
-  return np;
-}
-
-// Block b sorts bucket b.  A bucket of at most cap (<= kCap) elements is
-// loaded into shared memory and split by its top in-bucket bits (up to 9:
-// at most 512 groups of a few elements each, placed by shared-memory
-// atomics in any order inside a group); each thread then sorts two groups
-// with insertion sort and finds their pairs, and one scan over the groups
-// places the pairs in mer order.  If a group has more than kGroupMax
-// elements the bucket is instead sorted by stable radix passes of up to 9
-// bits.  Larger buckets are sorted in chunks between their region of `buf`
-// and the same region of `alt` in an odd number of passes of up to 6 bits,
-// which leaves them in `alt`.  The staged pairs go to the bucket's region of
-// `buf`, which the sorted data no longer occupies.
+// Block b finds the unique pairs of bucket b.  A bucket of at most cap
+// (<= kCap) keys is loaded into shared memory as (in-bucket key | strand <<
+// 31, position) and split by its top in-bucket bits (up to 9) into at most
+// 512 groups of a few keys each (shared-memory atomics place a group's keys
+// in any order).  Then one thread per key: a key whose mer occurs exactly
+// twice in its group, once per genome, and which is the A occurrence, is a
+// pair (marked, and counted for its group); after one scan over the groups
+// each pair's slot is its group's first slot plus the number of the group's
+// pairs with a smaller mer.  If a group holds more than kGroupMax keys the
+// bucket is instead sorted by stable radix passes of up to 9 bits.  Larger
+// buckets are sorted in chunks between their region of `buf` and the same
+// region of `alt` in an odd number of passes of up to 6 bits, which leaves
+// them in `alt`.  The staged pairs go to the bucket's region of `buf`, which
+// the keys no longer occupy.
 __global__ void __launch_bounds__(pb::kLocThreads) k_pb_local(uint2* __restrict__ buf, uint2* __restrict__ alt,
                                                               const uint32_t* __restrict__ bstart,
                                                               const uint32_t* __restrict__ bsize, int lbits, int npass,
@@ -486,7 +462,8 @@ __global__ void __launch_bounds__(pb::kLocThreads) k_pb_local(uint2* __restrict_
                                                               uint32_t* __restrict__ pcount) {
   extern __shared__ __align__(16) uint2 sbuf[];  // 2 * kCap elements
   __shared__ LocalSmem S;
-  __shared__ uint32_t gcnt[pb::kGroups], gend[pb::kGroups];
+  __shared__ uint32_t gcnt[pb::kGroups], gbeg[pb::kGroups], gcur[pb::kGroups], gpair[pb::kGroups];
+  constexpr uint32_t kMark = 1u << 30, kKey = kMark - 1u;
   const int tid = threadIdx.x;
   const int b = blockIdx.x;
   const int n = (int)bsize[b];
@@ -494,80 +471,79 @@ __global__ void __launch_bounds__(pb::kLocThreads) k_pb_local(uint2* __restrict_
   uint2* h = alt + bstart[b];
   uint32_t np;
   if (n <= cap) {
-    const int hbits = lbits < 9 ? lbits : 9, lo = lbits - hbits, ng = 1 << hbits;
+    // group bits: mer bits only (never the genome bit), at most 9
+    const int hbits = lbits - 1 < 9 ? lbits - 1 : 9, lo = lbits - hbits, ng = 1 << hbits;
     uint2* s0 = sbuf;
     uint2* s1 = sbuf + pb::kCap;
-    for (int d = tid; d < pb::kGroups; d += pb::kLocThreads) gcnt[d] = 0;
+    for (int d = tid; d < pb::kGroups; d += pb::kLocThreads) {
+      gcnt[d] = 0;
+      gpair[d] = 0;
+    }
     __syncthreads();
     for (int i = tid; i < n; i += pb::kLocThreads) {
       const uint2 it = g[i];
-      s0[i] = it;
-      atomicAdd(&gcnt[pb_lkey(it.x, lbits) >> lo], 1u);
+      const uint32_t lk = pb_lkey(it.x, lbits);
+      s0[i] = make_uint2(lk | (((it.x >> 1) & 1u) << 31), it.y);
+      atomicAdd(&gcnt[lk >> lo], 1u);
     }
     __syncthreads();
     // thread t: groups 2t and 2t + 1
     const int d0 = 2 * tid;
     const uint32_t c0 = d0 < ng ? gcnt[d0] : 0u, c1 = d0 + 1 < ng ? gcnt[d0 + 1] : 0u;
     const uint32_t st = block_excl_scan256(c0 + c1, nullptr);
-    if (d0 < ng) gend[d0] = st;
-    if (d0 + 1 < ng) gend[d0 + 1] = st + c0;
+    if (d0 < ng) gbeg[d0] = gcur[d0] = st;
+    if (d0 + 1 < ng) gbeg[d0 + 1] = gcur[d0 + 1] = st + c0;
     __syncthreads();
     for (int i = tid; i < n; i += pb::kLocThreads) {
-      const uint2 it = s0[i];
-      s1[atomicAdd(&gend[pb_lkey(it.x, lbits) >> lo], 1u)] = it;
+      const uint2 e = s0[i];
+      s1[atomicAdd(&gcur[(e.x & kKey) >> lo], 1u)] = e;
     }
-    __syncthreads();
-    const int b0 = (int)st, e0 = b0 + (int)c0, e1 = e0 + (int)c1;
     const bool big = __syncthreads_or(c0 > (uint32_t)pb::kGroupMax || c1 > (uint32_t)pb::kGroupMax);
     if (!big) {
-      if (tid == 0) S.total = 0;
-      __syncthreads();
-      for (int k = 0; k < 2; ++k) {
-        const int beg = k ? e0 : b0, end = k ? e1 : e0;
-        if (end - beg > pb::kGroupSmall) {  // sorted by a warp below
-          S.whist[0][atomicAdd(&S.total, 1u)] = (uint32_t)(d0 + k);
-          continue;
-        }
-        for (int i = beg + 1; i < end; ++i) {  // insertion sort by in-bucket key
-          const uint2 x = s1[i];
-          const uint32_t kx = pb_lkey(x.x, lbits);
-          int j = i - 1;
-          while (j >= beg && pb_lkey(s1[j].x, lbits) > kx) {
-            s1[j + 1] = s1[j];
-            --j;
+      // the A occurrence of each pair: its pair record into s0 (free now)
+      for (int i = tid; i < n; i += pb::kLocThreads) {
+        const uint32_t x = s1[i].x, lk = x & kKey, m = lk >> 1;
+        const int d = (int)(lk >> lo), e0 = (int)gbeg[d], e1 = e0 + (int)gcnt[d];
+        int cnt = 0, other = 0;
+        for (int j = e0; j < e1; ++j)
+          if (((s1[j].x & kKey) >> 1) == m) {
+            ++cnt;
+            if (j != i) other = j;
           }
-          s1[j + 1] = x;
+        if (cnt == 2 && (lk & 1u) == 0) {
+          const uint2 y = s1[other];
+          if (y.x & 1u) {
+            // SetDirection (LM/MemHash.cpp:189-207): B is reversed relative
+            // to A when the two occurrences have different strand bits
+            const uint32_t rev = (x ^ y.x) >> 31;
+            s0[i] = make_uint2(s1[i].y, y.y | (rev << 31));
+            atomicOr(&s1[i].x, kMark);
+            atomicAdd(&gpair[d], 1u);
+          }
         }
       }
       __syncthreads();
-      // larger groups, a warp each: every element's rank is the number of
-      // smaller keys (ties by index), written to the group's range of s0
-      // (free since the split) and copied back
-      const int nbig = (int)S.total, lane = tid & 31, wid = tid >> 5;
-      for (int q = wid; q < nbig; q += pb::kLocWarps) {
-        const int d = (int)S.whist[0][q];
-        const int end = (int)gend[d], beg = end - (int)gcnt[d];
-        for (int i = beg + lane; i < end; i += 32) {
-          const uint2 x = s1[i];
-          const uint32_t kx = pb_lkey(x.x, lbits);
-          int r = 0;
-          for (int j = beg; j < end; ++j) {
-            const uint32_t kj = pb_lkey(s1[j].x, lbits);
-            r += (kj < kx) || (kj == kx && j < i);
-          }
-          s0[beg + r] = x;
-        }
-        __syncwarp();
-        for (int i = beg + lane; i < end; i += 32) s1[i] = s0[i];
-        __syncwarp();
-      }
+      const uint32_t q0 = d0 < ng ? gpair[d0] : 0u, q1 = d0 + 1 < ng ? gpair[d0 + 1] : 0u;
+      const uint32_t pst = block_excl_scan256(q0 + q1, &S.total);
+      if (d0 < ng) gcur[d0] = pst;
+      if (d0 + 1 < ng) gcur[d0 + 1] = pst + q0;
       __syncthreads();
-      const uint32_t p0 = pb_group_pairs(s1, b0, e0, nullptr), p1 = pb_group_pairs(s1, e0, e1, nullptr);
-      const uint32_t pst = block_excl_scan256(p0 + p1, &S.total);
-      pb_group_pairs(s1, b0, e0, g + pst);
-      pb_group_pairs(s1, e0, e1, g + pst + p0);
+      for (int i = tid; i < n; i += pb::kLocThreads) {
+        const uint32_t x = s1[i].x;
+        if (!(x & kMark)) continue;
+        const uint32_t m = (x & kKey) >> 1;
+        const int d = (int)((x & kKey) >> lo), e0 = (int)gbeg[d], e1 = e0 + (int)gcnt[d];
+        uint32_t r = 0;
+        for (int j = e0; j < e1; ++j) {
+          const uint32_t y = s1[j].x;
+          r += (y & kMark) && ((y & kKey) >> 1) < m;
+        }
+        g[gcur[d] + r] = s0[i];
+      }
       np = S.total;
     } else {
+      for (int i = tid; i < n; i += pb::kLocThreads) s0[i] = g[i];
+      __syncthreads();
       const uint32_t mask = (1u << sbits) - 1u;
       for (int p = 0; p < spass; ++p) {
         pb_pass_smem(s0, s1, n, p * sbits, mask, lbits, S);
