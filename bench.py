@@ -151,7 +151,7 @@ LB_NPROB = 200_000
 # DRAM bytes of the seed-path kernels per match-finding call on the recoded
 # pair, from one ncu capture (profiles/anchoring_launch_list_recoded_pair.md);
 # below the algorithmic bytes because the sort passes' outputs stay in L2
-SEED_PATH_TRAFFIC = 0.61e9
+SEED_PATH_TRAFFIC = 0.36e9
 # stages of the seed path (pack, seed keys, bucket or radix sort, unique-pair join)
 SEED_STAGES = ("pack", "sml_sort", "seed_scatter", "seed_local", "unique_join")
 

@@ -150,6 +150,31 @@ int h2d_async(Ctx* c, void* dst, const void* src, size_t bytes, cudaStream_t st)
 
 }  // namespace mvg
 
+namespace mvg {
+
+// Both offset arrays of a device gap-DP batch to the host, through a
+// pinned buffer (one synchronisation, no pageable staging).
+static int offsets_to_host(Ctx* c, const uint64_t* d_a, const uint64_t* d_b, int64_t nprob,
+                           std::vector<uint64_t>& oa, std::vector<uint64_t>& ob) {
+  const size_t bytes = (size_t)(nprob + 1) * 8;
+  if (c->h_off_cap < 2 * bytes) {
+    if (c->h_off) cudaFreeHost(c->h_off);
+    c->h_off = nullptr;
+    c->h_off_cap = 0;
+    MVG_CUDA_TRY(cudaMallocHost(&c->h_off, 2 * bytes + bytes / 4));
+    c->h_off_cap = 2 * bytes + bytes / 4;
+  }
+  uint8_t* hb = (uint8_t*)c->h_off;
+  MVG_CUDA_TRY(cudaMemcpyAsync(hb, d_a, bytes, cudaMemcpyDeviceToHost, c->stream));
+  MVG_CUDA_TRY(cudaMemcpyAsync(hb + bytes, d_b, bytes, cudaMemcpyDeviceToHost, c->stream));
+  MVG_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  oa.assign((const uint64_t*)hb, (const uint64_t*)hb + nprob + 1);
+  ob.assign((const uint64_t*)(hb + bytes), (const uint64_t*)(hb + bytes) + nprob + 1);
+  return 0;
+}
+
+}  // namespace mvg
+
 extern "C" {
 
 const char* mvg_last_error(void) { return g_last_error; }
@@ -199,6 +224,7 @@ int mvg_destroy(mvg_handle h) {
   if (h->h_err) cudaFreeHost(h->h_err);
   if (h->h_scalars) cudaFreeHost(h->h_scalars);
   if (h->h_stage) cudaFreeHost(h->h_stage);
+  if (h->h_off) cudaFreeHost(h->h_off);
   for (cudaEvent_t ev : {h->fork, h->join, h->fork2, h->join2, h->fork3, h->join3})
     if (ev) cudaEventDestroy(ev);
   for (cudaStream_t st : {h->aux3, h->aux2, h->aux, h->stream})
@@ -315,10 +341,8 @@ int mvg_gapdp_batch_dev(mvg_handle h, const uint8_t* d_seq_a, const uint64_t* d_
     return report_error(MVG_ERR_ARG, "null argument");
   if (nprob == 0) return 0;
   MVG_CUDA_TRY(cudaSetDevice(h->device));
-  std::vector<uint64_t> oa(nprob + 1), ob(nprob + 1);
-  MVG_CUDA_TRY(cudaMemcpyAsync(oa.data(), d_off_a, (nprob + 1) * 8, cudaMemcpyDeviceToHost, h->stream));
-  MVG_CUDA_TRY(cudaMemcpyAsync(ob.data(), d_off_b, (nprob + 1) * 8, cudaMemcpyDeviceToHost, h->stream));
-  MVG_CUDA_TRY(cudaStreamSynchronize(h->stream));
+  std::vector<uint64_t> oa, ob;
+  if (int rc = offsets_to_host(h, d_off_a, d_off_b, nprob, oa, ob)) return rc;
   return gapdp_batch_dev(h, d_seq_a, d_off_a, d_seq_b, d_off_b, nprob, d_scores, d_paths, d_path_off, d_path_len,
                          oa.data(), ob.data());
 }
@@ -365,10 +389,8 @@ int mvg_gapdp_envelope_dev(mvg_handle h, const uint8_t* d_seq_a, const uint64_t*
     return report_error(MVG_ERR_ARG, "null argument");
   if (nprob == 0) return 0;
   MVG_CUDA_TRY(cudaSetDevice(h->device));
-  std::vector<uint64_t> oa(nprob + 1), ob(nprob + 1);
-  MVG_CUDA_TRY(cudaMemcpyAsync(oa.data(), d_off_a, (nprob + 1) * 8, cudaMemcpyDeviceToHost, h->stream));
-  MVG_CUDA_TRY(cudaMemcpyAsync(ob.data(), d_off_b, (nprob + 1) * 8, cudaMemcpyDeviceToHost, h->stream));
-  MVG_CUDA_TRY(cudaStreamSynchronize(h->stream));
+  std::vector<uint64_t> oa, ob;
+  if (int rc = offsets_to_host(h, d_off_a, d_off_b, nprob, oa, ob)) return rc;
   return gapdp_batch_dev(h, d_seq_a, d_off_a, d_seq_b, d_off_b, nprob, d_scores, nullptr, nullptr, nullptr, oa.data(),
                          ob.data(), d_env);
 }
@@ -382,10 +404,8 @@ int mvg_gapdp_banded_dev(mvg_handle h, const uint8_t* d_seq_a, const uint64_t* d
     return report_error(MVG_ERR_ARG, "null argument");
   if (nprob == 0) return 0;
   MVG_CUDA_TRY(cudaSetDevice(h->device));
-  std::vector<uint64_t> oa(nprob + 1), ob(nprob + 1);
-  MVG_CUDA_TRY(cudaMemcpyAsync(oa.data(), d_off_a, (nprob + 1) * 8, cudaMemcpyDeviceToHost, h->stream));
-  MVG_CUDA_TRY(cudaMemcpyAsync(ob.data(), d_off_b, (nprob + 1) * 8, cudaMemcpyDeviceToHost, h->stream));
-  MVG_CUDA_TRY(cudaStreamSynchronize(h->stream));
+  std::vector<uint64_t> oa, ob;
+  if (int rc = offsets_to_host(h, d_off_a, d_off_b, nprob, oa, ob)) return rc;
   return gapdp_banded_dev(h, d_seq_a, d_off_a, d_seq_b, d_off_b, nprob, band_delta, band_half, d_scores, d_paths,
                           d_path_off, d_path_len, used_band, oa.data(), ob.data(), cells);
 }

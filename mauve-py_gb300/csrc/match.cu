@@ -848,10 +848,10 @@ int pairwise_matches_dev(Ctx* c, const uint8_t* d_a, uint64_t na, const uint8_t*
   if (bucketed) {
     if ((rc = pair_buckets(c, ga, ca, gb, cb, s, &ps))) return rc;
     stage_mark(c, "unique_join");
-    uint32_t* sscr = (uint32_t*)ws.get(c, 34, (scan_scratch_words(ps.nbuckets) + 8) * 4);
-    if (!sscr) return report_error(MVG_ERR_NOMEM, "workspace allocation failed");
-    d_npairs = sscr + scan_scratch_words(ps.nbuckets) + 1;
-    exclusive_scan(ps.pcount, ps.pbase, ps.nbuckets, sscr, d_npairs, c->stream, &c->launches);
+    d_npairs = (uint32_t*)ws.get(c, 34, 64);
+    if (!d_npairs) return report_error(MVG_ERR_NOMEM, "workspace allocation failed");
+    pair_scan_small(ps.pcount, ps.nbuckets, ps.pbase, d_npairs, c->stream);
+    c->launches++;
   } else {
     if ((rc = pair_sort(c, ga, ca, gb, cb, s, &sk))) return rc;
     stage_mark(c, "unique_join");

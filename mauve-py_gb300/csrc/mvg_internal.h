@@ -40,6 +40,8 @@ struct Ctx {
   uint64_t* h_scalars = nullptr; // pinned scalars for small device->host reads
   uint8_t* h_stage = nullptr;    // pinned staging of one call's host->device copies (bump allocated)
   size_t h_stage_cap = 0, h_stage_used = 0;
+  void* h_off = nullptr;         // pinned buffer for gap-DP offsets read back from the device
+  size_t h_off_cap = 0;
   uint64_t launches = 0;
   uint64_t tb_arena = ~0ull;  // capped per call at 60% of free device memory
   int dp_rows = 8;            // full gap-DP rows per lane (4 or 8)
@@ -131,6 +133,8 @@ struct PairStage {
 };
 int pair_buckets(Ctx* c, const uint32_t* ga, uint64_t ca, const uint32_t* gb, uint64_t cb, const SeedDesc& s,
                  PairStage* out);
+// Exclusive scan of n <= 16384 counts in one launch; *total gets the sum.
+void pair_scan_small(const uint32_t* in, int n, uint32_t* out, uint32_t* total, cudaStream_t st);
 int pair_sort(Ctx* c, const uint32_t* ga, uint64_t ca, const uint32_t* gb, uint64_t cb, const SeedDesc& s,
               SmlKeys* out);
 int check_device_error(Ctx* c);

@@ -143,11 +143,10 @@ __global__ void __launch_bounds__(256) k_pb_csum(const uint32_t* __restrict__ co
 }
 
 // One block of 1024 threads, 16 consecutive buckets per thread (nbk <=
-// 16384): bucket totals, starts (exclusive scan over buckets) and each
-// chunk's first slot per bucket (cbase).
+// 16384): every bucket's total over the chunks and its start (exclusive
+// scan over buckets).
 __global__ void __launch_bounds__(1024) k_pb_scan(const uint32_t* __restrict__ csum, int64_t nchunks, int nbk,
-                                                  uint32_t* __restrict__ cbase, uint32_t* __restrict__ bstart,
-                                                  uint32_t* __restrict__ bsize) {
+                                                  uint32_t* __restrict__ bstart, uint32_t* __restrict__ bsize) {
   constexpr int kPer = 16;
   __shared__ uint32_t wsum[32];
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
@@ -155,7 +154,8 @@ __global__ void __launch_bounds__(1024) k_pb_scan(const uint32_t* __restrict__ c
   uint32_t tot[kPer];
 #pragma unroll
   for (int k = 0; k < kPer; ++k) tot[k] = 0;
-  if (d0 < nbk)
+  if (d0 < nbk) {
+#pragma unroll 4
     for (int64_t c = 0; c < nchunks; ++c) {
       const uint4* q = reinterpret_cast<const uint4*>(csum + c * nbk + d0);
 #pragma unroll
@@ -167,6 +167,7 @@ __global__ void __launch_bounds__(1024) k_pb_scan(const uint32_t* __restrict__ c
         tot[4 * k + 3] += v.w;
       }
     }
+  }
   uint32_t mine = 0;
 #pragma unroll
   for (int k = 0; k < kPer; ++k) mine += tot[k];
@@ -180,34 +181,21 @@ __global__ void __launch_bounds__(1024) k_pb_scan(const uint32_t* __restrict__ c
   }
   __syncthreads();
   if (d0 >= nbk) return;
-  uint32_t run[kPer];
   uint32_t start = wsum[wid] + inc - mine;
 #pragma unroll
   for (int k = 0; k < kPer; ++k) {
     bstart[d0 + k] = start;
     bsize[d0 + k] = tot[k];
-    run[k] = start;
     start += tot[k];
-  }
-  for (int64_t c = 0; c < nchunks; ++c) {
-    const uint4* q = reinterpret_cast<const uint4*>(csum + c * nbk + d0);
-    uint4* o = reinterpret_cast<uint4*>(cbase + c * nbk + d0);
-#pragma unroll
-    for (int k = 0; k < kPer / 4; ++k) {
-      const uint4 v = q[k];
-      o[k] = make_uint4(run[4 * k], run[4 * k + 1], run[4 * k + 2], run[4 * k + 3]);
-      run[4 * k] += v.x;
-      run[4 * k + 1] += v.y;
-      run[4 * k + 2] += v.z;
-      run[4 * k + 3] += v.w;
-    }
   }
 }
 
-// Block (x, c): chunk c's tiles' first slots per bucket (offs), the chunk's
-// count rows loaded before any store.
+// Block (x, c): chunk c's tiles' first slots per bucket (offs): the
+// bucket's start plus the earlier chunks' sums, then the chunk's count rows
+// (all loads issued before any store).
 __global__ void __launch_bounds__(256) k_pb_offsets(const uint32_t* __restrict__ counts, int64_t ntiles, int nbk,
-                                                    const uint32_t* __restrict__ cbase, uint32_t* __restrict__ offs) {
+                                                    const uint32_t* __restrict__ csum,
+                                                    const uint32_t* __restrict__ bstart, uint32_t* __restrict__ offs) {
   const int d = blockIdx.x * 256 + threadIdx.x;
   if (d >= nbk) return;
   const int64_t c = blockIdx.y;
@@ -216,12 +204,49 @@ __global__ void __launch_bounds__(256) k_pb_offsets(const uint32_t* __restrict__
   uint32_t v[pb::kChunkTiles];
 #pragma unroll
   for (int k = 0; k < pb::kChunkTiles; ++k) v[k] = k < nt ? counts[(t0 + k) * nbk + d] : 0u;
-  uint32_t run = cbase[c * nbk + d];
+  uint32_t run = bstart[d];
+  for (int64_t cc = 0; cc < c; ++cc) run += csum[cc * nbk + d];
 #pragma unroll
   for (int k = 0; k < pb::kChunkTiles; ++k) {
     if (k < nt) offs[(t0 + k) * nbk + d] = run;
     run += v[k];
   }
+}
+
+// Exclusive scan of n <= 16384 counts by one block of 1024 threads (16
+// consecutive counts each); *total gets the sum.
+__global__ void __launch_bounds__(1024) k_pb_scan_small(const uint32_t* __restrict__ in, int n,
+                                                        uint32_t* __restrict__ out, uint32_t* __restrict__ total) {
+  constexpr int kPer = 16;
+  __shared__ uint32_t wsum[32];
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const int i0 = tid * kPer;
+  uint32_t v[kPer], mine = 0;
+#pragma unroll
+  for (int k = 0; k < kPer; ++k) {
+    v[k] = i0 + k < n ? in[i0 + k] : 0u;
+    mine += v[k];
+  }
+  const uint32_t inc = warp_incl_scan(mine);
+  if (lane == 31) wsum[wid] = inc;
+  __syncthreads();
+  if (wid == 0) {
+    const uint32_t x = wsum[lane];
+    const uint32_t y = warp_incl_scan(x);
+    wsum[lane] = y - x;
+    if (lane == 31 && total) *total = y;
+  }
+  __syncthreads();
+  uint32_t r = wsum[wid] + inc - mine;
+#pragma unroll
+  for (int k = 0; k < kPer; ++k) {
+    if (i0 + k < n) out[i0 + k] = r;
+    r += v[k];
+  }
+}
+
+void pair_scan_small(const uint32_t* in, int n, uint32_t* out, uint32_t* total, cudaStream_t st) {
+  k_pb_scan_small<<<1, 1024, 0, st>>>(in, n, out, total);
 }
 
 // ------------------------------------------------------------- scatter
@@ -581,14 +606,13 @@ int pair_buckets(Ctx* c, const uint32_t* ga, uint64_t ca, const uint32_t* gb, ui
   uint2* bufp = (uint2*)ws.get(c, 31, (size_t)n * 8 + 64);
   // count rows, then the tiles' first slots (ntiles x nbk each)
   uint32_t* counts = (uint32_t*)ws.get(c, 32, (size_t)g.ntiles * nbk * 8 + 64);
-  uint32_t* tabs = (uint32_t*)ws.get(c, 33, (2 * (size_t)g.nchunks * nbk + 4 * (size_t)nbk) * 4 + 256);
+  uint32_t* tabs = (uint32_t*)ws.get(c, 33, ((size_t)g.nchunks * nbk + 4 * (size_t)nbk) * 4 + 256);
   if (!kp || !bufp || !counts || !tabs) return report_error(MVG_ERR_NOMEM, "workspace allocation failed");
   uint32_t* keys = kp;
   uint32_t* pos = kp + n4;
   uint32_t* offs = counts + (size_t)g.ntiles * nbk;
   uint32_t* csum = tabs;
-  uint32_t* cbase = csum + (size_t)g.nchunks * nbk;
-  uint32_t* bstart = cbase + (size_t)g.nchunks * nbk;
+  uint32_t* bstart = csum + (size_t)g.nchunks * nbk;
   uint32_t* bsize = bstart + nbk;
   uint32_t* pcount = bsize + nbk;
   uint32_t* pbase = pcount + nbk;
@@ -605,8 +629,8 @@ int pair_buckets(Ctx* c, const uint32_t* ga, uint64_t ca, const uint32_t* gb, ui
                                                                      g.tile);
   const dim3 grid2((unsigned)((nbk + 255) / 256), (unsigned)g.nchunks);
   k_pb_csum<<<grid2, 256, 0, c->stream>>>(counts, g.ntiles, nbk, csum);
-  k_pb_scan<<<1, 1024, 0, c->stream>>>(csum, g.nchunks, nbk, cbase, bstart, bsize);
-  k_pb_offsets<<<grid2, 256, 0, c->stream>>>(counts, g.ntiles, nbk, cbase, offs);
+  k_pb_scan<<<1, 1024, 0, c->stream>>>(csum, g.nchunks, nbk, bstart, bsize);
+  k_pb_offsets<<<grid2, 256, 0, c->stream>>>(counts, g.ntiles, nbk, csum, bstart, offs);
   stage_mark(c, "seed_scatter");
   k_pb_scatter<<<(unsigned)g.ntiles, pb::kKeyThreads, hsm, c->stream>>>(keys, pos, n, offs, g.bbits,
                                                                         2 * s.w + 2 - g.bbits, g.tile, bufp);
