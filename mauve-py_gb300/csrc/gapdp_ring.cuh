@@ -422,14 +422,6 @@ __global__ void k_traceback_ring(const uint64_t* __restrict__ oa, const uint64_t
     char cur = (char)end_edge[p];
     int64_t n = 0;
     const int64_t limit = (int64_t)LA + LB;
-    // The walk's traceback words only move down its group's column (word
-    // indices never increase along the path), so the 8 words below the
-    // current one are kept in registers and each step that moves down loads
-    // the word 8 below: a load is consumed about 8 steps after it is issued
-    // instead of stalling every step.
-    uint32_t qv[8];
-    int64_t qw = -1;  // word index of qv[0] (none loaded)
-    int qt = -1;      // column of the queue
     for (;;) {
       if (n >= limit) {
         set_error(err, kDevCapacity);
@@ -445,23 +437,19 @@ __global__ void k_traceback_ring(const uint64_t* __restrict__ oa, const uint64_t
           set_error(err, kDevCapacity);
           break;
         }
-        int64_t X;
+        int64_t word;
         int sh;
-        ring_tb_at(R, (int64_t)(pb + g - b.lo0), r, X, sh);
-        const int t = g & 31;
-        if (t != qt || X > qw || X < qw - 7) {  // (re)fill the queue from X down
-          qt = t;
-          qw = X;
-#pragma unroll
-          for (int k = 0; k < 8; ++k) qv[k] = X - k >= 0 ? T[(X - k) * 32 + t] : 0u;
+        const int64_t st = (int64_t)(pb + g - b.lo0);
+        ring_tb_at(R, st, r, word, sh);
+        bits = (T[word * 32 + (g & 31)] >> sh) & 15u;
+        // the path runs right to left along the group: start fetching the
+        // word 8 steps back (each step's word is otherwise a dependent miss)
+        if (st >= 8) {
+          int64_t w8;
+          int sh8;
+          ring_tb_at(R, st - 8, r, w8, sh8);
+          asm volatile("prefetch.global.L1 [%0];" ::"l"(T + w8 * 32 + (g & 31)));
         }
-        while (qw > X) {  // move down, fetching the word 8 below
-#pragma unroll
-          for (int k = 0; k < 7; ++k) qv[k] = qv[k + 1];
-          qv[7] = qw - 8 >= 0 ? T[(qw - 8) * 32 + t] : 0u;
-          --qw;
-        }
-        bits = (qv[0] >> sh) & 15u;
       }
       char next;
       if (cur == 'M') {
