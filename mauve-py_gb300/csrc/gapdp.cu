@@ -157,11 +157,17 @@ __global__ void k_traceback(const uint64_t* __restrict__ oa, const uint64_t* __r
         }
         const int nib = s * rows + r;
         bits = (T[base + (nib >> 3) * 32 + t] >> (4 * (nib & 7))) & 15u;
-        // the path runs right to left through the strip: start fetching the
-        // word 8 steps ahead (each step's word is otherwise a dependent miss)
-        if (s >= 8) {
-          const int nib_ahead = (s - 8) * rows + r;
-          asm volatile("prefetch.global.L1 [%0];" ::"l"(T + base + (nib_ahead >> 3) * 32 + t));
+        // start fetching the word of the cell 8 steps further along the
+        // diagonal (most steps are matches): 8 rows up in this strip, which
+        // is another lane's stream (each step's word is otherwise a
+        // dependent miss)
+        if (rem >= 8 && pb > 8) {
+          const int t8 = (rem - 8) / rows, r8 = (rem - 8) % rows;
+          const int s8 = (pb - 8) - cur_lo + t8;
+          if (s8 >= t8) {
+            const int nib8 = s8 * rows + r8;
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(T + base + (nib8 >> 3) * 32 + t8));
+          }
         }
       }
       char next;

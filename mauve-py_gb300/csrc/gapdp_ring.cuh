@@ -422,6 +422,7 @@ __global__ void k_traceback_ring(const uint64_t* __restrict__ oa, const uint64_t
     char cur = (char)end_edge[p];
     int64_t n = 0;
     const int64_t limit = (int64_t)LA + LB;
+    int gc = -1, loc = 0, gc8 = -1, loc8 = 0;  // first column of the last group looked up (and 8 cells back)
     for (;;) {
       if (n >= limit) {
         set_error(err, kDevCapacity);
@@ -432,23 +433,34 @@ __global__ void k_traceback_ring(const uint64_t* __restrict__ oa, const uint64_t
       uint32_t bits = 0;
       if (pa >= 1 && pb >= 1) {
         const int g = (pa - 1) / R, r = (pa - 1) - g * R;
-        const int lo = ring_lo(b, g);
-        if (pb < lo || pb > lo + b.W - 1) {  // outside an accepted band cannot happen
+        if (g != gc) {
+          gc = g;
+          loc = ring_lo(b, g);
+        }
+        if (pb < loc || pb > loc + b.W - 1) {  // outside an accepted band cannot happen
           set_error(err, kDevCapacity);
           break;
         }
         int64_t word;
         int sh;
-        const int64_t st = (int64_t)(pb + g - b.lo0);
-        ring_tb_at(R, st, r, word, sh);
+        ring_tb_at(R, (int64_t)(pb + g - b.lo0), r, word, sh);
         bits = (T[word * 32 + (g & 31)] >> sh) & 15u;
-        // the path runs right to left along the group: start fetching the
-        // word 8 steps back (each step's word is otherwise a dependent miss)
-        if (st >= 8) {
-          int64_t w8;
-          int sh8;
-          ring_tb_at(R, st - 8, r, w8, sh8);
-          asm volatile("prefetch.global.L1 [%0];" ::"l"(T + w8 * 32 + (g & 31)));
+        // start fetching the word of the cell 8 steps further along the
+        // diagonal (most steps are matches), which may lie in another group
+        // and column: each step's word is otherwise a dependent miss
+        if (pa > 8 && pb > 8) {
+          const int pa8 = pa - 8, pb8 = pb - 8;
+          const int g8 = (pa8 - 1) / R, r8 = (pa8 - 1) - g8 * R;
+          if (g8 != gc8) {
+            gc8 = g8;
+            loc8 = ring_lo(b, g8);
+          }
+          if (pb8 >= loc8 && pb8 <= loc8 + b.W - 1) {
+            int64_t w8;
+            int sh8;
+            ring_tb_at(R, (int64_t)(pb8 + g8 - b.lo0), r8, w8, sh8);
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(T + w8 * 32 + (g8 & 31)));
+          }
         }
       }
       char next;
