@@ -23,6 +23,7 @@
 #include <cmath>
 #include <functional>
 #include <numeric>
+#include <thread>
 #include <vector>
 
 #include "gapdp_kernel.cuh"
@@ -82,6 +83,27 @@ template __global__ void k_gapdp_ring<32>(RingJob);
 // The group heights the ring schedule offers, smallest first.
 static const int kRingRows[] = {4, 6, 8, 12, 16, 24, 32};
 constexpr int kRingHeights = (int)(sizeof(kRingRows) / sizeof(kRingRows[0]));
+
+// Runs f(begin, end, t) over [0, n) in up to 16 contiguous chunks on host
+// threads (one chunk below 20,000 items), chunk t covering items before
+// chunk t + 1's; returns the number of chunks.
+template <class F>
+static int host_chunks(int64_t n, F f) {
+  int nt = 1;
+  if (n >= 20000) {
+    const unsigned hw = std::thread::hardware_concurrency();
+    nt = (int)std::min<int64_t>(std::min<unsigned>(hw ? hw : 1, 16u), n / 5000);
+    if (nt < 1) nt = 1;
+  }
+  if (nt == 1) {
+    f((int64_t)0, n, 0);
+    return 1;
+  }
+  std::vector<std::thread> th;
+  for (int t = 0; t < nt; ++t) th.emplace_back(f, n * t / nt, n * (t + 1) / nt, t);
+  for (auto& x : th) x.join();
+  return nt;
+}
 
 static void (*ring_kernel(int R))(RingJob) {
   switch (R) {
@@ -490,19 +512,36 @@ static int run_ring(Ctx* c, const TbLanes& L, const DpInputs& in, const std::vec
   if (nwork == 0) return 0;
   std::unique_ptr<HostSpan> span(new HostSpan(c, "ring_plan"));
   std::vector<uint64_t> bytes(nwork), cost(nwork);
-  for (int64_t w = 0; w < nwork; ++w) {
-    const uint32_t p = ids[w];
-    const RingBand b = make_ring_band((int)la[p], (int)lb[p], dv[p], hv[p], rsel[w]);
-    bytes[w] = (ring_tb_words(b) * 4 + 255) & ~255ull;
-    cost[w] = (uint64_t)b.steps * (uint64_t)(rsel[w] * 18 + 50);
-  }
+  host_chunks(nwork, [&](int64_t w0, int64_t w1, int) {
+    for (int64_t w = w0; w < w1; ++w) {
+      const uint32_t p = ids[w];
+      const RingBand b = make_ring_band((int)la[p], (int)lb[p], dv[p], hv[p], rsel[w]);
+      bytes[w] = (ring_tb_words(b) * 4 + 255) & ~255ull;
+      cost[w] = (uint64_t)b.steps * (uint64_t)(rsel[w] * 18 + 50);
+    }
+  });
   // by group height, each class most expensive first, ties in input order
+  // (the classes gathered in order, then sorted on their own threads)
   std::vector<uint32_t> idx(nwork);
   {
     std::vector<std::pair<uint64_t, uint32_t>> key(nwork);
+    int64_t cls_begin[kRingHeights + 1] = {};
     for (int64_t w = 0; w < nwork; ++w)
-      key[w] = {((uint64_t)rsel[w] << 56) | ((~cost[w]) & ((1ull << 56) - 1)), (uint32_t)w};
-    std::sort(key.begin(), key.end());
+      for (int q = 0; q < kRingHeights; ++q)
+        if (rsel[w] == kRingRows[q]) cls_begin[q + 1]++;
+    for (int q = 0; q < kRingHeights; ++q) cls_begin[q + 1] += cls_begin[q];
+    int64_t fill[kRingHeights];
+    for (int q = 0; q < kRingHeights; ++q) fill[q] = cls_begin[q];
+    for (int64_t w = 0; w < nwork; ++w)
+      for (int q = 0; q < kRingHeights; ++q)
+        if (rsel[w] == kRingRows[q]) key[fill[q]++] = {~cost[w], (uint32_t)w};
+    std::vector<std::thread> th;
+    for (int q = 0; q < kRingHeights; ++q)
+      if (cls_begin[q + 1] - cls_begin[q] > 1)
+        th.emplace_back([&key, &cls_begin, q]() {
+          std::sort(key.begin() + cls_begin[q], key.begin() + cls_begin[q + 1]);
+        });
+    for (auto& x : th) x.join();
     for (int64_t w = 0; w < nwork; ++w) idx[w] = key[w].second;
   }
   uint64_t arena = c->tb_arena;
@@ -536,7 +575,7 @@ static int run_ring(Ctx* c, const TbLanes& L, const DpInputs& in, const std::vec
   uint32_t* d_order = (uint32_t*)ws.get(c, 64, (size_t)nwork * 4);
   uint64_t* d_tboff = (uint64_t*)ws.get(c, 65, (size_t)nwork * 8);
   uint8_t* d_edge = (uint8_t*)ws.get(c, 13, la.size() + 16);
-  unsigned* d_counter = (unsigned*)ws.get(c, 66, 64);
+  unsigned* d_counter = (unsigned*)ws.get(c, 66, 64 * kRingHeights);  // one claim counter per height
   uint8_t* d_rows = (uint8_t*)ws.get(c, 60, (size_t)nwork + 16);
   uint32_t* tb = (uint32_t*)ws.get(c, 67, arena_need);
   if (!d_order || !d_tboff || !d_edge || !d_counter || !d_rows || !tb)
@@ -549,10 +588,24 @@ static int run_ring(Ctx* c, const TbLanes& L, const DpInputs& in, const std::vec
   span.reset();
   for (size_t wv = 0; wv + 1 < wave_begin.size(); ++wv) {
     const int64_t w0 = wave_begin[wv], w1 = wave_begin[wv + 1];
+    // heights of 16 rows and more run on the side stream beside the smaller
+    // ones: their few long problems end in a latency-bound tail (one warp,
+    // one problem) that would otherwise hold up the next launch
+    bool side_used = false;
+    for (int64_t a = w0; a < w1 && !side_used; ++a) side_used = rows_of[a] >= 16;
+    if (side_used) {  // the side stream starts with the wave, not after the smaller heights
+      MVG_CUDA_TRY(cudaEventRecord(L.fork, L.st));
+      MVG_CUDA_TRY(cudaStreamWaitEvent(L.side, L.fork, 0));
+    }
     for (int64_t a = w0; a < w1;) {
       int64_t e = a;
       while (e < w1 && rows_of[e] == rows_of[a]) ++e;
       const int R = rows_of[a];
+      int hq = 0;
+      while (hq + 1 < kRingHeights && kRingRows[hq] != R) ++hq;
+      const bool side = R >= 16;
+      const cudaStream_t ks = side ? L.side : L.st;
+      unsigned* ctr = d_counter + 16 * hq;
       void (*kern)(RingJob) = ring_kernel(R);
       int bps = 0;
       MVG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, kern, kRingThreads, 0));
@@ -574,12 +627,16 @@ static int run_ring(Ctx* c, const TbLanes& L, const DpInputs& in, const std::vec
       J.band_half = d_half;
       J.accept = d_accept;
       J.base_max = g_base_max;
-      J.counter = d_counter;
+      J.counter = ctr;
       J.cells = d_cells;
-      MVG_CUDA_TRY(cudaMemsetAsync(d_counter, 0, 4, L.st));
-      kern<<<grid, kRingThreads, 0, L.st>>>(J);
+      MVG_CUDA_TRY(cudaMemsetAsync(ctr, 0, 4, ks));
+      kern<<<grid, kRingThreads, 0, ks>>>(J);
       c->launches++;
       a = e;
+    }
+    if (side_used) {
+      MVG_CUDA_TRY(cudaEventRecord(L.join, L.side));
+      MVG_CUDA_TRY(cudaStreamWaitEvent(L.st, L.join, 0));
     }
     const int nw = (int)(w1 - w0);
     std::vector<uint32_t> slot_len(w1 - w0);
@@ -701,50 +758,75 @@ int gapdp_banded_dev(Ctx* c, const uint8_t* d_sa, const uint64_t* d_oa, const ui
   std::vector<uint32_t> ids, rids, wids;
   std::vector<uint8_t> rsel;
   std::vector<uint8_t> whole(nprob, 0);
-  for (int64_t p = 0; p < nprob; ++p) {
-    if (hv[p] < 0) return report_error(MVG_ERR_ARG, "negative band half-width");
-    const uint64_t full = (uint64_t)la[p] * (uint64_t)lb[p];
-    bool is_whole;
-    uint64_t cells = 0;
-    if (c->band_ring) {
-      // columns a row keeps: both half-widths, the row's own cells and the
-      // diagonal's drift over one row
-      const double cols = 2.0 * hv[p] + 2.0 + std::ceil((double)lb[p] / (double)la[p]);
-      is_whole = cols >= c->band_whole * (double)lb[p];
-    } else {
-      cells = band_cells(make_band((int)la[p], (int)lb[p], dv[p], hv[p], 32 * c->band_rows));
-      is_whole = (double)cells >= c->band_whole * (double)full;
-    }
-    if (is_whole) {
-      whole[p] = 1;
-      dv[p] = 0;
-      hv[p] = (int32_t)std::max(la[p], lb[p]) + 2;
-      bc += full;
-      // long ones through the full DP's taller strips, short ones beside
-      // the strip kernel's bands
-      (la[p] >= kWholeFullRows ? wids : ids).push_back((uint32_t)p);
-      continue;
-    }
-    int rr = 0;
-    if (c->band_ring) {
-      // the lane-reuse condition W <= 32 + 32*R*LB/LA decides most heights;
-      // only heights that pass it (with a column of slack) get the exact test
-      const double slope = (double)lb[p] / (double)la[p];
-      for (int q = 0; q < kRingHeights && !rr; ++q) {
-        const int R = kRingRows[q];
-        const bool many = (la[p] + R - 1) / R > 32;
-        if (many && 2.0 * hv[p] + 2.0 + (R - 1) * slope > 32.0 + 32.0 * R * slope + 2.0) continue;
-        if (ring_eligible(make_ring_band((int)la[p], (int)lb[p], dv[p], hv[p], R))) rr = R;
+  // classified in chunks on host threads, each into its own lists, then
+  // joined in chunk order (the same lists as one pass in order)
+  struct Part {
+    std::vector<uint32_t> ids, rids, wids;
+    std::vector<uint8_t> rsel;
+    uint64_t bc = 0;
+    bool bad = false;
+  };
+  std::vector<Part> parts(16);
+  const int nparts = host_chunks(nprob, [&](int64_t p0, int64_t p1, int t) {
+    Part& P = parts[t];
+    for (int64_t p = p0; p < p1; ++p) {
+      if (hv[p] < 0) {
+        P.bad = true;
+        return;
+      }
+      const uint64_t full = (uint64_t)la[p] * (uint64_t)lb[p];
+      bool is_whole;
+      uint64_t cells = 0;
+      if (c->band_ring) {
+        // columns a row keeps: both half-widths, the row's own cells and
+        // the diagonal's drift over one row
+        const double cols = 2.0 * hv[p] + 2.0 + std::ceil((double)lb[p] / (double)la[p]);
+        is_whole = cols >= c->band_whole * (double)lb[p];
+      } else {
+        cells = band_cells(make_band((int)la[p], (int)lb[p], dv[p], hv[p], 32 * c->band_rows));
+        is_whole = (double)cells >= c->band_whole * (double)full;
+      }
+      if (is_whole) {
+        whole[p] = 1;
+        dv[p] = 0;
+        hv[p] = (int32_t)std::max(la[p], lb[p]) + 2;
+        P.bc += full;
+        // long ones through the full DP's taller strips, short ones beside
+        // the strip kernel's bands
+        (la[p] >= kWholeFullRows ? P.wids : P.ids).push_back((uint32_t)p);
+        continue;
+      }
+      int rr = 0;
+      if (c->band_ring) {
+        // the lane-reuse condition W <= 32 + 32*R*LB/LA decides most
+        // heights; only heights that pass it (with a column of slack) get
+        // the exact test
+        const double slope = (double)lb[p] / (double)la[p];
+        for (int q = 0; q < kRingHeights && !rr; ++q) {
+          const int R = kRingRows[q];
+          const bool many = (la[p] + R - 1) / R > 32;
+          if (many && 2.0 * hv[p] + 2.0 + (R - 1) * slope > 32.0 + 32.0 * R * slope + 2.0) continue;
+          if (ring_eligible(make_ring_band((int)la[p], (int)lb[p], dv[p], hv[p], R))) rr = R;
+        }
+      }
+      if (rr) {
+        P.rids.push_back((uint32_t)p);
+        P.rsel.push_back((uint8_t)rr);
+      } else {
+        if (c->band_ring) cells = band_cells(make_band((int)la[p], (int)lb[p], dv[p], hv[p], 32 * c->band_rows));
+        P.bc += cells;
+        P.ids.push_back((uint32_t)p);
       }
     }
-    if (rr) {
-      rids.push_back((uint32_t)p);
-      rsel.push_back((uint8_t)rr);
-    } else {
-      if (c->band_ring) cells = band_cells(make_band((int)la[p], (int)lb[p], dv[p], hv[p], 32 * c->band_rows));
-      bc += cells;
-      ids.push_back((uint32_t)p);
-    }
+  });
+  for (int t = 0; t < nparts; ++t) {
+    const Part& P = parts[t];
+    if (P.bad) return report_error(MVG_ERR_ARG, "negative band half-width");
+    ids.insert(ids.end(), P.ids.begin(), P.ids.end());
+    rids.insert(rids.end(), P.rids.begin(), P.rids.end());
+    wids.insert(wids.end(), P.wids.begin(), P.wids.end());
+    rsel.insert(rsel.end(), P.rsel.begin(), P.rsel.end());
+    bc += P.bc;
   }
   int32_t* d_delta = (int32_t*)c->ws.get(c, 23, (size_t)nprob * 4);
   int32_t* d_half = (int32_t*)c->ws.get(c, 25, (size_t)nprob * 4);
