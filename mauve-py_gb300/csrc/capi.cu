@@ -118,7 +118,7 @@ static const uint64_t kSeedTable[29][6] = {
 namespace mvg {
 
 int stage_reserve(Ctx* c, size_t need) {
-  for (cudaStream_t st : {c->stream, c->aux, c->aux2, c->aux3})
+  for (cudaStream_t st : {c->stream, c->aux, c->aux2, c->aux3, c->aux4, c->aux5})
     if (st) MVG_CUDA_TRY(cudaStreamSynchronize(st));
   c->h_stage_used = 0;
   if (c->h_stage_cap >= need) return 0;
@@ -195,6 +195,10 @@ int mvg_create(mvg_handle* out, int device) {
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->join2, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->fork3, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->join3, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->aux4, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->aux5, cudaStreamNonBlocking);
+  for (cudaEvent_t* ev : {&c->fork4, &c->join4, &c->fork5, &c->join5})
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaMalloc(&c->d_err, 64);
   if (e == cudaSuccess) e = cudaMallocHost(&c->h_err, 64);
   if (e == cudaSuccess) e = cudaMallocHost(&c->h_scalars, 64);
@@ -216,7 +220,7 @@ int mvg_create(mvg_handle* out, int device) {
 int mvg_destroy(mvg_handle h) {
   if (!h) return 0;
   cudaSetDevice(h->device);
-  for (cudaStream_t st : {h->stream, h->aux, h->aux2, h->aux3})
+  for (cudaStream_t st : {h->stream, h->aux, h->aux2, h->aux3, h->aux4, h->aux5})
     if (st) cudaStreamSynchronize(st);
   mlp_release(h);
   h->ws.release();
@@ -225,9 +229,10 @@ int mvg_destroy(mvg_handle h) {
   if (h->h_scalars) cudaFreeHost(h->h_scalars);
   if (h->h_stage) cudaFreeHost(h->h_stage);
   if (h->h_off) cudaFreeHost(h->h_off);
-  for (cudaEvent_t ev : {h->fork, h->join, h->fork2, h->join2, h->fork3, h->join3})
+  for (cudaEvent_t ev : {h->fork, h->join, h->fork2, h->join2, h->fork3, h->join3, h->fork4, h->join4, h->fork5,
+                         h->join5})
     if (ev) cudaEventDestroy(ev);
-  for (cudaStream_t st : {h->aux3, h->aux2, h->aux, h->stream})
+  for (cudaStream_t st : {h->aux5, h->aux4, h->aux3, h->aux2, h->aux, h->stream})
     if (st) cudaStreamDestroy(st);
   delete h;
   return 0;

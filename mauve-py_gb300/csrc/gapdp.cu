@@ -334,10 +334,18 @@ static int tb_long_join(const TbLanes& L, bool forked) {
 // Runs the DP for the problems in `ids` (full, or banded with per-problem
 // delta/half on the device): LPT order, size-mixed waves that fit the
 // traceback arena, then traceback and path compaction per wave.
+// Workspace slots of one run_dp lane: row buffers, order, traceback
+// offsets, claim counter, traceback arena.
+struct DpSlots {
+  int rowbuf, order, tboff, counter, arena;
+};
+constexpr DpSlots kDpSlots{10, 11, 12, 14, 18};
+constexpr DpSlots kDpSlotsLane2{49, 50, 51, 52, 53};
+
 static int run_dp(Ctx* c, const DpInputs& in, const std::vector<uint32_t>& ids, const std::vector<int64_t>& la,
                   const std::vector<int64_t>& lb, const int32_t* d_delta, const int32_t* d_half,
                   const std::vector<int32_t>* h_delta, const std::vector<int32_t>* h_half, uint8_t* d_accept,
-                  const TbLanes* lanes = nullptr) {
+                  const TbLanes* lanes = nullptr, const DpSlots& sl = kDpSlots) {
   const TbLanes L = lanes ? *lanes : main_lanes(c);
   const int64_t nwork = (int64_t)ids.size();
   if (nwork == 0) return 0;
@@ -381,7 +389,7 @@ static int run_dp(Ctx* c, const DpInputs& in, const std::vector<uint32_t>& ids, 
   {
     size_t free_b = 0, total_b = 0;
     if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess) {
-      const size_t have = c->ws.size[18] + free_b;  // the arena slot itself may be re-allocated
+      const size_t have = c->ws.size[sl.arena] + free_b;  // the arena slot itself may be re-allocated
       const uint64_t cap = (uint64_t)(have * 0.6);
       if (arena > cap) arena = cap;
     }
@@ -442,12 +450,12 @@ static int run_dp(Ctx* c, const DpInputs& in, const std::vector<uint32_t>& ids, 
   const int64_t nwarps = (int64_t)grid * (kDpThreads / 32);
   Workspace& ws = c->ws;
   const int64_t rb_stride = maxlb + 2;
-  int4* rowbuf = (int4*)ws.get(c, 10, (size_t)nwarps * rb_stride * sizeof(int4));
-  uint32_t* d_order = (uint32_t*)ws.get(c, 11, (size_t)nwork * 4);
-  uint64_t* d_tboff = (uint64_t*)ws.get(c, 12, (size_t)nwork * 8);
-  uint8_t* d_edge = (uint8_t*)ws.get(c, 13, (size_t)(la.size()) + 16);
-  unsigned* d_counter = (unsigned*)ws.get(c, 14, 64);
-  uint32_t* tb = (uint32_t*)ws.get(c, 18, arena_need);
+  int4* rowbuf = (int4*)ws.get(c, sl.rowbuf, (size_t)nwarps * rb_stride * sizeof(int4));
+  uint32_t* d_order = (uint32_t*)ws.get(c, sl.order, (size_t)nwork * 4);
+  uint64_t* d_tboff = (uint64_t*)ws.get(c, sl.tboff, (size_t)nwork * 8);
+  uint8_t* d_edge = (uint8_t*)ws.get(c, 13, (size_t)(la.size()) + 16);  // per problem, shared by all lanes
+  unsigned* d_counter = (unsigned*)ws.get(c, sl.counter, 64);
+  uint32_t* tb = (uint32_t*)ws.get(c, sl.arena, arena_need);
   if (!rowbuf || !d_order || !d_tboff || !d_edge || !d_counter || !tb)
     return report_error(MVG_ERR_NOMEM, "workspace allocation failed");
   if (int e = h2d_async(c, d_order, order.data(), (size_t)nwork * 4, L.st)) return e;
@@ -844,6 +852,7 @@ int gapdp_banded_dev(Ctx* c, const uint8_t* d_sa, const uint64_t* d_oa, const ui
   // problems on the main stream (their launches have separate tails)
   const TbLanes ring_lanes{c->aux, c->aux2, c->fork2, c->join2, 68, 69};
   const TbLanes strip_lanes{c->stream, c->aux3, c->fork3, c->join3, 57, 58};
+  const TbLanes band_lanes{c->aux4, c->aux5, c->fork5, c->join5, 54, 55};
   if (!rids.empty()) {
     MVG_CUDA_TRY(cudaEventRecord(c->fork, c->stream));
     MVG_CUDA_TRY(cudaStreamWaitEvent(c->aux, c->fork, 0));
@@ -851,14 +860,20 @@ int gapdp_banded_dev(Ctx* c, const uint8_t* d_sa, const uint64_t* d_oa, const ui
     if (rc) return rc;
     MVG_CUDA_TRY(cudaEventRecord(c->join, c->aux));
   }
+  // the strip kernel's problems on a third lane beside the long
+  // whole-matrix problems' full DP on the main stream
+  if (!ids.empty()) {
+    MVG_CUDA_TRY(cudaEventRecord(c->fork4, c->stream));
+    MVG_CUDA_TRY(cudaStreamWaitEvent(c->aux4, c->fork4, 0));
+    rc = run_dp(c, in, ids, la, lb, d_delta, d_half, &dv, &hv, d_accept, &band_lanes, kDpSlotsLane2);
+    if (rc) return rc;
+    MVG_CUDA_TRY(cudaEventRecord(c->join4, c->aux4));
+  }
   if (!wids.empty()) {
     rc = run_dp(c, in, wids, la, lb, nullptr, nullptr, nullptr, nullptr, nullptr, &strip_lanes);
     if (rc) return rc;
   }
-  if (!ids.empty()) {
-    rc = run_dp(c, in, ids, la, lb, d_delta, d_half, &dv, &hv, d_accept, &strip_lanes);
-    if (rc) return rc;
-  }
+  if (!ids.empty()) MVG_CUDA_TRY(cudaStreamWaitEvent(c->stream, c->join4, 0));
   if (!rids.empty()) MVG_CUDA_TRY(cudaStreamWaitEvent(c->stream, c->join, 0));
   stage_mark(c, "banded_done");
   std::vector<uint8_t> acc(nprob);

@@ -35,6 +35,8 @@ struct Ctx {
   cudaEvent_t fork = nullptr, join = nullptr;
   cudaStream_t aux2 = nullptr, aux3 = nullptr;  // side streams of work already on two streams
   cudaEvent_t fork2 = nullptr, join2 = nullptr, fork3 = nullptr, join3 = nullptr;
+  cudaStream_t aux4 = nullptr, aux5 = nullptr;  // a third lane of banded work and its side stream
+  cudaEvent_t fork4 = nullptr, join4 = nullptr, fork5 = nullptr, join5 = nullptr;
   uint32_t* d_err = nullptr;     // device error word
   uint32_t* h_err = nullptr;     // pinned mirror
   uint64_t* h_scalars = nullptr; // pinned scalars for small device->host reads
