@@ -152,6 +152,23 @@ int h2d_async(Ctx* c, void* dst, const void* src, size_t bytes, cudaStream_t st)
 
 namespace mvg {
 
+// bytes from the device into host memory through the handle's pinned
+// buffer (one synchronisation, no pageable staging).
+int pinned_d2h(Ctx* c, void* dst, const void* d_src, size_t bytes) {
+  if (bytes == 0) return 0;
+  if (c->h_off_cap < bytes) {
+    if (c->h_off) cudaFreeHost(c->h_off);
+    c->h_off = nullptr;
+    c->h_off_cap = 0;
+    MVG_CUDA_TRY(cudaMallocHost(&c->h_off, bytes + bytes / 4));
+    c->h_off_cap = bytes + bytes / 4;
+  }
+  MVG_CUDA_TRY(cudaMemcpyAsync(c->h_off, d_src, bytes, cudaMemcpyDeviceToHost, c->stream));
+  MVG_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  memcpy(dst, c->h_off, bytes);
+  return 0;
+}
+
 // Both offset arrays of a device gap-DP batch to the host, through a
 // pinned buffer (one synchronisation, no pageable staging).
 static int offsets_to_host(Ctx* c, const uint64_t* d_a, const uint64_t* d_b, int64_t nprob,

@@ -612,11 +612,9 @@ int mvg_band_propose_dev(mvg_handle h, const uint8_t* d_sa, const uint64_t* d_oa
   }
   k_to_band<<<grid_for(nprob, 256), 256, 0, c->stream>>>(s.out, nprob, alpha, beta, dd, dd + nprob, gate);
   c->launches++;
-  MVG_CUDA_TRY(cudaMemcpyAsync(h_delta, dd, nprob * 4, cudaMemcpyDeviceToHost, c->stream));
-  MVG_CUDA_TRY(cudaMemcpyAsync(h_half, dd + nprob, nprob * 4, cudaMemcpyDeviceToHost, c->stream));
   MVG_CUDA_TRY(cudaGetLastError());
-  MVG_CUDA_TRY(cudaStreamSynchronize(c->stream));
-  return 0;
+  if ((rc = pinned_d2h(c, h_delta, dd, (size_t)nprob * 4))) return rc;
+  return pinned_d2h(c, h_half, dd + nprob, (size_t)nprob * 4);
 }
 
 }  // extern "C"

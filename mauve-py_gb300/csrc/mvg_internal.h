@@ -147,6 +147,9 @@ int check_device_error(Ctx* c);
 // the pageable source when the staging is full.
 int stage_reserve(Ctx* c, size_t need);
 int h2d_async(Ctx* c, void* dst, const void* src, size_t bytes, cudaStream_t st);
+// bytes from the device to host memory through a pinned buffer, waiting
+// for the handle's stream.
+int pinned_d2h(Ctx* c, void* dst, const void* d_src, size_t bytes);
 size_t sml_key_bytes(const SeedDesc& s);
 int sml_build_into(const uint8_t* d_seq, uint64_t n, uint64_t count, const SeedDesc& s, uint32_t* packed, void* k0,
                    void* k1, uint32_t* v0, uint32_t* v1, uint32_t* scr, uint32_t* d_pos_out, uint64_t* d_mer_out,
