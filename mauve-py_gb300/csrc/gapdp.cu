@@ -893,7 +893,7 @@ int gapdp_banded_dev(Ctx* c, const uint8_t* d_sa, const uint64_t* d_oa, const ui
     }
   }
   tail.reset();
-  // rejected bands: the full DP is both the fallback and the judge
+  // rejected bands: the full DP is both the fallback and the exact result
   rc = run_dp(c, in, fallback, la, lb, nullptr, nullptr, nullptr, nullptr, nullptr);
   if (rc) return rc;
   stage_end(c);
