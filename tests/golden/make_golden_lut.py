@@ -1,8 +1,8 @@
 #!/usr/bin/env python3
 """Writes tests/golden/lut.npz from the reference's own code.
 
-    sh oracle/build_ref_indexutils.sh /root/reference
-    python tests/golden/make_golden_lut.py /root/reference
+    sh oracle/build_ref_indexutils.sh <reference checkout>
+    python tests/golden/make_golden_lut.py <reference checkout>
 
 Runs, in this container only:
   * mauve/buildindex.py's buildIndex() itself, compiled from the reference
@@ -21,7 +21,9 @@ import types
 
 import numpy as np
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("MAUVE_REFERENCE", "")
+if not os.path.isdir(os.path.join(REF, "mauve")):
+    sys.exit("give the reference checkout as the first argument or in MAUVE_REFERENCE")
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path[:0] = [os.path.join(ROOT, "oracle", "refshim_py"), os.path.join(ROOT, "oracle", "_ref"),

@@ -3,8 +3,8 @@
 its own recoded E. coli fixture pair (tests/mds42_recoded.fa vs
 tests/mds42_full.fa in the reference tree), with both genomes packed.
 
-    make -f oracle/Makefile.ref REF=/root/reference
-    python tests/golden/make_golden_mds42.py /root/reference
+    make -f oracle/Makefile.ref REF=<reference checkout>
+    python tests/golden/make_golden_mds42.py <reference checkout>
 
 The match list comes from the reference's own PairwiseMatchFinder (compiled
 into oracle/_ref/libmauveref.so) with progressiveMauve's default seed: the
@@ -18,7 +18,9 @@ import sys
 
 import numpy as np
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("MAUVE_REFERENCE", "")
+if not os.path.isdir(os.path.join(REF, "mauve")):
+    sys.exit("give the reference checkout as the first argument or in MAUVE_REFERENCE")
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 R = ctypes.CDLL(os.path.join(ROOT, "oracle", "_ref", "libmauveref.so"))

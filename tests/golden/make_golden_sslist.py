@@ -6,7 +6,7 @@ struct, libMems/SortedMerList.h:48-63), the header members an SML holds
 after Create (members the reference never sets are zero), the packed
 sequence words, and the sorted positions with their mers.
 
-    make -f oracle/Makefile.ref REF=/root/reference
+    make -f oracle/Makefile.ref REF=<reference checkout>
     python tests/golden/make_golden_sslist.py
 """
 import ctypes
