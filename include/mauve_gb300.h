@@ -78,9 +78,14 @@ int mvg_sml_build_dev(mvg_handle h, const uint8_t* d_seq, uint64_t n, uint64_t s
  * about 6.3 MB that every GPU loading the library holds until exit, which
  * limits n to 262,144 bases; longer input returns MVG_ERR_CAPACITY.  The first
  * call on a device looks up that array's device address (with the device
- * current) and uploads the base table, so make it before any stream capture.
- * All calls share the array: calls whose GPU work overlaps (other streams or
- * host threads) race and must be serialised by the caller. */
+ * current) and uploads the base table, so make it before any stream capture;
+ * a call with n = 0 does only that set-up.  Under CUDA's default lazy module
+ * loading that first look-up is also when the array's device memory is
+ * committed, so a caller about to give the rest of the device to another
+ * allocator makes its first call before doing so.  The set-up is repeated
+ * when the current context changes (after cudaDeviceReset).  All calls share
+ * the array: calls whose GPU work overlaps (other streams or host threads)
+ * race and must be serialised by the caller. */
 int mvg_sml_build_noalloc(const uint8_t* d_seq, uint64_t n, uint64_t seed, uint32_t* d_pos_out,
                           uint64_t* d_mer_out, uint64_t cap, uint64_t* count, void* stream);
 
@@ -320,6 +325,15 @@ int mvg_set_band_whole_fraction(mvg_handle h, double fraction);
  * bands no height fits run in the strip kernel.  on = 0 runs every band in
  * the strip kernel.  Results are identical either way. */
 int mvg_set_band_ring(mvg_handle h, int on);
+
+/* Watchdog of the gap DP's whole-CTA mode: each wait of a warp for the
+ * previous strip's warp polls at most `polls` times (default 2^26, about a
+ * second) before it gives up; the kernel then stops that problem, the other
+ * warps of the CTA stop at their next wait, and the call returns
+ * MVG_ERR_DEVICE instead of hanging.  The handle stays usable.  A very small
+ * limit makes the waits give up on purpose (a test of the watchdog).  No
+ * counterpart in the reference (single-threaded). */
+int mvg_set_dp_spin_limit(mvg_handle h, long long polls);
 
 /* Per-stage timing with CUDA events on the handle's stream (off by default;
  * no extra synchronisation).  After a call, mvg_stage_times gives the stage

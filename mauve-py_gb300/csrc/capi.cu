@@ -497,6 +497,12 @@ int mvg_set_band_ring(mvg_handle h, int on) {
   return 0;
 }
 
+int mvg_set_dp_spin_limit(mvg_handle h, long long polls) {
+  if (!h || polls < 1) return report_error(MVG_ERR_ARG, "spin limit must be at least 1");
+  h->dp_spin_limit = polls;
+  return 0;
+}
+
 int mvg_set_profiling(mvg_handle h, int on) {
   if (!h) return report_error(MVG_ERR_ARG, "null handle");
   h->profiling = on != 0;

@@ -483,6 +483,7 @@ static int run_dp(Ctx* c, const DpInputs& in, const std::vector<uint32_t>& ids, 
     J.base_max = g_base_max;
     J.counter = d_counter;
     J.err = c->d_err;
+    J.spin_limit = c->dp_spin_limit;
     MVG_CUDA_TRY(cudaMemsetAsync(d_counter, 0, 8, L.st));
     stage_mark(c, banded ? "dp_banded" : "dp");
     kern<<<grid, kDpThreads, 0, L.st>>>(J);

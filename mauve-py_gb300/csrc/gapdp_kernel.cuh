@@ -49,7 +49,6 @@ constexpr int32_t kMaxPair = 160;        // max NUC_SP + 60 (C/C, G/G)
 constexpr int kDpThreads = 256;
 constexpr int kDpWarps = kDpThreads / 32;
 constexpr int kCoopMinStrips = 16;       // problems with at least this many strips use a whole CTA
-constexpr long long kSpinLimit = 1ll << 26;  // bounded waits (about a second)
 
 enum : uint32_t { TB_MM = 0, TB_DM = 1, TB_IM = 2, TB_MD = 4, TB_MI = 8 };
 
@@ -78,6 +77,7 @@ struct DpJob {
   uint32_t base_max;          // banded mode: best score of each base code, byte c = max + kScoreBias
   unsigned* counter;          // [0] large-problem claims (per CTA), [1] small-problem claims (per warp)
   uint32_t* err;
+  long long spin_limit;       // polls before a cooperative-mode wait gives up (watchdog)
 };
 
 __host__ __device__ __forceinline__ int tb_words_per_lane(int W, int R) { return band_words_per_lane(W, R); }
@@ -207,7 +207,7 @@ __device__ void dp_solve(const DpJob& J, DpShared& sh, int w, int kstart, int ks
       if (lane == 0) {
         long long spins = 0;
         while (sh.prog[producer] < need) {
-          if (*(volatile int*)&sh.abort || ++spins > kSpinLimit) {
+          if (*(volatile int*)&sh.abort || ++spins > J.spin_limit) {
             ok = false;
             break;
           }

@@ -52,6 +52,7 @@ struct Ctx {
   int band_ring = 1;          // banded problems on the ring schedule where it is valid
   int band_gate = 0;          // band proposals: divergence gate window threshold (0 = off)
   int pair_bucket_cap = 3072;  // seed-join buckets sorted in shared memory up to this size
+  long long dp_spin_limit = 1ll << 26;  // polls before a whole-CTA gap-DP wait gives up (about a second)
   Workspace ws;
   MatchStats stats;
   bool profiling = false;

@@ -10,13 +10,22 @@
 // and output buffers.
 //
 // In host code the array's name is only a host-side stand-in, not a device
-// address, so its device address is looked up once per device, with that
-// device current, through cudaGetSymbolAddress.  The first call on a device
-// does this set-up (and uploads the 2-bit translation table), so that first
-// call should come before any stream capture.  All calls share the one array
-// and it keeps the previous call's contents: everything read is written
-// first, except the error word, which every call clears.  Calls whose GPU
-// work overlaps (two streams, or host threads) race on the array.
+// address, so its device address is looked up once per device (and context),
+// with that device current, through cudaGetSymbolAddress.  The first call on a
+// device does this set-up (and uploads the 2-bit translation table), so that
+// first call should come before any stream capture.  A call with n = 0 does
+// the set-up alone.  Under CUDA's default lazy module loading the array's
+// device memory is committed by that first look-up, not when the library is
+// loaded: a caller that is about to hand the rest of the device to another
+// allocator makes its first call (n = 0 is enough) before doing so.  The
+// look-up is keyed on the current context's ID, so after cudaDeviceReset the
+// next call repeats the set-up in the new context instead of using a stale
+// address.  All calls share the one array and it keeps the previous call's
+// contents: everything read is written first, except the error word, which
+// every call clears.  Calls whose GPU work overlaps (two streams, or host
+// threads) race on the array.
+#include <cuda.h>
+
 #include <mutex>
 
 #include "mvg_internal.h"
@@ -43,19 +52,50 @@ static __device__ __align__(256) uint8_t g_noalloc_scratch[kNoAllocScratchBytes]
 constexpr int kMaxDevices = 64;
 static std::mutex g_na_mu;
 static uint8_t* g_na_addr[kMaxDevices] = {};
+static unsigned long long g_na_ctx[kMaxDevices] = {};
 
-// Once per device, with that device current: translation table and the
-// scratch array's device address.
+// ID of the calling thread's current CUDA context (0 if none), read through
+// the driver entry points the runtime exposes, so the library does not link
+// the driver library itself.
+static unsigned long long current_context_id() {
+  using GetCurrent = CUresult (*)(CUcontext*);
+  using GetId = CUresult (*)(CUcontext, unsigned long long*);
+  static GetCurrent get_current = nullptr;
+  static GetId get_id = nullptr;
+  static bool resolved = false;
+  if (!resolved) {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = (GetCurrent)f;
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = (GetId)f;
+    resolved = true;
+  }
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (get_current && get_id && get_current(&ctx) == CUDA_SUCCESS && ctx && get_id(ctx, &id) == CUDA_SUCCESS)
+    return id;
+  return 0;
+}
+
+// Once per device and context, with that device current: translation table
+// and the scratch array's device address.
 static int noalloc_setup(int dev, uint8_t** out) {
   if (dev < 0 || dev >= kMaxDevices) return report_error(MVG_ERR_ARG, "device index out of range");
   std::lock_guard<std::mutex> lk(g_na_mu);
-  if (!g_na_addr[dev]) {
+  const unsigned long long ctx = current_context_id();
+  if (!g_na_addr[dev] || ctx == 0 || ctx != g_na_ctx[dev]) {
     int rc = upload_base_table();
     if (rc) return rc;
     void* p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess) return report_cuda(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
     g_na_addr[dev] = (uint8_t*)p;
+    g_na_ctx[dev] = current_context_id();  // the look-up made the primary context current
   }
   *out = g_na_addr[dev];
   return 0;

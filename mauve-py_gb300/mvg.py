@@ -44,7 +44,8 @@ EXPORTS = ["mvg_create", "mvg_destroy", "mvg_last_error", "mvg_stream", "mvg_ker
            "mvg_lut_smooth_edges_dev", "mvg_lut_find_gaps", "mvg_lut_find_gaps_dev", "mvg_lut_find_edges",
            "mvg_lut_find_mismatches", "mvg_lut_find_duplicate_mappings", "mvg_build_index_lut",
            "mvg_build_index_lut_dev", "mvg_set_band_whole_fraction", "mvg_set_band_ring",
-           "mvg_set_band_gate", "mvg_sslist_write", "mvg_sslist_read", "mvg_set_pair_bucket_cap"]
+           "mvg_set_band_gate", "mvg_sslist_write", "mvg_sslist_read", "mvg_set_pair_bucket_cap",
+           "mvg_set_dp_spin_limit"]
 
 TUNING_PATH = os.path.join(HERE, "dp_tuning.json")
 
@@ -84,6 +85,7 @@ def load_library(path=LIB_PATH):
         "mvg_set_band_ring": (ci, [vp, ci]),
         "mvg_set_band_gate": (ci, [vp, ci]),
         "mvg_set_pair_bucket_cap": (ci, [vp, ci]),
+        "mvg_set_dp_spin_limit": (ci, [vp, ctypes.c_longlong]),
         "mvg_sslist_write": (ci, [vp, vp, u64, u64, ctypes.c_char_p]),
         "mvg_sslist_read": (ci, [ctypes.c_char_p, vp, vp, u64, vp, u64]),
         "mvg_gapdp_envelope_dev": (ci, [vp, vp, vp, vp, vp, i64, vp, vp]),
@@ -213,6 +215,10 @@ class Context:
     def set_band_gate(self, min_match):
         """Divergence gate of the band proposal (0 = off); see mvg_set_band_gate."""
         _check(load_library().mvg_set_band_gate(self._h, int(min_match)))
+
+    def set_dp_spin_limit(self, polls=1 << 26):
+        """Polls before a whole-CTA gap-DP wait gives up (watchdog); see mvg_set_dp_spin_limit."""
+        _check(load_library().mvg_set_dp_spin_limit(self._h, int(polls)))
 
     def set_band_ring(self, on=True):
         """Banded passes on the ring schedule (default) or all in the strip kernel."""

@@ -197,3 +197,65 @@ def test_divergence_gate_matches_reference_and_sends_divergent_gaps_whole(ctx):
     big = la >= 256
     assert gated[big & (rate > 40)].mean() > 0.9
     assert gated[big & (rate < 10)].mean() < 0.05
+
+
+def test_trained_network_beats_the_band_without_it(ctx):
+    """What the trained network gains over the method without it: on 60,000
+    gaps drawn like the recoded-genome pair's (a seed no training or
+    calibration draw used), the network's bands and the heuristic band
+    (bandnet.heuristic_band: centred, |LA - LB| + 10% + 32) both give output
+    identical to the full DP, and the network's run computes at least 20%
+    fewer DP cells (banded cells plus the full-DP reruns) and takes less
+    time than the heuristic's."""
+    import os
+    import time
+
+    import torch
+    wpath = os.path.join(os.path.dirname(mvg.__file__), "bandnet_weights.npz")
+    w = np.load(wpath)
+    net = bandnet.BandNet(ctx, params=w["params"])
+    alpha, beta = float(w["alpha"]), float(w["beta"])
+    ctx.set_band_whole_fraction(float(w["whole"]))
+    ctx.set_band_gate(int(w["gate"]))
+    try:
+        sa, oa, sb, ob = synth.gap_batch_recoded(seed=2026, nprob=60_000)
+        n = len(oa) - 1
+        la, lb = np.diff(oa), np.diff(ob)
+        path_off = np.zeros(n + 1, np.uint64)
+        path_off[1:] = np.cumsum(la + lb)
+        t, ptrs = _batch_ptrs(sa, oa, sb, ob)
+        d_poff = torch.from_numpy(path_off.view(np.int64)).cuda()
+
+        def outputs():
+            return (torch.zeros(n, dtype=torch.int32, device="cuda"),
+                    torch.zeros(int(path_off[-1]) + 16, dtype=torch.uint8, device="cuda"),
+                    torch.zeros(n, dtype=torch.int64, device="cuda"))
+
+        full = outputs()
+        ctx.gap_align_batch_dev(*ptrs, n, full[0].data_ptr(), full[1].data_ptr(), d_poff.data_ptr(),
+                                full[2].data_ptr())
+
+        def run(propose):
+            best = None
+            for _ in range(3):
+                out = outputs()
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                d, h = propose()
+                used, cells = ctx.gap_align_banded_dev(*ptrs, n, d, h, out[0].data_ptr(), out[1].data_ptr(),
+                                                       d_poff.data_ptr(), out[2].data_ptr())
+                torch.cuda.synchronize()
+                dt = time.perf_counter() - t0
+                assert all(bool(torch.equal(x, y)) for x, y in zip(out, full))
+                best = (dt, used, cells) if best is None or dt < best[0] else best
+            return best
+
+        t_net, used_net, cells_net = run(lambda: net.propose_dev(*ptrs, n, alpha, beta))
+        t_heu, used_heu, cells_heu = run(lambda: bandnet.heuristic_band(la, lb))
+    finally:
+        ctx.set_band_whole_fraction(0.5)
+        ctx.set_band_gate(0)
+    msg = "network %.1f ms, %.3g cells, kept %.3f; heuristic %.1f ms, %.3g cells, kept %.3f" % (
+        1e3 * t_net, cells_net, (used_net == 1).mean(), 1e3 * t_heu, cells_heu, (used_heu == 1).mean())
+    assert cells_net < 0.8 * cells_heu, msg
+    assert t_net < t_heu, msg

@@ -156,6 +156,42 @@ def test_matches_wide_seed_keys(ctx, weight, rank):
     np.testing.assert_array_equal(ctx.pairwise_matches(a, b, seed), O.pairwise_matches(a, b, seed))
 
 
+def test_matches_recoded_pair_config(ctx):
+    """The synthetic recoded-genome pair (4.6 Mbp, coding seed w=15): the GPU
+    match list equals the oracle's, element by element."""
+    a, b = synth.genome_pair_recoded()
+    seed = mvg.get_seed(mvg.default_seed_weight((len(a) + len(b)) // 2), 3)
+    np.testing.assert_array_equal(ctx.pairwise_matches(a, b, seed), O.pairwise_matches(a, b, seed))
+
+
+def test_matches_large_pair_config(ctx):
+    """The 12 Mbp, 16-contig pair at GC 0.38 with 300 repeat copies: weight
+    17 has no coding seed, so the solid 17-mer and 64-bit keys (the one-sort
+    join) are used; the match list equals the oracle's."""
+    a, b = synth.genome_pair_large()
+    w = mvg.default_seed_weight((len(a) + len(b)) // 2)
+    seed = mvg.get_seed(w, 3)
+    assert w == 17 and seed == (1 << 17) - 1
+    np.testing.assert_array_equal(ctx.pairwise_matches(a, b, seed), O.pairwise_matches(a, b, seed))
+
+
+def test_matches_gap_search_fixtures(ctx):
+    """The reference's gap anchor search runs MemHash::FindMatches with the
+    rank-0 seed of the gap's default weight (LM/ProgressiveAligner.cpp:590-679).
+    On 44 gap pairs of 9 bp to 50 kbp its match list (before the overlap and
+    length filters) equals the pairwise matcher's with the same seed."""
+    g = load_golden("gapsearch.npz")
+    tested = 0
+    for k in range(int(g["count"])):
+        w = int(g["w%d" % k])
+        if w < 5:  # the reference does not search such gaps
+            continue
+        m = ctx.pairwise_matches(g["a%d" % k], g["b%d" % k], mvg.get_seed(w, 0))
+        np.testing.assert_array_equal(m, g["mh%d" % k], err_msg="gap %d" % k)
+        tested += 1
+    assert tested >= 40
+
+
 def test_matches_degenerate_inputs(ctx):
     seed = mvg.get_seed(15, 3)
     assert ctx.pairwise_matches(b"ACGT", b"ACGTACGT", seed).shape == (0, 3)
@@ -227,6 +263,69 @@ def test_gapdp_rejects_bad_codes_and_empty(ctx):
         ctx.gap_align_batch(np.array([0, 5, 1], np.uint8), [0, 3], np.array([1, 2], np.uint8), [0, 2])
     with pytest.raises(ValueError):
         ctx.gap_align_batch(np.array([0, 1], np.uint8), [0, 0, 2], np.array([1, 2], np.uint8), [0, 1, 2])
+
+
+def test_gapdp_whole_cta_mode_paths_vs_oracle(ctx):
+    """Problems of at least 16 strips (A above 4,096 rows at 8 rows per lane)
+    are solved by a whole CTA whose 8 warps pipeline the strips through a
+    shared row buffer.  Scores and traceback paths equal the oracle's on 8
+    pairs of 4.2-20 kbp at 0-30% divergence, one of them 20,000 x 20,000."""
+    rng = np.random.default_rng(4020)
+    pairs = []
+    for la, d in zip([4200, 5000, 6500, 8000, 10000, 13000, 16000], np.linspace(0.0, 0.30, 7)):
+        a = rng.integers(0, 4, la).astype(np.uint8)
+        pairs.append((a, synth.mutate_codes(rng, a, 0.9 * d, int(0.1 * d * la / 3.0), 3.0)))
+    a = rng.integers(0, 4, 20_000).astype(np.uint8)
+    b = a.copy()
+    m = rng.random(20_000) < 0.15  # substitutions only: 20,000 x 20,000
+    b[m] = (b[m] + rng.integers(1, 4, int(m.sum()))).astype(np.uint8) % 4
+    pairs.append((a, b))
+    sa = np.concatenate([x for x, _ in pairs])
+    sb = np.concatenate([y for _, y in pairs])
+    oa = np.concatenate([[0], np.cumsum([len(x) for x, _ in pairs])]).astype(np.uint64)
+    ob = np.concatenate([[0], np.cumsum([len(y) for _, y in pairs])]).astype(np.uint64)
+    assert min(len(x) for x, _ in pairs) >= 16 * 32 * ctx.full_rows
+    _check_batch(ctx, sa, oa, sb, ob)
+
+
+def test_gapdp_whole_cta_mode_many_problems_vs_oracle(ctx):
+    """More whole-CTA problems than resident CTAs, so each CTA claims
+    several in turn (with the one-warp problems after them): 360 pairs of
+    4.1-4.6 kbp plus 200 short ones, scores and paths equal to the oracle's."""
+    rng = np.random.default_rng(4100)
+    pairs = []
+    for k in range(360):
+        a = rng.integers(0, 4, int(rng.integers(4100, 4600))).astype(np.uint8)
+        pairs.append((a, synth.mutate_codes(rng, a, float(rng.uniform(0, 0.27)), int(rng.integers(0, 40)), 3.0)))
+    for k in range(200):
+        a = rng.integers(0, 4, int(rng.integers(1, 900))).astype(np.uint8)
+        pairs.append((a, synth.mutate_codes(rng, a, float(rng.uniform(0, 0.3)), int(rng.integers(0, 5)), 3.0)))
+    order = rng.permutation(len(pairs))
+    pairs = [pairs[i] for i in order]
+    sa = np.concatenate([x for x, _ in pairs])
+    sb = np.concatenate([y for _, y in pairs])
+    oa = np.concatenate([[0], np.cumsum([len(x) for x, _ in pairs])]).astype(np.uint64)
+    ob = np.concatenate([[0], np.cumsum([len(y) for _, y in pairs])]).astype(np.uint64)
+    _check_batch(ctx, sa, oa, sb, ob)
+
+
+def test_gapdp_watchdog_gives_up_and_handle_recovers(ctx):
+    """The whole-CTA mode's waits are bounded.  With the limit at one poll a
+    warp gives up waiting for its predecessor: the call returns
+    MVG_ERR_DEVICE (a RuntimeError here) instead of hanging, and after the
+    limit is restored the same handle solves the same batch exactly."""
+    rng = np.random.default_rng(77)
+    a = rng.integers(0, 4, 9000).astype(np.uint8)
+    b = synth.mutate_codes(rng, a, 0.05, 20, 3.0)
+    ctx.set_dp_spin_limit(1)
+    try:
+        with pytest.raises(RuntimeError, match="error 7"):
+            ctx.gap_align_batch(a, [0, len(a)], b, [0, len(b)])
+    finally:
+        ctx.set_dp_spin_limit()
+    scores, paths = ctx.gap_align_batch(a, [0, len(a)], b, [0, len(b)])
+    p, s = O.nw_align(a, b)
+    assert paths[0] == p and int(scores[0]) == s
 
 
 def test_gapdp_long_pair_property(ctx):

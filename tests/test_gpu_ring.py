@@ -1,6 +1,7 @@
 """GPU tests of the ring-scheduled banded gap DP (csrc/gapdp_ring.cuh).
 
-Every banded result must equal the full DP's (scores and paths), whichever
+Every banded result must equal the oracle's NWSmall (scores and paths) and
+so the full DP's, whichever
 group height the schedule picks; the tests build bands that land in each
 height class and at the edges of the schedule's validity."""
 import numpy as np
@@ -81,9 +82,16 @@ def related_pair(rng, la, sub=0.02, indels=2):
 
 
 def check_identical(ctx, sa, oa, sb, ob, delta, half):
+    """Banded output equals the oracle's NWSmall scores and paths (and so the
+    full DP's, checked as well)."""
     s_full, p_full = ctx.gap_align_batch(sa, oa, sb, ob)
     s, p, used, cells = ctx.gap_align_banded(sa, oa, sb, ob, np.asarray(delta, np.int32), np.asarray(half, np.int32))
-    np.testing.assert_array_equal(s, s_full)
+    oscores, oplen, opaths, opoff = O.nw_batch(sa, oa, sb, ob)
+    np.testing.assert_array_equal(s, oscores)
+    raw = opaths.tobytes()
+    for k in range(len(oa) - 1):
+        assert p[k] == raw[int(opoff[k]):int(opoff[k]) + int(oplen[k])].decode(), k
+    np.testing.assert_array_equal(s_full, oscores)
     assert p == p_full
     return used, cells, s_full
 

@@ -6,8 +6,9 @@ memory for its own pool.  Another is a latency-bound loop that cannot take
 cudaMalloc's implicit synchronisation.  It keeps its scratch in one static
 device array of the library.  This test calls it through the C ABI on device
 buffers and checks that its output equals the allocating entry point's
-(mvg_sml_build_dev) bit for bit, on two calls in a row, and that input over
-its size limit is refused.  The file sorts last so that a run stopping at
+(mvg_sml_build_dev) bit for bit, on two calls in a row, that the second
+call leaves the device's free memory unchanged (nothing allocated), and
+that input over its size limit is refused.  The file sorts last so that a run stopping at
 the first failure has already run every other test.  The test also passes
 alone in a fresh process.
 """
@@ -42,7 +43,7 @@ def test_no_alloc_sml_equals_allocating_entry_point():
     f = _noalloc_fn()
     rng = np.random.default_rng(2026)
     cases = [(MAX_BASES, mvg.get_seed(15, 3)), (150_001, mvg.get_seed(17, 3))]  # two calls in a row
-    for n, seed in cases:
+    for call, (n, seed) in enumerate(cases):
         seq = synth.random_bases(rng, n, float(rng.uniform(0.35, 0.6)))
         d_seq = torch.from_numpy(seq).cuda()
         L = mvg.seed_length(seed)
@@ -54,8 +55,14 @@ def test_no_alloc_sml_equals_allocating_entry_point():
         assert ctx.sml_build_dev(d_seq.data_ptr(), n, seed, ref_pos.data_ptr(), ref_mer.data_ptr(), cnt) == cnt
         torch.cuda.synchronize()
         out = ctypes.c_uint64(0)
+        torch.cuda.synchronize()
+        free_before = torch.cuda.mem_get_info()[0]
         rc = f(d_seq.data_ptr(), n, seed, got_pos.data_ptr(), got_mer.data_ptr(), cnt, ctypes.byref(out), None)
+        torch.cuda.synchronize()
+        free_after = torch.cuda.mem_get_info()[0]
         assert rc == 0, mvg.load_library().mvg_last_error()
+        if call > 0:  # the first call may commit the library's static array; later ones allocate nothing
+            assert free_after == free_before
         assert out.value == cnt
         assert torch.equal(got_pos, ref_pos)
         assert torch.equal(got_mer, ref_mer)
