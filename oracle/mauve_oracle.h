@@ -41,6 +41,16 @@ int64_t mo_sml_build(const uint8_t* seq, uint64_t n, uint64_t seed, uint32_t* po
 int64_t mo_pairwise_matches(const uint8_t* a, uint64_t na, const uint8_t* b, uint64_t nb,
                             uint64_t seed, int64_t* out, uint64_t cap);
 
+/* Gap anchor search (oracle/gap_oracle.cpp): pairwiseAnchorSearch
+ * (libMems/ProgressiveAligner.cpp:590-679) on two gap sequences.
+ * mo_gap_anchor_filter applies EliminateOverlaps_v2 and LengthFilter(12) in
+ * place to (start0, start1, length) rows and returns the count kept;
+ * mo_gap_anchor_search runs the seed matching first (-2: seed weight below
+ * the minimum, no search; -1: cap too small). */
+int64_t mo_gap_anchor_filter(int64_t* rows, int64_t n);
+int64_t mo_gap_anchor_search(const uint8_t* a, uint64_t la, const uint8_t* b, uint64_t lb, int64_t* out,
+                             uint64_t cap, uint32_t* weight);
+
 /* Same, stopping after the join: the unique seed pairs in processing order
  * (posA, posB, canonical-mer parity bits), for checking the join kernel. */
 int64_t mo_unique_pairs(const uint8_t* a, uint64_t na, const uint8_t* b, uint64_t nb,

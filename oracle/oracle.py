@@ -17,12 +17,19 @@ _lib = None
 
 def build(force=False):
     """Compile oracle/mauve_oracle.c into oracle/lib/libmauve_oracle.so."""
-    srcs = [os.path.join(_HERE, f) for f in ("mauve_oracle.c", "lut_oracle.c", "mauve_oracle.h")]
+    srcs = [os.path.join(_HERE, f) for f in ("mauve_oracle.c", "lut_oracle.c", "gap_oracle.cpp", "mauve_oracle.h")]
     if not force and os.path.exists(LIB_PATH) and all(
             os.path.getmtime(LIB_PATH) >= os.path.getmtime(s) for s in srcs):
         return LIB_PATH
-    os.makedirs(os.path.dirname(LIB_PATH), exist_ok=True)
-    subprocess.check_call(["gcc", "-O2", "-fPIC", "-shared", "-o", LIB_PATH, *srcs[:2], "-lm", "-lpthread"])
+    objdir = os.path.join(os.path.dirname(LIB_PATH), "obj")
+    os.makedirs(objdir, exist_ok=True)
+    objs = []
+    for src in srcs[:3]:
+        obj = os.path.join(objdir, os.path.basename(src) + ".o")
+        cc = ["g++", "-std=c++17"] if src.endswith(".cpp") else ["gcc"]
+        subprocess.check_call([*cc, "-O2", "-fPIC", "-c", src, "-o", obj])
+        objs.append(obj)
+    subprocess.check_call(["g++", "-shared", "-o", LIB_PATH, *objs, "-lm", "-lpthread"])
     return LIB_PATH
 
 
@@ -48,6 +55,10 @@ def lib():
         L.mo_pairwise_matches.argtypes = [vp, u64, vp, u64, u64, vp, u64]
         L.mo_unique_pairs.restype = i64
         L.mo_unique_pairs.argtypes = [vp, u64, vp, u64, u64, vp, vp, u64]
+        L.mo_gap_anchor_filter.restype = i64
+        L.mo_gap_anchor_filter.argtypes = [vp, i64]
+        L.mo_gap_anchor_search.restype = i64
+        L.mo_gap_anchor_search.argtypes = [vp, u64, vp, u64, vp, u64, vp]
         L.mo_nw_align.restype = i64
         L.mo_nw_align.argtypes = [vp, ctypes.c_int, vp, ctypes.c_int, vp, vp]
         L.mo_nw_score.restype = ctypes.c_int32
@@ -142,6 +153,28 @@ def pairwise_matches(a, b, seed):
     if n < 0:
         raise RuntimeError("mo_pairwise_matches failed: %d" % n)
     return out[: 3 * n].reshape(-1, 3)
+
+
+def gap_anchor_filter(rows):
+    """EliminateOverlaps_v2 + LengthFilter(12) on (start0, start1, length) rows."""
+    m = np.ascontiguousarray(rows, np.int64).reshape(-1, 3).copy()
+    n = lib().mo_gap_anchor_filter(_p(m), len(m))
+    return m[:n]
+
+
+def gap_anchor_search(a, b):
+    """pairwiseAnchorSearch on two gap sequences: (weight, anchors rows);
+    anchors is None when the weight is below the minimum (no search)."""
+    a, b = _u8(a), _u8(b)
+    cap = max(min(len(a), len(b)), 16)
+    out = np.zeros(3 * cap, np.int64)
+    w = ctypes.c_uint32(0)
+    n = lib().mo_gap_anchor_search(_p(a), len(a), _p(b), len(b), _p(out), cap, ctypes.byref(w))
+    if n == -2:
+        return int(w.value), None
+    if n < 0:
+        raise RuntimeError("mo_gap_anchor_search failed: %d" % n)
+    return int(w.value), out[:3 * n].reshape(-1, 3)
 
 
 def nw_align(a, b):

@@ -39,6 +39,35 @@ def test_pairwise_match_lists_match_reference():
         np.testing.assert_array_equal(m, g["m%d" % k], err_msg="case %d" % k)
 
 
+def test_gap_search_memhash_equals_pairwise_matcher():
+    """pairwiseAnchorSearch's MemHash::FindMatches (rank-0 seed of the gap's
+    default weight, LM/ProgressiveAligner.cpp:590-679) hashes exactly the
+    seeds unique in both gap sequences, so its list equals the pairwise
+    matcher's (the oracle) with that seed on every fixture gap."""
+    g = load_golden("gapsearch.npz")
+    for k in range(int(g["count"])):
+        a, b, w = g["a%d" % k], g["b%d" % k], int(g["w%d" % k])
+        assert w == O.default_seed_weight((len(a) + len(b)) // 2)
+        if w < 5:
+            assert len(g["anc%d" % k]) == 0
+            continue
+        np.testing.assert_array_equal(O.pairwise_matches(a, b, O.get_seed(w, 0)), g["mh%d" % k], err_msg="gap %d" % k)
+
+
+def test_gap_anchor_search_matches_reference():
+    """The oracle's gap anchor search (matches, EliminateOverlaps_v2,
+    LengthFilter(12)) gives the reference's anchors, in order."""
+    g = load_golden("gapsearch.npz")
+    for k in range(int(g["count"])):
+        w, anc = O.gap_anchor_search(g["a%d" % k], g["b%d" % k])
+        assert w == int(g["w%d" % k])
+        if anc is None:
+            assert len(g["anc%d" % k]) == 0
+            continue
+        np.testing.assert_array_equal(anc, g["anc%d" % k], err_msg="gap %d" % k)
+        np.testing.assert_array_equal(O.gap_anchor_filter(g["mh%d" % k]), g["anc%d" % k])
+
+
 def test_gap_dp_paths_match_reference():
     g = load_golden("gapdp.npz")
     sa, sb, oa, ob, paths, op = g["seq_a"], g["seq_b"], g["off_a"], g["off_b"], g["paths"], g["off_p"]
