@@ -113,6 +113,32 @@ int mvg_pairwise_matches_dev(mvg_handle h, const uint8_t* d_seq_a, uint64_t na, 
  * [2] = matches, [3] = non-empty hash buckets. */
 int mvg_pairwise_stats(mvg_handle h, uint64_t stats[4]);
 
+/* Batched gap anchor search: ProgressiveAligner::pairwiseAnchorSearch
+ * (LM/ProgressiveAligner.cpp:590-679) for many inter-anchor gaps in one call,
+ * as recurseOnPairs (:682-924) issues it for every gap of a recursion round.
+ * gaps holds 4 int64 per gap: start in A (0-based), length in A, start in
+ * B, length in B -- the subsequences the reference cuts out (ToString(diff,
+ * gap_start), :600-611).  Per gap: seed weight getDefaultSeedWeight of the
+ * mean length (LM/SeedMasks.h:389-401; below 5 the gap is not searched),
+ * the rank-0 seed, MemHash::FindMatches over the two gap sequences,
+ * EliminateOverlaps_v2 (LM/ProgressiveAligner.h:302-392) and
+ * LengthFilter(12) (LM/MatchList.h:680-692), coordinates shifted to the
+ * genomes (:657-665).  out receives 3 int64 per anchor (start in A, start
+ * in B, 1-based genome coordinates, negative = reverse strand; length), the
+ * anchors of gap g at rows gap_off[g] .. gap_off[g+1]-1 (gap_off has
+ * ngaps+1 entries) in the reference's list order.  *count gets the total;
+ * MVG_ERR_CAPACITY if it exceeds cap (gap_off and *count are still set),
+ * MVG_ERR_RANGE for a gap outside its genome, MVG_ERR_ARG for a gap whose
+ * mean length needs a seed weight above 15 (above about 5.9 Mbp: search
+ * such a gap with mvg_pairwise_matches and the rank-0 seed). */
+int mvg_gap_anchor_search(mvg_handle h, const uint8_t* seq_a, uint64_t na, const uint8_t* seq_b, uint64_t nb,
+                          const int64_t* gaps, uint64_t ngaps, int64_t* out, uint64_t cap, uint64_t* gap_off,
+                          uint64_t* count);
+/* The same with the genomes in device memory (gaps and outputs on the host). */
+int mvg_gap_anchor_search_dev(mvg_handle h, const uint8_t* d_seq_a, uint64_t na, const uint8_t* d_seq_b,
+                              uint64_t nb, const int64_t* gaps, uint64_t ngaps, int64_t* out, uint64_t cap,
+                              uint64_t* gap_off, uint64_t* count);
+
 /* The seed join groups both genomes' seeds into buckets by the mer's top
  * bits and sorts each bucket in shared memory when it holds at most cap
  * seeds, else in chunks through global memory.  cap in 32..3072 (default

@@ -25,6 +25,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "lib", "libmauve_gb300.so")
 
 MVG_OK = 0
+MVG_ERR_CAPACITY = 5
 _ERRORS = {1: ValueError, 2: RuntimeError, 3: ValueError, 4: ValueError, 5: OverflowError, 6: MemoryError,
            7: RuntimeError, 8: IndexError, 9: OverflowError}
 
@@ -45,7 +46,7 @@ EXPORTS = ["mvg_create", "mvg_destroy", "mvg_last_error", "mvg_stream", "mvg_ker
            "mvg_lut_find_mismatches", "mvg_lut_find_duplicate_mappings", "mvg_build_index_lut",
            "mvg_build_index_lut_dev", "mvg_set_band_whole_fraction", "mvg_set_band_ring",
            "mvg_set_band_gate", "mvg_sslist_write", "mvg_sslist_read", "mvg_set_pair_bucket_cap",
-           "mvg_set_dp_spin_limit"]
+           "mvg_set_dp_spin_limit", "mvg_gap_anchor_search", "mvg_gap_anchor_search_dev"]
 
 TUNING_PATH = os.path.join(HERE, "dp_tuning.json")
 
@@ -74,6 +75,8 @@ def load_library(path=LIB_PATH):
         "mvg_pairwise_matches": (ci, [vp, vp, u64, vp, u64, u64, vp, u64, ctypes.POINTER(u64)]),
         "mvg_pairwise_matches_dev": (ci, [vp, vp, u64, vp, u64, u64, vp, u64, ctypes.POINTER(u64)]),
         "mvg_pairwise_stats": (ci, [vp, vp]),
+        "mvg_gap_anchor_search": (ci, [vp, vp, u64, vp, u64, vp, u64, vp, u64, vp, ctypes.POINTER(u64)]),
+        "mvg_gap_anchor_search_dev": (ci, [vp, vp, u64, vp, u64, vp, u64, vp, u64, vp, ctypes.POINTER(u64)]),
         "mvg_gapdp_batch": (ci, [vp, vp, vp, vp, vp, i64, vp, vp, vp, vp]),
         "mvg_gapdp_batch_dev": (ci, [vp, vp, vp, vp, vp, i64, vp, vp, vp, vp]),
         "mvg_set_tb_arena": (ci, [vp, u64]),
@@ -299,6 +302,37 @@ class Context:
         _check(load_library().mvg_pairwise_matches_dev(self._h, d_a, na, d_b, nb, seed, d_out, cap,
                                                        ctypes.byref(cnt)))
         return int(cnt.value)
+
+    def gap_anchor_search(self, seq_a, seq_b, gaps):
+        """Batched pairwiseAnchorSearch over gaps (rows: start A, length A,
+        start B, length B; 0-based).  Returns (anchors int64[m, 3] in genome
+        coordinates, gap_off uint64[ngaps + 1])."""
+        seq_a, seq_b = _u8(seq_a), _u8(seq_b)
+        g = np.ascontiguousarray(gaps, np.int64).reshape(-1, 4)
+        n = len(g)
+        off = np.zeros(n + 1, np.uint64)
+        cnt = ctypes.c_uint64(0)
+        cap = int(max(16, min(len(seq_a), len(seq_b)) // 4))
+        while True:
+            out = np.zeros(3 * cap, np.int64)
+            rc = load_library().mvg_gap_anchor_search(self._h, _ptr(seq_a), len(seq_a), _ptr(seq_b), len(seq_b),
+                                                      _ptr(g), n, _ptr(out), cap, _ptr(off), ctypes.byref(cnt))
+            if rc == MVG_ERR_CAPACITY and cnt.value > cap:
+                cap = int(cnt.value)
+                continue
+            _check(rc)
+            return out[: 3 * cnt.value].reshape(-1, 3), off
+
+    def gap_anchor_search_dev(self, d_a, na, d_b, nb, gaps, cap):
+        """Device-genome variant; gaps and outputs on the host."""
+        wait_producers()
+        g = np.ascontiguousarray(gaps, np.int64).reshape(-1, 4)
+        off = np.zeros(len(g) + 1, np.uint64)
+        out = np.zeros(3 * max(cap, 1), np.int64)
+        cnt = ctypes.c_uint64(0)
+        _check(load_library().mvg_gap_anchor_search_dev(self._h, d_a, na, d_b, nb, _ptr(g), len(g), _ptr(out), cap,
+                                                        _ptr(off), ctypes.byref(cnt)))
+        return out[: 3 * cnt.value].reshape(-1, 3), off
 
     def pairwise_stats(self):
         st = np.zeros(4, np.uint64)
