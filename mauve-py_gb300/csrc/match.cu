@@ -124,6 +124,7 @@ constexpr int kClusterCtas = 8;
 constexpr int kLocalCap = 1536;
 constexpr uint32_t kRedo = 0xffffffffu;
 extern __shared__ __align__(16) unsigned char replay_dyn_smem[];
+static_assert(sizeof(CtaExtRing) <= 8 * sizeof(ExtRing), "the CTA ring reuses the eight warp rings");
 
 __global__ void __launch_bounds__(256) k_bucket_replay(MatchCtx c, const Mhe* __restrict__ mhe,
                                                        const uint32_t* __restrict__ sorted_pair,
@@ -274,9 +275,9 @@ __global__ void __launch_bounds__(256) k_bucket_replay(MatchCtx c, const Mhe* __
         break;
       }
       ncoll += mine_in(cbase, pos, f);
+      Mhe x = s_chunk[f - cbase];
+      cta_extend(c, x, *reinterpret_cast<CtaExtRing*>(s_ring));  // the warp rings are idle in this mode
       if (wid == 0) {
-        Mhe x = s_chunk[f - cbase];
-        warp_extend(c, x, s_ring[0]);
         const int64_t at = lower_bound_mapped(G, Mp, n, x, L);
         if (lane == 0) {
           s_x = x;
@@ -350,7 +351,7 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(256, 1)
   const unsigned rank = cl.block_rank();
   Mhe* lent = reinterpret_cast<Mhe*>(replay_dyn_smem);                  // kLocalCap entries
   uint16_t* lmap = reinterpret_cast<uint16_t*>(lent + kLocalCap);      // kLocalCap map words
-  __shared__ ExtRing s_ring;
+  __shared__ CtaExtRing s_ring;
   __shared__ uint32_t s_wmin[8];
   __shared__ uint32_t s_cmin[kClusterCtas];  // written by every CTA of the cluster
   __shared__ Mhe s_seed;                     // the fresh seed, inside the owning CTA
@@ -409,9 +410,9 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(256, 1)
         if (rank == owner) {
           if (slot == f) s_seed = m;
           __syncthreads();
+          Mhe x = s_seed;
+          cta_extend(c, x, s_ring);  // the whole owning CTA
           if (wid == 0) {
-            Mhe x = s_seed;
-            warp_extend(c, x, s_ring);
             const int64_t at = lower_bound_local(lent, lmap, n, x, L);
             if (lane < kClusterCtas) {  // lane j sends the entry to CTA j
               *cl.map_shared_rank(&s_x, lane) = x;

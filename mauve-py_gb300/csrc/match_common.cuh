@@ -121,14 +121,12 @@ __device__ __forceinline__ int64_t lower_bound_mhe(const Mhe* __restrict__ v, in
 // from the entry right edge (MR = total moved in odd phases); positive
 // starts move by exactly those amounts and negative starts stay.  The room
 // a phase has (the genome-end clamp) is likewise C - ML or C' - MR.  So the
-// two sides never interact: each side's total is the fixpoint of (jump,
-// single) on its own match bits, and the four-phase cycle only interleaves
-// the two fixpoint iterations.  Here the warp computes the two fixpoints one
-// after the other on match bits cached in per-warp shared rings (1024
-// displacements per fill); the walk itself is warp-uniform scalar work.
-// For a same-strand pair a window pair matches iff the pattern-selected
-// bases are equal (equal canonical mers with equal strand bits); other
-// pairs use the canonical-mer test itself.
+// two sides never interact: each side's total is where its own walk stops.
+// The match bits are filled 1024 displacements at a time into a per-warp
+// ring, and each fill's 32 words are searched for the stop (stop_in_word),
+// one word per lane.  For a same-strand pair a window pair matches iff the
+// pattern-selected bases are equal (equal canonical mers with equal strand
+// bits); other pairs use the canonical-mer test itself.
 constexpr int kExtRing = 128;    // words per side: the last 4096 displacements
 constexpr int kExtChunk = 1024;  // displacements per fill (32 per lane)
 
@@ -171,8 +169,11 @@ __device__ __forceinline__ void window128(const uint32_t* __restrict__ g, uint64
   }
 }
 
-static __device__ void ext_fill(const MatchCtx& c, int64_t st0, int64_t st1, int64_t len, int64_t u0, uint64_t pmask,
-                         uint32_t* ring) {
+// One warp's fill: match bits of displacements u0 .. u0 + 1023 into ring
+// words (u0 / 32 + lane) mod RING (no synchronisation).
+template <int RING>
+__device__ __forceinline__ void ext_fill_ring(const MatchCtx& c, int64_t st0, int64_t st1, int64_t len, int64_t u0,
+                                              uint64_t pmask, uint32_t* ring) {
   const int lane = threadIdx.x & 31;
   const int L = c.s.L;
   const bool same = (st0 > 0) == (st1 > 0);
@@ -220,8 +221,35 @@ static __device__ void ext_fill(const MatchCtx& c, int64_t st0, int64_t st1, int
     }
     word |= (uint32_t)b << t;
   }
-  ring[((u0 >> 5) + lane) & (kExtRing - 1)] = word;
+  ring[((u0 >> 5) + lane) & (RING - 1)] = word;
+}
+
+static __device__ void ext_fill(const MatchCtx& c, int64_t st0, int64_t st1, int64_t len, int64_t u0, uint64_t pmask,
+                                uint32_t* ring) {
+  ext_fill_ring<kExtRing>(c, st0, st1, len, u0, pmask, ring);
   __syncwarp();
+}
+
+// Where a side's walk stops.  On one side of the entry the walk starts at
+// displacement 0 and, with bit(u) = "the window pair at displacement u
+// matches" (0 beyond the genome ends), jumps by L while the window L further
+// matches, then moves to the furthest matching window within L, and repeats.
+// Every position it reaches is 0 or a matching window, every move is at most
+// L, and it moves on from q exactly when one of bits q+1 .. q+L is set.  So
+// it can never pass a run of L clear bits, and it stops at the first
+// position q in {0} or the set bits whose next L bits are all clear.  Here
+// that q is found word by word: for the 64 bits of words i, i+1, the clear
+// runs of length L are the bits of y = AND of L shifts of ~x, and the
+// candidates of word i whose next L bits are clear are its set bits (and
+// the start) at positions r with bit r+1 of y set.
+__device__ __forceinline__ uint32_t stop_in_word(uint32_t w, uint32_t w_next, bool first, int L) {
+  uint64_t y = ~(((uint64_t)w_next << 32) | w);
+  for (int have = 1; have < L;) {  // y bit j: clear bits j .. j+have-1
+    const int sh = have < L - have ? have : L - have;
+    y &= y >> sh;
+    have += sh;
+  }
+  return (w | (first ? 1u : 0u)) & (uint32_t)(y >> 1);
 }
 
 static __device__ void warp_extend(const MatchCtx& c, Mhe& m, ExtRing& R) {
@@ -237,50 +265,91 @@ static __device__ void warp_extend(const MatchCtx& c, Mhe& m, ExtRing& R) {
     // room of this side: min over both genomes of the distance to the end
     const int64_t r0 = s0 > 0 ? s0 - 1 : (s0 < 0 ? c.n[0] - elen + s0 + 1 : -1);
     const int64_t r1 = s1 > 0 ? s1 - 1 : (s1 < 0 ? c.n[1] - elen + s1 + 1 : -1);
-    const int64_t room0 = r0 < r1 ? r0 : r1;
+    const int64_t room = r0 < r1 ? r0 : r1;
     uint32_t* ring = R.w[sd];
-    int64_t filled = 0;
-    auto ensure = [&](int64_t umax) {
-      while (filled <= umax) {
-        ext_fill(c, s0, s1, elen, filled, pmask, ring);
-        filled += kExtChunk;
-      }
-    };
-    auto bit = [&](int64_t u) -> bool { return (ring[(u >> 5) & (kExtRing - 1)] >> (u & 31)) & 1u; };
-    int64_t u = 0;
+    int64_t filled = 0, checked = 0;  // displacements filled, words checked
     for (;;) {
-      // jump phase: k-1 good jumps before the first mismatching window
-      int64_t room = room0 - u;
-      const int64_t nj = room >= L ? room / L : 0;
-      // 32 jumps per ballot: lane t tests jump kb + t
-      int64_t good = nj;
-      for (int64_t kb = 1; kb <= nj; kb += 32) {
-        const int64_t klast = kb + 31 < nj ? kb + 31 : nj;
-        ensure(u + klast * L);
-        const int64_t kk = kb + lane;
-        const bool miss = kk <= nj && !bit(u + kk * L);
-        const unsigned mm = __ballot_sync(0xffffffffu, miss);
-        if (mm) {
-          good = kb - 1 + (__ffs(mm) - 1);
-          break;
-        }
+      ext_fill_ring<kExtRing>(c, s0, s1, elen, filled, pmask, ring);
+      __syncwarp();
+      filled += kExtChunk;
+      const int64_t last = filled / 32 - 1;  // words below it have their successor filled
+      const int64_t i = checked + lane;
+      uint32_t hit = 0;
+      if (i < last) hit = stop_in_word(ring[i & (kExtRing - 1)], ring[(i + 1) & (kExtRing - 1)], i == 0, L);
+      const unsigned any = __ballot_sync(0xffffffffu, hit != 0);
+      if (any) {
+        const int f = __ffs(any) - 1;  // the lowest word with a stop holds the first one
+        const uint32_t h = __shfl_sync(0xffffffffu, hit, f);
+        moved[sd] = 32 * (checked + f) + (__ffs(h) - 1);
+        break;
       }
-      u += good * L;
-      // single-base phase: the furthest matching offset in 1..min(room, L)
-      room = room0 - u;
-      const int64_t ms = room > 0 ? (room < L ? room : L) : 0;
-      if (ms <= 0) break;
-      ensure(u + ms);
-      // bits of displacements u+1 .. u+ms (ms <= 32): the highest set one
-      const int64_t b0 = u + 1;
-      const uint64_t two = ((uint64_t)ring[((b0 >> 5) + 1) & (kExtRing - 1)] << 32) |
-                           ring[(b0 >> 5) & (kExtRing - 1)];
-      uint64_t win = two >> (b0 & 31);
-      win &= ms >= 64 ? ~0ull : ((1ull << ms) - 1);
-      if (!win) break;
-      u += 64 - __clzll(win);
+      checked = last;
+      if (filled > room + 2 * kExtChunk + 64) {  // never reached: the bits beyond the room are clear
+        moved[sd] = room > 0 ? room : 0;
+        break;
+      }
     }
-    moved[sd] = u;
+  }
+  m.len = elen + moved[0] + moved[1];
+  m.s0 = e0 > 0 ? e0 - moved[0] : e0 + moved[1];
+  m.s1 = e1 > 0 ? e1 - moved[0] : e1 + moved[1];
+}
+
+// ExtendMatch by a whole CTA (every thread calls it with the same entry and
+// gets the same result): per side the match bits are filled in chunks of
+// 1024, 2048, 4096, then 8192 displacements (one warp per 1024), and after
+// each chunk every thread checks one word of it for the walk's stopping
+// point (stop_in_word); the first one wins.  The ring keeps the last 16,384
+// displacements, so the previous chunk's last word is still there.
+constexpr int kCtaRing = 512;  // words per side
+struct CtaExtRing {
+  uint32_t w[2][kCtaRing];
+  uint32_t red[32];
+};
+
+static __device__ void cta_extend(const MatchCtx& c, Mhe& m, CtaExtRing& R) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int nwarps = blockDim.x >> 5;  // at most 8: a chunk fits half the ring
+  const int L = c.s.L;
+  const uint64_t pmask = pattern_mask64(c.s);
+  const int64_t e0 = m.s0, e1 = m.s1, elen = m.len;
+  int64_t moved[2] = {0, 0};
+#pragma unroll 1
+  for (int sd = 0; sd < 2; ++sd) {
+    const int64_t sg = sd == 0 ? 1 : -1;
+    const int64_t s0 = sg * e0, s1 = sg * e1;
+    uint32_t* ring = R.w[sd];
+    // room: the nearer genome end; every bit beyond it is clear, so the stop
+    // is found once the fills pass it by L (the bound below is never reached)
+    const int64_t r0 = s0 > 0 ? s0 - 1 : (s0 < 0 ? c.n[0] - elen + s0 + 1 : -1);
+    const int64_t r1 = s1 > 0 ? s1 - 1 : (s1 < 0 ? c.n[1] - elen + s1 + 1 : -1);
+    const int64_t room = r0 < r1 ? r0 : r1;
+    int64_t filled = 0, checked = 0;  // displacements filled, words checked
+    for (int k = 0;; ++k) {
+      const int nw = k < 3 ? min(nwarps, 1 << k) : nwarps;
+      __syncthreads();  // every thread is past its reads of the words refilled now
+      if (wid < nw) ext_fill_ring<kCtaRing>(c, s0, s1, elen, filled + (int64_t)wid * kExtChunk, pmask, ring);
+      __syncthreads();
+      filled += (int64_t)nw * kExtChunk;
+      const int64_t last = filled / 32 - 1;  // words below it have their successor filled
+      uint32_t q = 0xffffffffu;
+      const int64_t i = checked + threadIdx.x;
+      if (i < last) {
+        const uint32_t hit = stop_in_word(ring[i & (kCtaRing - 1)], ring[(i + 1) & (kCtaRing - 1)], i == 0, L);
+        if (hit) q = (uint32_t)(32 * i) + (uint32_t)(__ffs(hit) - 1);
+      }
+      q = __reduce_min_sync(0xffffffffu, q);
+      if (lane == 0) R.red[wid] = q;
+      __syncthreads();
+      q = 0xffffffffu;
+      for (int w = 0; w < nwarps; ++w) q = min(q, R.red[w]);
+      checked = last;
+      if (q != 0xffffffffu || filled > room + 2 * kExtChunk * 8 + 64) {
+        moved[sd] = q != 0xffffffffu ? q : (room > 0 ? room : 0);
+        break;
+      }
+    }
+    __syncthreads();  // the ring and the reduction words are reused
   }
   m.len = elen + moved[0] + moved[1];
   m.s0 = e0 > 0 ? e0 - moved[0] : e0 + moved[1];

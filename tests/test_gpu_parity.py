@@ -106,6 +106,8 @@ def test_matches_reference_mds42_pair(ctx):
     from conftest import load_mds42
     a, b, seed, want = load_mds42()
     np.testing.assert_array_equal(ctx.pairwise_matches(a, b, seed), want)
+    st = ctx.pairwise_stats()
+    assert st["pairs"] == st["matches"] + st["collisions"]
     da, db = torch.from_numpy(a.copy()).cuda(), torch.from_numpy(b.copy()).cuda()
     out = torch.zeros(3 * (len(want) + 16), dtype=torch.int64, device="cuda")
     n = ctx.pairwise_matches_dev(da.data_ptr(), len(a), db.data_ptr(), len(b), seed, out.data_ptr(), len(want) + 16)
@@ -125,7 +127,10 @@ def test_matches_single_diagonal_buckets(ctx, n, sub):
     m = rng.random(n) < sub
     b[m] = acgt[(np.searchsorted(acgt, b[m]) + rng.integers(1, 4, int(m.sum()))) % 4]
     seed = O.get_seed(O.default_seed_weight(n), 3)
-    np.testing.assert_array_equal(ctx.pairwise_matches(a, b, seed), O.pairwise_matches(a, b, seed))
+    m = ctx.pairwise_matches(a, b, seed)
+    np.testing.assert_array_equal(m, O.pairwise_matches(a, b, seed))
+    st = ctx.pairwise_stats()  # every seed pair is either inserted or counted as contained
+    assert st["matches"] == len(m) and st["pairs"] == st["matches"] + st["collisions"]
 
 
 @pytest.mark.parametrize("cap", [32, 300])
