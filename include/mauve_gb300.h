@@ -361,6 +361,21 @@ int mvg_set_band_ring(mvg_handle h, int on);
  * counterpart in the reference (single-threaded). */
 int mvg_set_dp_spin_limit(mvg_handle h, long long polls);
 
+/* Full gap DP: problems of at least `strips` strips (of 32 * rows-per-lane
+ * rows) are solved by a whole CTA whose 8 warps pipeline the strips, smaller
+ * ones by one warp each (default 16; the Python binding applies the tuned
+ * choice in mauve-py_gb300/dp_tuning.json).  Results do not depend on it. */
+int mvg_set_dp_coop_strips(mvg_handle h, int strips);
+
+/* Gap-DP passes as one CUDA graph (on = 1, the default): the launches of a
+ * call's waves (claim counters, the persistent DP kernel, both traceback
+ * walkers, path compaction) are recorded into one graph and launched at
+ * once; the handle keeps the executable graph per DP lane and updates it in
+ * place from the next call's recording when its shape is the same.  on = 0
+ * launches them one by one.  Results are identical either way.  No
+ * counterpart in the reference. */
+int mvg_set_dp_graph(mvg_handle h, int on);
+
 /* Per-stage timing with CUDA events on the handle's stream (off by default;
  * no extra synchronisation).  After a call, mvg_stage_times gives the stage
  * names (comma separated into names, of capacity names_cap) and each stage's

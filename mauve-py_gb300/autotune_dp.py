@@ -3,8 +3,12 @@
 
     python mauve-py_gb300/autotune_dp.py [--nprob 4000]
 
-Knobs: rows per lane of the full-DP kernel (4 or 8: strips of 128 or 256
-rows) and of the banded kernel (1, 2, 4 or 8).  The full DP is timed on a
+Knobs: rows per lane of the full-DP kernel (4 or 8: the tile is a strip of
+128 or 256 rows swept column by column) and of the banded kernel (1, 2, 4
+or 8); warps per problem of the full DP, i.e. the bucket edge between the
+problems a whole CTA (8 warps) pipelines and those one warp solves (at
+least S strips: S in 8, 12, 16, 24, 32, 48); and, for the record, the
+batch launched as one CUDA graph or launch by launch.  The full DP is timed on a
 sample of the gap-DP distribution (lengths log-uniform 10-20,000,
 divergence U(0,30%)); the banded DP on gaps drawn like the recoded-genome
 pair's, with the trained band-proposal network's bands when weights are
@@ -46,6 +50,22 @@ def run(args):
         secs = min(timed_full(ctx, full)[0] for _ in range(2))
         res["full"][rows] = {"seconds": secs, "gcups": full.cells / secs / 1e9}
     best_full = max(res["full"], key=lambda r: res["full"][r]["gcups"])
+    ctx.set_dp_rows(best_full, 4)
+    res["coop_min_strips"] = {}
+    for strips in (8, 12, 16, 24, 32, 48):
+        ctx.set_dp_coop_strips(strips)
+        timed_full(ctx, full)  # warm
+        secs = min(timed_full(ctx, full)[0] for _ in range(2))
+        res["coop_min_strips"][strips] = {"seconds": secs, "gcups": full.cells / secs / 1e9}
+    best_coop = max(res["coop_min_strips"], key=lambda r: res["coop_min_strips"][r]["gcups"])
+    ctx.set_dp_coop_strips(best_coop)
+    res["graph"] = {}
+    for on in (True, False):
+        ctx.set_dp_graph(on)
+        timed_full(ctx, full)  # warm
+        secs = min(timed_full(ctx, full)[0] for _ in range(2))
+        res["graph"]["on" if on else "off"] = {"seconds": secs, "gcups": full.cells / secs / 1e9}
+    ctx.set_dp_graph(True)
     band = DeviceBatch(*synth.gap_batch_recoded(seed=22, nprob=args.nprob * 5), dev)
     if os.path.exists(args.weights):
         w = np.load(args.weights)
@@ -67,6 +87,7 @@ def run(args):
                                "accept_rate": float((used == 1).mean()), "cells": cells}
     best_band = max(res["banded"], key=lambda r: res["banded"][r]["effective_gcups"])
     out = {"full_rows_per_lane": int(best_full), "band_rows_per_lane": int(best_band),
+           "coop_min_strips": int(best_coop),
            "measured": res, "band_source": src, "gpu": torch.cuda.get_device_name(0),
            "when": time.strftime("%Y-%m-%dT%H:%M:%SZ", time.gmtime())}
     print(json.dumps(out, indent=1))

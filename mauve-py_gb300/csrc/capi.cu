@@ -240,6 +240,10 @@ int mvg_destroy(mvg_handle h) {
   for (cudaStream_t st : {h->stream, h->aux, h->aux2, h->aux3, h->aux4, h->aux5})
     if (st) cudaStreamSynchronize(st);
   mlp_release(h);
+  for (cudaGraphExec_t& g : h->dp_exec)
+    if (g) cudaGraphExecDestroy(g);
+  for (cudaEvent_t ev : h->ev)
+    if (ev) cudaEventDestroy(ev);
   h->ws.release();
   if (h->d_err) cudaFree(h->d_err);
   if (h->h_err) cudaFreeHost(h->h_err);
@@ -506,6 +510,23 @@ int mvg_set_dp_spin_limit(mvg_handle h, long long polls) {
 int mvg_set_profiling(mvg_handle h, int on) {
   if (!h) return report_error(MVG_ERR_ARG, "null handle");
   h->profiling = on != 0;
+  if (h->profiling) {  // created here, not at the first mark: marks may be recorded into a graph
+    MVG_CUDA_TRY(cudaSetDevice(h->device));
+    for (int k = 0; k <= kMaxStages; ++k)
+      if (!h->ev[k]) MVG_CUDA_TRY(cudaEventCreate(&h->ev[k]));
+  }
+  return 0;
+}
+
+int mvg_set_dp_coop_strips(mvg_handle h, int strips) {
+  if (!h || strips < 2 || strips > 1 << 20) return report_error(MVG_ERR_ARG, "strips must be in 2 .. 2^20");
+  h->dp_coop_strips = strips;
+  return 0;
+}
+
+int mvg_set_dp_graph(mvg_handle h, int on) {
+  if (!h || (on != 0 && on != 1)) return report_error(MVG_ERR_ARG, "on must be 0 or 1");
+  h->dp_graph = on;
   return 0;
 }
 

@@ -272,12 +272,13 @@ struct TbLanes {
 
 static TbLanes main_lanes(Ctx* c) { return TbLanes{c->stream, c->aux, c->fork, c->join, 62, 63}; }
 
-static int tb_long_fork(Ctx* c, const TbLanes& L, const DpInputs& in, const std::vector<uint32_t>& slot_len,
-                        const uint32_t* d_order, const uint64_t* d_tboff, const uint32_t* tb, const uint8_t* d_edge,
-                        const int32_t* d_delta, const int32_t* d_half, const uint8_t* d_accept, int rows,
-                        const uint8_t* d_rows, int* long_path, bool* forked) {
-  *forked = false;
+// Host side of the long-path walker: the slots (of this wave's order) whose
+// paths go to warps, longest first, and the length from which they do.
+static int tb_long_plan(Ctx* c, const std::vector<uint32_t>& slot_len, std::vector<uint32_t>* long_slots,
+                        int* long_path, int* grid) {
+  long_slots->clear();
   *long_path = INT_MAX;
+  *grid = 0;
   static bool attr = false;  // once per process: more than 48 KB of shared memory
   static int cap = 0;
   int sms = 0;
@@ -305,23 +306,49 @@ static int tb_long_fork(Ctx* c, const TbLanes& L, const DpInputs& in, const std:
   std::sort(sel.begin(), sel.end(), [](const std::pair<uint32_t, uint32_t>& a, const std::pair<uint32_t, uint32_t>& b) {
     return a.first != b.first ? a.first > b.first : a.second < b.second;
   });
-  std::vector<uint32_t> long_slots(sel.size());
-  for (size_t q = 0; q < sel.size(); ++q) long_slots[q] = sel[q].second;
-  const int n = (int)long_slots.size();
-  uint32_t* d_slots = (uint32_t*)c->ws.get(c, L.slot_list, (size_t)n * 4 + 16);
-  unsigned* d_ctr = (unsigned*)c->ws.get(c, L.slot_ctr, 64);
-  if (!d_slots || !d_ctr) return report_error(MVG_ERR_NOMEM, "workspace allocation failed");
-  if (int e = h2d_async(c, d_slots, long_slots.data(), (size_t)n * 4, L.st)) return e;
+  long_slots->resize(sel.size());
+  for (size_t q = 0; q < sel.size(); ++q) (*long_slots)[q] = sel[q].second;
+  const int n = (int)long_slots->size();
+  *grid = std::min(sms * (cap / kTbWarps), (n + kTbWarps - 1) / kTbWarps);
+  *long_path = (int)thr;
+  return 0;
+}
+
+// Device side: the walker's launch on the side stream, forked from and
+// joined back to the pass's stream (tb_long_join).  Stream operations only,
+// so a pass's launches can be recorded into a CUDA graph.
+static int tb_long_launch(Ctx* c, const TbLanes& L, const DpInputs& in, const uint32_t* d_order,
+                          const uint64_t* d_tboff, const uint32_t* tb, const uint8_t* d_edge, const int32_t* d_delta,
+                          const int32_t* d_half, const uint8_t* d_accept, int rows, const uint8_t* d_rows,
+                          const uint32_t* d_slots, int n, int grid, unsigned* d_ctr) {
   MVG_CUDA_TRY(cudaMemsetAsync(d_ctr, 0, 4, L.st));
   MVG_CUDA_TRY(cudaEventRecord(L.fork, L.st));
   MVG_CUDA_TRY(cudaStreamWaitEvent(L.side, L.fork, 0));
-  const int grid = std::min(sms * (cap / kTbWarps), (n + kTbWarps - 1) / kTbWarps);
   k_traceback_win<<<grid, kTbWarps * 32, kTbSmem, L.side>>>(in.oa, in.ob, d_order, d_tboff, d_slots, n, tb, d_edge,
                                                             d_delta, d_half, d_accept, in.path_off, in.paths,
                                                             in.path_len, c->d_err, rows, d_rows, in.env, d_ctr);
   MVG_CUDA_TRY(cudaEventRecord(L.join, L.side));
   c->launches++;
-  *long_path = (int)thr;
+  return 0;
+}
+
+static int tb_long_fork(Ctx* c, const TbLanes& L, const DpInputs& in, const std::vector<uint32_t>& slot_len,
+                        const uint32_t* d_order, const uint64_t* d_tboff, const uint32_t* tb, const uint8_t* d_edge,
+                        const int32_t* d_delta, const int32_t* d_half, const uint8_t* d_accept, int rows,
+                        const uint8_t* d_rows, int* long_path, bool* forked) {
+  *forked = false;
+  std::vector<uint32_t> long_slots;
+  int grid = 0;
+  if (int e = tb_long_plan(c, slot_len, &long_slots, long_path, &grid)) return e;
+  if (long_slots.empty()) return 0;
+  const int n = (int)long_slots.size();
+  uint32_t* d_slots = (uint32_t*)c->ws.get(c, L.slot_list, (size_t)n * 4 + 16);
+  unsigned* d_ctr = (unsigned*)c->ws.get(c, L.slot_ctr, 64);
+  if (!d_slots || !d_ctr) return report_error(MVG_ERR_NOMEM, "workspace allocation failed");
+  if (int e = h2d_async(c, d_slots, long_slots.data(), (size_t)n * 4, L.st)) return e;
+  if (int e = tb_long_launch(c, L, in, d_order, d_tboff, tb, d_edge, d_delta, d_half, d_accept, rows, d_rows,
+                             d_slots, n, grid, d_ctr))
+    return e;
   *forked = true;
   return 0;
 }
@@ -330,6 +357,79 @@ static int tb_long_join(const TbLanes& L, bool forked) {
   if (forked) MVG_CUDA_TRY(cudaStreamWaitEvent(L.st, L.join, 0));
   return 0;
 }
+
+// Records the stream work issued between begin() and launch() into a CUDA
+// graph (stream capture in thread-local mode, so only this thread's calls
+// are restricted) and launches it as one graph; the executable graph is
+// kept by the caller and updated in place from the next recording when the
+// shape is unchanged (kernel arguments and grid sizes may differ), else
+// instantiated anew.  With recording off, or when the caller's stream is
+// already being captured, the work is issued directly and launch() does
+// nothing.  An error while recording ends the capture and discards it.
+class GraphRecorder {
+ public:
+  GraphRecorder(Ctx* c, cudaStream_t st, bool on) : c_(c), st_(st), on_(on) {}
+  ~GraphRecorder() { discard(); }
+  int begin() {
+    if (!on_) return 0;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    MVG_CUDA_TRY(cudaStreamIsCapturing(st_, &cs));
+    if (cs != cudaStreamCaptureStatusNone) return 0;
+    MVG_CUDA_TRY(cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal));
+    active_ = true;
+    return 0;
+  }
+  int check(cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return 0;
+    discard();
+    return report_cuda(e, what);
+  }
+  int check(int rc) {
+    if (rc) discard();
+    return rc;
+  }
+  int launch(cudaGraphExec_t* exec) {
+    if (!active_) return 0;
+    active_ = false;
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(st_, &g);
+    if (e != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      return report_cuda(e, "cudaStreamEndCapture");
+    }
+    if (*exec) {
+      cudaGraphExecUpdateResultInfo info;
+      if (cudaGraphExecUpdate(*exec, g, &info) != cudaSuccess) {
+        cudaGetLastError();  // a different shape: instantiate below
+        cudaGraphExecDestroy(*exec);
+        *exec = nullptr;
+      }
+    }
+    if (!*exec && (e = cudaGraphInstantiate(exec, g, 0)) != cudaSuccess) {
+      *exec = nullptr;
+      cudaGraphDestroy(g);
+      return report_cuda(e, "cudaGraphInstantiate");
+    }
+    cudaGraphDestroy(g);
+    MVG_CUDA_TRY(cudaGraphLaunch(*exec, st_));
+    c_->graph_launches++;
+    return 0;
+  }
+
+ private:
+  void discard() {
+    if (!active_) return;
+    active_ = false;
+    cudaGraph_t g = nullptr;
+    cudaStreamEndCapture(st_, &g);
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+  }
+  Ctx* c_;
+  cudaStream_t st_;
+  bool on_;
+  bool active_ = false;
+};
 
 // Runs the DP for the problems in `ids` (full, or banded with per-problem
 // delta/half on the device): LPT order, size-mixed waves that fit the
@@ -373,7 +473,7 @@ static int run_dp(Ctx* c, const DpInputs& in, const std::vector<uint32_t>& ids, 
   std::vector<char> is_big(nwork);
   for (int64_t w = 0; w < nwork; ++w) {
     const int64_t a = la[ids[w]];
-    const bool many = (a + 32 * rows - 1) / (32 * rows) >= kCoopMinStrips;
+    const bool many = (a + 32 * rows - 1) / (32 * rows) >= (banded ? kCoopMinStrips : c->dp_coop_strips);
     is_big[w] = many && (!banded || cells[w] >= (uint64_t)a * 8 * 32 * rows);
   }
   // largest first, ties in input order: one sort of packed (cells, index) keys
@@ -460,8 +560,34 @@ static int run_dp(Ctx* c, const DpInputs& in, const std::vector<uint32_t>& ids, 
     return report_error(MVG_ERR_NOMEM, "workspace allocation failed");
   if (int e = h2d_async(c, d_order, order.data(), (size_t)nwork * 4, L.st)) return e;
   if (int e = h2d_async(c, d_tboff, tboff.data(), (size_t)nwork * 8, L.st)) return e;
+  // the long-path walkers of all waves: slot lists concatenated, one counter each
+  const size_t nwaves_run = wave_begin.size() - 1;
+  std::vector<int> long_path(nwaves_run, INT_MAX), long_n(nwaves_run, 0), long_grid(nwaves_run, 0);
+  std::vector<size_t> long_at(nwaves_run, 0);
+  std::vector<uint32_t> all_long;
+  for (size_t wv = 0; wv < nwaves_run; ++wv) {
+    const int64_t w0 = wave_begin[wv], w1 = wave_begin[wv + 1];
+    std::vector<uint32_t> slot_len(w1 - w0), ls;
+    for (int64_t q = w0; q < w1; ++q) slot_len[q - w0] = (uint32_t)(la[order[q]] + lb[order[q]]);
+    if (int e = tb_long_plan(c, slot_len, &ls, &long_path[wv], &long_grid[wv])) return e;
+    long_at[wv] = all_long.size();
+    long_n[wv] = (int)ls.size();
+    all_long.insert(all_long.end(), ls.begin(), ls.end());
+  }
+  uint32_t* d_long = (uint32_t*)ws.get(c, L.slot_list, all_long.size() * 4 + 16);
+  unsigned* d_long_ctr = (unsigned*)ws.get(c, L.slot_ctr, nwaves_run * 4 + 64);
+  if (!d_long || !d_long_ctr) return report_error(MVG_ERR_NOMEM, "workspace allocation failed");
+  if (!all_long.empty())
+    if (int e = h2d_async(c, d_long, all_long.data(), all_long.size() * 4, L.st)) return e;
   span.reset();
-  for (size_t wv = 0; wv + 1 < wave_begin.size(); ++wv) {
+  // Every wave's launches (claim counters, the persistent DP kernel, the two
+  // traceback walkers, path compaction) are recorded into one CUDA graph and
+  // launched at once; the executable graph is kept per lane and updated in
+  // place when the next call has the same shape.
+  const int lane_id = sl.arena == kDpSlots.arena ? 0 : 1;
+  GraphRecorder rec(c, L.st, c->dp_graph != 0);
+  if (int e = rec.begin()) return e;
+  for (size_t wv = 0; wv < nwaves_run; ++wv) {
     const int64_t w0 = wave_begin[wv], w1 = wave_begin[wv + 1];
     DpJob J;
     J.sa = in.sa;
@@ -484,29 +610,27 @@ static int run_dp(Ctx* c, const DpInputs& in, const std::vector<uint32_t>& ids, 
     J.counter = d_counter;
     J.err = c->d_err;
     J.spin_limit = c->dp_spin_limit;
-    MVG_CUDA_TRY(cudaMemsetAsync(d_counter, 0, 8, L.st));
+    if (int e = rec.check(cudaMemsetAsync(d_counter, 0, 8, L.st), "cudaMemsetAsync")) return e;
     stage_mark(c, banded ? "dp_banded" : "dp");
     kern<<<grid, kDpThreads, 0, L.st>>>(J);
     stage_mark(c, "traceback");
-    std::vector<uint32_t> slot_len(w1 - w0);
-    for (int64_t q = w0; q < w1; ++q)
-      slot_len[q - w0] = (uint32_t)(la[order[q]] + lb[order[q]]);
-    bool forked = false;
-    int long_path = INT_MAX;
-    int trc = tb_long_fork(c, L, in, slot_len, J.order, J.tb_off, tb, d_edge, d_delta, d_half, d_accept, rows,
-                           nullptr, &long_path, &forked);
-    if (trc) return trc;
+    const bool forked = long_n[wv] > 0;
+    if (forked)
+      if (int e = rec.check(tb_long_launch(c, L, in, J.order, J.tb_off, tb, d_edge, d_delta, d_half, d_accept, rows,
+                                           nullptr, d_long + long_at[wv], long_n[wv], long_grid[wv],
+                                           d_long_ctr + wv)))
+        return e;
     k_traceback<<<grid_for(J.nwork, 128), 128, 0, L.st>>>(in.oa, in.ob, J.order, J.tb_off, J.nwork, tb, d_edge,
                                                                 d_delta, d_half, d_accept, in.path_off, in.paths,
-                                                                in.path_len, c->d_err, rows, in.env, long_path);
-    if ((trc = tb_long_join(L, forked))) return trc;
+                                                                in.path_len, c->d_err, rows, in.env, long_path[wv]);
+    if (int e = rec.check(tb_long_join(L, forked))) return e;
     stage_mark(c, "path_compact");
     k_path_compact<<<grid_for((int64_t)J.nwork * 32, 256), 256, 0, L.st>>>(
         in.oa, in.ob, J.order, J.nwork, d_accept, in.path_off, in.paths, in.path_len);
     c->launches += 3;
-    MVG_CUDA_TRY(cudaGetLastError());
+    if (int e = rec.check(cudaGetLastError(), "kernel launch")) return e;
   }
-  return 0;
+  return rec.launch(&c->dp_exec[lane_id]);
 }
 
 // Ring-scheduled banded problems (gapdp_ring.cuh): rsel[w] is the group

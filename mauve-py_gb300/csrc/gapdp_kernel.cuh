@@ -48,7 +48,7 @@ constexpr int32_t kGap = -200;           // half of gap open -400
 constexpr int32_t kMaxPair = 160;        // max NUC_SP + 60 (C/C, G/G)
 constexpr int kDpThreads = 256;
 constexpr int kDpWarps = kDpThreads / 32;
-constexpr int kCoopMinStrips = 16;       // problems with at least this many strips use a whole CTA
+constexpr int kCoopMinStrips = 16;       // banded problems with at least this many strips use a whole CTA
 
 enum : uint32_t { TB_MM = 0, TB_DM = 1, TB_IM = 2, TB_MD = 4, TB_MI = 8 };
 

@@ -317,14 +317,18 @@ __global__ void __launch_bounds__(256) k_bucket_replay(MatchCtx c, const Mhe* __
 
 // The largest buckets, one per cluster of kClusterCtas CTAs on as many SMs.
 // Every CTA keeps its own copy of the bucket's entries (appended, with a
-// uint16 sorted-order map) in shared memory and tests its 256 seeds of each
-// 2048-seed chunk against it; the CTAs' first fresh seeds meet in every
+// uint16 sorted-order map) in shared memory and tests its seeds of each
+// 16384-seed chunk (8 per thread, in rows of 2048) against it, one row per
+// round at first and twice as many rows after every round that finds no
+// fresh seed (halved after an insert); the CTAs' first fresh seeds meet in every
 // CTA's shared memory (distributed shared memory stores + cluster barrier),
 // the CTA owning the first one extends it and sends the new entry and its
 // sorted position to every CTA, and all insert it.  The result is the same
 // sequence of tests and inserts as the one-CTA replay.  A bucket that grows
 // past kLocalCap entries is left untouched and marked kRedo.
-constexpr int kClusterChunk = kClusterCtas * 256;
+constexpr int kClusterItems = 8;  // seeds per thread and chunk
+constexpr int kClusterRow = kClusterCtas * 256;
+constexpr int kClusterChunk = kClusterRow * kClusterItems;
 
 __device__ __forceinline__ int64_t lower_bound_local(const Mhe* __restrict__ E, const uint16_t* __restrict__ M,
                                                      int64_t n, const Mhe& x, int L) {
@@ -368,20 +372,31 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(256, 1)
     int64_t n = 0;
     bool overflow = false;
     unsigned long long ncoll = 0;
+    int rows = 1;  // item rows tested per round
     for (uint32_t cbase = 0; cbase < cnt && !overflow; cbase += kClusterChunk) {
       const uint32_t cend = min(cnt, cbase + (uint32_t)kClusterChunk);
-      const uint32_t slot = cbase + rank * 256 + tid;
-      const bool have = slot < cend;
-      Mhe m = {0, 0, 0, 0};
-      if (have) m = mhe[sp[slot]];
+      // slot of item j: cbase + j * kClusterRow + rank * 256 + tid (item order = slot order)
+      const uint32_t slot0 = cbase + rank * 256 + tid;
+      Mhe m[kClusterItems];
+#pragma unroll
+      for (int j = 0; j < kClusterItems; ++j) {
+        const uint32_t slot = slot0 + j * kClusterRow;
+        m[j] = slot < cend ? mhe[sp[slot]] : Mhe{0, 0, 0, 0};
+      }
       uint32_t pos = cbase;
       while (pos < cend) {
-        bool fresh = false;
-        if (have && slot >= pos) {
-          const int64_t at = lower_bound_local(lent, lmap, n, m, L);
-          fresh = !(at != n && !mhe_less(lent[lmap[at]], m, L) && !mhe_less(m, lent[lmap[at]], L));
+        const int rlo = (int)((pos - cbase) / kClusterRow);
+        const uint32_t limit = min(cend, cbase + (uint32_t)min(kClusterItems, rlo + rows) * kClusterRow);
+        uint32_t myf = kRedo;
+#pragma unroll
+        for (int j = 0; j < kClusterItems; ++j) {
+          const uint32_t slot = slot0 + j * kClusterRow;
+          if (myf == kRedo && slot < limit && slot >= pos) {
+            const int64_t at = lower_bound_local(lent, lmap, n, m[j], L);
+            if (!(at != n && !mhe_less(lent[lmap[at]], m[j], L) && !mhe_less(m[j], lent[lmap[at]], L))) myf = slot;
+          }
         }
-        const uint32_t wmin = __reduce_min_sync(0xffffffffu, fresh ? slot : kRedo);
+        const uint32_t wmin = __reduce_min_sync(0xffffffffu, myf);
         if (lane == 0) s_wmin[wid] = wmin;
         __syncthreads();
         if (tid < kClusterCtas) {
@@ -394,21 +409,28 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(256, 1)
         uint32_t f = kRedo;
 #pragma unroll
         for (int q = 0; q < kClusterCtas; ++q) f = min(f, s_cmin[q]);
-        if (f == kRedo) {
-          if (have && slot >= pos) ++ncoll;
-          pos = cend;
-          cl.sync();  // every CTA has read s_cmin before the next round writes it
-          break;
+        // this thread's seeds in [pos, min(f, limit)) were tested and are collisions
+#pragma unroll
+        for (int j = 0; j < kClusterItems; ++j) {
+          const uint32_t slot = slot0 + j * kClusterRow;
+          if (slot < limit && slot >= pos && slot < f) ++ncoll;
         }
-        if (have && slot >= pos && slot < f) ++ncoll;
-        const unsigned owner = (f - cbase) / 256;
+        if (f == kRedo) {
+          pos = limit;
+          rows = min(kClusterItems, 2 * rows);
+          cl.sync();  // every CTA has read s_cmin before the next round writes it
+          continue;
+        }
+        const unsigned owner = ((f - cbase) % kClusterRow) / 256;
         if (n == kLocalCap) {  // no room for the entry: hand the bucket to the one-CTA replay
           overflow = true;
           cl.sync();
           break;
         }
         if (rank == owner) {
-          if (slot == f) s_seed = m;
+#pragma unroll
+          for (int j = 0; j < kClusterItems; ++j)
+            if (slot0 + j * kClusterRow == f) s_seed = m[j];
           __syncthreads();
           Mhe x = s_seed;
           cta_extend(c, x, s_ring);  // the whole owning CTA
@@ -445,6 +467,7 @@ __global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(256, 1)
         ++n;
         __syncthreads();
         pos = f + 1;
+        rows = rows > 1 ? rows / 2 : 1;
       }
     }
     // ncoll of the CTAs that finished: summed per CTA

@@ -26,7 +26,7 @@ struct MatchStats {
 };
 
 // Optional per-stage CUDA-event timing on the handle's stream (off by default).
-constexpr int kMaxStages = 24;
+constexpr int kMaxStages = 256;  // a many-wave gap-DP call marks three stages per wave
 
 struct Ctx {
   int device = 0;
@@ -53,6 +53,10 @@ struct Ctx {
   int band_gate = 0;          // band proposals: divergence gate window threshold (0 = off)
   int pair_bucket_cap = 3072;  // seed-join buckets sorted in shared memory up to this size
   long long dp_spin_limit = 1ll << 26;  // polls before a whole-CTA gap-DP wait gives up (about a second)
+  int dp_graph = 1;                      // gap-DP passes launched as one recorded CUDA graph
+  int dp_coop_strips = 16;               // full-DP problems of at least this many strips use a whole CTA
+  cudaGraphExec_t dp_exec[2] = {};       // the executable graph of each DP lane, updated per call
+  uint64_t graph_launches = 0;
   Workspace ws;
   MatchStats stats;
   bool profiling = false;
@@ -72,7 +76,13 @@ inline void stage_mark(Ctx* c, const char* name) {
   if (c->nstage < 0) c->nstage = 0;
   if (c->nstage >= kMaxStages) return;
   if (!c->ev[c->nstage]) cudaEventCreate(&c->ev[c->nstage]);
-  cudaEventRecord(c->ev[c->nstage], c->stream);
+  // inside a recorded graph the mark must be an event-record node of its own
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaStreamIsCapturing(c->stream, &cs);
+  if (cs == cudaStreamCaptureStatusActive)
+    cudaEventRecordWithFlags(c->ev[c->nstage], c->stream, cudaEventRecordExternal);
+  else
+    cudaEventRecord(c->ev[c->nstage], c->stream);
   c->stage_name[c->nstage] = name;
   c->nstage++;
 }

@@ -46,7 +46,8 @@ EXPORTS = ["mvg_create", "mvg_destroy", "mvg_last_error", "mvg_stream", "mvg_ker
            "mvg_lut_find_mismatches", "mvg_lut_find_duplicate_mappings", "mvg_build_index_lut",
            "mvg_build_index_lut_dev", "mvg_set_band_whole_fraction", "mvg_set_band_ring",
            "mvg_set_band_gate", "mvg_sslist_write", "mvg_sslist_read", "mvg_set_pair_bucket_cap",
-           "mvg_set_dp_spin_limit", "mvg_gap_anchor_search", "mvg_gap_anchor_search_dev"]
+           "mvg_set_dp_spin_limit", "mvg_gap_anchor_search", "mvg_gap_anchor_search_dev", "mvg_set_dp_graph",
+           "mvg_set_dp_coop_strips"]
 
 TUNING_PATH = os.path.join(HERE, "dp_tuning.json")
 
@@ -89,6 +90,8 @@ def load_library(path=LIB_PATH):
         "mvg_set_band_gate": (ci, [vp, ci]),
         "mvg_set_pair_bucket_cap": (ci, [vp, ci]),
         "mvg_set_dp_spin_limit": (ci, [vp, ctypes.c_longlong]),
+        "mvg_set_dp_graph": (ci, [vp, ci]),
+        "mvg_set_dp_coop_strips": (ci, [vp, ci]),
         "mvg_sslist_write": (ci, [vp, vp, u64, u64, ctypes.c_char_p]),
         "mvg_sslist_read": (ci, [ctypes.c_char_p, vp, vp, u64, vp, u64]),
         "mvg_gapdp_envelope_dev": (ci, [vp, vp, vp, vp, vp, i64, vp, vp]),
@@ -206,6 +209,7 @@ class Context:
             with open(TUNING_PATH) as f:
                 t = json.load(f)
             self.set_dp_rows(int(t.get("full_rows_per_lane", 8)), int(t.get("band_rows_per_lane", 4)))
+            self.set_dp_coop_strips(int(t.get("coop_min_strips", 16)))
 
     def set_band_whole_fraction(self, fraction):
         """Bands covering at least this share of their matrix run whole (default 0.5)."""
@@ -222,6 +226,14 @@ class Context:
     def set_dp_spin_limit(self, polls=1 << 26):
         """Polls before a whole-CTA gap-DP wait gives up (watchdog); see mvg_set_dp_spin_limit."""
         _check(load_library().mvg_set_dp_spin_limit(self._h, int(polls)))
+
+    def set_dp_coop_strips(self, strips):
+        """Full-DP problems of at least this many strips go to a whole CTA; see mvg_set_dp_coop_strips."""
+        _check(load_library().mvg_set_dp_coop_strips(self._h, int(strips)))
+
+    def set_dp_graph(self, on=True):
+        """Gap-DP waves as one recorded CUDA graph (default) or launched one by one."""
+        _check(load_library().mvg_set_dp_graph(self._h, 1 if on else 0))
 
     def set_band_ring(self, on=True):
         """Banded passes on the ring schedule (default) or all in the strip kernel."""

@@ -370,3 +370,36 @@ def _path_score(a, b, path):
             j += 1
         prev = e
     return s
+
+
+def test_gapdp_graph_and_direct_launches_identical(ctx):
+    """The DP waves recorded into one CUDA graph (default) and launched one by
+    one give identical scores and paths, across calls of different shapes
+    (the kept executable graph updated or rebuilt), with many waves (a small
+    traceback arena) and long paths (the warp walker on the side stream),
+    and with stage timing on (event nodes inside the graph)."""
+    sa, oa, sb, ob = synth.gap_batch(seed=57, nprob=300, lmin=50, lmax=6000)
+    ctx.set_dp_graph(False)
+    try:
+        s_direct, p_direct = ctx.gap_align_batch(sa, oa, sb, ob)
+    finally:
+        ctx.set_dp_graph(True)
+    for arena in (1 << 62, 64 << 20, 16 << 20):
+        ctx.set_tb_arena(arena)
+        try:
+            s_graph, p_graph = ctx.gap_align_batch(sa, oa, sb, ob)
+        finally:
+            ctx.set_tb_arena(1 << 62)
+        np.testing.assert_array_equal(s_graph, s_direct)
+        assert p_graph == p_direct
+    ctx.set_profiling(True)
+    try:
+        s_prof, p_prof = ctx.gap_align_batch(sa, oa, sb, ob)
+        st = ctx.stage_times()
+    finally:
+        ctx.set_profiling(False)
+    np.testing.assert_array_equal(s_prof, s_direct)
+    assert p_prof == p_direct
+    assert st.get("dp", 0) > 0 and st.get("traceback", 0) > 0
+    oscores, _, _, _ = O.nw_batch(sa, oa, sb, ob, with_paths=False)
+    np.testing.assert_array_equal(s_direct, oscores)
