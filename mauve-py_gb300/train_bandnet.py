@@ -174,6 +174,9 @@ def train(args):
     ev = DeviceBatch(*subset(sa, oa, sb, ob, np.arange(n_tr, n_tr + n_ev)), dev)
     del sa, sb
     print("data", tr.n, ev.n, "%.1fs" % (time.time() - t_all), flush=True)
+    if args.calibrate_only:
+        return calibrate_and_evaluate(args, ctx, dev, bandnet.BandNet(ctx, params=np.load(args.calibrate_only)["params"]),
+                                      tr, ev, tot_a, tot_b, n_tr, [], 0, 0, 0.0, t_all)
     t0 = time.time()
     sc_tr, env_tr = label(ctx, tr)
     print("labels %.1fs (%.3g cells)" % (time.time() - t0, tr.cells), flush=True)
@@ -231,18 +234,23 @@ def train(args):
         print("epoch %d loss %.4f (non-finite minibatches so far: %d)" % (
             ep, losses[-1][1] if losses else float("nan"), skipped), flush=True)
     train_s = time.time() - t0
+    return calibrate_and_evaluate(args, ctx, dev, net, tr, ev, tot_a, tot_b, n_tr, losses, step, skipped, train_s, t_all)
+
+
+def calibrate_and_evaluate(args, ctx, dev, net, tr, ev, tot_a, tot_b, n_tr, losses, step, skipped, train_s, t_all):
+    import torch
     # calibrate alpha / beta on a separate draw of calibration gaps, as many
     # as a production batch, by timing the exact banded DP (with its
     # fallbacks) for each candidate margin (the faster of two runs)
     import synth
     vb = DeviceBatch(*synth.gap_batch_recoded(seed=args.seed + 7, nprob=args.calib), dev)
     best = None
-    for gate in (0, 22, 24):
+    for gate in (0, 18, 20, 22, 24):
         ctx.set_band_gate(gate)
-        for whole in (0.35, 0.5, 0.7):
+        for whole in (0.3, 0.35, 0.45):
             ctx.set_band_whole_fraction(whole)
-            for alpha in (0.9, 1.0, 1.15, 1.3):
-                for beta in (0.0, 16.0, 48.0):
+            for alpha in (1.15, 1.45, 1.6, 1.8, 2.0, 2.3):
+                for beta in (0.0, 8.0, 16.0, 32.0):
                     d, h = net.propose_dev(*vb.ptrs(), vb.n, alpha, beta)
                     runs = [timed_banded(ctx, vb, d, h)[:3] for _ in range(2)]
                     secs, used, cells = min(runs, key=lambda r: r[0])
@@ -327,6 +335,8 @@ def main():
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--seed", type=int, default=4)
     ap.add_argument("--out", default=os.path.join(HERE, "bandnet_weights.npz"))
+    ap.add_argument("--calibrate-only", default="",
+                    help="weights file whose network is kept: only recalibrate the margins and evaluate")
     train(ap.parse_args())
 
 
