@@ -328,6 +328,43 @@ int mvg_build_index_lut_dev(mvg_handle h, const int64_t* d_genome_start, const i
                             uint64_t ref_len, int fill_gaps, int max_gap_width, int smooth_edges,
                             int smoothing_radius, int32_t* d_lut, uint64_t n);
 
+/* Aligned rows from gap-DP paths: AlignTwoMSAsGivenPath
+ * (MU/aligngivenpath.cpp:256) for single-sequence profiles, for a batch.
+ * Edge t of path p is column t: 'M' takes the next character of both
+ * sequences, 'D' the next of A against '-', 'I' '-' against the next of B.
+ * seq_a / seq_b / off_a / off_b as for mvg_gapdp_batch (the characters are
+ * copied as given, so ASCII bases may be passed); paths / path_off /
+ * path_len as mvg_gapdp_batch writes them.  rows_a and rows_b receive the
+ * two gapped rows of problem p at [path_off[p], path_off[p] + path_len[p]).
+ * MVG_ERR_ARG if a path does not consume exactly its two sequences. */
+int mvg_path_rows(mvg_handle h, const uint8_t* seq_a, const uint64_t* off_a, const uint8_t* seq_b,
+                  const uint64_t* off_b, int64_t nprob, const char* paths, const uint64_t* path_off,
+                  const int64_t* path_len, uint8_t* rows_a, uint8_t* rows_b);
+int mvg_path_rows_dev(mvg_handle h, const uint8_t* d_seq_a, const uint64_t* d_off_a, const uint8_t* d_seq_b,
+                      const uint64_t* d_off_b, int64_t nprob, const char* d_paths, const uint64_t* d_path_off,
+                      const int64_t* d_path_len, uint8_t* d_rows_a, uint8_t* d_rows_b);
+
+/* XMFA writer: GenericIntervalList::WriteStandardAlignment
+ * (LM/IntervalList.h:353-440) for pairwise blocks, as progressiveMauve
+ * writes the file buildIndex parses (MA/progressiveMauve.cpp:727).
+ * file_a / file_b: the two sequence file names (written as the sequence
+ * names; the format line follows the name's extension as libGenome's
+ * source factory does); backbone_file may be NULL or "".  Block b has
+ * columns col_off[b] .. col_off[b+1]-1 of rows_a / rows_b (the gapped rows,
+ * '-' for gaps, already reverse-complemented for a reverse-strand
+ * sequence), signed starts starts[2b], starts[2b+1] (1-based left end,
+ * negative = reverse strand, 0 = absent) and base counts lengths[2b],
+ * lengths[2b+1].  out receives the text (not NUL-terminated); *out_len gets
+ * its length, MVG_ERR_CAPACITY if it exceeds cap.  The text is assembled on
+ * the device. */
+int mvg_xmfa_write(mvg_handle h, const char* file_a, const char* file_b, const char* backbone_file,
+                   int64_t nblocks, const int64_t* starts, const int64_t* lengths, const uint8_t* rows_a,
+                   const uint8_t* rows_b, const uint64_t* col_off, char* out, uint64_t cap, uint64_t* out_len);
+/* The same with the rows in device memory (the other arrays on the host). */
+int mvg_xmfa_write_dev(mvg_handle h, const char* file_a, const char* file_b, const char* backbone_file,
+                       int64_t nblocks, const int64_t* starts, const int64_t* lengths, const uint8_t* d_rows_a,
+                       const uint8_t* d_rows_b, const uint64_t* col_off, char* out, uint64_t cap, uint64_t* out_len);
+
 /* Upper bound on the device bytes the gap-DP traceback arena may use.  Each
  * call uses min(bound, 60% of free device memory); problems run in waves of
  * mixed sizes that fit it.  Default: no bound beyond the 60% cap. */

@@ -47,7 +47,8 @@ EXPORTS = ["mvg_create", "mvg_destroy", "mvg_last_error", "mvg_stream", "mvg_ker
            "mvg_build_index_lut_dev", "mvg_set_band_whole_fraction", "mvg_set_band_ring",
            "mvg_set_band_gate", "mvg_sslist_write", "mvg_sslist_read", "mvg_set_pair_bucket_cap",
            "mvg_set_dp_spin_limit", "mvg_gap_anchor_search", "mvg_gap_anchor_search_dev", "mvg_set_dp_graph",
-           "mvg_set_dp_coop_strips"]
+           "mvg_set_dp_coop_strips", "mvg_path_rows", "mvg_path_rows_dev",
+           "mvg_xmfa_write", "mvg_xmfa_write_dev"]
 
 TUNING_PATH = os.path.join(HERE, "dp_tuning.json")
 
@@ -92,6 +93,12 @@ def load_library(path=LIB_PATH):
         "mvg_set_dp_spin_limit": (ci, [vp, ctypes.c_longlong]),
         "mvg_set_dp_graph": (ci, [vp, ci]),
         "mvg_set_dp_coop_strips": (ci, [vp, ci]),
+        "mvg_path_rows": (ci, [vp, vp, vp, vp, vp, i64, vp, vp, vp, vp, vp]),
+        "mvg_xmfa_write": (ci, [vp, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, i64, vp, vp, vp, vp, vp, vp,
+                                u64, ctypes.POINTER(u64)]),
+        "mvg_xmfa_write_dev": (ci, [vp, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, i64, vp, vp, vp, vp, vp,
+                                    vp, u64, ctypes.POINTER(u64)]),
+        "mvg_path_rows_dev": (ci, [vp, vp, vp, vp, vp, i64, vp, vp, vp, vp, vp]),
         "mvg_sslist_write": (ci, [vp, vp, u64, u64, ctypes.c_char_p]),
         "mvg_sslist_read": (ci, [ctypes.c_char_p, vp, vp, u64, vp, u64]),
         "mvg_gapdp_envelope_dev": (ci, [vp, vp, vp, vp, vp, i64, vp, vp]),
@@ -422,6 +429,41 @@ class Context:
                                                    d_scores, d_paths, d_path_off, d_path_len, _ptr(used),
                                                    ctypes.byref(cells)))
         return used[:n].copy(), int(cells.value)
+
+    def path_rows(self, seq_a, off_a, seq_b, off_b, paths):
+        """AlignTwoMSAsGivenPath for a batch: the two gapped rows (bytes, '-'
+        for gaps) of each problem from its path (a list of 'M'/'D'/'I' strings)."""
+        seq_a, seq_b = _u8(seq_a), _u8(seq_b)
+        off_a = np.ascontiguousarray(off_a, np.uint64)
+        off_b = np.ascontiguousarray(off_b, np.uint64)
+        n = len(off_a) - 1
+        plen = np.array([len(p) for p in paths], np.int64)
+        poff = np.zeros(n + 1, np.uint64)
+        poff[1:] = np.cumsum(plen)
+        flat = np.frombuffer("".join(paths).encode() or b"\0", np.uint8)
+        ra = np.zeros(max(int(poff[-1]), 1), np.uint8)
+        rb = np.zeros(max(int(poff[-1]), 1), np.uint8)
+        _check(load_library().mvg_path_rows(self._h, _ptr(seq_a), _ptr(off_a), _ptr(seq_b), _ptr(off_b), n,
+                                            _ptr(flat), _ptr(poff), _ptr(plen), _ptr(ra), _ptr(rb)))
+        return [(ra[poff[k]:poff[k + 1]].tobytes(), rb[poff[k]:poff[k + 1]].tobytes()) for k in range(n)]
+
+    def xmfa_write(self, file_a, file_b, starts, lengths, rows_a, rows_b, col_off, backbone_file=""):
+        """WriteStandardAlignment for pairwise blocks; returns the XMFA text (bytes)."""
+        starts = np.ascontiguousarray(starts, np.int64).reshape(-1)
+        lengths = np.ascontiguousarray(lengths, np.int64).reshape(-1)
+        col_off = np.ascontiguousarray(col_off, np.uint64)
+        ra, rb = _u8(rows_a), _u8(rows_b)
+        n = len(col_off) - 1
+        cnt = ctypes.c_uint64(0)
+        L = load_library()
+        args = (self._h, file_a.encode(), file_b.encode(), backbone_file.encode(), n, _ptr(starts), _ptr(lengths),
+                _ptr(ra) if len(ra) else None, _ptr(rb) if len(rb) else None, _ptr(col_off))
+        rc = L.mvg_xmfa_write(*args, None, 0, ctypes.byref(cnt))
+        if rc not in (MVG_OK, MVG_ERR_CAPACITY):
+            _check(rc)
+        out = ctypes.create_string_buffer(max(int(cnt.value), 1))
+        _check(L.mvg_xmfa_write(*args, out, int(cnt.value), ctypes.byref(cnt)))
+        return out.raw[:cnt.value]
 
     def gap_align_batch_raw(self, seq_a, off_a, seq_b, off_b, scores, paths, path_off, path_len):
         """Host-buffer call with caller-owned numpy outputs (no per-call Python decoding)."""

@@ -403,3 +403,51 @@ def test_gapdp_graph_and_direct_launches_identical(ctx):
     assert st.get("dp", 0) > 0 and st.get("traceback", 0) > 0
     oscores, _, _, _ = O.nw_batch(sa, oa, sb, ob, with_paths=False)
     np.testing.assert_array_equal(s_direct, oscores)
+
+
+def _rows_from_path(a, b, path):
+    ra, rb, i, j = [], [], 0, 0
+    for e in path:
+        ra.append(a[i] if e != "I" else ord("-"))
+        rb.append(b[j] if e != "D" else ord("-"))
+        i += e != "I"
+        j += e != "D"
+    return bytes(ra), bytes(rb)
+
+
+def test_path_rows_reference_fixtures(ctx):
+    """The gapped rows of the reference's own profile-profile alignments
+    (gapdp.npz holds MUSCLE's rows as paths over A/C/G/T): the GPU's paths
+    turned into rows by the batched AlignTwoMSAsGivenPath equal them."""
+    g = load_golden("gapdp.npz")
+    sa, sb, oa, ob = g["seq_a"], g["seq_b"], g["off_a"], g["off_b"]
+    _, paths = ctx.gap_align_batch(sa, oa, sb, ob)
+    acgt = np.frombuffer(b"ACGT", np.uint8)
+    ta, tb = acgt[sa], acgt[sb]
+    rows = ctx.path_rows(ta, oa, tb, ob, paths)
+    for k in range(len(oa) - 1):
+        ref_path = g["paths"][g["off_p"][k]:g["off_p"][k + 1]].tobytes().decode()
+        want = _rows_from_path(ta[oa[k]:oa[k + 1]], tb[ob[k]:ob[k + 1]], ref_path)
+        assert rows[k] == want, k
+
+
+def test_path_rows_ascii_batch_and_bad_path(ctx):
+    """Rows of a random batch with IUPAC/lower-case letters copied through,
+    against rows built from the oracle's paths; a path that does not consume
+    its sequences is refused."""
+    sa, oa, sb, ob = synth.gap_batch(seed=88, nprob=500, lmin=1, lmax=4000)
+    rng = np.random.default_rng(88)
+    letters = np.frombuffer(b"acgtNRYKM", np.uint8)
+    ta = np.frombuffer(b"ACGT", np.uint8)[sa].copy()
+    tb = np.frombuffer(b"ACGT", np.uint8)[sb].copy()
+    for t in (ta, tb):
+        m = rng.random(len(t)) < 0.05
+        t[m] = rng.choice(letters, int(m.sum()))
+    _, oplen, opaths, opoff = O.nw_batch(sa, oa, sb, ob)
+    raw = opaths.tobytes()
+    paths = [raw[int(opoff[k]):int(opoff[k]) + int(oplen[k])].decode() for k in range(len(oa) - 1)]
+    rows = ctx.path_rows(ta, oa, tb, ob, paths)
+    for k in range(len(oa) - 1):
+        assert rows[k] == _rows_from_path(ta[oa[k]:oa[k + 1]], tb[ob[k]:ob[k + 1]], paths[k]), k
+    with pytest.raises(ValueError):
+        ctx.path_rows(ta[:10], [0, 10], tb[:10], [0, 10], ["M" * 9])
