@@ -29,6 +29,7 @@
 //                    LengthFilter, shift to genome coordinates
 #include <algorithm>
 #include <mutex>
+#include <thread>
 #include <vector>
 
 #include "match_common.cuh"
@@ -503,38 +504,60 @@ int gap_anchor_search_dev(Ctx* c, const uint8_t* d_a, uint64_t na, const uint8_t
     }
   }
 host_filter:
-  // host: per gap, overlap elimination and length filter, then genome coordinates
+  // host: per gap, overlap elimination and length filter, then genome
+  // coordinates; gaps are independent, so host threads take contiguous
+  // ranges of them and the survivors are packed in gap order afterwards
   std::vector<Anchor> anc(rows.size() / 3);
   for (size_t k = 0; k < anc.size(); ++k) anc[k] = Anchor{{rows[3 * k], rows[3 * k + 1]}, rows[3 * k + 2]};
-  std::vector<Anchor*> scratch;
-  std::vector<uint64_t> kept_at(ngaps + 1, 0);
-  std::vector<Anchor> kept;
-  kept.reserve(anc.size());
-  size_t r = 0, s = 0;
-  for (int gi = 0; gi < ng; ++gi) {
-    const size_t r0 = r;
+  std::vector<size_t> gap_r(ng + 1, 0);  // rows of searched gap gi: [gap_r[gi], gap_r[gi+1])
+  for (size_t s = 0, r = 0, gi = 0; gi < (size_t)ng; ++gi) {
     while (s < seg_gap.size() && seg_gap[s] == (uint32_t)gi) r += seg_n[s++];
-    const int64_t k = filter_gap(anc.data() + r0, (int64_t)(r - r0), scratch);
-    const GapDev& d = gd[gi];
-    for (int64_t t = 0; t < k; ++t) {
-      Anchor x = anc[r0 + t];
-      for (int q = 0; q < 2; ++q) x.s[q] = x.s[q] > 0 ? x.s[q] + (int64_t)d.src[q] : x.s[q] - (int64_t)d.src[q];
-      kept.push_back(x);
+    gap_r[gi + 1] = r;
+  }
+  std::vector<int64_t> nkept(ng, 0);
+  const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  const int nthreads = (int)std::min<uint64_t>(hw, std::max<uint64_t>(1, anc.size() / 20000));
+  auto work = [&](int t) {
+    std::vector<Anchor*> scratch;
+    for (int gi = (int)((int64_t)ng * t / nthreads); gi < (int)((int64_t)ng * (t + 1) / nthreads); ++gi) {
+      const size_t r0 = gap_r[gi];
+      const int64_t k = filter_gap(anc.data() + r0, (int64_t)(gap_r[gi + 1] - r0), scratch);
+      const GapDev& d = gd[gi];
+      for (int64_t u = 0; u < k; ++u)
+        for (int q = 0; q < 2; ++q) {
+          int64_t& x = anc[r0 + u].s[q];
+          x = x > 0 ? x + (int64_t)d.src[q] : x - (int64_t)d.src[q];
+        }
+      nkept[gi] = k;
     }
-    per_gap[gid[gi]] = (uint64_t)k;
+  };
+  if (nthreads > 1) {
+    std::vector<std::thread> pool;
+    for (int t = 0; t < nthreads; ++t) pool.emplace_back(work, t);
+    for (std::thread& th : pool) th.join();
+  } else {
+    work(0);
+  }
+  uint64_t total = 0;
+  for (int gi = 0; gi < ng; ++gi) {
+    per_gap[gid[gi]] = (uint64_t)nkept[gi];
+    total += (uint64_t)nkept[gi];
   }
   if (gap_off) {
     gap_off[0] = 0;
     for (uint64_t g = 0; g < ngaps; ++g) gap_off[g + 1] = gap_off[g] + per_gap[g];
   }
-  *count = kept.size();
-  if (kept.size() > cap) return report_error(MVG_ERR_CAPACITY, "anchor output buffer too small");
-  // kept is in searched-gap order, which is the caller's gap order
-  for (size_t k = 0; k < kept.size(); ++k) {
-    out[3 * k + 0] = kept[k].s[0];
-    out[3 * k + 1] = kept[k].s[1];
-    out[3 * k + 2] = kept[k].len;
-  }
+  *count = total;
+  if (total > cap) return report_error(MVG_ERR_CAPACITY, "anchor output buffer too small");
+  // searched-gap order is the caller's gap order
+  uint64_t o = 0;
+  for (int gi = 0; gi < ng; ++gi)
+    for (int64_t u = 0; u < nkept[gi]; ++u, ++o) {
+      const Anchor& x = anc[gap_r[gi] + u];
+      out[3 * o + 0] = x.s[0];
+      out[3 * o + 1] = x.s[1];
+      out[3 * o + 2] = x.len;
+    }
   return 0;
 }
 

@@ -169,11 +169,13 @@ __device__ __forceinline__ void window128(const uint32_t* __restrict__ g, uint64
   }
 }
 
-// One warp's fill: match bits of displacements u0 .. u0 + 1023 into ring
-// words (u0 / 32 + lane) mod RING (no synchronisation).
+// One warp's fill: match bits of displacements u0 .. u0 + 32 * nlanes - 1
+// into ring words (u0 / 32 + lane) mod RING, lanes below nlanes (no
+// synchronisation).
 template <int RING>
 __device__ __forceinline__ void ext_fill_ring(const MatchCtx& c, int64_t st0, int64_t st1, int64_t len, int64_t u0,
-                                              uint64_t pmask, uint32_t* ring) {
+                                              uint64_t pmask, uint32_t* ring, int nlanes = 32) {
+  if ((int)(threadIdx.x & 31) >= nlanes) return;
   const int lane = threadIdx.x & 31;
   const int L = c.s.L;
   const bool same = (st0 > 0) == (st1 > 0);
@@ -268,10 +270,12 @@ static __device__ void warp_extend(const MatchCtx& c, Mhe& m, ExtRing& R) {
     const int64_t room = r0 < r1 ? r0 : r1;
     uint32_t* ring = R.w[sd];
     int64_t filled = 0, checked = 0;  // displacements filled, words checked
-    for (;;) {
-      ext_fill_ring<kExtRing>(c, s0, s1, elen, filled, pmask, ring);
+    for (int k = 0;; ++k) {
+      // most matches stop within a few windows: the first fill is 256 displacements
+      const int nlanes = k == 0 ? 8 : 32;
+      ext_fill_ring<kExtRing>(c, s0, s1, elen, filled, pmask, ring, nlanes);
       __syncwarp();
-      filled += kExtChunk;
+      filled += 32 * nlanes;
       const int64_t last = filled / 32 - 1;  // words below it have their successor filled
       const int64_t i = checked + lane;
       uint32_t hit = 0;
@@ -326,11 +330,14 @@ static __device__ void cta_extend(const MatchCtx& c, Mhe& m, CtaExtRing& R) {
     const int64_t room = r0 < r1 ? r0 : r1;
     int64_t filled = 0, checked = 0;  // displacements filled, words checked
     for (int k = 0;; ++k) {
-      const int nw = k < 3 ? min(nwarps, 1 << k) : nwarps;
+      // 256 displacements first (most matches stop there), then 1, 2, 4 and 8 warps' worth
+      const int nw = k == 0 ? 1 : (k < 4 ? min(nwarps, 1 << (k - 1)) : nwarps);
+      const int nlanes = k == 0 ? 8 : 32;
       __syncthreads();  // every thread is past its reads of the words refilled now
-      if (wid < nw) ext_fill_ring<kCtaRing>(c, s0, s1, elen, filled + (int64_t)wid * kExtChunk, pmask, ring);
+      if (wid < nw)
+        ext_fill_ring<kCtaRing>(c, s0, s1, elen, filled + (int64_t)wid * kExtChunk, pmask, ring, nlanes);
       __syncthreads();
-      filled += (int64_t)nw * kExtChunk;
+      filled += (int64_t)nw * 32 * nlanes;
       const int64_t last = filled / 32 - 1;  // words below it have their successor filled
       uint32_t q = 0xffffffffu;
       const int64_t i = checked + threadIdx.x;
