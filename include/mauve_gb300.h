@@ -202,7 +202,8 @@ int mvg_gapdp_envelope_dev(mvg_handle h, const uint8_t* d_seq_a, const uint64_t*
 
 /* The band proposal for mvg_gapdp_banded: a 528 -> 256 -> 256 -> 256 -> 2
  * MLP (GELU, BF16 weights and activations, FP32 accumulation on the tensor
- * cores, FP32 master weights and Adam state), one per handle.  Its input per
+ * cores: tcgen05 for the forward hidden layers, mma.sync for the backward
+ * GEMMs; FP32 master weights and Adam state), one per handle.  Its input per
  * gap is the 4-mer spectra of both sequences (2 x 256) and their log lengths;
  * its outputs are the band's diagonal offset / 100 and log(1 + half-width).
  * No counterpart in the reference.
@@ -225,6 +226,18 @@ int mvg_mlp_grad_dev(mvg_handle h, const void* d_x_bf16, const float* d_target, 
  * is not finite changes nothing (its loss is still returned). */
 int mvg_mlp_train_step_dev(mvg_handle h, const void* d_x_bf16, const float* d_target, int64_t n, float lr,
                            int step, float* loss);
+/* Forward hidden layers on the tcgen05 tensor cores (on = 1, the default):
+ * TMA loads the operand tiles, the accumulators live in tensor memory, and
+ * bias, GELU and (last hidden layer) the 256 -> 2 output layer run in the
+ * epilogue.  on = 0 runs them as mma.sync GEMMs plus elementwise kernels.
+ * The tcgen05 path also needs every operand in TMA form (16-byte aligned,
+ * rows a multiple of 8; inputs the library allocates are padded, an input
+ * passed to mvg_mlp_forward_dev with n not a multiple of 8 is not), else
+ * the pass runs on mma.sync.  The two paths differ only in the order of
+ * fp32 sums.  mvg_mlp_tcgen05_passes counts the forward passes that ran on
+ * tcgen05.  No counterpart in the reference. */
+int mvg_set_mlp_tcgen05(mvg_handle h, int on);
+int mvg_mlp_tcgen05_passes(mvg_handle h, uint64_t* passes);
 /* Features + forward + mapping to integer bands: delta = round(100 * o0),
  * half = ceil(alpha * (exp(o1) - 1) + beta); host outputs. */
 int mvg_band_propose_dev(mvg_handle h, const uint8_t* d_seq_a, const uint64_t* d_off_a, const uint8_t* d_seq_b,

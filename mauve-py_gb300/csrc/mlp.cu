@@ -4,13 +4,17 @@
 // sequences (2 x 256, counts scaled to mean 1) and log(LA)/5, log(LB)/5.
 // Network: 528 -> 256 -> 256 -> 256 -> 2, GELU (erf form) on the hidden
 // layers, BF16 weights and activations feeding the tensor cores with FP32
-// accumulation (mma.sync m16n8k16), FP32 master weights and Adam state.
+// accumulation, FP32 master weights and Adam state.
 // Outputs: [0] the band's diagonal offset / kDeltaScale, [1] log(1 + half).
 //
-// GEMM: C[M x N] (fp32) = op(A)[M x K] * op(B)[K x N] with bf16 operands; a
-// 64x64 block tile, four warps of 32x32 (2 x 4 mma tiles), K step 32 staged in
-// shared memory with both operands stored k-contiguous so every fragment is
-// one 32-bit shared load.
+// Forward hidden layers: tcgen05 tensor-core GEMMs fed by TMA with bias,
+// GELU and (last layer) the 256 -> 2 output layer in the epilogue
+// (mlp_tc.cuh).  Backward GEMMs, and the forward when the tcgen05 path is
+// switched off or an operand does not meet its TMA rules: C[M x N] (fp32) =
+// op(A)[M x K] * op(B)[K x N] with bf16 operands; a 64x64 block tile, four
+// warps of 32x32 (2 x 4 mma.sync tiles), K step 32 staged in shared memory
+// with both operands stored k-contiguous so every fragment is one 32-bit
+// shared load.
 #include <cuda_bf16.h>
 #include <math.h>
 #include <string.h>
@@ -156,6 +160,12 @@ __device__ __forceinline__ float gelu(float x) { return 0.5f * x * (1.f + erff(x
 __device__ __forceinline__ float gelu_grad(float x) {
   return 0.5f * (1.f + erff(x * 0.70710678118654752f)) + x * 0.39894228040143268f * expf(-0.5f * x * x);
 }
+
+}  // namespace mvg
+
+#include "mlp_tc.cuh"
+
+namespace mvg {
 
 __global__ void k_bias_gelu(float* __restrict__ z, const float* __restrict__ b, __nv_bfloat16* __restrict__ h,
                             int64_t n, int d) {
@@ -338,6 +348,10 @@ __global__ void k_to_band(const float* __restrict__ o, int64_t n, float alpha, f
 
 // ------------------------------------------------------------- driver
 
+// Rows of an activation buffer: a multiple of 8, so the tensor maps' 8-row
+// groups never reach past the allocation.
+static int64_t rows8(int64_t n) { return (n + 7) & ~(int64_t)7; }
+
 static int mlp_alloc(Ctx* c, MlpState& s, int64_t n) {
   if (!s.w) {
     if (cudaMalloc(&s.w, kNumParams * 4) != cudaSuccess || cudaMalloc(&s.g, kNumParams * 4) != cudaSuccess ||
@@ -363,7 +377,7 @@ static int mlp_alloc(Ctx* c, MlpState& s, int64_t n) {
     bool ok = true;
     for (int q = 0; q < 3; ++q) {
       ok = ok && cudaMalloc(&s.z[q], n * kHid * 4) == cudaSuccess;
-      ok = ok && cudaMalloc(&s.h[q], n * kHid * 2) == cudaSuccess;
+      ok = ok && cudaMalloc(&s.h[q], rows8(n) * kHid * 2) == cudaSuccess;
     }
     ok = ok && cudaMalloc(&s.out, n * kOut * 4) == cudaSuccess;
     ok = ok && cudaMalloc(&s.dh, n * kHid * 4) == cudaSuccess;
@@ -403,9 +417,93 @@ static void mlp_free(MlpState& s) {
 
 static int eltwise_grid(int64_t n) { return grid_for((uint64_t)n, 256); }
 
-static void mlp_forward(Ctx* c, MlpState& s, const __nv_bfloat16* X, int64_t n) {
+using EncodeTiled = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                 const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiled encode_tiled() {
+  static EncodeTiled fn = nullptr;
+  static bool resolved = false;
+  if (!resolved) {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (EncodeTiled)f;
+    resolved = true;
+  }
+  return fn;
+}
+
+// The 4-D view of a K-contiguous bf16 matrix described in mlp_tc.cuh: rows
+// (a multiple of 8) x K (a multiple of 8), leading dimension ld elements.
+// False when the driver entry point is missing or an operand breaks a TMA
+// rule (16-byte aligned base, strides multiples of 16 bytes).
+static bool tc_map(CUtensorMap* m, const __nv_bfloat16* p, int64_t rows, int K, int ld, int box_rows) {
+  EncodeTiled enc = encode_tiled();
+  if (!enc || rows <= 0 || rows % 8 || K % 8 || ld % 8 || ((uintptr_t)p & 15)) return false;
+  const cuuint64_t dims[4] = {8, 8, (cuuint64_t)(K / 8), (cuuint64_t)(rows / 8)};
+  const cuuint64_t strides[3] = {(cuuint64_t)ld * 2, 16, (cuuint64_t)ld * 16};
+  const cuuint32_t box[4] = {8, 8, 8, (cuuint32_t)(box_rows / 8)};
+  const cuuint32_t estr[4] = {1, 1, 1, 1};
+  return enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, (void*)p, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+             CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// Per device: the tcgen05 layer kernel's shared-memory opt-in has been set.
+static bool tc_kernel_ready(int device) {
+  static bool ready[64] = {};
+  if (device < 0 || device >= 64) return false;
+  if (!ready[device]) {
+    if (cudaFuncSetAttribute(k_mlp_layer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem) !=
+        cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    ready[device] = true;
+  }
+  return true;
+}
+
+// Forward pass into s.out.  X holds n rows of kIn features in an allocation
+// of x_rows rows; train keeps the pre-activations and every activation for
+// the backward pass.  The tcgen05 path runs when it is switched on and all
+// six operands can be described to TMA (else the mma.sync GEMMs run).
+static void mlp_forward(Ctx* c, MlpState& s, const __nv_bfloat16* X, int64_t n, int64_t x_rows, bool train) {
   cudaStream_t st = c->stream;
   const int nn = (int)n;
+  if (c->mlp_tc && tc_kernel_ready(c->device)) {
+    const int64_t offW[3] = {kOffW1, kOffW2, kOffW3};
+    const int64_t offB[3] = {kOffB1, kOffB2, kOffB3};
+    CUtensorMap ma[3], mw[3];
+    bool ok = true;
+    for (int q = 0; q < 3 && ok; ++q) {
+      const int K = q == 0 ? kIn : kHid;
+      const int64_t a_rows = q == 0 ? x_rows : rows8(n);
+      ok = a_rows % 8 == 0 && tc_map(&ma[q], q == 0 ? X : s.h[q - 1], a_rows, K, K, kTcM) &&
+           tc_map(&mw[q], s.wb + offW[q], kTcN, K, K, kTcN);
+    }
+    if (ok) {
+      for (int q = 0; q < 3; ++q) {
+        TcEpilogue ep;
+        ep.bias = s.w + offB[q];
+        ep.z = train ? s.z[q] : nullptr;
+        ep.h = (train || q < 2) ? s.h[q] : nullptr;
+        if (q == 2) {
+          ep.w_out = s.wb + kOffW4;
+          ep.b_out = s.w + kOffB4;
+          ep.out = s.out;
+        }
+        k_mlp_layer_tc<<<(int)((n + kTcM - 1) / kTcM), kTcThreads, kTcSmem, st>>>(ma[q], mw[q], nn,
+                                                                                   q == 0 ? kIn : kHid, ep, c->d_err);
+      }
+      c->launches += 3;
+      ++c->mlp_tc_passes;
+      return;
+    }
+  }
   gemm<false, true>(st, X, kIn, s.wb + kOffW1, kIn, s.z[0], kHid, nn, kHid, kIn, &c->launches);
   k_bias_gelu<<<eltwise_grid(n * kHid), 256, 0, st>>>(s.z[0], s.w + kOffB1, s.h[0], n, kHid);
   gemm<false, true>(st, s.h[0], kHid, s.wb + kOffW2, kHid, s.z[1], kHid, nn, kHid, kHid, &c->launches);
@@ -522,11 +620,11 @@ int mvg_mlp_forward_dev(mvg_handle h, const void* d_x_bf16, int64_t n, float* d_
   MVG_CUDA_TRY(cudaSetDevice(c->device));
   int rc = mlp_alloc(c, s, n);
   if (rc) return rc;
-  mlp_forward(c, s, (const __nv_bfloat16*)d_x_bf16, n);
+  MVG_CUDA_TRY(cudaMemsetAsync(c->d_err, 0, 4, c->stream));
+  mlp_forward(c, s, (const __nv_bfloat16*)d_x_bf16, n, n, false);
   MVG_CUDA_TRY(cudaMemcpyAsync(d_out, s.out, n * kOut * 4, cudaMemcpyDeviceToDevice, c->stream));
   MVG_CUDA_TRY(cudaGetLastError());
-  MVG_CUDA_TRY(cudaStreamSynchronize(c->stream));
-  return 0;
+  return check_device_error(c);
 }
 
 int mvg_mlp_grad_dev(mvg_handle h, const void* d_x_bf16, const float* d_target, int64_t n, float* h_grads,
@@ -538,7 +636,8 @@ int mvg_mlp_grad_dev(mvg_handle h, const void* d_x_bf16, const float* d_target, 
   MVG_CUDA_TRY(cudaSetDevice(c->device));
   int rc = mlp_alloc(c, s, n);
   if (rc) return rc;
-  mlp_forward(c, s, (const __nv_bfloat16*)d_x_bf16, n);
+  MVG_CUDA_TRY(cudaMemsetAsync(c->d_err, 0, 4, c->stream));
+  mlp_forward(c, s, (const __nv_bfloat16*)d_x_bf16, n, n, true);
   mlp_backward(c, s, (const __nv_bfloat16*)d_x_bf16, d_target, n);
   if (h_grads) MVG_CUDA_TRY(cudaMemcpyAsync(h_grads, s.g, kNumParams * 4, cudaMemcpyDeviceToHost, c->stream));
   float loss = 0;
@@ -546,7 +645,7 @@ int mvg_mlp_grad_dev(mvg_handle h, const void* d_x_bf16, const float* d_target, 
   MVG_CUDA_TRY(cudaGetLastError());
   MVG_CUDA_TRY(cudaStreamSynchronize(c->stream));
   if (h_loss) *h_loss = loss;
-  return 0;
+  return check_device_error(c);
 }
 
 int mvg_mlp_train_step_dev(mvg_handle h, const void* d_x_bf16, const float* d_target, int64_t n, float lr, int step,
@@ -558,7 +657,8 @@ int mvg_mlp_train_step_dev(mvg_handle h, const void* d_x_bf16, const float* d_ta
   MVG_CUDA_TRY(cudaSetDevice(c->device));
   int rc = mlp_alloc(c, s, n);
   if (rc) return rc;
-  mlp_forward(c, s, (const __nv_bfloat16*)d_x_bf16, n);
+  MVG_CUDA_TRY(cudaMemsetAsync(c->d_err, 0, 4, c->stream));
+  mlp_forward(c, s, (const __nv_bfloat16*)d_x_bf16, n, n, true);
   mlp_backward(c, s, (const __nv_bfloat16*)d_x_bf16, d_target, n);
   const float b1 = 0.9f, b2 = 0.999f;
   const float c1 = 1.f - powf(b1, (float)step), c2 = 1.f - powf(b2, (float)step);
@@ -574,7 +674,7 @@ int mvg_mlp_train_step_dev(mvg_handle h, const void* d_x_bf16, const float* d_ta
     *h_loss = loss;
   }
   MVG_CUDA_TRY(cudaGetLastError());
-  return 0;
+  return check_device_error(c);
 }
 
 int mvg_set_band_gate(mvg_handle h, int min_match) {
@@ -594,14 +694,15 @@ int mvg_band_propose_dev(mvg_handle h, const uint8_t* d_sa, const uint64_t* d_oa
   MVG_CUDA_TRY(cudaSetDevice(c->device));
   int rc = mlp_alloc(c, s, nprob);
   if (rc) return rc;
-  __nv_bfloat16* X = (__nv_bfloat16*)c->ws.get(c, 27, (size_t)nprob * kIn * 2);
+  __nv_bfloat16* X = (__nv_bfloat16*)c->ws.get(c, 27, (size_t)rows8(nprob) * kIn * 2);
   int32_t* dd = (int32_t*)c->ws.get(c, 28, (size_t)nprob * 8);
   if (!X || !dd) return report_error(MVG_ERR_NOMEM, "workspace allocation failed");
+  MVG_CUDA_TRY(cudaMemsetAsync(c->d_err, 0, 4, c->stream));
   stage_mark(c, "band_features");
   k_band_features<<<grid_for((uint64_t)nprob * 32, 256), 256, 0, c->stream>>>(d_sa, d_oa, d_sb, d_ob, nprob, X);
   c->launches++;
   stage_mark(c, "mlp_forward");
-  mlp_forward(c, s, X, nprob);
+  mlp_forward(c, s, X, nprob, rows8(nprob), false);
   float* gate = nullptr;
   if (c->band_gate > 0) {
     gate = (float*)c->ws.get(c, 59, (size_t)nprob * 4 + 16);
@@ -614,7 +715,20 @@ int mvg_band_propose_dev(mvg_handle h, const uint8_t* d_sa, const uint64_t* d_oa
   c->launches++;
   MVG_CUDA_TRY(cudaGetLastError());
   if ((rc = pinned_d2h(c, h_delta, dd, (size_t)nprob * 4))) return rc;
-  return pinned_d2h(c, h_half, dd + nprob, (size_t)nprob * 4);
+  if ((rc = pinned_d2h(c, h_half, dd + nprob, (size_t)nprob * 4))) return rc;
+  return check_device_error(c);
+}
+
+int mvg_set_mlp_tcgen05(mvg_handle h, int on) {
+  if (!h || (on != 0 && on != 1)) return report_error(MVG_ERR_ARG, "on must be 0 or 1");
+  reinterpret_cast<Ctx*>(h)->mlp_tc = on;
+  return 0;
+}
+
+int mvg_mlp_tcgen05_passes(mvg_handle h, uint64_t* passes) {
+  if (!h || !passes) return report_error(MVG_ERR_ARG, "null argument");
+  *passes = reinterpret_cast<Ctx*>(h)->mlp_tc_passes;
+  return 0;
 }
 
 }  // extern "C"

@@ -57,6 +57,8 @@ struct Ctx {
   int dp_coop_strips = 16;               // full-DP problems of at least this many strips use a whole CTA
   cudaGraphExec_t dp_exec[2] = {};       // the executable graph of each DP lane, updated per call
   uint64_t graph_launches = 0;
+  int mlp_tc = 1;              // MLP forward hidden layers on tcgen05 (else mma.sync)
+  uint64_t mlp_tc_passes = 0;  // forward passes that ran on tcgen05
   Workspace ws;
   MatchStats stats;
   bool profiling = false;

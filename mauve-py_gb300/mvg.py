@@ -48,7 +48,7 @@ EXPORTS = ["mvg_create", "mvg_destroy", "mvg_last_error", "mvg_stream", "mvg_ker
            "mvg_set_band_gate", "mvg_sslist_write", "mvg_sslist_read", "mvg_set_pair_bucket_cap",
            "mvg_set_dp_spin_limit", "mvg_gap_anchor_search", "mvg_gap_anchor_search_dev", "mvg_set_dp_graph",
            "mvg_set_dp_coop_strips", "mvg_path_rows", "mvg_path_rows_dev",
-           "mvg_xmfa_write", "mvg_xmfa_write_dev"]
+           "mvg_xmfa_write", "mvg_xmfa_write_dev", "mvg_set_mlp_tcgen05", "mvg_mlp_tcgen05_passes"]
 
 TUNING_PATH = os.path.join(HERE, "dp_tuning.json")
 
@@ -92,6 +92,8 @@ def load_library(path=LIB_PATH):
         "mvg_set_pair_bucket_cap": (ci, [vp, ci]),
         "mvg_set_dp_spin_limit": (ci, [vp, ctypes.c_longlong]),
         "mvg_set_dp_graph": (ci, [vp, ci]),
+        "mvg_set_mlp_tcgen05": (ci, [vp, ci]),
+        "mvg_mlp_tcgen05_passes": (ci, [vp, ctypes.POINTER(ctypes.c_uint64)]),
         "mvg_set_dp_coop_strips": (ci, [vp, ci]),
         "mvg_path_rows": (ci, [vp, vp, vp, vp, vp, i64, vp, vp, vp, vp, vp]),
         "mvg_xmfa_write": (ci, [vp, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, i64, vp, vp, vp, vp, vp, vp,
@@ -237,6 +239,16 @@ class Context:
     def set_dp_coop_strips(self, strips):
         """Full-DP problems of at least this many strips go to a whole CTA; see mvg_set_dp_coop_strips."""
         _check(load_library().mvg_set_dp_coop_strips(self._h, int(strips)))
+
+    def set_mlp_tcgen05(self, on=True):
+        """MLP forward hidden layers on tcgen05 (default) or on mma.sync GEMMs; see mvg_set_mlp_tcgen05."""
+        _check(load_library().mvg_set_mlp_tcgen05(self._h, 1 if on else 0))
+
+    def mlp_tcgen05_passes(self):
+        """Forward passes of this handle's MLP that ran on tcgen05."""
+        n = ctypes.c_uint64(0)
+        _check(load_library().mvg_mlp_tcgen05_passes(self._h, ctypes.byref(n)))
+        return n.value
 
     def set_dp_graph(self, on=True):
         """Gap-DP waves as one recorded CUDA graph (default) or launched one by one."""
