@@ -181,7 +181,7 @@ __global__ void k_gs_seg_fill(const uint64_t* __restrict__ bkey, int64_t n, cons
 // bucket's sorted entries; the first one not contained is extended
 // (ExtendMatch, LM/MatchFinder.h:218-374, inside the gap's sequences) and
 // inserted at its lower_bound, and testing resumes after it.
-__global__ void __launch_bounds__(256) k_gs_replay(const uint32_t* __restrict__ pa, const uint32_t* __restrict__ pb,
+__global__ void __launch_bounds__(256, 3) k_gs_replay(const uint32_t* __restrict__ pa, const uint32_t* __restrict__ pb,
                                                    const GapDev* __restrict__ gaps, const Mhe* __restrict__ mhe,
                                                    const uint32_t* __restrict__ sorted,
                                                    const uint32_t* __restrict__ seg_start,

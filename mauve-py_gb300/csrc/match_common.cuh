@@ -169,6 +169,20 @@ __device__ __forceinline__ void window128(const uint32_t* __restrict__ g, uint64
   }
 }
 
+// Reverse complement of 32 bases in 64 bits (complement = the 2-bit code
+// inverted; base order reversed).
+__device__ __forceinline__ uint64_t revcomp64(uint64_t x) {
+  const uint64_t r = __brevll(~x);  // groups reversed, bits inside groups swapped
+  return ((r >> 1) & 0x5555555555555555ull) | ((r & 0x5555555555555555ull) << 1);
+}
+
+// The top 64 bits of the 128-bit value hi:lo shifted left by s (0 <= s < 128).
+__device__ __forceinline__ uint64_t top64(uint64_t hi, uint64_t lo, int s) {
+  if (s == 0) return hi;
+  if (s < 64) return (hi << s) | (lo >> (64 - s));
+  return lo << (s - 64);
+}
+
 // One warp's fill: match bits of displacements u0 .. u0 + 32 * nlanes - 1
 // into ring words (u0 / 32 + lane) mod RING, lanes below nlanes (no
 // synchronisation).
@@ -200,6 +214,42 @@ __device__ __forceinline__ void ext_fill_ring(const MatchCtx& c, int64_t st0, in
         const int j = down ? 31 - t : t;  // window start amin + j
         const uint64_t w = j == 0 ? dh : ((dh << (2 * j)) | (dl >> (64 - 2 * j)));
         word |= (uint32_t)((w & pmask) == 0) << t;
+      }
+      if (U == 0) word &= ~1u;  // displacement 0 is not a step
+      done = true;
+    }
+  } else if (c.s.sym) {
+    // Opposite strands with a symmetric pattern.  Per window the reference's
+    // test is "canonical mers equal and strands opposite", which for a mer
+    // set {f, rc(f)} means: B's forward mer is the reverse complement of A's,
+    // and A's mer is not its own reverse complement (then both canonical
+    // forms are the forward one).  With a symmetric pattern rc(mer(x)) =
+    // mer(rc(x)), so both are masked window comparisons: A's window against
+    // the reverse complement of B's (which moves the same way as A's, at a
+    // fixed offset), and, where that holds, A's window against its own
+    // reverse complement.
+    const int64_t U = u0 + lane * 32;
+    const int64_t a0 = ext_start(st0, len, U, L, c.n[0]), a31 = ext_start(st0, len, U + 31, L, c.n[0]);
+    const int64_t b0 = ext_start(st1, len, U, L, c.n[1]), b31 = ext_start(st1, len, U + 31, L, c.n[1]);
+    const bool adown = st0 > 0;  // A's window starts decrease with u, B's increase (and vice versa)
+    const int64_t amin = adown ? a31 : a0, bmin = adown ? b0 : b31;
+    if (a0 >= 0 && a31 >= 0 && b0 >= 0 && b31 >= 0 && amin + 80 <= c.n[0] && bmin + 80 <= c.n[1]) {
+      uint64_t ah, al, bh, bl;
+      window128(c.g[0], (uint64_t)amin, ah, al);
+      window128(c.g[1], (uint64_t)bmin, bh, bl);
+      // reverse complements of the two 64-base stretches: base k is the
+      // complement of base 63 - k
+      const uint64_t rah = revcomp64(al), ral = revcomp64(ah);
+      const uint64_t rbh = revcomp64(bl), rbl = revcomp64(bh);
+#pragma unroll 4
+      for (int t = 0; t < 32; ++t) {
+        const int ja = adown ? 31 - t : t;  // A's window start amin + ja
+        const int jb = adown ? t : 31 - t;  // B's window start bmin + jb
+        // rc of the window at stretch offset j is the reverse stretch's window at 64 - L - j
+        const uint64_t aw = top64(ah, al, 2 * ja);
+        bool b = ((aw ^ top64(rbh, rbl, 2 * (64 - L - jb))) & pmask) == 0;
+        if (b) b = ((aw ^ top64(rah, ral, 2 * (64 - L - ja))) & pmask) != 0;
+        word |= (uint32_t)b << t;
       }
       if (U == 0) word &= ~1u;  // displacement 0 is not a step
       done = true;

@@ -35,6 +35,10 @@ struct SeedDesc {
   uint64_t seed_mask;  // top 2w bits
   int L, w;
   int nruns;
+  // the pattern reads the same reversed (every rank-0 seed of weight >= 5
+  // and the coding seed): the reverse complement of a mer is then the mer
+  // of the reverse-complement window
+  int sym;
   // run r covers bases [run_start[r], run_start[r] + run_len[r]) of the window
   // and lands at output bit offset run_out[r] (from the MSB of the 2w-bit mer).
   int8_t run_start[32], run_len[32], run_out[32];

@@ -50,6 +50,9 @@ SeedDesc make_seed_desc(uint64_t pattern) {
   s.L = pattern ? 64 - __builtin_clzll(pattern) - __builtin_ctzll(pattern) : 0;
   s.w = __builtin_popcountll(pattern);
   s.seed_mask = s.w ? (~0ull << (64 - 2 * s.w)) : 0;
+  uint64_t rev = 0;
+  for (int k = 0; k < s.L; ++k) rev = (rev << 1) | ((pattern >> k) & 1ull);
+  s.sym = s.L > 0 && rev == pattern;
   int out = 0;
   for (int k = 0; k < s.L;) {
     if (pattern & (1ull << (s.L - 1 - k))) {
