@@ -89,28 +89,33 @@ struct DpLane {
 };
 
 // One wavefront step of one lane: rows r = 0..R-1 of column j.  Returns the
-// R traceback nibbles.  (up*) = cells (i0-1, j), (dg*) = cells (i0-1, j-1).
-template <int R>
-__device__ __forceinline__ uint32_t dp_column(DpLane<R>& L, int32_t upM, int32_t upD, int32_t dgM, int32_t dgD,
-                                              int32_t dgI, uint32_t bsel, int32_t goB, int32_t goA0) {
-  int32_t cuM = upM, cuD = upD;            // (i-1, j)
-  int32_t cdM = dgM, cdD = dgD, cdI = dgI;  // (i-1, j-1)
+// R traceback nibbles.  M is carried with the gap open already added
+// (Mg = M + kGap: the value both the D and the I recurrence read), so
+// neither needs an add; the M recurrence adds twice the close to max(D, I)
+// instead of once, which leaves every comparison, and so every tie-broken
+// traceback bit, as it was.  (up*) = cells (i0-1, j), (dg*) = cells
+// (i0-1, j-1); ADJ steps add goBadj to the left Mg (-kGap in column 1,
+// where the reference opens for free).
+template <int R, bool ADJ>
+__device__ __forceinline__ uint32_t dp_column(DpLane<R>& L, int32_t upMg, int32_t upD, int32_t dgMg, int32_t dgD,
+                                              int32_t dgI, uint32_t bsel, int32_t goBadj) {
+  int32_t cuM = upMg, cuD = upD;            // (i-1, j)
+  int32_t cdM = dgMg, cdD = dgD, cdI = dgI;  // (i-1, j-1)
   uint32_t nibs = 0;
 #pragma unroll
   for (int r = 0; r < R; ++r) {
-    const int32_t goA = r == 0 ? goA0 : kGap;  // only row 1 of the matrix opens for free
     // D(i,j) = max(M(i-1,j) + open, D(i-1,j)), ties to the M branch
     bool dm;
-    const int32_t D = __vibmax_s32(cuM + goA, cuD, &dm);
+    const int32_t D = __vibmax_s32(cuM, cuD, &dm);
     // I(i,j) = max(M(i,j-1) + open, I(i,j-1)), ties to the M branch
     bool mi;
-    const int32_t I = __vibmax_s32(L.lM[r] + goB, L.lI[r], &mi);
+    const int32_t I = __vibmax_s32(ADJ ? L.lM[r] + goBadj : L.lM[r], L.lI[r], &mi);
     // M(i,j) = s + max(M, D + close, I + close) at (i-1,j-1), tie M > D > I;
     // both closes are -200, so max(D, I) is taken before adding the close.
     bool dge, mge;
-    const int32_t DI = __vibmax_s32(cdD, cdI, &dge) + kGap;
+    const int32_t DI = __vibmax_s32(cdD, cdI, &dge) + 2 * kGap;
     const int32_t best = __vibmax_s32(cdM, DI, &mge);
-    const int32_t M = best + (int32_t)__byte_perm(L.arow[r], 0u, bsel) - kScoreBias;
+    const int32_t M = best + (int32_t)__byte_perm(L.arow[r], 0u, bsel) - kScoreBias;  // Mg
     const uint32_t tm = mge ? TB_MM : (dge ? TB_DM : TB_IM);
     nibs |= (tm | (dm ? TB_MD : 0u) | (mi ? TB_MI : 0u)) << (4 * r);
     cdM = L.lM[r];
@@ -161,7 +166,8 @@ __device__ void dp_solve(const DpJob& J, DpShared& sh, int w, int kstart, int ks
   const int wib = threadIdx.x >> 5;
   uint8_t* ringB = sh.ringB[wib];
   int4* ringR = sh.ringR[wib];
-  const int4 kNegCell = make_int4(kNeg, kNeg, kNeg, 0);
+  // a cell outside the matrix, M carried as Mg (see dp_column)
+  const int4 kNegCell = make_int4(kNeg + kGap, kNeg, kNeg, 0);
   const uint32_t p = J.order[w];
   const uint64_t a0 = J.oa[p], b0 = J.ob[p];
   const int LA = (int)(J.oa[p + 1] - a0), LB = (int)(J.ob[p + 1] - b0);
@@ -234,7 +240,6 @@ __device__ void dp_solve(const DpJob& J, DpShared& sh, int w, int kstart, int ks
       const int i = row0 + lane * R + r + 1;
       L.arow[r] = c_score_rows[(i <= LA ? A[i - 1] : 0u) & 3u];
     }
-    const int32_t goA0 = (row0 + lane * R + 1 == 1) ? 0 : kGap;
     // banded mode: prefix of the row maxima up to each owned row, the
     // strip's bottom row, and the column prefix at jlo-1 for lane 31
     int32_t rowpre[R];
@@ -267,10 +272,13 @@ __device__ void dp_solve(const DpJob& J, DpShared& sh, int w, int kstart, int ks
     }
     // Row above this strip at absolute column x: row 0 for the first strip,
     // else the previous strip's computed columns, its left boundary or -inf.
+    // M is Mg throughout, except row 0's M at x > 0, which is read only
+    // by matrix row 1, where the reference opens for free (M + 0), and as
+    // a diagonal that can never win (-inf against at most -400).
     auto above = [&](int x) -> int4 {
-      if (k == 0) return x == 0 ? make_int4(0, kNeg, kNeg, 0) : make_int4(kNeg, kNeg, 0, 0);
+      if (k == 0) return x == 0 ? make_int4(kGap, kNeg, kNeg, 0) : make_int4(kNeg, kNeg, 0, 0);
       if (x >= prev_lo && x <= prev_hi) return rb_in[x];
-      if (x == prev_lo - 1) return prev_lo == 1 ? make_int4(kNeg, 0, kNeg, 0) : kNegCell;
+      if (x == prev_lo - 1) return prev_lo == 1 ? make_int4(kNeg + kGap, 0, kNeg, 0) : kNegCell;
       return kNegCell;
     };
     if (!wait_for(jlo + 63)) return;
@@ -286,11 +294,11 @@ __device__ void dp_solve(const DpJob& J, DpShared& sh, int w, int kstart, int ks
     const int32_t leftD = jlo == 1 ? 0 : kNeg;
 #pragma unroll
     for (int r = 0; r < R; ++r) {
-      L.lM[r] = kNeg;
+      L.lM[r] = kNeg + kGap;
       L.lD[r] = leftD;
       L.lI[r] = kNeg;
     }
-    int32_t pubM = kNeg, pubD = leftD, pubI = kNeg;  // bottom row, last computed column
+    int32_t pubM = kNeg + kGap, pubD = leftD, pubI = kNeg;  // bottom row, last computed column (M as Mg)
     int32_t upM = kNeg, upD = kNeg, upI = kNeg;      // row above, current column
     uint32_t acc = 0;
     const bool bottom_exit = track && lane == 31 && row0 + SR < LA;
@@ -328,15 +336,16 @@ __device__ void dp_solve(const DpJob& J, DpShared& sh, int w, int kstart, int ks
       upD = lane == 0 ? v.y : rD;
       upI = lane == 0 ? v.z : rI;
       const uint32_t bsel = (uint32_t)ringB[jj & 127] | 0x4440u;
-      const int32_t goB = j == 1 ? 0 : kGap;
       uint32_t nibs = 0;
       if (!checked || (jj >= 0 && jj < W)) {
-        nibs = dp_column<R>(L, upM, upD, dgM, dgD, dgI, bsel, goB, goA0);
+        // column 1 (only in checked steps) opens for free
+        nibs = checked ? dp_column<R, true>(L, upM, upD, dgM, dgD, dgI, bsel, j == 1 ? -kGap : 0)
+                       : dp_column<R, false>(L, upM, upD, dgM, dgD, dgI, bsel, 0);
         if (checked && s == 0 && lane == 0 && k == 0 && LA == 1) {
           // NWSmall's last-row special case (MU/nwsmall.cpp:616-624) with
           // LA == 1: M(1,1) adds the open and close of position 0, and the
-          // close of a one-position profile is not zeroed.
-          L.lM[0] = (int32_t)__byte_perm(L.arow[0], 0u, bsel) - kScoreBias + kGap;
+          // close of a one-position profile is not zeroed (stored as Mg).
+          L.lM[0] = (int32_t)__byte_perm(L.arow[0], 0u, bsel) - kScoreBias + 2 * kGap;
           nibs = (nibs & ~3u) | TB_DM;
         }
         pubM = L.lM[R - 1];
@@ -347,12 +356,12 @@ __device__ void dp_solve(const DpJob& J, DpShared& sh, int w, int kstart, int ks
           run31 += best_of(J.base_max, bsel);  // prefix over B[0..j)
           if (j == next_lo - 1) pb_next = run31;
           if (bottom_exit && j < next_lo) {
-            const int32_t best = max(pubM, max(pubD, pubI));
+            const int32_t best = max(pubM - kGap, max(pubD, pubI));
             bound = max(bound, best + min(totA - strip_pre, totB - run31));
           }
         }
       } else if (jj == -1) {
-        pubM = kNeg;
+        pubM = kNeg + kGap;
         pubD = leftD;
         pubI = kNeg;
       }
@@ -369,8 +378,9 @@ __device__ void dp_solve(const DpJob& J, DpShared& sh, int w, int kstart, int ks
     };
 
     if (W >= 32) {
+      // unchecked steps: every lane inside the strip and past column 1
       int s = 0;
-      for (; s < 31 && alive; ++s) step(s, true);
+      for (; s < 32 && alive; ++s) step(s, true);
       for (; s < W && alive; ++s) step(s, false);
       for (; s < S && alive; ++s) step(s, true);
     } else {
@@ -385,7 +395,7 @@ __device__ void dp_solve(const DpJob& J, DpShared& sh, int w, int kstart, int ks
 #pragma unroll
       for (int r = 0; r < R; ++r)
         if (r == end_r) {
-          eM = L.lM[r];
+          eM = L.lM[r] - kGap;
           eD = L.lD[r];
           eI = L.lI[r];
         }
@@ -425,7 +435,7 @@ __device__ void dp_solve(const DpJob& J, DpShared& sh, int w, int kstart, int ks
       for (int r = 0; r < R; ++r) {
         const int i = row0 + lane * R + r + 1;
         if (i <= LA) {
-          const int32_t best = max(L.lM[r], max(L.lD[r], L.lI[r]));
+          const int32_t best = max(L.lM[r] - kGap, max(L.lD[r], L.lI[r]));
           bound = max(bound, best + min(totA - rowpre[r], totB - pb_hi));
         }
       }

@@ -369,6 +369,7 @@ int gap_anchor_search_dev(Ctx* c, const uint8_t* d_a, uint64_t na, const uint8_t
                           const int64_t* gaps, uint64_t ngaps, int64_t* out, uint64_t cap, uint64_t* gap_off,
                           uint64_t* count) {
   *count = 0;
+  stage_begin_call(c);
   if (ngaps >= (1ull << 31)) return report_error(MVG_ERR_ARG, "too many gaps");
   int rc = gs_upload_tables(c->device);
   if (rc) return rc;
@@ -426,6 +427,7 @@ int gap_anchor_search_dev(Ctx* c, const uint8_t* d_a, uint64_t na, const uint8_t
       return report_error(MVG_ERR_NOMEM, "workspace allocation failed");
     uint32_t* d_npairs = tsum + ptiles + 2;
     MVG_CUDA_TRY(cudaMemsetAsync(c->d_err, 0, 4, c->stream));
+    stage_mark(c, "gs_pack");
     MVG_CUDA_TRY(cudaMemcpyAsync(d_gaps, gd.data(), gd.size() * sizeof(GapDev), cudaMemcpyHostToDevice, c->stream));
     k_gs_pack<<<grid_for(words[0] + words[1], 256), 256, 0, c->stream>>>(d_a, d_b, d_gaps, ng, words[0], words[1],
                                                                           pa, pb, c->d_err);
@@ -435,12 +437,15 @@ int gap_anchor_search_dev(Ctx* c, const uint8_t* d_a, uint64_t na, const uint8_t
       if ((rc = check_device_error(c))) return rc;
       goto host_filter;
     }
+    stage_mark(c, "gs_keys");
     k_gs_keys<<<grid_for(nkeys, 256), 256, 0, c->stream>>>(pa, pb, d_gaps, ng, keys[0], keys[1], k0, v0);
     c->launches++;
+    stage_mark(c, "gs_seed_sort");
     int which = sort_pairs<uint64_t>(k0, v0, k1, v1, (int64_t)nkeys, 32 + gbits, sscr, c->stream, &c->launches,
                                      c->d_err);
     const uint64_t* sk = which ? k1 : k0;
     const uint32_t* sv = which ? v1 : v0;
+    stage_mark(c, "gs_pairs");
     k_pair_count<uint64_t><<<(unsigned)ptiles, 256, 0, c->stream>>>(sk, (int64_t)nkeys, tsum);
     k_scan_bsums<<<1, 256, 0, c->stream>>>(tsum, ptiles, d_npairs);
     c->launches += 2;
@@ -469,6 +474,7 @@ int gap_anchor_search_dev(Ctx* c, const uint8_t* d_a, uint64_t na, const uint8_t
       uint32_t* totals = scr + scan_scratch_words(npairs) * 2;  // [0] segments, [1] entries, [2] counter
       k_gs_pair_emit<<<(unsigned)ptiles, 256, 0, c->stream>>>(sk, sv, (int64_t)nkeys, tsum, d_gaps, mhe, bk0, o0);
       c->launches++;
+      stage_mark(c, "gs_bucket_sort");
       which = sort_pairs<uint64_t>(bk0, o0, bk1, o1, npairs, 16 + gbits, sscr, c->stream, &c->launches, c->d_err);
       const uint64_t* sbk = which ? bk1 : bk0;
       const uint32_t* sorted = which ? o1 : o0;
@@ -483,8 +489,10 @@ int gap_anchor_search_dev(Ctx* c, const uint8_t* d_a, uint64_t na, const uint8_t
       int sms = 0;
       MVG_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device));
       const uint32_t rblocks = std::min<uint32_t>((nseg + 7) / 8, (uint32_t)sms * 8);
+      stage_mark(c, "gs_replay");
       k_gs_replay<<<rblocks, 256, 0, c->stream>>>(pa, pb, d_gaps, mhe, sorted, seg_start, d_seg_gap, nseg,
                                                   (uint32_t)npairs, ent, nent, totals + 2);
+      stage_mark(c, "gs_emit");
       exclusive_scan(nent, ooff, nseg, scr, totals + 1, c->stream, &c->launches);
       MVG_CUDA_TRY(cudaMemcpyAsync(c->h_scalars, totals + 1, 4, cudaMemcpyDeviceToHost, c->stream));
       MVG_CUDA_TRY(cudaStreamSynchronize(c->stream));
@@ -499,11 +507,13 @@ int gap_anchor_search_dev(Ctx* c, const uint8_t* d_a, uint64_t na, const uint8_t
       if (nrows) MVG_CUDA_TRY(cudaMemcpyAsync(rows.data(), d_rows, nrows * 24, cudaMemcpyDeviceToHost, c->stream));
       MVG_CUDA_TRY(cudaMemcpyAsync(seg_gap.data(), d_seg_gap, (size_t)nseg * 4, cudaMemcpyDeviceToHost, c->stream));
       MVG_CUDA_TRY(cudaMemcpyAsync(seg_n.data(), nent, (size_t)nseg * 4, cudaMemcpyDeviceToHost, c->stream));
+      stage_end(c);
       MVG_CUDA_TRY(cudaStreamSynchronize(c->stream));
       if ((rc = check_device_error(c))) return rc;
     }
   }
 host_filter:
+  HostSpan span(c, "gs_filter");
   // host: per gap, overlap elimination and length filter, then genome
   // coordinates; gaps are independent, so host threads take contiguous
   // ranges of them and the survivors are packed in gap order afterwards
