@@ -417,6 +417,15 @@ int mvg_set_dp_spin_limit(mvg_handle h, long long polls);
  * choice in mauve-py_gb300/dp_tuning.json).  Results do not depend on it. */
 int mvg_set_dp_coop_strips(mvg_handle h, int strips);
 
+/* Full gap-DP passes checkpointed (on = 1, the default): the forward pass
+ * keeps every strip's bottom row and, every 128 columns, every strip's
+ * column of cell states instead of traceback bits (about 0.19 instead of
+ * 0.5 bytes per cell), and the traceback recomputes the bits of only the
+ * blocks of the matrix its path crosses, with the same recurrence and tie
+ * order.  on = 0 stores the bits.  Scores and paths are identical either
+ * way; banded passes always store bits.  No counterpart in the reference. */
+int mvg_set_dp_checkpoint(mvg_handle h, int on);
+
 /* Gap-DP passes as one CUDA graph (on = 1, the default): the launches of a
  * call's waves (claim counters, the persistent DP kernel, both traceback
  * walkers, path compaction) are recorded into one graph and launched at

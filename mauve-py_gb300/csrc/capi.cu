@@ -524,6 +524,12 @@ int mvg_set_dp_coop_strips(mvg_handle h, int strips) {
   return 0;
 }
 
+int mvg_set_dp_checkpoint(mvg_handle h, int on) {
+  if (!h || (on != 0 && on != 1)) return report_error(MVG_ERR_ARG, "on must be 0 or 1");
+  h->dp_ckpt = on;
+  return 0;
+}
+
 int mvg_set_dp_graph(mvg_handle h, int on) {
   if (!h || (on != 0 && on != 1)) return report_error(MVG_ERR_ARG, "on must be 0 or 1");
   h->dp_graph = on;

@@ -16,6 +16,9 @@
 // Kernels: k_gapdp_t (gapdp_kernel.cuh) fills the traceback arena;
 // k_traceback walks each problem's bits from (LA, LB) like BitTraceBack
 // (MU/bittraceback.cpp:138-210); k_path_compact moves paths to slot heads.
+// Full-DP passes run checkpointed by default: the forward kernel keeps
+// strip rows and block columns instead of traceback bits, and k_tb_ck
+// (traceback_ck.cuh) recomputes the bits of the blocks each path crosses.
 #include <limits.h>
 
 #include <algorithm>
@@ -28,6 +31,7 @@
 
 #include "gapdp_kernel.cuh"
 #include "traceback_win.cuh"
+#include "traceback_ck.cuh"
 #include "gapdp_ring.cuh"
 #include "mvg_internal.h"
 
@@ -72,6 +76,14 @@ template __global__ void k_gapdp_t<false, 8>(DpJob);
 template __global__ void k_gapdp_t<true, 8>(DpJob);
 template __global__ void k_gapdp_t<true, 2>(DpJob);
 template __global__ void k_gapdp_t<true, 1>(DpJob);
+template __global__ void k_gapdp_t<false, 4, true>(DpJob);
+template __global__ void k_gapdp_t<false, 8, true>(DpJob);
+template __global__ void k_tb_ck<4>(const uint8_t*, const uint64_t*, const uint8_t*, const uint64_t*, const uint32_t*,
+                                    const uint64_t*, int, const uint32_t*, const uint8_t*, const uint64_t*, char*,
+                                    int64_t*, uint32_t*, int32_t*, unsigned*);
+template __global__ void k_tb_ck<8>(const uint8_t*, const uint64_t*, const uint8_t*, const uint64_t*, const uint32_t*,
+                                    const uint64_t*, int, const uint32_t*, const uint8_t*, const uint64_t*, char*,
+                                    int64_t*, uint32_t*, int32_t*, unsigned*);
 template __global__ void k_gapdp_ring<4>(RingJob);
 template __global__ void k_gapdp_ring<6>(RingJob);
 template __global__ void k_gapdp_ring<8>(RingJob);
@@ -454,15 +466,18 @@ static int run_dp(Ctx* c, const DpInputs& in, const std::vector<uint32_t>& ids, 
   // banded passes may use shorter strips: the staircase of a narrow band
   // widens by the diagonal's drift over one strip
   const int rows = banded ? c->band_rows : c->dp_rows;
+  // full passes keep checkpoints instead of traceback bits (traceback_ck.cuh)
+  const bool ckpt = !banded && c->dp_ckpt && (rows == 4 || rows == 8);
   std::vector<uint64_t> bytes(nwork), cells(nwork);
   int64_t maxlb = 0;
   for (int64_t w = 0; w < nwork; ++w) {
     const uint32_t p = ids[w];
     const Band b = banded ? make_band((int)la[p], (int)lb[p], (*h_delta)[p], (*h_half)[p], 32 * rows)
                           : make_full((int)la[p], (int)lb[p], 32 * rows);
-    const uint64_t words = band_tb_words(b, rows);
+    const uint64_t slot = ckpt ? (uint64_t)ck_entries((int)la[p], (int)lb[p], rows) * sizeof(int4)
+                               : band_tb_words(b, rows) * 4;
     cells[w] = banded ? band_cells(b) : (uint64_t)la[p] * (uint64_t)lb[p];
-    bytes[w] = (words * 4 + 255) & ~255ull;
+    bytes[w] = (slot + 255) & ~255ull;
     maxlb = std::max(maxlb, lb[p]);
   }
   // Whole-CTA (pipelined) mode for problems with many strips.  A banded
@@ -502,7 +517,8 @@ static int run_dp(Ctx* c, const DpInputs& in, const std::vector<uint32_t>& ids, 
   if (max_tb > arena) return report_error(MVG_ERR_CAPACITY, "one gap-DP problem exceeds the traceback arena");
   // Waves: deal the size-sorted problems round-robin, so every wave holds the
   // same mix of sizes and stays largest-first inside.
-  int64_t nwaves = (int64_t)((total_tb + arena - 1) / arena);
+  // at least one wave: checkpointed slots of problems within one block hold nothing
+  int64_t nwaves = std::max<int64_t>(1, (int64_t)((total_tb + arena - 1) / arena));
   std::vector<uint32_t> order;
   std::vector<uint64_t> tboff;
   std::vector<int64_t> wave_begin, wave_nbig;
@@ -539,7 +555,8 @@ static int run_dp(Ctx* c, const DpInputs& in, const std::vector<uint32_t>& ids, 
 
   int dev_sms = 0;
   MVG_CUDA_TRY(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, c->device));
-  void (*kern)(DpJob) = rows == 8   ? (banded ? k_gapdp_t<true, 8> : k_gapdp_t<false, 8>)
+  void (*kern)(DpJob) = ckpt        ? (rows == 8 ? k_gapdp_t<false, 8, true> : k_gapdp_t<false, 4, true>)
+                        : rows == 8 ? (banded ? k_gapdp_t<true, 8> : k_gapdp_t<false, 8>)
                         : rows == 4 ? (banded ? k_gapdp_t<true, 4> : k_gapdp_t<false, 4>)
                         : rows == 2 ? k_gapdp_t<true, 2>
                                     : k_gapdp_t<true, 1>;
@@ -555,7 +572,7 @@ static int run_dp(Ctx* c, const DpInputs& in, const std::vector<uint32_t>& ids, 
   uint64_t* d_tboff = (uint64_t*)ws.get(c, sl.tboff, (size_t)nwork * 8);
   uint8_t* d_edge = (uint8_t*)ws.get(c, 13, (size_t)(la.size()) + 16);  // per problem, shared by all lanes
   unsigned* d_counter = (unsigned*)ws.get(c, sl.counter, 64);
-  uint32_t* tb = (uint32_t*)ws.get(c, sl.arena, arena_need);
+  uint32_t* tb = (uint32_t*)ws.get(c, sl.arena, std::max<uint64_t>(arena_need, 256));
   if (!rowbuf || !d_order || !d_tboff || !d_edge || !d_counter || !tb)
     return report_error(MVG_ERR_NOMEM, "workspace allocation failed");
   if (int e = h2d_async(c, d_order, order.data(), (size_t)nwork * 4, L.st)) return e;
@@ -569,10 +586,25 @@ static int run_dp(Ctx* c, const DpInputs& in, const std::vector<uint32_t>& ids, 
     const int64_t w0 = wave_begin[wv], w1 = wave_begin[wv + 1];
     std::vector<uint32_t> slot_len(w1 - w0), ls;
     for (int64_t q = w0; q < w1; ++q) slot_len[q - w0] = (uint32_t)(la[order[q]] + lb[order[q]]);
-    if (int e = tb_long_plan(c, slot_len, &ls, &long_path[wv], &long_grid[wv])) return e;
+    if (!ckpt)  // checkpointed passes walk every path on a warp
+      if (int e = tb_long_plan(c, slot_len, &ls, &long_path[wv], &long_grid[wv])) return e;
     long_at[wv] = all_long.size();
     long_n[wv] = (int)ls.size();
     all_long.insert(all_long.end(), ls.begin(), ls.end());
+  }
+  int ck_grid = 0;
+  if (ckpt) {
+    static bool ck_attr[2] = {false, false};  // once per process and kernel: more than 48 KB of shared memory
+    void (*tbk)(const uint8_t*, const uint64_t*, const uint8_t*, const uint64_t*, const uint32_t*, const uint64_t*,
+                int, const uint32_t*, const uint8_t*, const uint64_t*, char*, int64_t*, uint32_t*, int32_t*,
+                unsigned*) = rows == 8 ? k_tb_ck<8> : k_tb_ck<4>;
+    if (!ck_attr[rows == 8]) {
+      MVG_CUDA_TRY(cudaFuncSetAttribute(tbk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kCkSmem));
+      ck_attr[rows == 8] = true;
+    }
+    int cbps = 0;
+    MVG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&cbps, tbk, kCkWarps * 32, kCkSmem));
+    ck_grid = dev_sms * std::max(1, cbps);
   }
   uint32_t* d_long = (uint32_t*)ws.get(c, L.slot_list, all_long.size() * 4 + 16);
   unsigned* d_long_ctr = (unsigned*)ws.get(c, L.slot_ctr, nwaves_run * 4 + 64);
@@ -614,6 +646,24 @@ static int run_dp(Ctx* c, const DpInputs& in, const std::vector<uint32_t>& ids, 
     stage_mark(c, banded ? "dp_banded" : "dp");
     kern<<<grid, kDpThreads, 0, L.st>>>(J);
     stage_mark(c, "traceback");
+    if (ckpt) {
+      unsigned* ctr = d_long_ctr + wv;
+      if (int e = rec.check(cudaMemsetAsync(ctr, 0, 4, L.st), "cudaMemsetAsync")) return e;
+      if (rows == 8)
+        k_tb_ck<8><<<ck_grid, kCkWarps * 32, kCkSmem, L.st>>>(in.sa, in.oa, in.sb, in.ob, J.order, J.tb_off, J.nwork,
+                                                               tb, d_edge, in.path_off, in.paths, in.path_len,
+                                                               c->d_err, in.env, ctr);
+      else
+        k_tb_ck<4><<<ck_grid, kCkWarps * 32, kCkSmem, L.st>>>(in.sa, in.oa, in.sb, in.ob, J.order, J.tb_off, J.nwork,
+                                                               tb, d_edge, in.path_off, in.paths, in.path_len,
+                                                               c->d_err, in.env, ctr);
+      stage_mark(c, "path_compact");
+      k_path_compact<<<grid_for((int64_t)J.nwork * 32, 256), 256, 0, L.st>>>(
+          in.oa, in.ob, J.order, J.nwork, d_accept, in.path_off, in.paths, in.path_len);
+      c->launches += 3;
+      if (int e = rec.check(cudaGetLastError(), "kernel launch")) return e;
+      continue;
+    }
     const bool forked = long_n[wv] > 0;
     if (forked)
       if (int e = rec.check(tb_long_launch(c, L, in, J.order, J.tb_off, tb, d_edge, d_delta, d_half, d_accept, rows,

@@ -130,6 +130,55 @@ __device__ __forceinline__ uint32_t dp_column(DpLane<R>& L, int32_t upMg, int32_
   return nibs;
 }
 
+// The same step without traceback bits (checkpointed passes): plain maxima
+// instead of max-with-predicate, same values.
+template <int R, bool ADJ>
+__device__ __forceinline__ void dp_column_score(DpLane<R>& L, int32_t upMg, int32_t upD, int32_t dgMg, int32_t dgD,
+                                                int32_t dgI, uint32_t bsel, int32_t goBadj) {
+  int32_t cuM = upMg, cuD = upD;
+  int32_t cdM = dgMg, cdD = dgD, cdI = dgI;
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const int32_t D = max(cuM, cuD);
+    const int32_t I = max(ADJ ? L.lM[r] + goBadj : L.lM[r], L.lI[r]);
+    const int32_t best = max(cdM, max(cdD, cdI) + 2 * kGap);
+    const int32_t M = best + (int32_t)__byte_perm(L.arow[r], 0u, bsel) - kScoreBias;
+    cdM = L.lM[r];
+    cdD = L.lD[r];
+    cdI = L.lI[r];
+    cuM = M;
+    cuD = D;
+    L.lM[r] = M;
+    L.lD[r] = D;
+    L.lI[r] = I;
+  }
+}
+
+// Checkpointed full DP.  Instead of traceback bits the forward pass keeps
+// the cell states (Mg, D, I) the traceback needs to recompute any block of
+// the matrix: the bottom row of every strip but the last (which the next
+// strip reads as its top row, so it also replaces the row buffer), and,
+// every kCkCols columns, the column of every strip.  The traceback then
+// recomputes, with traceback bits, only the blocks of 32*R rows x kCkCols
+// columns its path crosses (k_tb_ck).  Per problem slot (int4 entries):
+//   row (k, j), k < nstrips - 1, 1 <= j <= LB   at k * LB + j - 1
+//   column (k, b, q), 1 <= b < ncb, q < 32 R    at rows + (k * (ncb - 1) + b - 1) * 32 R + q
+// (the state left of block b's first column b * kCkCols + 1).
+constexpr int kCkCols = 128;
+
+__host__ __device__ __forceinline__ int ck_nblocks(int LB) { return (LB + kCkCols - 1) / kCkCols; }
+__host__ __device__ __forceinline__ int64_t ck_row_entries(int LA, int LB, int R) {
+  const int nstrips = (LA + 32 * R - 1) / (32 * R);
+  return (int64_t)(nstrips - 1) * LB;
+}
+__host__ __device__ __forceinline__ int64_t ck_col_entry(int LA, int LB, int R, int k, int b) {
+  return ck_row_entries(LA, LB, R) + ((int64_t)k * (ck_nblocks(LB) - 1) + (b - 1)) * (32 * R);
+}
+__host__ __device__ __forceinline__ int64_t ck_entries(int LA, int LB, int R) {
+  const int nstrips = (LA + 32 * R - 1) / (32 * R);
+  return ck_row_entries(LA, LB, R) + (int64_t)nstrips * (ck_nblocks(LB) - 1) * (32 * R);
+}
+
 // Sum over s[from, to) of each base's best score (warp-wide, every lane
 // gets the total).  base_max packs the biased maxima of codes 0..3.
 __device__ __forceinline__ int32_t warp_best_sum(const uint8_t* s, int from, int to, uint32_t base_max) {
@@ -158,9 +207,10 @@ struct DpShared {
 
 // Solves problem slot w.  Strips kstart, kstart + kstep, ... are run by this
 // warp; coop = true when the CTA's warps share the problem.
-template <bool BANDED, int R>
+template <bool BANDED, int R, bool CK>
 __device__ void dp_solve(const DpJob& J, DpShared& sh, int w, int kstart, int kstep, bool coop, int4* rowbuf_base,
                          int4* own_rowbuf) {
+  static_assert(!(BANDED && CK), "checkpoints are kept for the full DP only");
   constexpr int SR = 32 * R;
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
@@ -189,7 +239,9 @@ __device__ void dp_solve(const DpJob& J, DpShared& sh, int w, int kstart, int ks
     totB = warp_best_sum(B, 0, LB, J.base_max);
   }
   uint32_t* tbs = J.tb + J.tb_off[w] / 4;
-  for (int k = 0; k < kstart; ++k) tbs += (int64_t)tb_words_per_lane(band_hi(band, k) - band_lo(band, k) + 1, R) * 32;
+  int4* ck = reinterpret_cast<int4*>(tbs);  // checkpointed pass: the slot's checkpoints
+  if (!CK)
+    for (int k = 0; k < kstart; ++k) tbs += (int64_t)tb_words_per_lane(band_hi(band, k) - band_lo(band, k) + 1, R) * 32;
 
   for (int k = kstart; k < nstrips; k += kstep) {
     const int row0 = k * SR;
@@ -200,8 +252,11 @@ __device__ void dp_solve(const DpJob& J, DpShared& sh, int w, int kstart, int ks
     const int S = W + 31;
     const int wpl = tb_words_per_lane(W, R);
     // row buffers: the one this strip reads (previous strip's bottom row) and the one it writes
-    int4* rb_in = coop ? rowbuf_base + (int64_t)((k - 1) & (kDpWarps - 1)) * J.rowbuf_stride : own_rowbuf;
-    int4* rb_out = coop ? rowbuf_base + (int64_t)(k & (kDpWarps - 1)) * J.rowbuf_stride : own_rowbuf;
+    // (checkpointed: the slot's row checkpoints k - 1 and k, indexed by column from 1)
+    int4* rb_in = CK ? ck + (int64_t)(k - 1) * LB - 1
+                     : coop ? rowbuf_base + (int64_t)((k - 1) & (kDpWarps - 1)) * J.rowbuf_stride : own_rowbuf;
+    int4* rb_out = CK ? ck + (int64_t)k * LB - 1
+                      : coop ? rowbuf_base + (int64_t)(k & (kDpWarps - 1)) * J.rowbuf_stride : own_rowbuf;
     const int producer = (k - 1) & (kDpWarps - 1);
     // cooperative mode: wait until the previous strip published column `col`
     auto wait_for = [&](int col) -> bool {
@@ -339,8 +394,15 @@ __device__ void dp_solve(const DpJob& J, DpShared& sh, int w, int kstart, int ks
       uint32_t nibs = 0;
       if (!checked || (jj >= 0 && jj < W)) {
         // column 1 (only in checked steps) opens for free
-        nibs = checked ? dp_column<R, true>(L, upM, upD, dgM, dgD, dgI, bsel, j == 1 ? -kGap : 0)
-                       : dp_column<R, false>(L, upM, upD, dgM, dgD, dgI, bsel, 0);
+        if (CK) {
+          if (checked)
+            dp_column_score<R, true>(L, upM, upD, dgM, dgD, dgI, bsel, j == 1 ? -kGap : 0);
+          else
+            dp_column_score<R, false>(L, upM, upD, dgM, dgD, dgI, bsel, 0);
+        } else {
+          nibs = checked ? dp_column<R, true>(L, upM, upD, dgM, dgD, dgI, bsel, j == 1 ? -kGap : 0)
+                         : dp_column<R, false>(L, upM, upD, dgM, dgD, dgI, bsel, 0);
+        }
         if (checked && s == 0 && lane == 0 && k == 0 && LA == 1) {
           // NWSmall's last-row special case (MU/nwsmall.cpp:616-624) with
           // LA == 1: M(1,1) adds the open and close of position 0, and the
@@ -352,6 +414,12 @@ __device__ void dp_solve(const DpJob& J, DpShared& sh, int w, int kstart, int ks
         pubD = L.lD[R - 1];
         pubI = L.lI[R - 1];
         if (lane == 31 && writes_row) rb_out[j] = make_int4(pubM, pubD, pubI, 0);
+        if (CK && ((jj + 1) & (kCkCols - 1)) == 0 && jj + 1 < W) {
+          // column checkpoint: the state left of block (jj + 1) / kCkCols
+          int4* col = ck + ck_col_entry(LA, LB, R, k, (jj + 1) / kCkCols) + lane * R;
+#pragma unroll
+          for (int r = 0; r < R; ++r) col[r] = make_int4(L.lM[r], L.lD[r], L.lI[r], 0);
+        }
         if (track && lane == 31) {
           run31 += best_of(J.base_max, bsel);  // prefix over B[0..j)
           if (j == next_lo - 1) pb_next = run31;
@@ -365,7 +433,9 @@ __device__ void dp_solve(const DpJob& J, DpShared& sh, int w, int kstart, int ks
         pubD = leftD;
         pubI = kNeg;
       }
-      if (R == 8) {
+      if (CK) {
+        // no traceback bits
+      } else if (R == 8) {
         tbs[s * 32 + lane] = nibs;
       } else {  // 8/R steps per 32-bit word
         constexpr int kPer = 8 / R;
@@ -441,8 +511,9 @@ __device__ void dp_solve(const DpJob& J, DpShared& sh, int w, int kstart, int ks
       }
     }
     // advance the traceback pointer past this warp's strip and the skipped ones
-    for (int q = k; q < k + kstep && q < nstrips; ++q)
-      tbs += (int64_t)tb_words_per_lane(band_hi(band, q) - band_lo(band, q) + 1, R) * 32;
+    if (!CK)
+      for (int q = k; q < k + kstep && q < nstrips; ++q)
+        tbs += (int64_t)tb_words_per_lane(band_hi(band, q) - band_lo(band, q) + 1, R) * 32;
   }
   if (BANDED) {
     // paths along row 0 past the band, or down column 0 past it (added once)
@@ -467,7 +538,7 @@ __device__ void dp_solve(const DpJob& J, DpShared& sh, int w, int kstart, int ks
   }
 }
 
-template <bool BANDED, int R>
+template <bool BANDED, int R, bool CK = false>
 __global__ void __launch_bounds__(kDpThreads, 2) k_gapdp_t(DpJob J) {
   __shared__ DpShared sh;
   const int lane = threadIdx.x & 31;
@@ -485,7 +556,7 @@ __global__ void __launch_bounds__(kDpThreads, 2) k_gapdp_t(DpJob J) {
     __syncthreads();
     const int w = sh.claim;
     if (w >= J.nbig) break;
-    dp_solve<BANDED, R>(J, sh, w, wib, kDpWarps, true, rowbuf_cta, own_rowbuf);
+    dp_solve<BANDED, R, CK>(J, sh, w, wib, kDpWarps, true, rowbuf_cta, own_rowbuf);
     __syncthreads();
     if (BANDED && threadIdx.x == 0) {
       const uint32_t p = J.order[w];
@@ -499,7 +570,7 @@ __global__ void __launch_bounds__(kDpThreads, 2) k_gapdp_t(DpJob J) {
     if (lane == 0) w = J.nbig + (int)atomicAdd(&J.counter[1], 1u);
     w = __shfl_sync(0xffffffffu, w, 0);
     if (w >= J.nwork) break;
-    dp_solve<BANDED, R>(J, sh, w, 0, 1, false, rowbuf_cta, own_rowbuf);
+    dp_solve<BANDED, R, CK>(J, sh, w, 0, 1, false, rowbuf_cta, own_rowbuf);
   }
 }
 

@@ -54,6 +54,7 @@ struct Ctx {
   int pair_bucket_cap = 3072;  // seed-join buckets sorted in shared memory up to this size
   long long dp_spin_limit = 1ll << 26;  // polls before a whole-CTA gap-DP wait gives up (about a second)
   int dp_graph = 1;                      // gap-DP passes launched as one recorded CUDA graph
+  int dp_ckpt = 1;                       // full-DP passes keep checkpoints, the traceback recomputes blocks
   int dp_coop_strips = 16;               // full-DP problems of at least this many strips use a whole CTA
   cudaGraphExec_t dp_exec[2] = {};       // the executable graph of each DP lane, updated per call
   uint64_t graph_launches = 0;

@@ -48,7 +48,8 @@ EXPORTS = ["mvg_create", "mvg_destroy", "mvg_last_error", "mvg_stream", "mvg_ker
            "mvg_set_band_gate", "mvg_sslist_write", "mvg_sslist_read", "mvg_set_pair_bucket_cap",
            "mvg_set_dp_spin_limit", "mvg_gap_anchor_search", "mvg_gap_anchor_search_dev", "mvg_set_dp_graph",
            "mvg_set_dp_coop_strips", "mvg_path_rows", "mvg_path_rows_dev",
-           "mvg_xmfa_write", "mvg_xmfa_write_dev", "mvg_set_mlp_tcgen05", "mvg_mlp_tcgen05_passes"]
+           "mvg_xmfa_write", "mvg_xmfa_write_dev", "mvg_set_mlp_tcgen05", "mvg_mlp_tcgen05_passes",
+           "mvg_set_dp_checkpoint"]
 
 TUNING_PATH = os.path.join(HERE, "dp_tuning.json")
 
@@ -92,6 +93,7 @@ def load_library(path=LIB_PATH):
         "mvg_set_pair_bucket_cap": (ci, [vp, ci]),
         "mvg_set_dp_spin_limit": (ci, [vp, ctypes.c_longlong]),
         "mvg_set_dp_graph": (ci, [vp, ci]),
+        "mvg_set_dp_checkpoint": (ci, [vp, ci]),
         "mvg_set_mlp_tcgen05": (ci, [vp, ci]),
         "mvg_mlp_tcgen05_passes": (ci, [vp, ctypes.POINTER(ctypes.c_uint64)]),
         "mvg_set_dp_coop_strips": (ci, [vp, ci]),
@@ -249,6 +251,10 @@ class Context:
         n = ctypes.c_uint64(0)
         _check(load_library().mvg_mlp_tcgen05_passes(self._h, ctypes.byref(n)))
         return n.value
+
+    def set_dp_checkpoint(self, on=True):
+        """Full gap-DP passes checkpointed (default) or with stored traceback bits; see mvg_set_dp_checkpoint."""
+        _check(load_library().mvg_set_dp_checkpoint(self._h, 1 if on else 0))
 
     def set_dp_graph(self, on=True):
         """Gap-DP waves as one recorded CUDA graph (default) or launched one by one."""

@@ -372,6 +372,64 @@ def _path_score(a, b, path):
     return s
 
 
+def test_gapdp_checkpointed_equals_stored_bits(ctx):
+    """Full-DP passes keep checkpoints and recompute the blocks the path
+    crosses (default) or store every traceback bit: identical scores, paths
+    and path envelopes, at both strip heights, on shapes around the block
+    edges (strips of 32 * R rows, column blocks of 128), a whole-CTA pair and
+    a random batch, with many waves (a small arena) too."""
+    import torch
+    import bandnet
+    rng = np.random.default_rng(128)
+    a_list, b_list = [], []
+    for la in (1, 2, 127, 128, 129, 255, 256, 257, 513, 2100):
+        for lb in (1, 2, 127, 128, 129, 255, 256, 257, 385, 1000):
+            a = rng.integers(0, 4, la).astype(np.uint8)
+            # a mutated copy of A cut or padded with random bases to exactly lb
+            m = synth.mutate_codes(rng, a, 0.1, la // 100, 3.0)[:lb]
+            b = np.concatenate([m, rng.integers(0, 4, lb - len(m)).astype(np.uint8)])
+            a_list.append(a)
+            b_list.append(b)
+    a = rng.integers(0, 4, 4300).astype(np.uint8)
+    a_list.append(a)
+    b_list.append(synth.mutate_codes(rng, a, 0.2, 30, 3.0))
+    sa2, oa2, sb2, ob2 = synth.gap_batch(seed=129, nprob=300, lmin=1, lmax=3000)
+    sa = np.concatenate(a_list + [sa2])
+    sb = np.concatenate(b_list + [sb2])
+    oa = np.concatenate([[0], np.cumsum([len(x) for x in a_list])]).astype(np.uint64)
+    ob = np.concatenate([[0], np.cumsum([len(x) for x in b_list])]).astype(np.uint64)
+    oa = np.concatenate([oa, oa[-1] + oa2[1:].astype(np.uint64)])
+    ob = np.concatenate([ob, ob[-1] + ob2[1:].astype(np.uint64)])
+    n = len(oa) - 1
+    dev = torch.device("cuda", 0)
+    d = [torch.from_numpy(np.ascontiguousarray(x)).to(dev) for x in (sa, oa.astype(np.int64), sb, ob.astype(np.int64))]
+    full0, band0 = ctx.full_rows, ctx.band_rows
+    try:
+        for rows in (4, 8):
+            ctx.set_dp_rows(rows, band0)
+            res = {}
+            for ck in (True, False):
+                ctx.set_dp_checkpoint(ck)
+                sc, paths = ctx.gap_align_batch(sa, oa, sb, ob)
+                lsc, env = bandnet.full_dp_labels_dev(ctx, *[x.data_ptr() for x in d], n, torch_device=dev)
+                res[ck] = (sc, paths, lsc, env)
+            np.testing.assert_array_equal(res[True][0], res[False][0])
+            assert res[True][1] == res[False][1], rows
+            np.testing.assert_array_equal(res[True][2], res[False][2])
+            np.testing.assert_array_equal(res[True][3], res[False][3])
+        ctx.set_dp_checkpoint(True)
+        ctx.set_tb_arena(8 << 20)  # many waves
+        try:
+            s_w, p_w = ctx.gap_align_batch(sa, oa, sb, ob)
+        finally:
+            ctx.set_tb_arena(1 << 62)
+        np.testing.assert_array_equal(s_w, res[True][0])
+        assert p_w == res[True][1]
+    finally:
+        ctx.set_dp_checkpoint(True)
+        ctx.set_dp_rows(full0, band0)
+
+
 def test_gapdp_graph_and_direct_launches_identical(ctx):
     """The DP waves recorded into one CUDA graph (default) and launched one by
     one give identical scores and paths, across calls of different shapes
