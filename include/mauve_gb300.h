@@ -417,6 +417,18 @@ int mvg_set_dp_spin_limit(mvg_handle h, long long polls);
  * choice in mauve-py_gb300/dp_tuning.json).  Results do not depend on it. */
 int mvg_set_dp_coop_strips(mvg_handle h, int strips);
 
+/* mvg_gapdp_banded: the tallest group height (rows per lane) a band may use
+ * on the ring schedule (0..32, default 32); bands no allowed height fits run
+ * in the strip kernel.  Results do not depend on it. */
+int mvg_set_ring_max_rows(mvg_handle h, int rows);
+
+/* mvg_gapdp_banded: problems whose band covers so much of the matrix that
+ * they run whole (see mvg_set_band_whole_fraction) go to the full DP when A
+ * has at least `rows` rows, else into the strip kernel's launch with a band
+ * covering the matrix (default 512, measured on 200,000 gaps drawn like the
+ * recoded pair's).  Results do not depend on it. */
+int mvg_set_band_whole_full_rows(mvg_handle h, int64_t rows);
+
 /* Full gap-DP passes checkpointed (on = 1, the default): the forward pass
  * keeps every strip's bottom row and, every 128 columns, every strip's
  * column of cell states instead of traceback bits (about 0.19 instead of

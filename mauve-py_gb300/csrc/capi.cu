@@ -524,6 +524,18 @@ int mvg_set_dp_coop_strips(mvg_handle h, int strips) {
   return 0;
 }
 
+int mvg_set_ring_max_rows(mvg_handle h, int rows) {
+  if (!h || rows < 0 || rows > 32) return report_error(MVG_ERR_ARG, "rows must be in 0..32");
+  h->ring_max_rows = rows;
+  return 0;
+}
+
+int mvg_set_band_whole_full_rows(mvg_handle h, int64_t rows) {
+  if (!h || rows < 1) return report_error(MVG_ERR_ARG, "rows must be at least 1");
+  h->whole_full_rows = rows;
+  return 0;
+}
+
 int mvg_set_dp_checkpoint(mvg_handle h, int on) {
   if (!h || (on != 0 && on != 1)) return report_error(MVG_ERR_ARG, "on must be 0 or 1");
   h->dp_ckpt = on;

@@ -844,7 +844,6 @@ static int run_ring(Ctx* c, const TbLanes& L, const DpInputs& in, const std::vec
 // Whole-matrix problems with at least this many rows run in the full DP's
 // launch (strips of 32 * dp_rows rows), shorter ones in the banded strip
 // launch (32 * band_rows rows).
-constexpr int64_t kWholeFullRows = 1024;
 
 // Every base code must be 0..3 (the kernels mask to 2 bits; this reports it).
 static int check_codes(Ctx* c, const uint8_t* d_sa, uint64_t na, const uint8_t* d_sb, uint64_t nb) {
@@ -976,7 +975,7 @@ int gapdp_banded_dev(Ctx* c, const uint8_t* d_sa, const uint64_t* d_oa, const ui
         P.bc += full;
         // long ones through the full DP's taller strips, short ones beside
         // the strip kernel's bands
-        (la[p] >= kWholeFullRows ? P.wids : P.ids).push_back((uint32_t)p);
+        (la[p] >= c->whole_full_rows ? P.wids : P.ids).push_back((uint32_t)p);
         continue;
       }
       int rr = 0;
@@ -987,6 +986,7 @@ int gapdp_banded_dev(Ctx* c, const uint8_t* d_sa, const uint64_t* d_oa, const ui
         const double slope = (double)lb[p] / (double)la[p];
         for (int q = 0; q < kRingHeights && !rr; ++q) {
           const int R = kRingRows[q];
+          if (R > c->ring_max_rows) break;  // taller groups go to the strip kernel
           const bool many = (la[p] + R - 1) / R > 32;
           if (many && 2.0 * hv[p] + 2.0 + (R - 1) * slope > 32.0 + 32.0 * R * slope + 2.0) continue;
           if (ring_eligible(make_ring_band((int)la[p], (int)lb[p], dv[p], hv[p], R))) rr = R;
@@ -1060,7 +1060,8 @@ int gapdp_banded_dev(Ctx* c, const uint8_t* d_sa, const uint64_t* d_oa, const ui
   std::vector<uint32_t> fallback;
   for (int64_t p = 0; p < nprob; ++p) {
     if (whole[p]) {
-      if (!acc[p] && la[p] < kWholeFullRows) return report_error(MVG_ERR_DEVICE, "whole-matrix band failed its check");
+      if (!acc[p] && la[p] < c->whole_full_rows)
+        return report_error(MVG_ERR_DEVICE, "whole-matrix band failed its check");
       acc[p] = 2;  // not banded: the proposed band covered most of the matrix
     } else if (!acc[p]) {
       fallback.push_back((uint32_t)p);

@@ -55,6 +55,8 @@ struct Ctx {
   long long dp_spin_limit = 1ll << 26;  // polls before a whole-CTA gap-DP wait gives up (about a second)
   int dp_graph = 1;                      // gap-DP passes launched as one recorded CUDA graph
   int dp_ckpt = 1;                       // full-DP passes keep checkpoints, the traceback recomputes blocks
+  int64_t whole_full_rows = 512;         // banded calls: whole-matrix problems from this many rows go to the full DP
+  int ring_max_rows = 32;                // banded calls: tallest ring group height used
   int dp_coop_strips = 16;               // full-DP problems of at least this many strips use a whole CTA
   cudaGraphExec_t dp_exec[2] = {};       // the executable graph of each DP lane, updated per call
   uint64_t graph_launches = 0;

@@ -49,7 +49,7 @@ EXPORTS = ["mvg_create", "mvg_destroy", "mvg_last_error", "mvg_stream", "mvg_ker
            "mvg_set_dp_spin_limit", "mvg_gap_anchor_search", "mvg_gap_anchor_search_dev", "mvg_set_dp_graph",
            "mvg_set_dp_coop_strips", "mvg_path_rows", "mvg_path_rows_dev",
            "mvg_xmfa_write", "mvg_xmfa_write_dev", "mvg_set_mlp_tcgen05", "mvg_mlp_tcgen05_passes",
-           "mvg_set_dp_checkpoint"]
+           "mvg_set_dp_checkpoint", "mvg_set_band_whole_full_rows", "mvg_set_ring_max_rows"]
 
 TUNING_PATH = os.path.join(HERE, "dp_tuning.json")
 
@@ -94,6 +94,8 @@ def load_library(path=LIB_PATH):
         "mvg_set_dp_spin_limit": (ci, [vp, ctypes.c_longlong]),
         "mvg_set_dp_graph": (ci, [vp, ci]),
         "mvg_set_dp_checkpoint": (ci, [vp, ci]),
+        "mvg_set_band_whole_full_rows": (ci, [vp, i64]),
+        "mvg_set_ring_max_rows": (ci, [vp, ci]),
         "mvg_set_mlp_tcgen05": (ci, [vp, ci]),
         "mvg_mlp_tcgen05_passes": (ci, [vp, ctypes.POINTER(ctypes.c_uint64)]),
         "mvg_set_dp_coop_strips": (ci, [vp, ci]),
@@ -251,6 +253,14 @@ class Context:
         n = ctypes.c_uint64(0)
         _check(load_library().mvg_mlp_tcgen05_passes(self._h, ctypes.byref(n)))
         return n.value
+
+    def set_ring_max_rows(self, rows):
+        """Banded calls: tallest ring group height used (taller bands run in the strip kernel)."""
+        _check(load_library().mvg_set_ring_max_rows(self._h, int(rows)))
+
+    def set_band_whole_full_rows(self, rows):
+        """Banded calls: whole-matrix problems from this many rows of A run in the full DP."""
+        _check(load_library().mvg_set_band_whole_full_rows(self._h, int(rows)))
 
     def set_dp_checkpoint(self, on=True):
         """Full gap-DP passes checkpointed (default) or with stored traceback bits; see mvg_set_dp_checkpoint."""

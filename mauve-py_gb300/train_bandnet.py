@@ -247,7 +247,7 @@ def calibrate_and_evaluate(args, ctx, dev, net, tr, ev, tot_a, tot_b, n_tr, loss
     best = None
     for gate in (0, 18, 20, 22, 24):
         ctx.set_band_gate(gate)
-        for whole in (0.3, 0.35, 0.45):
+        for whole in (0.25, 0.3, 0.35, 0.45):
             ctx.set_band_whole_fraction(whole)
             for alpha in (1.15, 1.45, 1.6, 1.8, 2.0, 2.3):
                 for beta in (0.0, 8.0, 16.0, 32.0):
