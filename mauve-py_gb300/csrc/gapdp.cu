@@ -99,6 +99,24 @@ constexpr int kRingHeights = (int)(sizeof(kRingRows) / sizeof(kRingRows[0]));
 // Runs f(begin, end, t) over [0, n) in up to 16 contiguous chunks on host
 // threads (one chunk below 20,000 items), chunk t covering items before
 // chunk t + 1's; returns the number of chunks.
+// Indices 0..n-1 ordered by key (ascending, ties in index order): a stable
+// LSD radix sort with 11-bit digits over the key's used bits.
+static std::vector<uint32_t> radix_order(const std::vector<uint64_t>& key) {
+  const size_t n = key.size();
+  std::vector<uint32_t> a(n), b(n);
+  for (size_t i = 0; i < n; ++i) a[i] = (uint32_t)i;
+  uint64_t all = 0;
+  for (uint64_t k : key) all |= k;
+  for (int shift = 0; shift < 64 && (all >> shift) != 0; shift += 11) {
+    uint32_t count[2049] = {};
+    for (size_t i = 0; i < n; ++i) ++count[((key[a[i]] >> shift) & 2047u) + 1];
+    for (int d = 0; d < 2048; ++d) count[d + 1] += count[d];
+    for (size_t i = 0; i < n; ++i) b[count[(key[a[i]] >> shift) & 2047u]++] = a[i];
+    a.swap(b);
+  }
+  return a;
+}
+
 template <class F>
 static int host_chunks(int64_t n, F f) {
   int nt = 1;
@@ -468,6 +486,7 @@ static int run_dp(Ctx* c, const DpInputs& in, const std::vector<uint32_t>& ids, 
   const int rows = banded ? c->band_rows : c->dp_rows;
   // full passes keep checkpoints instead of traceback bits (traceback_ck.cuh)
   const bool ckpt = !banded && c->dp_ckpt && (rows == 4 || rows == 8);
+  std::unique_ptr<HostSpan> sub(new HostSpan(c, "dp_sizes"));
   std::vector<uint64_t> bytes(nwork), cells(nwork);
   int64_t maxlb = 0;
   for (int64_t w = 0; w < nwork; ++w) {
@@ -492,17 +511,19 @@ static int run_dp(Ctx* c, const DpInputs& in, const std::vector<uint32_t>& ids, 
     is_big[w] = many && (!banded || cells[w] >= (uint64_t)a * 8 * 32 * rows);
   }
   // largest first, ties in input order: one sort of packed (cells, index) keys
-  std::vector<uint32_t> idx(nwork);
+  sub.reset(new HostSpan(c, "dp_sort"));
+  std::vector<uint32_t> idx;
   {
-    std::vector<std::pair<uint64_t, uint32_t>> key(nwork);
-    for (int64_t w = 0; w < nwork; ++w) key[w] = {~cells[w], (uint32_t)w};
-    std::sort(key.begin(), key.end());
-    for (int64_t w = 0; w < nwork; ++w) idx[w] = key[w].second;
+    constexpr uint64_t kMax = (1ull << 40) - 1;  // at most 1e6 x 1e6 cells
+    std::vector<uint64_t> key(nwork);
+    for (int64_t w = 0; w < nwork; ++w) key[w] = kMax - std::min(cells[w], kMax);
+    idx = radix_order(key);
   }
 
   uint64_t arena = c->tb_arena;
   {
     size_t free_b = 0, total_b = 0;
+    HostSpan mem_span(c, "meminfo");
     if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess) {
       const size_t have = c->ws.size[sl.arena] + free_b;  // the arena slot itself may be re-allocated
       const uint64_t cap = (uint64_t)(have * 0.6);
@@ -515,6 +536,7 @@ static int run_dp(Ctx* c, const DpInputs& in, const std::vector<uint32_t>& ids, 
     max_tb = std::max(max_tb, bytes[w]);
   }
   if (max_tb > arena) return report_error(MVG_ERR_CAPACITY, "one gap-DP problem exceeds the traceback arena");
+  sub.reset(new HostSpan(c, "dp_waves"));
   // Waves: deal the size-sorted problems round-robin, so every wave holds the
   // same mix of sizes and stays largest-first inside.
   // at least one wave: checkpointed slots of problems within one block hold nothing
@@ -553,6 +575,7 @@ static int run_dp(Ctx* c, const DpInputs& in, const std::vector<uint32_t>& ids, 
   }
   wave_begin.push_back(nwork);
 
+  sub.reset(new HostSpan(c, "dp_copy"));
   int dev_sms = 0;
   MVG_CUDA_TRY(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, c->device));
   void (*kern)(DpJob) = ckpt        ? (rows == 8 ? k_gapdp_t<false, 8, true> : k_gapdp_t<false, 4, true>)
@@ -611,6 +634,7 @@ static int run_dp(Ctx* c, const DpInputs& in, const std::vector<uint32_t>& ids, 
   if (!d_long || !d_long_ctr) return report_error(MVG_ERR_NOMEM, "workspace allocation failed");
   if (!all_long.empty())
     if (int e = h2d_async(c, d_long, all_long.data(), all_long.size() * 4, L.st)) return e;
+  sub.reset();
   span.reset();
   // Every wave's launches (claim counters, the persistent DP kernel, the two
   // traceback walkers, path compaction) are recorded into one CUDA graph and
@@ -704,32 +728,21 @@ static int run_ring(Ctx* c, const TbLanes& L, const DpInputs& in, const std::vec
     }
   });
   // by group height, each class most expensive first, ties in input order
-  // (the classes gathered in order, then sorted on their own threads)
-  std::vector<uint32_t> idx(nwork);
+  std::vector<uint32_t> idx;
   {
-    std::vector<std::pair<uint64_t, uint32_t>> key(nwork);
-    int64_t cls_begin[kRingHeights + 1] = {};
-    for (int64_t w = 0; w < nwork; ++w)
-      for (int q = 0; q < kRingHeights; ++q)
-        if (rsel[w] == kRingRows[q]) cls_begin[q + 1]++;
-    for (int q = 0; q < kRingHeights; ++q) cls_begin[q + 1] += cls_begin[q];
-    int64_t fill[kRingHeights];
-    for (int q = 0; q < kRingHeights; ++q) fill[q] = cls_begin[q];
-    for (int64_t w = 0; w < nwork; ++w)
-      for (int q = 0; q < kRingHeights; ++q)
-        if (rsel[w] == kRingRows[q]) key[fill[q]++] = {~cost[w], (uint32_t)w};
-    std::vector<std::thread> th;
-    for (int q = 0; q < kRingHeights; ++q)
-      if (cls_begin[q + 1] - cls_begin[q] > 1)
-        th.emplace_back([&key, &cls_begin, q]() {
-          std::sort(key.begin() + cls_begin[q], key.begin() + cls_begin[q + 1]);
-        });
-    for (auto& x : th) x.join();
-    for (int64_t w = 0; w < nwork; ++w) idx[w] = key[w].second;
+    constexpr uint64_t kMax = (1ull << 40) - 1;
+    std::vector<uint64_t> key(nwork);
+    for (int64_t w = 0; w < nwork; ++w) {
+      int q = 0;
+      while (q + 1 < kRingHeights && kRingRows[q] != rsel[w]) ++q;
+      key[w] = ((uint64_t)q << 40) | (kMax - std::min(cost[w], kMax));
+    }
+    idx = radix_order(key);
   }
   uint64_t arena = c->tb_arena;
   {
     size_t free_b = 0, total_b = 0;
+    HostSpan mem_span(c, "meminfo");
     if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess) {
       const uint64_t cap = (uint64_t)((c->ws.size[67] + free_b) * 0.6);
       if (arena > cap) arena = cap;

@@ -69,7 +69,7 @@ struct Ctx {
   const char* stage_name[kMaxStages] = {};
   int nstage = -1;  // -1: no stage recorded yet in this call
   // host-side planning time of the call, by name (summed), when profiling
-  static constexpr int kMaxHost = 8;
+  static constexpr int kMaxHost = 12;
   double host_ms[kMaxHost] = {};
   const char* host_name[kMaxHost] = {};
   int nhost = 0;
