@@ -28,6 +28,7 @@
 //                    left ends is the library sort's, as in the reference),
 //                    LengthFilter, shift to genome coordinates
 #include <algorithm>
+#include <atomic>
 #include <mutex>
 #include <thread>
 #include <vector>
@@ -515,10 +516,11 @@ int gap_anchor_search_dev(Ctx* c, const uint8_t* d_a, uint64_t na, const uint8_t
 host_filter:
   HostSpan span(c, "gs_filter");
   // host: per gap, overlap elimination and length filter, then genome
-  // coordinates; gaps are independent, so host threads take contiguous
-  // ranges of them and the survivors are packed in gap order afterwards
+  // coordinates.  Gaps are independent and their anchor counts differ by
+  // orders of magnitude, so host threads claim runs of gaps from a counter,
+  // each converting, filtering and shifting its gaps' rows in place; a
+  // second pass, claimed the same way, copies the survivors out in gap order.
   std::vector<Anchor> anc(rows.size() / 3);
-  for (size_t k = 0; k < anc.size(); ++k) anc[k] = Anchor{{rows[3 * k], rows[3 * k + 1]}, rows[3 * k + 2]};
   std::vector<size_t> gap_r(ng + 1, 0);  // rows of searched gap gi: [gap_r[gi], gap_r[gi+1])
   for (size_t s = 0, r = 0, gi = 0; gi < (size_t)ng; ++gi) {
     while (s < seg_gap.size() && seg_gap[s] == (uint32_t)gi) r += seg_n[s++];
@@ -527,31 +529,43 @@ host_filter:
   std::vector<int64_t> nkept(ng, 0);
   const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
   const int nthreads = (int)std::min<uint64_t>(hw, std::max<uint64_t>(1, anc.size() / 20000));
-  auto work = [&](int t) {
-    std::vector<Anchor*> scratch;
-    for (int gi = (int)((int64_t)ng * t / nthreads); gi < (int)((int64_t)ng * (t + 1) / nthreads); ++gi) {
-      const size_t r0 = gap_r[gi];
-      const int64_t k = filter_gap(anc.data() + r0, (int64_t)(gap_r[gi + 1] - r0), scratch);
-      const GapDev& d = gd[gi];
-      for (int64_t u = 0; u < k; ++u)
-        for (int q = 0; q < 2; ++q) {
-          int64_t& x = anc[r0 + u].s[q];
-          x = x > 0 ? x + (int64_t)d.src[q] : x - (int64_t)d.src[q];
-        }
-      nkept[gi] = k;
+  constexpr int kGapRun = 16;  // gaps per claim
+  auto run_claimed = [&](auto&& per_gap_fn) {
+    std::atomic<int> next{0};
+    auto worker = [&]() {
+      for (;;) {
+        const int g0 = next.fetch_add(kGapRun);
+        if (g0 >= ng) break;
+        for (int gi = g0; gi < std::min(ng, g0 + kGapRun); ++gi) per_gap_fn(gi);
+      }
+    };
+    if (nthreads > 1) {
+      std::vector<std::thread> pool;
+      for (int t = 0; t < nthreads; ++t) pool.emplace_back(worker);
+      for (std::thread& th : pool) th.join();
+    } else {
+      worker();
     }
   };
-  if (nthreads > 1) {
-    std::vector<std::thread> pool;
-    for (int t = 0; t < nthreads; ++t) pool.emplace_back(work, t);
-    for (std::thread& th : pool) th.join();
-  } else {
-    work(0);
-  }
+  run_claimed([&](int gi) {
+    thread_local std::vector<Anchor*> scratch;
+    const size_t r0 = gap_r[gi], r1 = gap_r[gi + 1];
+    for (size_t k = r0; k < r1; ++k) anc[k] = Anchor{{rows[3 * k], rows[3 * k + 1]}, rows[3 * k + 2]};
+    const int64_t k = filter_gap(anc.data() + r0, (int64_t)(r1 - r0), scratch);
+    const GapDev& d = gd[gi];
+    for (int64_t u = 0; u < k; ++u)
+      for (int q = 0; q < 2; ++q) {
+        int64_t& x = anc[r0 + u].s[q];
+        x = x > 0 ? x + (int64_t)d.src[q] : x - (int64_t)d.src[q];
+      }
+    nkept[gi] = k;
+  });
   uint64_t total = 0;
+  std::vector<uint64_t> obase(ng + 1, 0);  // output row of each searched gap's first survivor
   for (int gi = 0; gi < ng; ++gi) {
     per_gap[gid[gi]] = (uint64_t)nkept[gi];
     total += (uint64_t)nkept[gi];
+    obase[gi + 1] = total;
   }
   if (gap_off) {
     gap_off[0] = 0;
@@ -560,14 +574,15 @@ host_filter:
   *count = total;
   if (total > cap) return report_error(MVG_ERR_CAPACITY, "anchor output buffer too small");
   // searched-gap order is the caller's gap order
-  uint64_t o = 0;
-  for (int gi = 0; gi < ng; ++gi)
-    for (int64_t u = 0; u < nkept[gi]; ++u, ++o) {
+  run_claimed([&](int gi) {
+    for (int64_t u = 0; u < nkept[gi]; ++u) {
       const Anchor& x = anc[gap_r[gi] + u];
-      out[3 * o + 0] = x.s[0];
-      out[3 * o + 1] = x.s[1];
-      out[3 * o + 2] = x.len;
+      int64_t* o = out + 3 * (obase[gi] + (uint64_t)u);
+      o[0] = x.s[0];
+      o[1] = x.s[1];
+      o[2] = x.len;
     }
+  });
   return 0;
 }
 
