@@ -366,24 +366,53 @@ int64_t filter_gap(Anchor* a, int64_t n, std::vector<Anchor*>& ml) {
 }
 }  // namespace
 
-int gap_anchor_search_dev(Ctx* c, const uint8_t* d_a, uint64_t na, const uint8_t* d_b, uint64_t nb,
-                          const int64_t* gaps, uint64_t ngaps, int64_t* out, uint64_t cap, uint64_t* gap_off,
-                          uint64_t* count) {
-  *count = 0;
-  stage_begin_call(c);
-  if (ngaps >= (1ull << 31)) return report_error(MVG_ERR_ARG, "too many gaps");
-  int rc = gs_upload_tables(c->device);
-  if (rc) return rc;
-  // host plan: the gaps that are searched, their seeds, word and key ranges
+namespace {
+// One chunk of a call's gaps: the searched gaps' device descriptors and
+// caller indices, the device pass's rows and segment tables, and the host
+// pass's filtered anchors.
+struct GsChunk {
   std::vector<GapDev> gd;
   std::vector<uint32_t> gid;  // caller's gap index of each searched gap
   uint64_t words[2] = {0, 0}, keys[2] = {0, 0};
-  for (uint64_t g = 0; g < ngaps; ++g) {
+  std::vector<int64_t> rows;  // (start A, start B, length) per entry, GetMatchList order per gap
+  std::vector<uint32_t> seg_gap, seg_n;
+  std::vector<Anchor> anc;     // searched gap gi's survivors at [gap_r[gi], gap_r[gi] + nkept[gi])
+  std::vector<size_t> gap_r;
+  std::vector<int64_t> nkept;
+};
+
+// Runs fn(i) for i in [0, n) on up to nthreads host threads that claim runs
+// of 16 indices from a counter.
+template <class F>
+void run_claimed(int n, int nthreads, F&& fn) {
+  std::atomic<int> next{0};
+  auto worker = [&]() {
+    for (;;) {
+      const int i0 = next.fetch_add(16);
+      if (i0 >= n) break;
+      for (int i = i0; i < std::min(n, i0 + 16); ++i) fn(i);
+    }
+  };
+  if (nthreads > 1) {
+    std::vector<std::thread> pool;
+    for (int t = 0; t < nthreads; ++t) pool.emplace_back(worker);
+    for (std::thread& th : pool) th.join();
+  } else {
+    worker();
+  }
+}
+
+int host_threads_for(size_t items) {
+  const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  return (int)std::min<uint64_t>(hw, std::max<uint64_t>(1, items / 20000));
+}
+}  // namespace
+
+// Host plan of gaps [g0, g1) (already validated): seed weights, word and key
+// ranges of the gaps that are searched.
+static int gs_plan(const int64_t* gaps, uint64_t g0, uint64_t g1, GsChunk& ch) {
+  for (uint64_t g = g0; g < g1; ++g) {
     const int64_t* q = gaps + 4 * g;
-    if (q[0] < 0 || q[1] < 0 || q[2] < 0 || q[3] < 0 || (uint64_t)(q[0] + q[1]) > na ||
-        (uint64_t)(q[2] + q[3]) > nb)
-      return report_error(MVG_ERR_RANGE, "gap outside its genome");
-    if (q[1] >= (1ll << 31) || q[3] >= (1ll << 31)) return report_error(MVG_ERR_ARG, "gap longer than 2^31-1");
     const unsigned w = mvg_default_seed_weight((uint64_t)(q[1] + q[3]) / 2);
     if (w < (unsigned)kGsMinWeight) continue;  // the reference returns without searching
     if (w > 15)
@@ -396,177 +425,222 @@ int gap_anchor_search_dev(Ctx* c, const uint8_t* d_a, uint64_t na, const uint8_t
       const uint64_t len = (uint64_t)q[1 + 2 * s];
       d.src[s] = (uint64_t)q[2 * s];
       d.len[s] = (uint32_t)len;
-      d.word[s] = words[s];
-      d.key[s] = keys[s];
-      words[s] += packed_words(len);  // translate32's layout: two zero words after each gap
-      keys[s] += len >= (uint64_t)L ? len - L + 1 : 0;
+      d.word[s] = ch.words[s];
+      d.key[s] = ch.keys[s];
+      ch.words[s] += packed_words(len);  // translate32's layout: two zero words after each gap
+      ch.keys[s] += len >= (uint64_t)L ? len - L + 1 : 0;
     }
-    gd.push_back(d);
-    gid.push_back((uint32_t)g);
+    ch.gd.push_back(d);
+    ch.gid.push_back((uint32_t)g);
   }
-  std::vector<uint64_t> per_gap(ngaps, 0);
-  const int ng = (int)gd.size();
+  return 0;
+}
+
+// Device pass of one chunk, from packing to the emitted rows, which are
+// copied to the host with the segment tables.  Synchronous.
+static int gs_device(Ctx* c, const uint8_t* d_a, const uint8_t* d_b, GsChunk& ch) {
+  const int ng = (int)ch.gd.size();
+  if (ng == 0) return 0;
+  const std::vector<GapDev>& gd = ch.gd;
+  const uint64_t* words = ch.words;
+  const uint64_t* keys = ch.keys;
+  std::vector<int64_t>& rows = ch.rows;
+  std::vector<uint32_t>& seg_gap = ch.seg_gap;
+  std::vector<uint32_t>& seg_n = ch.seg_n;
   const uint64_t nkeys = keys[0] + keys[1];
-  std::vector<int64_t> rows;
-  std::vector<uint32_t> seg_gap, seg_n;
-  if (ng > 0) {
-    if (nkeys >= (1ull << 31)) return report_error(MVG_ERR_ARG, "gaps hold more than 2^31 seed positions");
-    Workspace& ws = c->ws;
-    GapDev* d_gaps = (GapDev*)ws.get(c, kGsSlot + 0, gd.size() * sizeof(GapDev));
-    uint32_t* pa = (uint32_t*)ws.get(c, kGsSlot + 1, words[0] * 4 + 64);
-    uint32_t* pb = (uint32_t*)ws.get(c, kGsSlot + 2, words[1] * 4 + 64);
-    uint64_t* k0 = (uint64_t*)ws.get(c, kGsSlot + 3, nkeys * 8);
-    uint64_t* k1 = (uint64_t*)ws.get(c, kGsSlot + 4, nkeys * 8);
-    uint32_t* v0 = (uint32_t*)ws.get(c, kGsSlot + 5, nkeys * 4);
-    uint32_t* v1 = (uint32_t*)ws.get(c, kGsSlot + 6, nkeys * 4);
-    int gbits = 1;
-    while ((1ll << gbits) < ng) ++gbits;
-    const int64_t ptiles = ((int64_t)nkeys + kPairTile - 1) / kPairTile;
-    uint32_t* sscr = (uint32_t*)ws.get(c, kGsSlot + 7, sort_scratch_words((int64_t)nkeys, 32 + gbits) * 4);
-    uint32_t* tsum = (uint32_t*)ws.get(c, kGsSlot + 8, (ptiles + 4) * 4 + 64);
-    if (!d_gaps || !pa || !pb || !k0 || !k1 || !v0 || !v1 || !sscr || !tsum)
+  int rc = 0;
+  if (nkeys >= (1ull << 31)) return report_error(MVG_ERR_ARG, "gaps hold more than 2^31 seed positions");
+  Workspace& ws = c->ws;
+  GapDev* d_gaps = (GapDev*)ws.get(c, kGsSlot + 0, gd.size() * sizeof(GapDev));
+  uint32_t* pa = (uint32_t*)ws.get(c, kGsSlot + 1, words[0] * 4 + 64);
+  uint32_t* pb = (uint32_t*)ws.get(c, kGsSlot + 2, words[1] * 4 + 64);
+  uint64_t* k0 = (uint64_t*)ws.get(c, kGsSlot + 3, nkeys * 8);
+  uint64_t* k1 = (uint64_t*)ws.get(c, kGsSlot + 4, nkeys * 8);
+  uint32_t* v0 = (uint32_t*)ws.get(c, kGsSlot + 5, nkeys * 4);
+  uint32_t* v1 = (uint32_t*)ws.get(c, kGsSlot + 6, nkeys * 4);
+  int gbits = 1;
+  while ((1ll << gbits) < ng) ++gbits;
+  const int64_t ptiles = ((int64_t)nkeys + kPairTile - 1) / kPairTile;
+  uint32_t* sscr = (uint32_t*)ws.get(c, kGsSlot + 7, sort_scratch_words((int64_t)nkeys, 32 + gbits) * 4);
+  uint32_t* tsum = (uint32_t*)ws.get(c, kGsSlot + 8, (ptiles + 4) * 4 + 64);
+  if (!d_gaps || !pa || !pb || !k0 || !k1 || !v0 || !v1 || !sscr || !tsum)
+    return report_error(MVG_ERR_NOMEM, "workspace allocation failed");
+  uint32_t* d_npairs = tsum + ptiles + 2;
+  MVG_CUDA_TRY(cudaMemsetAsync(c->d_err, 0, 4, c->stream));
+  stage_mark(c, "gs_pack");
+  MVG_CUDA_TRY(cudaMemcpyAsync(d_gaps, gd.data(), gd.size() * sizeof(GapDev), cudaMemcpyHostToDevice, c->stream));
+  k_gs_pack<<<grid_for(words[0] + words[1], 256), 256, 0, c->stream>>>(d_a, d_b, d_gaps, ng, words[0], words[1],
+                                                                        pa, pb, c->d_err);
+  c->launches++;
+  if (keys[0] == 0 || keys[1] == 0) {  // no seed in one genome's gaps: no match anywhere
+    MVG_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    return check_device_error(c);
+  }
+  stage_mark(c, "gs_keys");
+  k_gs_keys<<<grid_for(nkeys, 256), 256, 0, c->stream>>>(pa, pb, d_gaps, ng, keys[0], keys[1], k0, v0);
+  c->launches++;
+  stage_mark(c, "gs_seed_sort");
+  int which = sort_pairs<uint64_t>(k0, v0, k1, v1, (int64_t)nkeys, 32 + gbits, sscr, c->stream, &c->launches,
+                                   c->d_err);
+  const uint64_t* sk = which ? k1 : k0;
+  const uint32_t* sv = which ? v1 : v0;
+  stage_mark(c, "gs_pairs");
+  k_pair_count<uint64_t><<<(unsigned)ptiles, 256, 0, c->stream>>>(sk, (int64_t)nkeys, tsum);
+  k_scan_bsums<<<1, 256, 0, c->stream>>>(tsum, ptiles, d_npairs);
+  c->launches += 2;
+  MVG_CUDA_TRY(cudaMemcpyAsync(c->h_scalars, d_npairs, 4, cudaMemcpyDeviceToHost, c->stream));
+  MVG_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  if ((rc = check_device_error(c))) return rc;
+  const int64_t npairs = (int64_t)(uint32_t)c->h_scalars[0];
+  if (npairs > 0) {
+    Mhe* mhe = (Mhe*)ws.get(c, kGsSlot + 9, npairs * sizeof(Mhe));
+    Mhe* ent = (Mhe*)ws.get(c, kGsSlot + 10, npairs * sizeof(Mhe));
+    uint64_t* bk0 = (uint64_t*)ws.get(c, kGsSlot + 11, npairs * 8);
+    uint64_t* bk1 = (uint64_t*)ws.get(c, kGsSlot + 12, npairs * 8);
+    uint32_t* o0 = (uint32_t*)ws.get(c, kGsSlot + 13, npairs * 4);
+    uint32_t* o1 = (uint32_t*)ws.get(c, kGsSlot + 14, npairs * 4);
+    // per entry: segment flag, segment index; per segment: start, gap, entries, output offset
+    uint32_t* segtab = (uint32_t*)ws.get(c, kGsSlot + 15, (size_t)npairs * 4 * 6 + scan_scratch_words(npairs) * 8 + 256);
+    if (!mhe || !ent || !bk0 || !bk1 || !o0 || !o1 || !segtab)
       return report_error(MVG_ERR_NOMEM, "workspace allocation failed");
-    uint32_t* d_npairs = tsum + ptiles + 2;
-    MVG_CUDA_TRY(cudaMemsetAsync(c->d_err, 0, 4, c->stream));
-    stage_mark(c, "gs_pack");
-    MVG_CUDA_TRY(cudaMemcpyAsync(d_gaps, gd.data(), gd.size() * sizeof(GapDev), cudaMemcpyHostToDevice, c->stream));
-    k_gs_pack<<<grid_for(words[0] + words[1], 256), 256, 0, c->stream>>>(d_a, d_b, d_gaps, ng, words[0], words[1],
-                                                                          pa, pb, c->d_err);
+    uint32_t* flag = segtab;
+    uint32_t* sidx = flag + npairs;
+    uint32_t* seg_start = sidx + npairs;
+    uint32_t* d_seg_gap = seg_start + npairs;
+    uint32_t* nent = d_seg_gap + npairs;
+    uint32_t* ooff = nent + npairs;
+    uint32_t* scr = ooff + npairs;
+    uint32_t* totals = scr + scan_scratch_words(npairs) * 2;  // [0] segments, [1] entries, [2] counter
+    k_gs_pair_emit<<<(unsigned)ptiles, 256, 0, c->stream>>>(sk, sv, (int64_t)nkeys, tsum, d_gaps, mhe, bk0, o0);
     c->launches++;
-    if (keys[0] == 0 || keys[1] == 0) {  // no seed in one genome's gaps: no match anywhere
-      MVG_CUDA_TRY(cudaStreamSynchronize(c->stream));
-      if ((rc = check_device_error(c))) return rc;
-      goto host_filter;
-    }
-    stage_mark(c, "gs_keys");
-    k_gs_keys<<<grid_for(nkeys, 256), 256, 0, c->stream>>>(pa, pb, d_gaps, ng, keys[0], keys[1], k0, v0);
-    c->launches++;
-    stage_mark(c, "gs_seed_sort");
-    int which = sort_pairs<uint64_t>(k0, v0, k1, v1, (int64_t)nkeys, 32 + gbits, sscr, c->stream, &c->launches,
-                                     c->d_err);
-    const uint64_t* sk = which ? k1 : k0;
-    const uint32_t* sv = which ? v1 : v0;
-    stage_mark(c, "gs_pairs");
-    k_pair_count<uint64_t><<<(unsigned)ptiles, 256, 0, c->stream>>>(sk, (int64_t)nkeys, tsum);
-    k_scan_bsums<<<1, 256, 0, c->stream>>>(tsum, ptiles, d_npairs);
+    stage_mark(c, "gs_bucket_sort");
+    which = sort_pairs<uint64_t>(bk0, o0, bk1, o1, npairs, 16 + gbits, sscr, c->stream, &c->launches, c->d_err);
+    const uint64_t* sbk = which ? bk1 : bk0;
+    const uint32_t* sorted = which ? o1 : o0;
+    k_gs_seg_flags<<<grid_for(npairs, 256), 256, 0, c->stream>>>(sbk, npairs, flag);
+    exclusive_scan(flag, sidx, npairs, scr, totals, c->stream, &c->launches);
+    k_gs_seg_fill<<<grid_for(npairs, 256), 256, 0, c->stream>>>(sbk, npairs, flag, sidx, seg_start, d_seg_gap);
     c->launches += 2;
-    MVG_CUDA_TRY(cudaMemcpyAsync(c->h_scalars, d_npairs, 4, cudaMemcpyDeviceToHost, c->stream));
+    MVG_CUDA_TRY(cudaMemcpyAsync(c->h_scalars, totals, 4, cudaMemcpyDeviceToHost, c->stream));
+    MVG_CUDA_TRY(cudaMemsetAsync(totals + 2, 0, 4, c->stream));
+    MVG_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    const uint32_t nseg = (uint32_t)c->h_scalars[0];
+    int sms = 0;
+    MVG_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device));
+    const uint32_t rblocks = std::min<uint32_t>((nseg + 7) / 8, (uint32_t)sms * 8);
+    stage_mark(c, "gs_replay");
+    k_gs_replay<<<rblocks, 256, 0, c->stream>>>(pa, pb, d_gaps, mhe, sorted, seg_start, d_seg_gap, nseg,
+                                                (uint32_t)npairs, ent, nent, totals + 2);
+    stage_mark(c, "gs_emit");
+    exclusive_scan(nent, ooff, nseg, scr, totals + 1, c->stream, &c->launches);
+    MVG_CUDA_TRY(cudaMemcpyAsync(c->h_scalars, totals + 1, 4, cudaMemcpyDeviceToHost, c->stream));
+    MVG_CUDA_TRY(cudaStreamSynchronize(c->stream));
+    const uint64_t nrows = (uint32_t)c->h_scalars[0];
+    int64_t* d_rows = (int64_t*)ws.get(c, kGsSlot + 3, nrows * 24 + 24);  // the key buffer is free again
+    if (!d_rows) return report_error(MVG_ERR_NOMEM, "workspace allocation failed");
+    k_gs_emit<<<grid_for((uint64_t)nseg * 32, 256), 256, 0, c->stream>>>(ent, seg_start, nent, ooff, nseg, d_rows);
+    c->launches += 2;
+    rows.resize(nrows * 3);
+    seg_gap.resize(nseg);
+    seg_n.resize(nseg);
+    if (nrows) MVG_CUDA_TRY(cudaMemcpyAsync(rows.data(), d_rows, nrows * 24, cudaMemcpyDeviceToHost, c->stream));
+    MVG_CUDA_TRY(cudaMemcpyAsync(seg_gap.data(), d_seg_gap, (size_t)nseg * 4, cudaMemcpyDeviceToHost, c->stream));
+    MVG_CUDA_TRY(cudaMemcpyAsync(seg_n.data(), nent, (size_t)nseg * 4, cudaMemcpyDeviceToHost, c->stream));
+    stage_mark(c, "gs_copy");
     MVG_CUDA_TRY(cudaStreamSynchronize(c->stream));
     if ((rc = check_device_error(c))) return rc;
-    const int64_t npairs = (int64_t)(uint32_t)c->h_scalars[0];
-    if (npairs > 0) {
-      Mhe* mhe = (Mhe*)ws.get(c, kGsSlot + 9, npairs * sizeof(Mhe));
-      Mhe* ent = (Mhe*)ws.get(c, kGsSlot + 10, npairs * sizeof(Mhe));
-      uint64_t* bk0 = (uint64_t*)ws.get(c, kGsSlot + 11, npairs * 8);
-      uint64_t* bk1 = (uint64_t*)ws.get(c, kGsSlot + 12, npairs * 8);
-      uint32_t* o0 = (uint32_t*)ws.get(c, kGsSlot + 13, npairs * 4);
-      uint32_t* o1 = (uint32_t*)ws.get(c, kGsSlot + 14, npairs * 4);
-      // per entry: segment flag, segment index; per segment: start, gap, entries, output offset
-      uint32_t* segtab = (uint32_t*)ws.get(c, kGsSlot + 15, (size_t)npairs * 4 * 6 + scan_scratch_words(npairs) * 8 + 256);
-      if (!mhe || !ent || !bk0 || !bk1 || !o0 || !o1 || !segtab)
-        return report_error(MVG_ERR_NOMEM, "workspace allocation failed");
-      uint32_t* flag = segtab;
-      uint32_t* sidx = flag + npairs;
-      uint32_t* seg_start = sidx + npairs;
-      uint32_t* d_seg_gap = seg_start + npairs;
-      uint32_t* nent = d_seg_gap + npairs;
-      uint32_t* ooff = nent + npairs;
-      uint32_t* scr = ooff + npairs;
-      uint32_t* totals = scr + scan_scratch_words(npairs) * 2;  // [0] segments, [1] entries, [2] counter
-      k_gs_pair_emit<<<(unsigned)ptiles, 256, 0, c->stream>>>(sk, sv, (int64_t)nkeys, tsum, d_gaps, mhe, bk0, o0);
-      c->launches++;
-      stage_mark(c, "gs_bucket_sort");
-      which = sort_pairs<uint64_t>(bk0, o0, bk1, o1, npairs, 16 + gbits, sscr, c->stream, &c->launches, c->d_err);
-      const uint64_t* sbk = which ? bk1 : bk0;
-      const uint32_t* sorted = which ? o1 : o0;
-      k_gs_seg_flags<<<grid_for(npairs, 256), 256, 0, c->stream>>>(sbk, npairs, flag);
-      exclusive_scan(flag, sidx, npairs, scr, totals, c->stream, &c->launches);
-      k_gs_seg_fill<<<grid_for(npairs, 256), 256, 0, c->stream>>>(sbk, npairs, flag, sidx, seg_start, d_seg_gap);
-      c->launches += 2;
-      MVG_CUDA_TRY(cudaMemcpyAsync(c->h_scalars, totals, 4, cudaMemcpyDeviceToHost, c->stream));
-      MVG_CUDA_TRY(cudaMemsetAsync(totals + 2, 0, 4, c->stream));
-      MVG_CUDA_TRY(cudaStreamSynchronize(c->stream));
-      const uint32_t nseg = (uint32_t)c->h_scalars[0];
-      int sms = 0;
-      MVG_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device));
-      const uint32_t rblocks = std::min<uint32_t>((nseg + 7) / 8, (uint32_t)sms * 8);
-      stage_mark(c, "gs_replay");
-      k_gs_replay<<<rblocks, 256, 0, c->stream>>>(pa, pb, d_gaps, mhe, sorted, seg_start, d_seg_gap, nseg,
-                                                  (uint32_t)npairs, ent, nent, totals + 2);
-      stage_mark(c, "gs_emit");
-      exclusive_scan(nent, ooff, nseg, scr, totals + 1, c->stream, &c->launches);
-      MVG_CUDA_TRY(cudaMemcpyAsync(c->h_scalars, totals + 1, 4, cudaMemcpyDeviceToHost, c->stream));
-      MVG_CUDA_TRY(cudaStreamSynchronize(c->stream));
-      const uint64_t nrows = (uint32_t)c->h_scalars[0];
-      int64_t* d_rows = (int64_t*)ws.get(c, kGsSlot + 3, nrows * 24 + 24);  // the key buffer is free again
-      if (!d_rows) return report_error(MVG_ERR_NOMEM, "workspace allocation failed");
-      k_gs_emit<<<grid_for((uint64_t)nseg * 32, 256), 256, 0, c->stream>>>(ent, seg_start, nent, ooff, nseg, d_rows);
-      c->launches += 2;
-      rows.resize(nrows * 3);
-      seg_gap.resize(nseg);
-      seg_n.resize(nseg);
-      if (nrows) MVG_CUDA_TRY(cudaMemcpyAsync(rows.data(), d_rows, nrows * 24, cudaMemcpyDeviceToHost, c->stream));
-      MVG_CUDA_TRY(cudaMemcpyAsync(seg_gap.data(), d_seg_gap, (size_t)nseg * 4, cudaMemcpyDeviceToHost, c->stream));
-      MVG_CUDA_TRY(cudaMemcpyAsync(seg_n.data(), nent, (size_t)nseg * 4, cudaMemcpyDeviceToHost, c->stream));
-      stage_end(c);
-      MVG_CUDA_TRY(cudaStreamSynchronize(c->stream));
-      if ((rc = check_device_error(c))) return rc;
-    }
   }
-host_filter:
-  HostSpan span(c, "gs_filter");
-  // host: per gap, overlap elimination and length filter, then genome
-  // coordinates.  Gaps are independent and their anchor counts differ by
-  // orders of magnitude, so host threads claim runs of gaps from a counter,
-  // each converting, filtering and shifting its gaps' rows in place; a
-  // second pass, claimed the same way, copies the survivors out in gap order.
-  std::vector<Anchor> anc(rows.size() / 3);
-  std::vector<size_t> gap_r(ng + 1, 0);  // rows of searched gap gi: [gap_r[gi], gap_r[gi+1])
+  return 0;
+}
+
+// Host pass of one chunk: per gap, overlap elimination and length filter,
+// then genome coordinates.  Gaps are independent and their anchor counts
+// differ by orders of magnitude, so host threads claim runs of gaps, each
+// converting, filtering and shifting its gaps' rows in place.
+static void gs_filter(GsChunk& ch) {
+  const int ng = (int)ch.gd.size();
+  ch.anc.resize(ch.rows.size() / 3);
+  ch.gap_r.assign(ng + 1, 0);  // rows of searched gap gi: [gap_r[gi], gap_r[gi+1])
   for (size_t s = 0, r = 0, gi = 0; gi < (size_t)ng; ++gi) {
-    while (s < seg_gap.size() && seg_gap[s] == (uint32_t)gi) r += seg_n[s++];
-    gap_r[gi + 1] = r;
+    while (s < ch.seg_gap.size() && ch.seg_gap[s] == (uint32_t)gi) r += ch.seg_n[s++];
+    ch.gap_r[gi + 1] = r;
   }
-  std::vector<int64_t> nkept(ng, 0);
-  const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
-  const int nthreads = (int)std::min<uint64_t>(hw, std::max<uint64_t>(1, anc.size() / 20000));
-  constexpr int kGapRun = 16;  // gaps per claim
-  auto run_claimed = [&](auto&& per_gap_fn) {
-    std::atomic<int> next{0};
-    auto worker = [&]() {
-      for (;;) {
-        const int g0 = next.fetch_add(kGapRun);
-        if (g0 >= ng) break;
-        for (int gi = g0; gi < std::min(ng, g0 + kGapRun); ++gi) per_gap_fn(gi);
-      }
-    };
-    if (nthreads > 1) {
-      std::vector<std::thread> pool;
-      for (int t = 0; t < nthreads; ++t) pool.emplace_back(worker);
-      for (std::thread& th : pool) th.join();
-    } else {
-      worker();
-    }
-  };
-  run_claimed([&](int gi) {
+  ch.nkept.assign(ng, 0);
+  run_claimed(ng, host_threads_for(ch.anc.size()), [&](int gi) {
     thread_local std::vector<Anchor*> scratch;
-    const size_t r0 = gap_r[gi], r1 = gap_r[gi + 1];
-    for (size_t k = r0; k < r1; ++k) anc[k] = Anchor{{rows[3 * k], rows[3 * k + 1]}, rows[3 * k + 2]};
-    const int64_t k = filter_gap(anc.data() + r0, (int64_t)(r1 - r0), scratch);
-    const GapDev& d = gd[gi];
+    const size_t r0 = ch.gap_r[gi], r1 = ch.gap_r[gi + 1];
+    for (size_t k = r0; k < r1; ++k)
+      ch.anc[k] = Anchor{{ch.rows[3 * k], ch.rows[3 * k + 1]}, ch.rows[3 * k + 2]};
+    const int64_t k = filter_gap(ch.anc.data() + r0, (int64_t)(r1 - r0), scratch);
+    const GapDev& d = ch.gd[gi];
     for (int64_t u = 0; u < k; ++u)
       for (int q = 0; q < 2; ++q) {
-        int64_t& x = anc[r0 + u].s[q];
+        int64_t& x = ch.anc[r0 + u].s[q];
         x = x > 0 ? x + (int64_t)d.src[q] : x - (int64_t)d.src[q];
       }
-    nkept[gi] = k;
+    ch.nkept[gi] = k;
   });
-  uint64_t total = 0;
-  std::vector<uint64_t> obase(ng + 1, 0);  // output row of each searched gap's first survivor
-  for (int gi = 0; gi < ng; ++gi) {
-    per_gap[gid[gi]] = (uint64_t)nkept[gi];
-    total += (uint64_t)nkept[gi];
-    obase[gi + 1] = total;
+}
+
+// Gaps are searched in up to four chunks of about equal sequence: the host
+// pass of one chunk runs on host threads while the device pass of the next
+// runs on the GPU.
+int gap_anchor_search_dev(Ctx* c, const uint8_t* d_a, uint64_t na, const uint8_t* d_b, uint64_t nb,
+                          const int64_t* gaps, uint64_t ngaps, int64_t* out, uint64_t cap, uint64_t* gap_off,
+                          uint64_t* count) {
+  *count = 0;
+  stage_begin_call(c);
+  if (ngaps >= (1ull << 31)) return report_error(MVG_ERR_ARG, "too many gaps");
+  int rc = gs_upload_tables(c->device);
+  if (rc) return rc;
+  uint64_t total_bases = 0;
+  for (uint64_t g = 0; g < ngaps; ++g) {
+    const int64_t* q = gaps + 4 * g;
+    if (q[0] < 0 || q[1] < 0 || q[2] < 0 || q[3] < 0 || (uint64_t)(q[0] + q[1]) > na ||
+        (uint64_t)(q[2] + q[3]) > nb)
+      return report_error(MVG_ERR_RANGE, "gap outside its genome");
+    if (q[1] >= (1ll << 31) || q[3] >= (1ll << 31)) return report_error(MVG_ERR_ARG, "gap longer than 2^31-1");
+    total_bases += (uint64_t)(q[1] + q[3]);
   }
+  const int nchunks = (int)std::max<uint64_t>(1, std::min<uint64_t>(4, total_bases / (32ull << 20)));
+  std::vector<uint64_t> bound(nchunks + 1, ngaps);
+  bound[0] = 0;
+  for (uint64_t g = 0, acc = 0, k = 1; g < ngaps && k < (uint64_t)nchunks; ++g) {
+    acc += (uint64_t)(gaps[4 * g + 1] + gaps[4 * g + 3]);
+    if (acc * nchunks >= total_bases * k) bound[k++] = g + 1;
+  }
+  std::vector<GsChunk> chunks(nchunks);
+  std::thread filt;  // the host pass of the previous chunk
+  struct Joiner {
+    std::thread& t;
+    ~Joiner() {
+      if (t.joinable()) t.join();
+    }
+  } joiner{filt};
+  for (int k = 0; k < nchunks; ++k) {
+    if ((rc = gs_plan(gaps, bound[k], bound[k + 1], chunks[k]))) return rc;
+    if ((rc = gs_device(c, d_a, d_b, chunks[k]))) return rc;
+    HostSpan wait(c, "gs_filter_wait");
+    if (filt.joinable()) filt.join();
+    filt = std::thread(gs_filter, std::ref(chunks[k]));
+  }
+  {
+    HostSpan wait(c, "gs_filter_wait");
+    filt.join();
+  }
+  stage_end(c);
+  std::vector<uint64_t> per_gap(ngaps, 0);
+  uint64_t total = 0;
+  std::vector<std::pair<int, int>> where;  // (chunk, searched gap) in caller order
+  std::vector<uint64_t> obase;             // output row of each searched gap's first survivor
+  for (int k = 0; k < nchunks; ++k)
+    for (size_t gi = 0; gi < chunks[k].gd.size(); ++gi) {
+      const int64_t n = chunks[k].nkept[gi];
+      per_gap[chunks[k].gid[gi]] = (uint64_t)n;
+      where.push_back({k, (int)gi});
+      obase.push_back(total);
+      total += (uint64_t)n;
+    }
   if (gap_off) {
     gap_off[0] = 0;
     for (uint64_t g = 0; g < ngaps; ++g) gap_off[g + 1] = gap_off[g] + per_gap[g];
@@ -574,10 +648,12 @@ host_filter:
   *count = total;
   if (total > cap) return report_error(MVG_ERR_CAPACITY, "anchor output buffer too small");
   // searched-gap order is the caller's gap order
-  run_claimed([&](int gi) {
-    for (int64_t u = 0; u < nkept[gi]; ++u) {
-      const Anchor& x = anc[gap_r[gi] + u];
-      int64_t* o = out + 3 * (obase[gi] + (uint64_t)u);
+  run_claimed((int)where.size(), host_threads_for(total), [&](int i) {
+    const GsChunk& ch = chunks[where[i].first];
+    const int gi = where[i].second;
+    for (int64_t u = 0; u < ch.nkept[gi]; ++u) {
+      const Anchor& x = ch.anc[ch.gap_r[gi] + u];
+      int64_t* o = out + 3 * (obase[i] + (uint64_t)u);
       o[0] = x.s[0];
       o[1] = x.s[1];
       o[2] = x.len;
