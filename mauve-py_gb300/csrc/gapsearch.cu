@@ -99,10 +99,12 @@ __global__ void k_gs_pack(const uint8_t* __restrict__ ga, const uint8_t* __restr
 }
 
 // One thread per seed position of all gaps (A positions, then B positions):
-// key = gap << 32 | (seed bits, strand) << 1 | genome, value = position in
-// the gap sequence.  The (2w+1)-bit SML key orders as the reference's mers.
+// key = gap << kshift | (seed bits, strand) << 1 | genome, value = position
+// in the gap sequence, kshift = 2 * (largest seed weight) + 2 so that the
+// sort covers no unused bits.  The (2w+1)-bit SML key orders as the
+// reference's mers.
 __global__ void k_gs_keys(const uint32_t* __restrict__ pa, const uint32_t* __restrict__ pb,
-                          const GapDev* __restrict__ gaps, int ngaps, uint64_t keys_a, uint64_t keys_b,
+                          const GapDev* __restrict__ gaps, int ngaps, uint64_t keys_a, uint64_t keys_b, int kshift,
                           uint64_t* __restrict__ keys, uint32_t* __restrict__ vals) {
   const uint64_t total = keys_a + keys_b, stride = (uint64_t)gridDim.x * blockDim.x;
   for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += stride) {
@@ -114,7 +116,7 @@ __global__ void k_gs_keys(const uint32_t* __restrict__ pa, const uint32_t* __res
     const uint64_t p = k - d.key[side];
     const uint64_t m = canonical_mer((side ? pb : pa) + d.word[side], p, s);
     const uint64_t sml = ((m >> (64 - 2 * s.w)) << 1) | (m & 1ull);
-    keys[t] = ((uint64_t)g << 32) | (sml << 1) | (uint64_t)side;
+    keys[t] = ((uint64_t)g << kshift) | (sml << 1) | (uint64_t)side;
     vals[t] = (uint32_t)p;
   }
 }
@@ -125,7 +127,7 @@ __global__ void k_gs_keys(const uint32_t* __restrict__ pa, const uint32_t* __res
 // puts the gap above the bucket so one sort groups (gap, bucket) segments.
 __global__ void __launch_bounds__(256) k_gs_pair_emit(const uint64_t* __restrict__ keys,
                                                       const uint32_t* __restrict__ pos, int64_t n,
-                                                      const uint32_t* __restrict__ tstart,
+                                                      const uint32_t* __restrict__ tstart, int kshift,
                                                       const GapDev* __restrict__ gaps, Mhe* __restrict__ mhe,
                                                       uint64_t* __restrict__ bkey, uint32_t* __restrict__ order) {
   const int64_t i0 = (int64_t)blockIdx.x * kPairTile + (int64_t)threadIdx.x * kPairItems;
@@ -142,7 +144,7 @@ __global__ void __launch_bounds__(256) k_gs_pair_emit(const uint64_t* __restrict
     const uint64_t k0 = keys[i], k1 = keys[i + 1];
     const bool a_first = (k0 & 1ull) == 0;
     const uint64_t ka = a_first ? k0 : k1, kb = a_first ? k1 : k0;
-    const uint32_t g = (uint32_t)(k0 >> 32);
+    const uint32_t g = (uint32_t)(k0 >> kshift);
     Mhe m;
     m.s0 = (int64_t)(a_first ? pos[i] : pos[i + 1]) + 1;
     m.s1 = (int64_t)(a_first ? pos[i + 1] : pos[i]) + 1;
@@ -460,8 +462,14 @@ static int gs_device(Ctx* c, const uint8_t* d_a, const uint8_t* d_b, GsChunk& ch
   uint32_t* v1 = (uint32_t*)ws.get(c, kGsSlot + 6, nkeys * 4);
   int gbits = 1;
   while ((1ll << gbits) < ng) ++gbits;
+  // (seed bits, strand, genome) below the gap index; a seed's bits are its
+  // pattern's selected positions, which for some table entries exceed the
+  // nominal weight (weight 11's rank-0 seed selects 12)
+  int wmax = 0;
+  for (const GapDev& d : gd) wmax = std::max(wmax, __builtin_popcountll(mvg_get_seed((int)d.w, 0)));
+  const int kshift = 2 * wmax + 2;
   const int64_t ptiles = ((int64_t)nkeys + kPairTile - 1) / kPairTile;
-  uint32_t* sscr = (uint32_t*)ws.get(c, kGsSlot + 7, sort_scratch_words((int64_t)nkeys, 32 + gbits) * 4);
+  uint32_t* sscr = (uint32_t*)ws.get(c, kGsSlot + 7, sort_scratch_words((int64_t)nkeys, std::max(kshift, 16) + gbits) * 4);  // both sorts below
   uint32_t* tsum = (uint32_t*)ws.get(c, kGsSlot + 8, (ptiles + 4) * 4 + 64);
   if (!d_gaps || !pa || !pb || !k0 || !k1 || !v0 || !v1 || !sscr || !tsum)
     return report_error(MVG_ERR_NOMEM, "workspace allocation failed");
@@ -477,10 +485,11 @@ static int gs_device(Ctx* c, const uint8_t* d_a, const uint8_t* d_b, GsChunk& ch
     return check_device_error(c);
   }
   stage_mark(c, "gs_keys");
-  k_gs_keys<<<grid_for(nkeys, 256), 256, 0, c->stream>>>(pa, pb, d_gaps, ng, keys[0], keys[1], k0, v0);
+  k_gs_keys<<<grid_for(nkeys, 256), 256, 0, c->stream>>>(pa, pb, d_gaps, ng, keys[0], keys[1], kshift, k0,
+                                                         v0);
   c->launches++;
   stage_mark(c, "gs_seed_sort");
-  int which = sort_pairs<uint64_t>(k0, v0, k1, v1, (int64_t)nkeys, 32 + gbits, sscr, c->stream, &c->launches,
+  int which = sort_pairs<uint64_t>(k0, v0, k1, v1, (int64_t)nkeys, kshift + gbits, sscr, c->stream, &c->launches,
                                    c->d_err);
   const uint64_t* sk = which ? k1 : k0;
   const uint32_t* sv = which ? v1 : v0;
@@ -511,7 +520,8 @@ static int gs_device(Ctx* c, const uint8_t* d_a, const uint8_t* d_b, GsChunk& ch
     uint32_t* ooff = nent + npairs;
     uint32_t* scr = ooff + npairs;
     uint32_t* totals = scr + scan_scratch_words(npairs) * 2;  // [0] segments, [1] entries, [2] counter
-    k_gs_pair_emit<<<(unsigned)ptiles, 256, 0, c->stream>>>(sk, sv, (int64_t)nkeys, tsum, d_gaps, mhe, bk0, o0);
+    k_gs_pair_emit<<<(unsigned)ptiles, 256, 0, c->stream>>>(sk, sv, (int64_t)nkeys, tsum, kshift, d_gaps, mhe, bk0,
+                                                            o0);
     c->launches++;
     stage_mark(c, "gs_bucket_sort");
     which = sort_pairs<uint64_t>(bk0, o0, bk1, o1, npairs, 16 + gbits, sscr, c->stream, &c->launches, c->d_err);
