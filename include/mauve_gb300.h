@@ -198,6 +198,31 @@ int mvg_gapdp_banded_dev(mvg_handle h, const uint8_t* d_seq_a, const uint64_t* d
 int mvg_gapdp_envelope_dev(mvg_handle h, const uint8_t* d_seq_a, const uint64_t* d_off_a, const uint8_t* d_seq_b,
                            const uint64_t* d_off_b, int64_t nprob, int32_t* d_scores, int32_t* d_env);
 
+/* ------------------------------------------------ recursive anchor search */
+
+/* The gaps one LCB of two genomes sends to the recursive anchor search:
+ * ProgressiveAligner::recurseOnPairs (LM/ProgressiveAligner.cpp:682-924)
+ * with getInterveningCoordinates (:566-588) and pairwiseAnchorSearch's cut
+ * of the gap sequences (:598-613).  Host code, no GPU work.
+ * row_a, row_b: the LCB's two gapped rows (ncols bytes each, '-' = gap);
+ * left_end_a/b: 1-based left end of each genome's aligned range;
+ * reverse_a/b: 1 if the genome is on the reverse strand in this LCB;
+ * genome_len_a/b: the genomes' lengths; min_gap: the reference's
+ * min_recursive_gap_length (200, LM/Aligner.cpp:183): a gap is searched when
+ * both genomes leave more than min_gap characters between two columns where
+ * both are aligned (or the LCB's end).
+ * Out: gaps[4k .. 4k+3] = (0-based start in A, length in A, 0-based start
+ * in B, length in B) in the reference's search order, ready for
+ * mvg_gap_anchor_search (an empty cut has length 0); *ngaps = their number
+ * (MVG_ERR_CAPACITY when above cap; nothing is written past cap);
+ * flanks (optional, 8 values): per genome up to two unaligned stretches at
+ * the LCB's ends (recurseOnPairs' iv_regions), 1-based [start, end), 0 where
+ * absent. */
+int mvg_recursion_gaps(const uint8_t* row_a, const uint8_t* row_b, uint64_t ncols, int64_t left_end_a,
+                       int reverse_a, int64_t left_end_b, int reverse_b, uint64_t genome_len_a,
+                       uint64_t genome_len_b, int64_t min_gap, int64_t* gaps, uint64_t cap, uint64_t* ngaps,
+                       int64_t* flanks);
+
 /* ------------------------------------------------ band-proposal network */
 
 /* The band proposal for mvg_gapdp_banded: a 528 -> 256 -> 256 -> 256 -> 2

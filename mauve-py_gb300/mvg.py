@@ -49,7 +49,8 @@ EXPORTS = ["mvg_create", "mvg_destroy", "mvg_last_error", "mvg_stream", "mvg_ker
            "mvg_set_dp_spin_limit", "mvg_gap_anchor_search", "mvg_gap_anchor_search_dev", "mvg_set_dp_graph",
            "mvg_set_dp_coop_strips", "mvg_path_rows", "mvg_path_rows_dev",
            "mvg_xmfa_write", "mvg_xmfa_write_dev", "mvg_set_mlp_tcgen05", "mvg_mlp_tcgen05_passes",
-           "mvg_set_dp_checkpoint", "mvg_set_band_whole_full_rows", "mvg_set_ring_max_rows"]
+           "mvg_set_dp_checkpoint", "mvg_set_band_whole_full_rows", "mvg_set_ring_max_rows",
+           "mvg_recursion_gaps"]
 
 TUNING_PATH = os.path.join(HERE, "dp_tuning.json")
 
@@ -96,6 +97,7 @@ def load_library(path=LIB_PATH):
         "mvg_set_dp_checkpoint": (ci, [vp, ci]),
         "mvg_set_band_whole_full_rows": (ci, [vp, i64]),
         "mvg_set_ring_max_rows": (ci, [vp, ci]),
+        "mvg_recursion_gaps": (ci, [vp, vp, u64, i64, ci, i64, ci, u64, u64, i64, vp, u64, ctypes.POINTER(u64), vp]),
         "mvg_set_mlp_tcgen05": (ci, [vp, ci]),
         "mvg_mlp_tcgen05_passes": (ci, [vp, ctypes.POINTER(ctypes.c_uint64)]),
         "mvg_set_dp_coop_strips": (ci, [vp, ci]),
@@ -185,6 +187,31 @@ def seed_length(seed):
 
 def seed_weight(seed):
     return int(load_library().mvg_seed_weight(seed))
+
+
+def recursion_gaps(row_a, row_b, left_end_a, reverse_a, left_end_b, reverse_b, genome_len_a, genome_len_b,
+                   min_gap=200):
+    """recurseOnPairs' gap finding for one LCB of two genomes (no GPU needed;
+    see mvg_recursion_gaps).  Returns (gaps int64[k, 4] as (start A, length A,
+    start B, length B), ready for Context.gap_anchor_search, and the flanks
+    int64[2, 2, 2]: per genome up to two 1-based [start, end) stretches)."""
+    a, b = _u8(row_a), _u8(row_b)
+    if len(a) != len(b):
+        raise ValueError("rows of different length")
+    L = load_library()
+    n = ctypes.c_uint64(0)
+    flanks = np.zeros(8, np.int64)
+    args = (_ptr(a), _ptr(b), len(a), int(left_end_a), int(bool(reverse_a)), int(left_end_b), int(bool(reverse_b)),
+            int(genome_len_a), int(genome_len_b), int(min_gap))
+    cap = max(1, len(a) // max(1, int(min_gap)) + 2)
+    gaps = np.zeros(4 * cap, np.int64)
+    rc = L.mvg_recursion_gaps(*args, _ptr(gaps), cap, ctypes.byref(n), _ptr(flanks))
+    if rc == MVG_ERR_CAPACITY:
+        cap = int(n.value)
+        gaps = np.zeros(4 * cap, np.int64)
+        rc = L.mvg_recursion_gaps(*args, _ptr(gaps), cap, ctypes.byref(n), _ptr(flanks))
+    _check(rc)
+    return gaps[:4 * int(n.value)].reshape(-1, 4), flanks.reshape(2, 2, 2)
 
 
 class SslistInfo(ctypes.Structure):

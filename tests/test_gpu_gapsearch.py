@@ -111,3 +111,41 @@ def test_gap_search_edge_gaps(ctx):
     with pytest.raises(IndexError):
         ctx.gap_anchor_search(a, b, np.array([(len(a) - 10, 20, 0, 100)], np.int64))
     assert ctx.gap_anchor_search(a, b, np.zeros((0, 4), np.int64))[0].shape == (0, 3)
+
+
+def test_recursion_gaps_feed_the_gap_search(ctx):
+    """One recursion round end to end: the gaps an LCB's alignment leaves
+    (mvg_recursion_gaps, recurseOnPairs' rule: both genomes more than 200
+    characters between two columns where both are aligned) are searched in
+    one call, and every gap's anchors equal the oracle's pairwiseAnchorSearch
+    on the same cut sequences, for a forward and a reverse-strand LCB."""
+    import recursion_oracle as RO
+    rng = np.random.default_rng(2024)
+    a = synth.random_bases(rng, 60_000)
+    b = synth.mutate(rng, a, 0.05, 40, 3.0, 0, (1, 2))
+    for rev_b in (False, True):
+        # an LCB whose rows alternate aligned stretches with one-sided runs
+        ra, rb = [], []
+        na = nb = 0
+        while na < 40_000 and nb < 40_000:
+            k = int(rng.integers(20, 200))
+            ra.append(b"A" * k)
+            rb.append(b"C" * k)
+            na += k
+            nb += k
+            ga, gb = int(rng.integers(0, 900)), int(rng.integers(0, 900))
+            ra.append(b"G" * ga + b"-" * gb)
+            rb.append(b"-" * ga + b"T" * gb)
+            na += ga
+            nb += gb
+        row_a = np.frombuffer(b"".join(ra), np.uint8)
+        row_b = np.frombuffer(b"".join(rb), np.uint8)
+        gaps, _ = mvg.recursion_gaps(row_a, row_b, 1001, False, 1501, rev_b, len(a), len(b))
+        og, _ = RO.recursion_gaps(row_a, row_b, 1001, False, 1501, rev_b, len(a), len(b))
+        assert [tuple(x) for x in gaps.tolist()] == og
+        assert len(gaps) > 10
+        anchors, off = ctx.gap_anchor_search(a, b, gaps)
+        for k, (sa, la, sb, lb) in enumerate(gaps.tolist()):
+            w, want = O.gap_anchor_search(a[sa:sa + la], b[sb:sb + lb])
+            want = np.zeros((0, 3), np.int64) if want is None else shift(want, sa, sb)
+            np.testing.assert_array_equal(anchors[off[k]:off[k + 1]], want, err_msg="gap %d" % k)

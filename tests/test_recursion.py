@@ -1,0 +1,101 @@
+"""Recursive anchor search gap finding (mvg_recursion_gaps) against the
+oracle's restatement of recurseOnPairs / getInterveningCoordinates.  Host
+code only: no GPU."""
+import numpy as np
+import pytest
+
+import mvg
+import recursion_oracle as RO
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    import build as pkg_build
+    pkg_build.build()
+
+
+def _rows(spec):
+    return np.frombuffer(spec[0].encode(), np.uint8), np.frombuffer(spec[1].encode(), np.uint8)
+
+
+def test_one_forward_gap_by_hand():
+    """Two aligned columns, 5 characters of A only, 5 of B only, two aligned
+    columns: the cut starts at the left anchor's own base and is one base
+    shorter than the stretch between the anchors (the reference's
+    arithmetic), in both genomes."""
+    a, b = _rows(("AC" + "GGGGG" + "-----" + "TT", "AC" + "-----" + "CCCCC" + "TT"))
+    gaps, flanks = mvg.recursion_gaps(a, b, 101, False, 201, False, 10_000, 10_000, min_gap=3)
+    np.testing.assert_array_equal(gaps, [[101, 5, 201, 5]])
+    assert not flanks.any()
+    og, of = RO.recursion_gaps(a, b, 101, False, 201, False, 10_000, 10_000, min_gap=3)
+    assert og == [tuple(x) for x in gaps.tolist()]
+
+
+def test_gap_at_or_below_min_is_not_searched():
+    a, b = _rows(("AC" + "GGG" + "---" + "TT", "AC" + "---" + "CCC" + "TT"))
+    gaps, _ = mvg.recursion_gaps(a, b, 1, False, 1, False, 100, 100, min_gap=4)
+    assert gaps.shape == (0, 4)
+
+
+def _random_lcb(rng, ncols, p_gap_a, p_gap_b, runs):
+    """Gapped rows with gap runs, so that long one-sided stretches occur."""
+    a = np.full(ncols, ord("A"), np.uint8)
+    b = np.full(ncols, ord("C"), np.uint8)
+    c = 0
+    while c < ncols:
+        ln = int(rng.integers(1, runs))
+        kind = rng.random()
+        if kind < p_gap_a:
+            a[c:c + ln] = ord("-")
+        elif kind < p_gap_a + p_gap_b:
+            b[c:c + ln] = ord("-")
+        c += ln
+    # no all-gap column
+    both_gap = (a == ord("-")) & (b == ord("-"))
+    a[both_gap] = ord("G")
+    return a, b
+
+
+@pytest.mark.parametrize("rev_a,rev_b", [(False, False), (False, True), (True, False), (True, True)])
+def test_random_lcbs_match_the_oracle(rev_a, rev_b):
+    """Gaps and flanks equal the oracle's on 200 random LCBs per orientation
+    pair: gap runs of up to 60 columns, minimum gap 8 and 30, LCBs starting
+    anywhere in the genome (including position 1, where the reference's
+    right-anchor test compares counts with coordinates)."""
+    rng = np.random.default_rng(7 + 2 * rev_a + rev_b)
+    for it in range(200):
+        ncols = int(rng.integers(0, 1500))
+        a, b = _random_lcb(rng, ncols, 0.35, 0.35, 60)
+        na, nb = int((a != ord("-")).sum()), int((b != ord("-")).sum())
+        la = 1 if it % 5 == 0 else int(rng.integers(1, 5000))
+        lb = 1 if it % 7 == 0 else int(rng.integers(1, 5000))
+        ga = la + na + int(rng.integers(0, 3))
+        gb = lb + nb + int(rng.integers(0, 3))
+        for min_gap in (8, 30):
+            gaps, flanks = mvg.recursion_gaps(a, b, la, rev_a, lb, rev_b, ga, gb, min_gap=min_gap)
+            og, of = RO.recursion_gaps(a, b, la, rev_a, lb, rev_b, ga, gb, min_gap=min_gap)
+            assert [tuple(x) for x in gaps.tolist()] == og, (it, min_gap)
+            for q in range(2):
+                want = list(of[q]) + [(0, 0)] * (2 - len(of[q]))
+                assert [tuple(x) for x in flanks[q].tolist()] == want, (it, q)
+
+
+def test_flanks_and_no_aligned_column():
+    """Unaligned ends become flanks (merged when they touch); an LCB with no
+    column where both genomes are aligned has one flank per genome and the
+    whole LCB as its only gap when long enough."""
+    a, b = _rows(("GGG" + "AC" + "TT", "---" + "AC" + "--"))
+    _, flanks = mvg.recursion_gaps(a, b, 11, False, 21, False, 100, 100, min_gap=1)
+    _, of = RO.recursion_gaps(a, b, 11, False, 21, False, 100, 100, min_gap=1)
+    np.testing.assert_array_equal(flanks[0], [[11, 14], [16, 18]])
+    assert [tuple(x) for x in flanks[0].tolist()] == list(of[0])
+    a, b = _rows(("GGGGG-----", "-----CCCCC"))
+    gaps, flanks = mvg.recursion_gaps(a, b, 5, False, 7, False, 100, 100, min_gap=2)
+    og, of = RO.recursion_gaps(a, b, 5, False, 7, False, 100, 100, min_gap=2)
+    assert [tuple(x) for x in gaps.tolist()] == og and len(og) == 1
+
+
+def test_rejects_lcb_past_the_genome():
+    a, b = _rows(("ACGT", "ACGT"))
+    with pytest.raises(Exception):
+        mvg.recursion_gaps(a, b, 10, False, 1, False, 12, 100)
