@@ -223,6 +223,22 @@ int mvg_recursion_gaps(const uint8_t* row_a, const uint8_t* row_b, uint64_t ncol
                        uint64_t genome_len_b, int64_t min_gap, int64_t* gaps, uint64_t cap, uint64_t* ngaps,
                        int64_t* flanks);
 
+/* ------------------------------------------------ anchored gap alignment */
+
+/* Anchor columns of one window of a two-genome alignment: MUSCLE's
+ * AnchoredProfileProfile as MuscleInterface::ProfileAlignFast calls it for
+ * two single-sequence profiles (muscle/libMUSCLE/anchoredpp.cpp:256-458,
+ * anchors.cpp:9-186; libMems/MuscleInterface.cpp:1053-1109), in the
+ * reference's single-precision arithmetic.  Host code, no GPU work.
+ * row_a, row_b: the window's two gapped rows (ncols bytes each, '-' or '.'
+ * = gap).  Out: cols[0 .. *n) ascending (MVG_ERR_CAPACITY when above cap).
+ * The n + 1 ranges [cols[i-1], cols[i]) (from column 0, to column ncols) are
+ * what the reference realigns: each range's rows without their gaps are one
+ * gap-DP problem (mvg_gapdp_batch), ranges of no column are skipped, and the
+ * aligned ranges are concatenated in order (MSAAppend). */
+int mvg_anchor_columns(const uint8_t* row_a, const uint8_t* row_b, uint64_t ncols, uint32_t* cols, uint64_t cap,
+                       uint64_t* n);
+
 /* ------------------------------------------------ band-proposal network */
 
 /* The band proposal for mvg_gapdp_banded: a 528 -> 256 -> 256 -> 256 -> 2

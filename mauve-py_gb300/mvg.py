@@ -50,7 +50,7 @@ EXPORTS = ["mvg_create", "mvg_destroy", "mvg_last_error", "mvg_stream", "mvg_ker
            "mvg_set_dp_coop_strips", "mvg_path_rows", "mvg_path_rows_dev",
            "mvg_xmfa_write", "mvg_xmfa_write_dev", "mvg_set_mlp_tcgen05", "mvg_mlp_tcgen05_passes",
            "mvg_set_dp_checkpoint", "mvg_set_band_whole_full_rows", "mvg_set_ring_max_rows",
-           "mvg_recursion_gaps"]
+           "mvg_recursion_gaps", "mvg_anchor_columns"]
 
 TUNING_PATH = os.path.join(HERE, "dp_tuning.json")
 
@@ -98,6 +98,7 @@ def load_library(path=LIB_PATH):
         "mvg_set_band_whole_full_rows": (ci, [vp, i64]),
         "mvg_set_ring_max_rows": (ci, [vp, ci]),
         "mvg_recursion_gaps": (ci, [vp, vp, u64, i64, ci, i64, ci, u64, u64, i64, vp, u64, ctypes.POINTER(u64), vp]),
+        "mvg_anchor_columns": (ci, [vp, vp, u64, vp, u64, ctypes.POINTER(u64)]),
         "mvg_set_mlp_tcgen05": (ci, [vp, ci]),
         "mvg_mlp_tcgen05_passes": (ci, [vp, ctypes.POINTER(ctypes.c_uint64)]),
         "mvg_set_dp_coop_strips": (ci, [vp, ci]),
@@ -212,6 +213,35 @@ def recursion_gaps(row_a, row_b, left_end_a, reverse_a, left_end_b, reverse_b, g
         rc = L.mvg_recursion_gaps(*args, _ptr(gaps), cap, ctypes.byref(n), _ptr(flanks))
     _check(rc)
     return gaps[:4 * int(n.value)].reshape(-1, 4), flanks.reshape(2, 2, 2)
+
+
+def anchor_columns(row_a, row_b):
+    """Anchor columns of a window of a two-genome alignment (no GPU needed;
+    see mvg_anchor_columns): uint32 array, ascending."""
+    a, b = _u8(row_a), _u8(row_b)
+    if len(a) != len(b):
+        raise ValueError("rows of different length")
+    n = ctypes.c_uint64(0)
+    cols = np.zeros(max(1, len(a)), np.uint32)
+    _check(load_library().mvg_anchor_columns(_ptr(a), _ptr(b), len(a), _ptr(cols), len(cols), ctypes.byref(n)))
+    return cols[:int(n.value)].copy()
+
+
+def anchored_problems(row_a, row_b):
+    """The gap-DP problems of a window cut at its anchor columns: a list of
+    (column range (left, right), A's bases, B's bases) for every range of at
+    least one column, in order (AnchoredProfileProfile's loop)."""
+    a, b = _u8(row_a), _u8(row_b)
+    cols = anchor_columns(a, b)
+    edges = [0] + [int(c) for c in cols] + [len(a)]
+    out = []
+    gap = np.frombuffer(b"-.", np.uint8)
+    for lo, hi in zip(edges[:-1], edges[1:]):
+        if hi <= lo:
+            continue
+        ra, rb = a[lo:hi], b[lo:hi]
+        out.append(((lo, hi), ra[~np.isin(ra, gap)], rb[~np.isin(rb, gap)]))
+    return out
 
 
 class SslistInfo(ctypes.Structure):
@@ -501,6 +531,49 @@ class Context:
         _check(load_library().mvg_path_rows(self._h, _ptr(seq_a), _ptr(off_a), _ptr(seq_b), _ptr(off_b), n,
                                             _ptr(flat), _ptr(poff), _ptr(plen), _ptr(ra), _ptr(rb)))
         return [(ra[poff[k]:poff[k + 1]].tobytes(), rb[poff[k]:poff[k + 1]].tobytes()) for k in range(n)]
+
+    def anchored_realign(self, windows):
+        """ProfileAlignFast(anchored) for windows of a two-genome alignment
+        (MuscleInterface::ProfileAlignFast with anchored = true,
+        libMems/MuscleInterface.cpp:1053-1109, calling AnchoredProfileProfile,
+        muscle/libMUSCLE/anchoredpp.cpp:429-552): each window is cut at its
+        anchor columns (mvg_anchor_columns), every range of every window is
+        one problem of a single batched gap-DP call on the GPU, the rows come
+        from the paths on the GPU (mvg_path_rows) and each window's ranges are
+        concatenated in order.  windows: list of (row A, row B) with '-' gaps
+        and bases A/C/G/T in either case.  Returns the realigned (row A,
+        row B) bytes of each window."""
+        code = np.full(256, 255, np.uint8)
+        for i, ch in enumerate(b"ACGT"):
+            code[ch] = code[ch | 0x20] = i
+        pieces = []  # per window: list of ("dp", problem index) or ("fixed", row A, row B)
+        sa, sb, oa, ob = [], [], [0], [0]
+        for ra, rb in windows:
+            parts = []
+            for _, a, b in anchored_problems(ra, rb):
+                if len(a) == 0 or len(b) == 0:  # nothing to align: the other side against gaps
+                    parts.append(("fixed", b"-" * len(b) if len(a) == 0 else a.tobytes(),
+                                  b.tobytes() if len(a) == 0 else b"-" * len(a)))
+                    continue
+                if (code[a] == 255).any() or (code[b] == 255).any():
+                    raise ValueError("the gap DP takes A, C, G and T only")
+                parts.append(("dp", len(oa) - 1))
+                sa.append(a)
+                sb.append(b)
+                oa.append(oa[-1] + len(a))
+                ob.append(ob[-1] + len(b))
+            pieces.append(parts)
+        rows = []
+        if len(oa) > 1:
+            chars_a, chars_b = np.concatenate(sa), np.concatenate(sb)
+            _, paths = self.gap_align_batch(code[chars_a], oa, code[chars_b], ob)
+            rows = self.path_rows(chars_a, oa, chars_b, ob, paths)
+        out = []
+        for parts in pieces:
+            ra = [rows[p[1]][0] if p[0] == "dp" else p[1] for p in parts]
+            rb = [rows[p[1]][1] if p[0] == "dp" else p[2] for p in parts]
+            out.append((b"".join(ra), b"".join(rb)))
+        return out
 
     def xmfa_write(self, file_a, file_b, starts, lengths, rows_a, rows_b, col_off, backbone_file=""):
         """WriteStandardAlignment for pairwise blocks; returns the XMFA text (bytes)."""
