@@ -239,6 +239,21 @@ int mvg_recursion_gaps(const uint8_t* row_a, const uint8_t* row_b, uint64_t ncol
 int mvg_anchor_columns(const uint8_t* row_a, const uint8_t* row_b, uint64_t ncols, uint32_t* cols, uint64_t cap,
                        uint64_t* n);
 
+/* The windows of the gapped-alignment pass over one LCB of two genomes:
+ * ProgressiveAligner::refineAlignment (LM/ProgressiveAligner.cpp:1119-1165)
+ * with removeLargeGapsPP (:1051-1117: stretches of more than 5,000 columns
+ * where the genomes are never aligned to each other become gap windows,
+ * 300 columns kept on either side) and IsDenseEnough (:1015-1038: windows
+ * halved while too long for their density; max_window_size is the
+ * reference's 20,000 unless its option changes it).  Host code.
+ * Out: windows[3k .. 3k+2] = (first column, end column, 1 for a gap window)
+ * in column order; *n their number (MVG_ERR_CAPACITY when above cap).  Each
+ * window that is not a gap window and holds bases of both genomes is
+ * realigned with mvg_anchor_columns and the gap DP; the LCB's new rows are
+ * the windows' rows in order. */
+int mvg_refine_windows(const uint8_t* row_a, const uint8_t* row_b, uint64_t ncols, double max_window_size,
+                       int64_t* windows, uint64_t cap, uint64_t* n);
+
 /* ------------------------------------------------ band-proposal network */
 
 /* The band proposal for mvg_gapdp_banded: a 528 -> 256 -> 256 -> 256 -> 2

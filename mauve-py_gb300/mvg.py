@@ -50,7 +50,7 @@ EXPORTS = ["mvg_create", "mvg_destroy", "mvg_last_error", "mvg_stream", "mvg_ker
            "mvg_set_dp_coop_strips", "mvg_path_rows", "mvg_path_rows_dev",
            "mvg_xmfa_write", "mvg_xmfa_write_dev", "mvg_set_mlp_tcgen05", "mvg_mlp_tcgen05_passes",
            "mvg_set_dp_checkpoint", "mvg_set_band_whole_full_rows", "mvg_set_ring_max_rows",
-           "mvg_recursion_gaps", "mvg_anchor_columns"]
+           "mvg_recursion_gaps", "mvg_anchor_columns", "mvg_refine_windows"]
 
 TUNING_PATH = os.path.join(HERE, "dp_tuning.json")
 
@@ -99,6 +99,7 @@ def load_library(path=LIB_PATH):
         "mvg_set_ring_max_rows": (ci, [vp, ci]),
         "mvg_recursion_gaps": (ci, [vp, vp, u64, i64, ci, i64, ci, u64, u64, i64, vp, u64, ctypes.POINTER(u64), vp]),
         "mvg_anchor_columns": (ci, [vp, vp, u64, vp, u64, ctypes.POINTER(u64)]),
+        "mvg_refine_windows": (ci, [vp, vp, u64, ctypes.c_double, vp, u64, ctypes.POINTER(u64)]),
         "mvg_set_mlp_tcgen05": (ci, [vp, ci]),
         "mvg_mlp_tcgen05_passes": (ci, [vp, ctypes.POINTER(ctypes.c_uint64)]),
         "mvg_set_dp_coop_strips": (ci, [vp, ci]),
@@ -225,6 +226,26 @@ def anchor_columns(row_a, row_b):
     cols = np.zeros(max(1, len(a)), np.uint32)
     _check(load_library().mvg_anchor_columns(_ptr(a), _ptr(b), len(a), _ptr(cols), len(cols), ctypes.byref(n)))
     return cols[:int(n.value)].copy()
+
+
+def refine_windows(row_a, row_b, max_window_size=20000.0):
+    """refineAlignment's windows of one LCB of two genomes (no GPU needed;
+    see mvg_refine_windows): int64[k, 3] rows (first column, end column,
+    1 for a gap window)."""
+    a, b = _u8(row_a), _u8(row_b)
+    if len(a) != len(b):
+        raise ValueError("rows of different length")
+    L = load_library()
+    n = ctypes.c_uint64(0)
+    cap = 16
+    while True:
+        w = np.zeros(3 * cap, np.int64)
+        rc = L.mvg_refine_windows(_ptr(a), _ptr(b), len(a), float(max_window_size), _ptr(w), cap, ctypes.byref(n))
+        if rc == MVG_ERR_CAPACITY:
+            cap = int(n.value)
+            continue
+        _check(rc)
+        return w[:3 * int(n.value)].reshape(-1, 3)
 
 
 def anchored_problems(row_a, row_b):
@@ -573,6 +594,34 @@ class Context:
             ra = [rows[p[1]][0] if p[0] == "dp" else p[1] for p in parts]
             rb = [rows[p[1]][1] if p[0] == "dp" else p[2] for p in parts]
             out.append((b"".join(ra), b"".join(rb)))
+        return out
+
+    def refine_alignment(self, lcbs, max_window_size=20000.0):
+        """The gapped-alignment pass of refineAlignment for LCBs of two
+        genomes (LM/ProgressiveAligner.cpp:1119-1230 with profile_aln, as
+        doGappedAlignment calls it at step 8 of alignProfileToProfile): each
+        LCB cut into windows (mvg_refine_windows), every window that is not a
+        gap window and holds bases of both genomes realigned with
+        anchored_realign (all windows of all LCBs in one batch), and each
+        LCB's windows concatenated.  lcbs: list of (row A, row B).  Returns
+        the new (row A, row B) bytes of each LCB."""
+        jobs, plan = [], []
+        for ra, rb in lcbs:
+            a, b = _u8(ra), _u8(rb)
+            parts = []
+            for lo, hi, gap in refine_windows(a, b, max_window_size).tolist():
+                wa, wb = a[lo:hi], b[lo:hi]
+                if not gap and (wa != ord("-")).any() and (wb != ord("-")).any():
+                    parts.append(len(jobs))
+                    jobs.append((wa, wb))
+                else:
+                    parts.append((wa.tobytes(), wb.tobytes()))
+            plan.append(parts)
+        done = self.anchored_realign(jobs) if jobs else []
+        out = []
+        for parts in plan:
+            rows = [done[p] if isinstance(p, int) else p for p in parts]
+            out.append((b"".join(r[0] for r in rows), b"".join(r[1] for r in rows)))
         return out
 
     def xmfa_write(self, file_a, file_b, starts, lengths, rows_a, rows_b, col_off, backbone_file=""):

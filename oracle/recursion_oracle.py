@@ -1,7 +1,9 @@
-"""CPU restatement of the recursive anchor search's gap finding.
+"""CPU restatement of the recursive anchor search's gap finding and of the
+gapped-alignment pass's windows.
 
 TEST INFRASTRUCTURE ONLY: the checker that tests/ compare the library's
-mvg_recursion_gaps against.  The product package never imports this module.
+mvg_recursion_gaps and mvg_refine_windows against.  The product package
+never imports this module.
 
 Follows ProgressiveAligner::recurseOnPairs (LM/ProgressiveAligner.cpp:682-924)
 for one LCB of two genomes, as libMems' Match objects behave
@@ -9,7 +11,8 @@ for one LCB of two genomes, as libMems' Match objects behave
 LM/AbstractMatch.h:209-214: End = Start + Length - 1 for a forward start,
 Start itself for a reverse one; LM/UngappedLocalAlignment.h:48-56: Length),
 and getInterveningCoordinates (LM/ProgressiveAligner.cpp:566-588) with the
-sequence cut of pairwiseAnchorSearch (:598-613).  Parity is unpinned: the
+sequence cut of pairwiseAnchorSearch (:598-613); refine_windows follows
+refineAlignment's windowing (:1015-1165).  Parity is unpinned: the
 reference's ProgressiveAligner.cpp needs boost::graph, which is not in the
 image, so the restatement is checked against the reference's source only by
 reading, line by line, in the cited ranges.
@@ -59,8 +62,8 @@ def recursion_gaps(row_a, row_b, left_a, rev_a, left_b, rev_b, glen_a, glen_b, m
     order, and the LCB's unaligned flanks per genome [(start, end), ...]
     (1-based, end exclusive)."""
     ncol = len(row_a)
-    ra = [c != ord("-") for c in row_a]
-    rb = [c != ord("-") for c in row_b]
+    ra = [bool(c != ord("-")) for c in row_a]
+    rb = [bool(c != ord("-")) for c in row_b]
     right_a = left_a + sum(ra) - 1
     right_b = left_b + sum(rb) - 1
     # outer aligned boundaries (:738-782)
@@ -168,3 +171,67 @@ def recursion_gaps(row_a, row_b, left_a, rev_a, left_b, rev_b, glen_a, glen_b, m
             if rb[col]:
                 cj += 1
     return gaps, flanks
+
+
+def refine_windows(row_a, row_b, max_window_size=20000.0):
+    """refineAlignment's windows of one LCB of two genomes
+    (LM/ProgressiveAligner.cpp:1119-1165): removeLargeGapsPP (:1051-1117,
+    max_gap_length 5000, lcb_hangover 300) then halving by IsDenseEnough
+    (:1015-1038, window sizes 200 .. max_window_size, densities .5 .. .9).
+    Returns [(first column, end column, gap window)]."""
+    ra = [bool(c != ord("-")) for c in row_a]
+    rb = [bool(c != ord("-")) for c in row_b]
+    ncol = len(ra)
+    wins = []
+    gap_cols, last, base = 0, None, 0
+    for c in range(ncol):
+        if ra[c] and rb[c]:
+            if gap_cols > 5000:
+                if last is not None:
+                    k = last + 300 - base
+                    wins.append([base, base + k, False])
+                    base += k
+                k = c - 300 - base
+                wins.append([base, base + k, True])
+                base += k
+            last = c
+            gap_cols = 0
+        else:
+            gap_cols += 1
+    if gap_cols > 5000:
+        if last is not None:
+            k = last + 300 - base
+            wins.append([base, base + k, False])
+            base += k
+        wins.append([base, ncol, True])
+    else:
+        wins.append([base, ncol, False])
+
+    def dclass(w):
+        n = w[1] - w[0]
+        na, nb = int(sum(ra[w[0]:w[1]])), int(sum(rb[w[0]:w[1]]))
+        total = float(na + nb)
+        mult = int(na > 0) + int(nb > 0)
+        den = n * float(mult)
+        density = total / den if den else float("nan")
+        thr = ((0.9 - 0.5) / (200.0 - max_window_size)) * (n - max_window_size) + 0.5
+        if density > 0.9:
+            return 2
+        if density > thr:
+            return 1
+        return 0
+
+    i = 0
+    while i < len(wins):
+        w = wins[i]
+        n = w[1] - w[0]
+        d = dclass(w)
+        if (d == 0 and n > max_window_size / 3) or (d == 1 and n > max_window_size) or \
+                (d == 2 and n > max_window_size * 3):
+            half = n // 2
+            right = [w[1] - half, w[1], w[2]]
+            w[1] -= half
+            wins.insert(i + 1, right)
+            continue
+        i += 1
+    return [tuple(w) for w in wins]

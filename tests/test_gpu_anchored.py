@@ -33,3 +33,22 @@ def test_anchored_realign_equals_the_reference(ctx):
     for k, (ra, rb) in zip(ids, out):
         assert ra == g["oa%d" % k].tobytes(), k
         assert rb == g["ob%d" % k].tobytes(), k
+
+
+def test_refine_alignment_pass_equals_reference_windows(ctx):
+    """The gapped-alignment pass over six LCBs (tests/golden/refine.npz):
+    refineAlignment's windows, each window that is not a gap window and holds
+    bases of both genomes realigned (all windows of all LCBs in one batch),
+    equal to the LCB rows built from the reference's own
+    ProfileAlignFast(anchored) output for each window."""
+    g = load_golden("refine.npz")
+    n = int(g["count"])
+    by_w = {}
+    for k in range(n):
+        by_w.setdefault(float(g["w%d" % k]), []).append(k)
+    for maxw, ks in by_w.items():
+        out = ctx.refine_alignment([(g["a%d" % k], g["b%d" % k]) for k in ks], max_window_size=maxw)
+        for k, (ra, rb) in zip(ks, out):
+            assert ra == g["oa%d" % k].tobytes(), k
+            assert rb == g["ob%d" % k].tobytes(), k
+            np.testing.assert_array_equal(mvg.refine_windows(g["a%d" % k], g["b%d" % k], maxw), g["win%d" % k])

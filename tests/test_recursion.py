@@ -1,6 +1,8 @@
-"""Recursive anchor search gap finding (mvg_recursion_gaps) against the
-oracle's restatement of recurseOnPairs / getInterveningCoordinates.  Host
-code only: no GPU."""
+"""Recursive anchor search gap finding (mvg_recursion_gaps) and the
+gapped-alignment pass's windows (mvg_refine_windows) against the oracle's
+restatements of recurseOnPairs / getInterveningCoordinates and of
+refineAlignment / removeLargeGapsPP / IsDenseEnough.  Host code only: no
+GPU."""
 import numpy as np
 import pytest
 
@@ -99,3 +101,30 @@ def test_rejects_lcb_past_the_genome():
     a, b = _rows(("ACGT", "ACGT"))
     with pytest.raises(Exception):
         mvg.recursion_gaps(a, b, 10, False, 1, False, 12, 100)
+
+
+def test_refine_windows_match_the_oracle():
+    """refineAlignment's windows (long one-genome stretches cut out as gap
+    windows with 300 columns kept on either side, windows halved while too
+    long for their density) equal the oracle's restatement on random LCBs
+    at several window limits, and tile the LCB."""
+    rng = np.random.default_rng(1015)
+    for it in range(60):
+        parts_a, parts_b = [], []
+        for s in range(int(rng.integers(1, 6))):
+            n = int(rng.integers(50, 3000))
+            a, b = _random_lcb(rng, n, 0.2, 0.2, 40)
+            parts_a.append(a)
+            parts_b.append(b)
+            run = int(rng.choice([10, 800, 5001, 5300, 7000]))
+            one = np.full(run, ord("A"), np.uint8)
+            gap = np.full(run, ord("-"), np.uint8)
+            parts_a.append(one if s % 2 else gap)
+            parts_b.append(gap if s % 2 else one)
+        ra, rb = np.concatenate(parts_a), np.concatenate(parts_b)
+        for maxw in (400.0, 2500.0, 20000.0):
+            got = [tuple(x) for x in mvg.refine_windows(ra, rb, maxw).tolist()]
+            want = [(a, b, int(g)) for a, b, g in RO.refine_windows(ra, rb, maxw)]
+            assert got == want, (it, maxw)
+            assert got[0][0] == 0 and got[-1][1] == len(ra)
+            assert all(x[1] == y[0] for x, y in zip(got[:-1], got[1:]))
