@@ -254,6 +254,50 @@ int mvg_anchor_columns(const uint8_t* row_a, const uint8_t* row_b, uint64_t ncol
 int mvg_refine_windows(const uint8_t* row_a, const uint8_t* row_b, uint64_t ncols, double max_window_size,
                        int64_t* windows, uint64_t cap, uint64_t* n);
 
+/* ------------------------------------------------ search outside LCBs */
+
+/* Match lists below are 3 int64 per match: libMems' signed 1-based start in
+ * A, start in B (negative = reverse strand, 0 = not in that genome), length.
+ * Regions are 1-based (left end, right end + 1) pairs, flattened, in
+ * concatenation order -- the iv_regions vectors of the reference. */
+
+/* SearchLCBGaps (LM/Aligner.cpp:784-928) for two genomes, as
+ * ProgressiveAligner::alignPP calls it after a recursion round
+ * (LM/ProgressiveAligner.cpp:2474-2488, regions sorted there).  The regions
+ * of each genome are concatenated and the concatenations searched on the GPU
+ * by the pairwise matcher with seed getSeed(getDefaultSeedWeight(mean
+ * concatenation length), 0) (no search below weight 5: *count = 0); the
+ * matches are then transposed back to genome coordinates, split at region
+ * seams, overlap-eliminated and length-filtered as mvg_lcb_gap_finish.
+ * *weight (optional) gets the seed weight.  MVG_ERR_RANGE for a region
+ * outside its genome (the reference catches the cut's exception and searches
+ * without that region), MVG_ERR_CAPACITY when the matches exceed cap
+ * (*count holds the number). */
+int mvg_search_lcb_gaps(mvg_handle h, const uint8_t* seq_a, uint64_t na, const uint8_t* seq_b, uint64_t nb,
+                        const int64_t* regions_a, uint64_t nra, const int64_t* regions_b, uint64_t nrb, int64_t* out,
+                        uint64_t cap, uint64_t* count, uint32_t* weight);
+/* The same with the genomes in device memory (regions and output on the
+ * host); the regions are gathered on the GPU. */
+int mvg_search_lcb_gaps_dev(mvg_handle h, const uint8_t* d_seq_a, uint64_t na, const uint8_t* d_seq_b, uint64_t nb,
+                            const int64_t* regions_a, uint64_t nra, const int64_t* regions_b, uint64_t nrb,
+                            int64_t* out, uint64_t cap, uint64_t* count, uint32_t* weight);
+
+/* The host steps after the search (LM/Aligner.cpp:891-923): matches of the
+ * two concatenations (pairwise-matcher order) -> MultiplicityFilter(2),
+ * transposeMatches for A then B, EliminateOverlaps, MultiplicityFilter(2),
+ * LengthFilter(MIN_ANCHOR_LENGTH = 9).  Host only. */
+int mvg_lcb_gap_finish(const int64_t* matches, uint64_t n, const int64_t* regions_a, uint64_t nra,
+                       const int64_t* regions_b, uint64_t nrb, int64_t* out, uint64_t cap, uint64_t* count);
+/* transposeMatches (LM/Aligner.cpp:973-1045) for genome seq (0 = A, 1 = B):
+ * sorts by MatchLeftEndComparator(seq), maps concatenation starts to genome
+ * starts and splits a match at each region seam it crosses (the pieces are
+ * appended after the sorted list).  Host only. */
+int mvg_transpose_matches(const int64_t* matches, uint64_t n, unsigned seq, const int64_t* regions,
+                          uint64_t nregions, int64_t* out, uint64_t cap, uint64_t* count);
+/* EliminateOverlaps (LM/Aligner.cpp:62-176) for two-genome matches.  Host
+ * only. */
+int mvg_eliminate_overlaps(const int64_t* matches, uint64_t n, int64_t* out, uint64_t cap, uint64_t* count);
+
 /* ------------------------------------------------ band-proposal network */
 
 /* The band proposal for mvg_gapdp_banded: a 528 -> 256 -> 256 -> 256 -> 2

@@ -50,7 +50,8 @@ EXPORTS = ["mvg_create", "mvg_destroy", "mvg_last_error", "mvg_stream", "mvg_ker
            "mvg_set_dp_coop_strips", "mvg_path_rows", "mvg_path_rows_dev",
            "mvg_xmfa_write", "mvg_xmfa_write_dev", "mvg_set_mlp_tcgen05", "mvg_mlp_tcgen05_passes",
            "mvg_set_dp_checkpoint", "mvg_set_band_whole_full_rows", "mvg_set_ring_max_rows",
-           "mvg_recursion_gaps", "mvg_anchor_columns", "mvg_refine_windows"]
+           "mvg_recursion_gaps", "mvg_anchor_columns", "mvg_refine_windows", "mvg_search_lcb_gaps",
+           "mvg_search_lcb_gaps_dev", "mvg_lcb_gap_finish", "mvg_transpose_matches", "mvg_eliminate_overlaps"]
 
 TUNING_PATH = os.path.join(HERE, "dp_tuning.json")
 
@@ -100,6 +101,13 @@ def load_library(path=LIB_PATH):
         "mvg_recursion_gaps": (ci, [vp, vp, u64, i64, ci, i64, ci, u64, u64, i64, vp, u64, ctypes.POINTER(u64), vp]),
         "mvg_anchor_columns": (ci, [vp, vp, u64, vp, u64, ctypes.POINTER(u64)]),
         "mvg_refine_windows": (ci, [vp, vp, u64, ctypes.c_double, vp, u64, ctypes.POINTER(u64)]),
+        "mvg_search_lcb_gaps": (ci, [vp, vp, u64, vp, u64, vp, u64, vp, u64, vp, u64, ctypes.POINTER(u64),
+                                     ctypes.POINTER(ctypes.c_uint32)]),
+        "mvg_search_lcb_gaps_dev": (ci, [vp, vp, u64, vp, u64, vp, u64, vp, u64, vp, u64, ctypes.POINTER(u64),
+                                         ctypes.POINTER(ctypes.c_uint32)]),
+        "mvg_lcb_gap_finish": (ci, [vp, u64, vp, u64, vp, u64, vp, u64, ctypes.POINTER(u64)]),
+        "mvg_transpose_matches": (ci, [vp, u64, ctypes.c_uint, vp, u64, vp, u64, ctypes.POINTER(u64)]),
+        "mvg_eliminate_overlaps": (ci, [vp, u64, vp, u64, ctypes.POINTER(u64)]),
         "mvg_set_mlp_tcgen05": (ci, [vp, ci]),
         "mvg_mlp_tcgen05_passes": (ci, [vp, ctypes.POINTER(ctypes.c_uint64)]),
         "mvg_set_dp_coop_strips": (ci, [vp, ci]),
@@ -214,6 +222,74 @@ def recursion_gaps(row_a, row_b, left_end_a, reverse_a, left_end_b, reverse_b, g
         rc = L.mvg_recursion_gaps(*args, _ptr(gaps), cap, ctypes.byref(n), _ptr(flanks))
     _check(rc)
     return gaps[:4 * int(n.value)].reshape(-1, 4), flanks.reshape(2, 2, 2)
+
+
+def _matches(m):
+    return np.ascontiguousarray(m, np.int64).reshape(-1, 3)
+
+
+def _regions(r):
+    return np.ascontiguousarray(r if r is not None else [], np.int64).reshape(-1)
+
+
+def _host_matches(call, n_in):
+    """Runs a host match-list step with a growing output buffer."""
+    cap = 2 * n_in + 16
+    cnt = ctypes.c_uint64(0)
+    while True:
+        out = np.zeros(3 * cap, np.int64)
+        rc = call(out, cap, cnt)
+        if rc == MVG_ERR_CAPACITY and cnt.value > cap:
+            cap = int(cnt.value)
+            continue
+        _check(rc)
+        return out[:3 * int(cnt.value)].reshape(-1, 3)
+
+
+def transpose_matches(matches, seq, regions):
+    """transposeMatches (libMems/Aligner.cpp:973-1045) for genome seq of
+    two-genome matches (rows: start A, start B, length; libMems' signed
+    1-based starts) given the 1-based (left, right + 1) regions the
+    concatenation was cut from (no GPU needed)."""
+    m, r = _matches(matches), _regions(regions)
+    L = load_library()
+    return _host_matches(lambda out, cap, cnt: L.mvg_transpose_matches(_ptr(m), len(m), int(seq), _ptr(r), len(r),
+                                                                       _ptr(out), cap, ctypes.byref(cnt)), len(m))
+
+
+def eliminate_overlaps(matches):
+    """EliminateOverlaps (libMems/Aligner.cpp:62-176) for two-genome matches
+    (no GPU needed)."""
+    m = _matches(matches)
+    L = load_library()
+    return _host_matches(lambda out, cap, cnt: L.mvg_eliminate_overlaps(_ptr(m), len(m), _ptr(out), cap,
+                                                                        ctypes.byref(cnt)), len(m))
+
+
+def lcb_gap_finish(matches, regions_a, regions_b):
+    """The steps SearchLCBGaps takes after its search (no GPU needed; see
+    mvg_lcb_gap_finish): matches of the two concatenations -> matches in
+    genome coordinates."""
+    m, ra, rb = _matches(matches), _regions(regions_a), _regions(regions_b)
+    L = load_library()
+    return _host_matches(lambda out, cap, cnt: L.mvg_lcb_gap_finish(_ptr(m), len(m), _ptr(ra), len(ra), _ptr(rb),
+                                                                    len(rb), _ptr(out), cap, ctypes.byref(cnt)),
+                         len(m))
+
+
+def lcb_gap_regions(flanks):
+    """The regions outside the LCBs, as alignPP hands them to SearchLCBGaps
+    (libMems/ProgressiveAligner.cpp:2474-2488): every LCB's flanks (the
+    second value recursion_gaps returns, int64[2, 2, 2]) collected per genome
+    and each genome's boundary list sorted.  Returns (regions A, regions B)."""
+    per = [[], []]
+    for fl in flanks:
+        fl = np.asarray(fl, np.int64).reshape(2, 2, 2)
+        for q in range(2):
+            for lo, hi in fl[q]:
+                if lo < hi:
+                    per[q] += [int(lo), int(hi)]
+    return tuple(np.sort(np.array(p, np.int64)) for p in per)
 
 
 def anchor_columns(row_a, row_b):
@@ -458,6 +534,33 @@ class Context:
         _check(load_library().mvg_gap_anchor_search_dev(self._h, d_a, na, d_b, nb, _ptr(g), len(g), _ptr(out), cap,
                                                         _ptr(off), ctypes.byref(cnt)))
         return out[: 3 * cnt.value].reshape(-1, 3), off
+
+    def search_lcb_gaps(self, seq_a, seq_b, regions_a, regions_b):
+        """SearchLCBGaps for two genomes (mvg_search_lcb_gaps): regions are
+        1-based (left, right + 1) boundaries per genome, as lcb_gap_regions
+        gives them.  Returns (matches int64[m, 3] as (start A, start B,
+        length) in genome coordinates, seed weight)."""
+        seq_a, seq_b = _u8(seq_a), _u8(seq_b)
+        ra, rb = _regions(regions_a), _regions(regions_b)
+        w = ctypes.c_uint32(0)
+        L = load_library()
+        m = _host_matches(lambda out, cap, cnt: L.mvg_search_lcb_gaps(
+            self._h, _ptr(seq_a), len(seq_a), _ptr(seq_b), len(seq_b), _ptr(ra), len(ra), _ptr(rb), len(rb),
+            _ptr(out), cap, ctypes.byref(cnt), ctypes.byref(w)), (int(np.diff(ra.reshape(-1, 2)).sum()) if len(ra)
+                                                                    else 0) // 8)
+        return m, int(w.value)
+
+    def search_lcb_gaps_dev(self, d_a, na, d_b, nb, regions_a, regions_b, cap):
+        """Device-genome variant; regions and output on the host."""
+        wait_producers()
+        ra, rb = _regions(regions_a), _regions(regions_b)
+        out = np.zeros(3 * max(cap, 1), np.int64)
+        cnt = ctypes.c_uint64(0)
+        w = ctypes.c_uint32(0)
+        _check(load_library().mvg_search_lcb_gaps_dev(self._h, d_a, na, d_b, nb, _ptr(ra), len(ra), _ptr(rb),
+                                                      len(rb), _ptr(out), cap, ctypes.byref(cnt),
+                                                      ctypes.byref(w)))
+        return out[:3 * int(cnt.value)].reshape(-1, 3), int(w.value)
 
     def pairwise_stats(self):
         st = np.zeros(4, np.uint64)

@@ -1,0 +1,3 @@
+// Test-only stand-in: MuscleInterface.cpp includes this header but calls
+// nothing from it.
+#pragma once
