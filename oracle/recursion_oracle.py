@@ -12,10 +12,11 @@ LM/AbstractMatch.h:209-214: End = Start + Length - 1 for a forward start,
 Start itself for a reverse one; LM/UngappedLocalAlignment.h:48-56: Length),
 and getInterveningCoordinates (LM/ProgressiveAligner.cpp:566-588) with the
 sequence cut of pairwiseAnchorSearch (:598-613); refine_windows follows
-refineAlignment's windowing (:1015-1165).  Parity is unpinned: the
-reference's ProgressiveAligner.cpp needs boost::graph, which is not in the
-image, so the restatement is checked against the reference's source only by
-reading, line by line, in the cited ranges.
+refineAlignment's windowing (:1015-1165).  Pinned through the reference's
+own recurseOnPairs and refineAlignment (compiled here by
+oracle/ref_progressive_driver.cpp; fixtures tests/golden/recursion.npz and
+refine.npz): the library equals those fixtures, and equals this restatement
+on random LCBs.
 """
 
 

@@ -7,12 +7,17 @@ reference's sources, oracle/_ref/libmauveref.so ref_anchored_align).
     make -f oracle/Makefile.ref -j8 REF=<reference checkout>
     python tests/golden/make_golden_refine.py
 
-The windows are refineAlignment's (LM/ProgressiveAligner.cpp:1119-1165), from
-the library's mvg_refine_windows checked here against the oracle's
-restatement (oracle/recursion_oracle.py); windows that are gap windows or
-hold bases of one genome only stay as they are.  LCBs: optimal alignments of
-seeded random sequences and mutated copies, joined by stretches where one
-genome only has bases (up to 6,500 columns, so that some become gap windows).
+The expected rows are the reference's own refineAlignment
+(LM/ProgressiveAligner.cpp:1119-1230, profile_aln = true, compiled from its
+sources with oracle/ref_progressive_driver.cpp as ref_refine_alignment).  The
+script also rebuilds them window by window -- refineAlignment's windows
+(:1015-1165) from the library's mvg_refine_windows, checked against the
+oracle's restatement (oracle/recursion_oracle.py), each window that is not a
+gap window and holds bases of both genomes realigned by ref_anchored_align --
+and requires the two to agree, which pins the windows to the reference.
+LCBs: optimal alignments of seeded random sequences and mutated copies,
+joined by stretches where one genome only has bases (up to 6,500 columns, so
+that some become gap windows).
 """
 import ctypes
 import os
@@ -27,7 +32,19 @@ for _p in (os.path.join(ROOT, "tests"), os.path.join(ROOT, "oracle"), os.path.jo
 import mvg  # noqa: E402
 import recursion_oracle as RO  # noqa: E402
 import synth  # noqa: E402
-from make_golden_anchors import ref_realign, window  # noqa: E402
+from make_golden_anchors import R, ref_realign, window  # noqa: E402
+
+R.ref_refine_alignment.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_uint64, ctypes.c_int64, ctypes.c_int64,
+                                   ctypes.c_uint64, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_uint64]
+R.ref_refine_alignment.restype = ctypes.c_int64
+
+
+def ref_refine(ra, rb, maxw):
+    cap = 2 * len(ra) + 64
+    oa, ob = ctypes.create_string_buffer(cap), ctypes.create_string_buffer(cap)
+    n = R.ref_refine_alignment(ra.tobytes(), rb.tobytes(), len(ra), 1, 1, int(maxw), oa, ob, cap)
+    assert n >= 0
+    return np.frombuffer(oa.raw[:n], np.uint8).copy(), np.frombuffer(ob.raw[:n], np.uint8).copy()
 
 
 def lcb(rng, nseg):
@@ -50,7 +67,8 @@ def main():
     rng = np.random.default_rng(1119)
     out = {}
     k = 0
-    for nseg, maxw in ((3, 20000.0), (4, 20000.0), (2, 1000.0), (5, 3000.0), (3, 600.0), (6, 20000.0)):
+    for nseg, maxw in ((3, 20000.0), (4, 20000.0), (2, 1000.0), (5, 3000.0), (3, 600.0), (6, 20000.0),
+                       (4, 400.0), (7, 2500.0)):
         ra, rb = lcb(rng, nseg)
         wins = mvg.refine_windows(ra, rb, maxw)
         assert [tuple(w) for w in wins.tolist()] == [(a, b, int(g)) for a, b, g in RO.refine_windows(ra, rb, maxw)]
@@ -61,9 +79,11 @@ def main():
                 wa, wb = ref_realign(wa, wb)
             rows_a.append(wa)
             rows_b.append(wb)
+        oa, ob = ref_refine(ra, rb, maxw)
+        assert oa.tobytes() == np.concatenate(rows_a).tobytes() and ob.tobytes() == np.concatenate(rows_b).tobytes()
         out["a%d" % k], out["b%d" % k] = ra, rb
         out["w%d" % k] = np.float64(maxw)
-        out["oa%d" % k], out["ob%d" % k] = np.concatenate(rows_a), np.concatenate(rows_b)
+        out["oa%d" % k], out["ob%d" % k] = oa, ob
         out["win%d" % k] = wins
         k += 1
     out["count"] = np.int64(k)

@@ -149,3 +149,28 @@ def test_recursion_gaps_feed_the_gap_search(ctx):
             w, want = O.gap_anchor_search(a[sa:sa + la], b[sb:sb + lb])
             want = np.zeros((0, 3), np.int64) if want is None else shift(want, sa, sb)
             np.testing.assert_array_equal(anchors[off[k]:off[k + 1]], want, err_msg="gap %d" % k)
+
+
+def test_recursion_round_equals_the_reference_recurse_on_pairs(ctx):
+    """The reference's own recurseOnPairs on 22 LCBs
+    (tests/golden/recursion.npz): every LCB's gaps (mvg_recursion_gaps) of a
+    genome pair searched in ONE batched call, as a recursion round does, give
+    each LCB the reference's anchors in its order."""
+    from test_recursion import _golden_lcb
+    g = load_golden("recursion.npz")
+    by_pair = {}
+    for k in range(int(g["count"])):
+        by_pair.setdefault(int(g["pair%d" % k]), []).append(k)
+    total = 0
+    for p, ks in by_pair.items():
+        rows_gaps, spans = [], []
+        for k in ks:
+            (ra, rb), a, b, (la, rva, lb, rvb), min_gap = _golden_lcb(g, k)
+            gaps, _ = mvg.recursion_gaps(ra, rb, la, rva, lb, rvb, len(a), len(b), min_gap=min_gap)
+            spans.append((k, len(rows_gaps), len(rows_gaps) + len(gaps)))
+            rows_gaps += gaps.tolist()
+        anchors, off = ctx.gap_anchor_search(g["a%d" % p], g["b%d" % p], np.array(rows_gaps, np.int64).reshape(-1, 4))
+        for k, g0, g1 in spans:
+            np.testing.assert_array_equal(anchors[off[g0]:off[g1]], g["c%d_anchors" % k], err_msg=str(k))
+            total += int(off[g1] - off[g0])
+    assert total > 1000

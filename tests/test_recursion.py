@@ -128,3 +128,43 @@ def test_refine_windows_match_the_oracle():
             assert got == want, (it, maxw)
             assert got[0][0] == 0 and got[-1][1] == len(ra)
             assert all(x[1] == y[0] for x, y in zip(got[:-1], got[1:]))
+
+
+def _golden_lcb(g, k):
+    """Rows of golden LCB k (bases as 'A', gaps as '-'), its genomes and its
+    parameters."""
+    n = int(g["c%d_ncols" % k])
+    rows = [np.where(np.unpackbits(g["c%d_mask_%s" % (k, q)])[:n] == 1, ord("A"), ord("-")).astype(np.uint8)
+            for q in "ab"]
+    p = int(g["pair%d" % k])
+    left_a, left_b, rev_a, rev_b, min_gap = [int(x) for x in g["c%d_left" % k]]
+    return rows, g["a%d" % p], g["b%d" % p], (left_a, bool(rev_a), left_b, bool(rev_b)), min_gap
+
+
+def test_recursion_equals_the_reference_recurse_on_pairs():
+    """22 LCBs (tests/golden/recursion.npz, the reference's own
+    recurseOnPairs): the regions outside each LCB equal the reference's
+    iv_regions, and the gaps, searched one by one with the oracle's
+    pairwiseAnchorSearch and shifted to genome coordinates, give the
+    reference's anchors in its order (all strand pairs, minimum gaps 200 and
+    60, LCBs at a genome's first and last base, one without an aligned
+    column)."""
+    import oracle as O
+    from conftest import load_golden
+    g = load_golden("recursion.npz")
+    total = 0
+    for k in range(int(g["count"])):
+        (ra, rb), a, b, (la, rva, lb, rvb), min_gap = _golden_lcb(g, k)
+        gaps, flanks = mvg.recursion_gaps(ra, rb, la, rva, lb, rvb, len(a), len(b), min_gap=min_gap)
+        for q, key in ((0, "ra"), (1, "rb")):
+            got = [int(v) for lo, hi in flanks[q] if lo < hi for v in (lo, hi)]
+            assert got == [int(v) for v in g["c%d_%s" % (k, key)]], (k, q)
+        anchors = []
+        for s0, l0, s1, l1 in gaps.tolist():
+            _, anc = O.gap_anchor_search(a[s0:s0 + l0], b[s1:s1 + l1])
+            for x, y, L in ([] if anc is None else anc.tolist()):
+                anchors.append((x + s0 if x > 0 else x - s0, y + s1 if y > 0 else y - s1, L))
+        want = g["c%d_anchors" % k]
+        assert anchors == [tuple(r) for r in want.tolist()], k
+        total += len(want)
+    assert total > 1000
