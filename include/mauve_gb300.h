@@ -254,6 +254,21 @@ int mvg_anchor_columns(const uint8_t* row_a, const uint8_t* row_b, uint64_t ncol
 int mvg_refine_windows(const uint8_t* row_a, const uint8_t* row_b, uint64_t ncols, double max_window_size,
                        int64_t* windows, uint64_t cap, uint64_t* n);
 
+/* The column ranges the final iterative-refinement pass realigns in one LCB
+ * of two genomes: refineAlignment with profile_aln = false
+ * (LM/ProgressiveAligner.cpp:1199-1212) over the same windows as
+ * mvg_refine_windows; every window that is not a gap window and has density
+ * class 1 or 2 (IsDenseEnough, :1015-1038) goes through
+ * MuscleInterface::RefineFast (LM/MuscleInterface.cpp:823-894) with RefineW
+ * column windows of 500 or 200 columns (MU/refinew.cpp:75-184), each
+ * realigned from its bases alone (for two sequences: one NWSmall problem,
+ * genome A as profile A).  Class-0 windows stay as they are (RefineVert
+ * returns at once for fewer than three sequences, MU/refinevert.cpp:60-61).
+ * Host only.  Out: ranges[2k] = (first column, end column), in column order;
+ * *n their number (MVG_ERR_CAPACITY when above cap). */
+int mvg_refine_fast_ranges(const uint8_t* row_a, const uint8_t* row_b, uint64_t ncols, double max_window_size,
+                           int64_t* ranges, uint64_t cap, uint64_t* n);
+
 /* ------------------------------------------------ search outside LCBs */
 
 /* Match lists below are 3 int64 per match: libMems' signed 1-based start in

@@ -7,6 +7,16 @@
 // (mvg_anchor_columns and the batched gap DP); the LCB's new rows are the
 // windows' rows concatenated in order (:1215-1230).
 //
+// The same windows drive the final iterative-refinement pass
+// (refineAlignment with profile_aln = false, :1199-1212): a window of
+// density class 1 or 2 goes through MuscleInterface::RefineFast
+// (LM/MuscleInterface.cpp:823-894) with RefineW's column windows of 500 or
+// 200 columns (MU/refinew.cpp:75-184), each of which MUSCLE realigns from
+// its bases alone -- for two sequences one NWSmall problem, the first
+// genome as profile A; a class-0 window goes through RefineVert, which
+// returns at once for fewer than three sequences (MU/refinevert.cpp:60-61).
+// mvg_refine_fast_ranges lists those column windows.
+//
 // Cuts follow GappedAlignment::Split / CropStart / CropEnd
 // (LM/GappedAlignment.h:123-229): Split(k) keeps columns [0, k) on the left;
 // halving a window of L columns keeps L - L/2 columns on the left and L/2 on
@@ -15,6 +25,7 @@
 // the window's multiplicity in the density test.
 #include <stdint.h>
 
+#include <algorithm>
 #include <list>
 #include <vector>
 
@@ -32,18 +43,18 @@ constexpr double kMaxDensity = .9;        // max_density (:61)
 struct Window {
   uint64_t lo, hi;  // columns [lo, hi)
   bool gap;
+  int density;  // IsDenseEnough's class of the final window: 0, 1 or 2
 };
 
-}  // namespace
-}  // namespace mvg
+// RefineW's window widths by density class (refineAlignment with
+// profile_aln = false, :1201-1212: RefineFast(w), RefineFast(w, 500),
+// RefineFast(w, 200)); 0 = no change (RefineVert needs three sequences,
+// MU/refinevert.cpp:60-61).
+constexpr uint64_t kRefineWidth[3] = {0, 500, 200};
 
-using namespace mvg;
-
-extern "C" int mvg_refine_windows(const uint8_t* row_a, const uint8_t* row_b, uint64_t ncols,
-                                  double max_window_size, int64_t* windows, uint64_t cap, uint64_t* nwindows) {
-  if (!nwindows || (ncols && (!row_a || !row_b)) || (cap && !windows) || !(max_window_size > kMinWindowSize))
-    return report_error(MVG_ERR_ARG, "bad argument");
-  *nwindows = 0;
+// refineAlignment's windows of one LCB (removeLargeGapsPP, then halving by
+// IsDenseEnough), each with its density class.
+std::vector<Window> lcb_windows(const uint8_t* row_a, const uint8_t* row_b, uint64_t ncols, double max_window_size) {
   const uint8_t* rows[2] = {row_a, row_b};
   // prefix base counts, for the bases of any column range
   std::vector<uint64_t> pre[2];
@@ -62,11 +73,11 @@ extern "C" int mvg_refine_windows(const uint8_t* row_a, const uint8_t* row_b, ui
       if (gap_cols > kMaxGapLength) {
         if (last_aln != kNone) {
           const uint64_t k = last_aln + kLcbHangover - base;
-          wins.push_back({base, base + k, false});
+          wins.push_back({base, base + k, false, 0});
           base += k;
         }
         const uint64_t k = c - kLcbHangover - base;
-        wins.push_back({base, base + k, true});
+        wins.push_back({base, base + k, true, 0});
         base += k;
       }
       last_aln = c;
@@ -78,12 +89,12 @@ extern "C" int mvg_refine_windows(const uint8_t* row_a, const uint8_t* row_b, ui
   if (gap_cols > kMaxGapLength) {
     if (last_aln != kNone) {
       const uint64_t k = last_aln + kLcbHangover - base;
-      wins.push_back({base, base + k, false});
+      wins.push_back({base, base + k, false, 0});
       base += k;
     }
-    wins.push_back({base, ncols, true});
+    wins.push_back({base, ncols, true, 0});
   } else {
-    wins.push_back({base, ncols, false});
+    wins.push_back({base, ncols, false, 0});
   }
   // halve windows too long for their density (IsDenseEnough)
   auto density_class = [&](const Window& w) {
@@ -110,13 +121,28 @@ extern "C" int mvg_refine_windows(const uint8_t* row_a, const uint8_t* row_b, ui
     if ((d == 0 && (double)len > max_window_size / 3) || (d == 1 && (double)len > max_window_size) ||
         (d == 2 && (double)len > max_window_size * 3)) {
       const uint64_t half = len / 2;  // CropEnd(half) on the left, CropStart(len - half) on the right
-      Window right{it->hi - half, it->hi, it->gap};
+      Window right{it->hi - half, it->hi, it->gap, 0};
       it->hi -= half;
       wins.insert(std::next(it), right);
       continue;
     }
+    it->density = d;
     ++it;
   }
+  return std::vector<Window>(wins.begin(), wins.end());
+}
+
+}  // namespace
+}  // namespace mvg
+
+using namespace mvg;
+
+extern "C" int mvg_refine_windows(const uint8_t* row_a, const uint8_t* row_b, uint64_t ncols,
+                                  double max_window_size, int64_t* windows, uint64_t cap, uint64_t* nwindows) {
+  if (!nwindows || (ncols && (!row_a || !row_b)) || (cap && !windows) || !(max_window_size > kMinWindowSize))
+    return report_error(MVG_ERR_ARG, "bad argument");
+  *nwindows = 0;
+  const std::vector<Window> wins = lcb_windows(row_a, row_b, ncols, max_window_size);
   uint64_t n = 0;
   for (const Window& w : wins) {
     if (n < cap) {
@@ -128,5 +154,27 @@ extern "C" int mvg_refine_windows(const uint8_t* row_a, const uint8_t* row_b, ui
   }
   *nwindows = n;
   if (n > cap) return report_error(MVG_ERR_CAPACITY, "window buffer too small");
+  return 0;
+}
+
+extern "C" int mvg_refine_fast_ranges(const uint8_t* row_a, const uint8_t* row_b, uint64_t ncols,
+                                      double max_window_size, int64_t* ranges, uint64_t cap, uint64_t* nranges) {
+  if (!nranges || (ncols && (!row_a || !row_b)) || (cap && !ranges) || !(max_window_size > kMinWindowSize))
+    return report_error(MVG_ERR_ARG, "bad argument");
+  *nranges = 0;
+  uint64_t n = 0;
+  for (const Window& w : lcb_windows(row_a, row_b, ncols, max_window_size)) {
+    const uint64_t width = kRefineWidth[w.density];
+    if (w.gap || width == 0) continue;
+    for (uint64_t lo = w.lo; lo < w.hi; lo += width) {  // RefineW's column windows (MU/refinew.cpp:113-118)
+      if (n < cap) {
+        ranges[2 * n] = (int64_t)lo;
+        ranges[2 * n + 1] = (int64_t)std::min(w.hi, lo + width);
+      }
+      ++n;
+    }
+  }
+  *nranges = n;
+  if (n > cap) return report_error(MVG_ERR_CAPACITY, "range buffer too small");
   return 0;
 }

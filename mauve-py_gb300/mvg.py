@@ -51,7 +51,7 @@ EXPORTS = ["mvg_create", "mvg_destroy", "mvg_last_error", "mvg_stream", "mvg_ker
            "mvg_xmfa_write", "mvg_xmfa_write_dev", "mvg_set_mlp_tcgen05", "mvg_mlp_tcgen05_passes",
            "mvg_set_dp_checkpoint", "mvg_set_band_whole_full_rows", "mvg_set_ring_max_rows",
            "mvg_recursion_gaps", "mvg_anchor_columns", "mvg_refine_windows", "mvg_search_lcb_gaps",
-           "mvg_search_lcb_gaps_dev", "mvg_lcb_gap_finish", "mvg_transpose_matches", "mvg_eliminate_overlaps"]
+           "mvg_refine_fast_ranges", "mvg_search_lcb_gaps_dev", "mvg_lcb_gap_finish", "mvg_transpose_matches", "mvg_eliminate_overlaps"]
 
 TUNING_PATH = os.path.join(HERE, "dp_tuning.json")
 
@@ -101,6 +101,7 @@ def load_library(path=LIB_PATH):
         "mvg_recursion_gaps": (ci, [vp, vp, u64, i64, ci, i64, ci, u64, u64, i64, vp, u64, ctypes.POINTER(u64), vp]),
         "mvg_anchor_columns": (ci, [vp, vp, u64, vp, u64, ctypes.POINTER(u64)]),
         "mvg_refine_windows": (ci, [vp, vp, u64, ctypes.c_double, vp, u64, ctypes.POINTER(u64)]),
+        "mvg_refine_fast_ranges": (ci, [vp, vp, u64, ctypes.c_double, vp, u64, ctypes.POINTER(u64)]),
         "mvg_search_lcb_gaps": (ci, [vp, vp, u64, vp, u64, vp, u64, vp, u64, vp, u64, ctypes.POINTER(u64),
                                      ctypes.POINTER(ctypes.c_uint32)]),
         "mvg_search_lcb_gaps_dev": (ci, [vp, vp, u64, vp, u64, vp, u64, vp, u64, vp, u64, ctypes.POINTER(u64),
@@ -322,6 +323,27 @@ def refine_windows(row_a, row_b, max_window_size=20000.0):
             continue
         _check(rc)
         return w[:3 * int(n.value)].reshape(-1, 3)
+
+
+def refine_fast_ranges(row_a, row_b, max_window_size=20000.0):
+    """The column ranges the final iterative-refinement pass realigns in one
+    LCB of two genomes (no GPU needed; see mvg_refine_fast_ranges):
+    int64[k, 2] rows (first column, end column)."""
+    a, b = _u8(row_a), _u8(row_b)
+    if len(a) != len(b):
+        raise ValueError("rows of different length")
+    L = load_library()
+    n = ctypes.c_uint64(0)
+    cap = max(16, len(a) // 200 + 8)
+    while True:
+        r = np.zeros(2 * cap, np.int64)
+        rc = L.mvg_refine_fast_ranges(_ptr(a), _ptr(b), len(a), float(max_window_size), _ptr(r), cap,
+                                      ctypes.byref(n))
+        if rc == MVG_ERR_CAPACITY:
+            cap = int(n.value)
+            continue
+        _check(rc)
+        return r[:2 * int(n.value)].reshape(-1, 2)
 
 
 def anchored_problems(row_a, row_b):
@@ -726,6 +748,70 @@ class Context:
             rows = [done[p] if isinstance(p, int) else p for p in parts]
             out.append((b"".join(r[0] for r in rows), b"".join(r[1] for r in rows)))
         return out
+
+    def _realign_ranges(self, jobs):
+        """Global NWSmall of each job's bases (job: (row A, row B) column
+        range), all in one gap-DP call on the GPU, rows rebuilt on the GPU;
+        a job with bases of one genome only keeps its columns.  Returns the
+        (row A, row B) bytes of each job."""
+        code = np.full(256, 255, np.uint8)
+        for i, ch in enumerate(b"ACGT"):
+            code[ch] = code[ch | 0x20] = i
+        sa, sb, oa, ob, slot = [], [], [0], [0], []
+        for wa, wb in jobs:
+            a, b = wa[wa != ord("-")], wb[wb != ord("-")]
+            if len(a) == 0 or len(b) == 0:
+                slot.append((wa.tobytes(), wb.tobytes()))
+                continue
+            if (code[a] == 255).any() or (code[b] == 255).any():
+                raise ValueError("the gap DP takes A, C, G and T only")
+            slot.append(len(oa) - 1)
+            sa.append(a)
+            sb.append(b)
+            oa.append(oa[-1] + len(a))
+            ob.append(ob[-1] + len(b))
+        rows = []
+        if len(oa) > 1:
+            chars_a, chars_b = np.concatenate(sa), np.concatenate(sb)
+            _, paths = self.gap_align_batch(code[chars_a], oa, code[chars_b], ob)
+            rows = self.path_rows(chars_a, oa, chars_b, ob, paths)
+        return [rows[s] if isinstance(s, int) else s for s in slot]
+
+    def iterative_refine(self, lcbs, max_window_size=20000.0):
+        """The final iterative-refinement pass for LCBs of two genomes
+        (refineAlignment with profile_aln = false,
+        LM/ProgressiveAligner.cpp:1119-1230, as alignProfileToProfile ends
+        with it, :3750-3755): RefineFast's column windows (refine_fast_ranges)
+        of every LCB realigned from their bases in one gap-DP call, the other
+        columns kept.  lcbs: list of (row A, row B).  Returns the new
+        (row A, row B) bytes of each LCB."""
+        jobs, plan = [], []
+        for ra, rb in lcbs:
+            a, b = _u8(ra), _u8(rb)
+            parts, at = [], 0
+            for lo, hi in refine_fast_ranges(a, b, max_window_size).tolist():
+                if lo > at:
+                    parts.append((a[at:lo].tobytes(), b[at:lo].tobytes()))
+                parts.append(len(jobs))
+                jobs.append((a[lo:hi], b[lo:hi]))
+                at = hi
+            if at < len(a):
+                parts.append((a[at:].tobytes(), b[at:].tobytes()))
+            plan.append(parts)
+        done = self._realign_ranges(jobs) if jobs else []
+        out = []
+        for parts in plan:
+            rows = [done[p] if isinstance(p, int) else p for p in parts]
+            out.append((b"".join(r[0] for r in rows), b"".join(r[1] for r in rows)))
+        return out
+
+    def gapped_alignment(self, lcbs, max_window_size=20000.0, refine=True):
+        """Both passes a two-genome progressiveMauve run makes over its LCBs:
+        the gapped-alignment pass (refine_alignment) and, unless refine is
+        False, the final iterative refinement (iterative_refine) on its
+        output."""
+        out = self.refine_alignment(lcbs, max_window_size)
+        return self.iterative_refine(out, max_window_size) if refine else out
 
     def xmfa_write(self, file_a, file_b, starts, lengths, rows_a, rows_b, col_off, backbone_file=""):
         """WriteStandardAlignment for pairwise blocks; returns the XMFA text (bytes)."""

@@ -14,8 +14,13 @@
 //       searched gap gives (pairwiseAnchorSearch, :590-679, appended gap by
 //       gap) and the regions outside the LCB (iv_regions, :784-834).
 //   ref_refine_alignment -> ProgressiveAligner::refineAlignment
-//       (:1119-1230) with profile_aln = true, as doGappedAlignment calls it:
-//       the LCB's rows after the gapped-alignment pass.
+//       (:1119-1230) as doGappedAlignment calls it: mode 0 = the
+//       gapped-alignment pass (profile_aln = true, step 8 of
+//       alignProfileToProfile, :2560-2565), 1 = the final iterative
+//       refinement pass (profile_aln = false, :3750-3755), 2 = the first then
+//       the second, as a two-genome progressiveMauve run does them.
+//   ref_refine_fast -> MuscleInterface::RefineFast
+//       (libMems/MuscleInterface.cpp:823-894) on one window.
 #include <cstdint>
 #include <cstring>
 #include <string>
@@ -24,6 +29,7 @@
 #include "libGenome/gnSequence.h"
 #include "libMems/CompactGappedAlignment.h"
 #include "libMems/GappedAlignment.h"
+#include "libMems/MuscleInterface.h"
 #include "libMems/ProgressiveAligner.h"
 
 using namespace mems;
@@ -116,10 +122,19 @@ int64_t ref_recurse_on_pairs(const char* seq_a, uint64_t la, const char* seq_b, 
   return r;
 }
 
+static int64_t rows_out(GappedAlignment& gal, char* out_a, char* out_b, uint64_t cap) {
+  const std::vector<std::string> rows = GetAlignment(gal, std::vector<gnSequence*>(2));
+  const uint64_t n = rows[0].size();
+  if (n > cap || rows[1].size() != n) return -1;
+  std::memcpy(out_a, rows[0].data(), n);
+  std::memcpy(out_b, rows[1].data(), n);
+  return (int64_t)n;
+}
+
 // out_a / out_b: the refined rows; returns their length, -1 when cap is too
 // small.
 int64_t ref_refine_alignment(const char* row_a, const char* row_b, uint64_t ncols, int64_t start_a, int64_t start_b,
-                             uint64_t max_window_size, char* out_a, char* out_b, uint64_t cap) {
+                             uint64_t max_window_size, int mode, char* out_a, char* out_b, uint64_t cap) {
   gnSequence sa, sb;  // leaves need a sequence; refineAlignment reads the rows only
   TwoGenomeAligner p(&sa, &sb);
   p.SetMaxGappedAlignmentLength(max_window_size);
@@ -128,12 +143,19 @@ int64_t ref_refine_alignment(const char* row_a, const char* row_b, uint64_t ncol
   apt.total_len = ncols ? ncols : 1;
   apt.cur_leftend = 0;
   apt.prev_progress = 0;
-  p.refineAlignment(gal, 2, true, apt);
-  const std::vector<std::string> rows = GetAlignment(gal, std::vector<gnSequence*>(2));
-  const uint64_t n = rows[0].size();
-  if (n > cap || rows[1].size() != n) return -1;
-  std::memcpy(out_a, rows[0].data(), n);
-  std::memcpy(out_b, rows[1].data(), n);
-  return (int64_t)n;
+  if (mode == 0 || mode == 2) p.refineAlignment(gal, 2, true, apt);
+  if (mode == 1 || mode == 2) {
+    apt.cur_leftend = 0;
+    apt.prev_progress = 0;
+    p.refineAlignment(gal, 2, false, apt);
+  }
+  return rows_out(gal, out_a, out_b, cap);
+}
+
+int64_t ref_refine_fast(const char* row_a, const char* row_b, uint64_t ncols, uint64_t windowsize, char* out_a,
+                        char* out_b, uint64_t cap) {
+  GappedAlignment gal = lcb(row_a, row_b, ncols, 1, 1);
+  MuscleInterface::getMuscleInterface().RefineFast(gal, windowsize);
+  return rows_out(gal, out_a, out_b, cap);
 }
 }

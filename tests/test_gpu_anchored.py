@@ -52,3 +52,20 @@ def test_refine_alignment_pass_equals_reference_windows(ctx):
             assert ra == g["oa%d" % k].tobytes(), k
             assert rb == g["ob%d" % k].tobytes(), k
             np.testing.assert_array_equal(mvg.refine_windows(g["a%d" % k], g["b%d" % k], maxw), g["win%d" % k])
+
+
+def test_iterative_refinement_equals_the_reference(ctx):
+    """The final iterative-refinement pass (Context.iterative_refine: every
+    RefineFast column window of every LCB in one gap-DP call) and both passes
+    together (Context.gapped_alignment) give the reference's own
+    refineAlignment rows on 11 LCBs (tests/golden/refine.npz)."""
+    g = load_golden("refine.npz")
+    by_w = {}
+    for k in range(int(g["count"])):
+        by_w.setdefault(float(g["w%d" % k]), []).append(k)
+    for maxw, ks in by_w.items():
+        lcbs = [(g["a%d" % k], g["b%d" % k]) for k in ks]
+        for (ra, rb), k in zip(ctx.iterative_refine(lcbs, max_window_size=maxw), ks):
+            assert ra == g["ia%d" % k].tobytes() and rb == g["ib%d" % k].tobytes(), k
+        for (ra, rb), k in zip(ctx.gapped_alignment(lcbs, max_window_size=maxw), ks):
+            assert ra == g["fa%d" % k].tobytes() and rb == g["fb%d" % k].tobytes(), k

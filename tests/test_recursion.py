@@ -168,3 +168,56 @@ def test_recursion_equals_the_reference_recurse_on_pairs():
         assert anchors == [tuple(r) for r in want.tolist()], k
         total += len(want)
     assert total > 1000
+
+
+def _nw_rows(a, b):
+    """Rows of the oracle's NWSmall alignment of two base arrays (either
+    case), letters kept."""
+    import oracle as O
+    acgt = np.frombuffer(b"ACGT", np.uint8)
+    path, _ = O.nw_align(np.searchsorted(acgt, a & 0xDF).astype(np.uint8),
+                         np.searchsorted(acgt, b & 0xDF).astype(np.uint8))
+    ra, rb, i, j = [], [], 0, 0
+    for e in path:
+        ra.append(a[i] if e in "MD" else ord("-"))
+        rb.append(b[j] if e in "MI" else ord("-"))
+        i += e in "MD"
+        j += e in "MI"
+    return np.array(ra, np.uint8), np.array(rb, np.uint8)
+
+
+def _refine_on_cpu(ra, rb, maxw):
+    out_a, out_b, at = [], [], 0
+    for lo, hi in mvg.refine_fast_ranges(ra, rb, maxw).tolist():
+        out_a.append(ra[at:lo])
+        out_b.append(rb[at:lo])
+        wa, wb = ra[lo:hi], rb[lo:hi]
+        a, b = wa[wa != ord("-")], wb[wb != ord("-")]
+        x, y = _nw_rows(a, b) if len(a) and len(b) else (wa, wb)
+        out_a.append(x)
+        out_b.append(y)
+        at = hi
+    out_a.append(ra[at:])
+    out_b.append(rb[at:])
+    return np.concatenate(out_a), np.concatenate(out_b)
+
+
+def test_refinement_ranges_rebuild_the_reference_refinement():
+    """The final iterative-refinement pass (refineAlignment with profile_aln
+    = false) of 11 LCBs (tests/golden/refine.npz, the reference's own
+    output), rebuilt on the CPU from mvg_refine_fast_ranges and the oracle's
+    NWSmall per range: equal to the reference alone and after the
+    gapped-alignment pass, including three LCBs made worse beforehand."""
+    from conftest import load_golden
+    g = load_golden("refine.npz")
+    changed = 0
+    for k in range(int(g["count"])):
+        maxw = float(g["w%d" % k])
+        ia, ib = _refine_on_cpu(g["a%d" % k], g["b%d" % k], maxw)
+        np.testing.assert_array_equal(ia, g["ia%d" % k], err_msg=str(k))
+        np.testing.assert_array_equal(ib, g["ib%d" % k], err_msg=str(k))
+        fa, fb = _refine_on_cpu(g["oa%d" % k], g["ob%d" % k], maxw)
+        np.testing.assert_array_equal(fa, g["fa%d" % k], err_msg=str(k))
+        np.testing.assert_array_equal(fb, g["fb%d" % k], err_msg=str(k))
+        changed += len(g["a%d" % k]) != len(ia) or bool((g["a%d" % k] != ia).any())
+    assert changed >= 3
