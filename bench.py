@@ -23,6 +23,10 @@ Measured in the same run, each with its own check:
   learned_band    plain full DP vs the network's bands (identical output)
   gap_search      the batched gap anchor search on 20,000 gaps drawn like a
                   recursion round's (oracle-checked on a sample of gaps)
+  outside_lcbs    the search outside LCBs on the recoded pair (300 regions
+                  per genome), checked against the oracle's matcher
+  refinement      both gapped-alignment passes over 120 stand-in LCBs
+                  (oracle-checked on the refinement ranges of 10 LCBs)
   index_lut       buildIndex's LUT step
 
     python bench.py [--gpus N --steps K --warmup W] [--impl gb300|reference]
@@ -379,6 +383,143 @@ def gap_search_section(ctx, dev, rank):
                              "kind": "port", "sample": "the same 100 gaps through the oracle, one thread"}}
 
 
+OL_NREG = 300
+
+
+def outside_lcbs_section(ctx, dev, rank):
+    """The search outside LCBs (SearchLCBGaps) on the recoded pair: 300
+    regions per genome (lengths uniform 0-4,000 bp, as LCB flanks), the
+    genomes resident on the device, one call; the result compared with the
+    oracle's matcher on the two concatenations finished by the library's
+    host steps (which equal the reference's own on the fixtures)."""
+    import torch
+
+    import mvg
+    import oracle as O
+    import synth
+    a, b = synth.genome_pair_recoded(seed=1 + rank)
+    rng = np.random.default_rng(90 + rank)
+
+    def regions(n):
+        cuts = np.sort(rng.choice(np.arange(1, n - 4000), OL_NREG, replace=False))
+        out, end = [], 1
+        for c in cuts:
+            lo = max(int(c), end)
+            hi = min(n + 1, lo + int(rng.integers(0, 4000)))
+            out += [lo, hi]
+            end = hi
+        return np.array(out, np.int64)
+
+    ra, rb = regions(len(a)), regions(len(b))
+    bases = float(np.diff(ra.reshape(-1, 2)).sum() + np.diff(rb.reshape(-1, 2)).sum())
+    da, db = torch.from_numpy(a).to(dev), torch.from_numpy(b).to(dev)
+    cap = 1 << 20
+    ctx.search_lcb_gaps_dev(da.data_ptr(), len(a), db.data_ptr(), len(b), ra, rb, cap)  # warm-up
+    ts = []
+    for _ in range(3):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        got, w = ctx.search_lcb_gaps_dev(da.data_ptr(), len(a), db.data_ptr(), len(b), ra, rb, cap)
+        ts.append(time.perf_counter() - t0)
+    t = min(ts)
+    ca = np.concatenate([a[l - 1:r - 1] for l, r in ra.reshape(-1, 2)])
+    cb = np.concatenate([b[l - 1:r - 1] for l, r in rb.reshape(-1, 2)])
+    t0 = time.perf_counter()
+    raw = O.pairwise_matches(ca, cb, mvg.get_seed(w, 0))
+    want = mvg.lcb_gap_finish(raw, ra, rb)
+    cpu_s = time.perf_counter() - t0
+    return {"workload": "recoded pair, %d regions per genome outside stand-in LCBs (0-4,000 bp), %.2f Mbp "
+                        "concatenated, seed weight %d, one call" % (OL_NREG, bases / 1e6, w),
+            "value": round(bases / 1e6 / t, 2), "unit": "Mbp/s searched", "ms": round(1e3 * t, 3),
+            "matches": int(len(got)),
+            "timing": "host wall clock around the device-genome call (gather, GPU matcher, host transposition "
+                      "and overlap elimination)",
+            "identical_to_oracle": bool(np.array_equal(got, want)),
+            "cpu_baseline": {"value": round(bases / 1e6 / cpu_s, 3), "unit": "Mbp/s searched", "cores": 1,
+                             "kind": "port", "sample": "the same regions: the oracle's matcher on the "
+                                                       "concatenations, then the host steps"}}
+
+
+RF_NLCB = 120
+
+
+def refinement_section(ctx, rank):
+    """Both gapped-alignment passes a two-genome run makes over its LCBs
+    (refineAlignment's anchored realignment of every window, then the final
+    RefineFast pass) on 120 stand-in LCBs (a random sequence and a copy with
+    2-25% substitutions and one-sided gap runs, about 12,000 columns each);
+    every pass is one batched gap-DP call; 200 of the refinement pass's
+    ranges compared with the oracle's NWSmall."""
+    import mvg
+    import oracle as O
+    rng = np.random.default_rng(120 + rank)
+    acgt = np.frombuffer(b"ACGT", np.uint8)
+    lcbs = []
+    for _ in range(RF_NLCB):
+        n = int(rng.integers(6000, 18000))
+        div = float(rng.uniform(0.02, 0.25))
+        ra = acgt[rng.integers(0, 4, n)]
+        rb = ra.copy()
+        sub = rng.random(n) < div
+        rb[sub] = acgt[(np.searchsorted(acgt, rb[sub]) + rng.integers(1, 4, int(sub.sum()))) % 4]
+        runs = rng.random(n) < 0.01
+        for c in np.nonzero(runs)[0]:
+            ln = int(rng.geometric(1 / 4.0))
+            (ra if rng.random() < 0.5 else rb)[c:c + ln] = ord("-")
+        both = (ra == ord("-")) & (rb == ord("-"))
+        ra, rb = ra[~both], rb[~both]
+        lcbs.append((ra, rb))
+    cols = float(sum(len(x[0]) for x in lcbs))
+    ctx.gapped_alignment(lcbs[:4])  # warm-up
+    t0 = time.perf_counter()
+    first = ctx.refine_alignment(lcbs)
+    t1 = time.perf_counter()
+    final = ctx.iterative_refine(first)
+    t2 = time.perf_counter()
+    # the refinement pass's ranges on a sample, against the oracle
+    same, cpu_s, cpu_cells, checked = True, 0.0, 0, 0
+    code = np.full(256, 0, np.uint8)
+    code[np.frombuffer(b"ACGT", np.uint8)] = np.arange(4, dtype=np.uint8)
+    for k in range(0, RF_NLCB, 12):
+        fa, fb = np.frombuffer(first[k][0], np.uint8), np.frombuffer(first[k][1], np.uint8)
+        outa, outb, at = [], [], 0
+        for lo, hi in mvg.refine_fast_ranges(fa, fb).tolist():
+            outa.append(fa[at:lo])
+            outb.append(fb[at:lo])
+            wa, wb = fa[lo:hi], fb[lo:hi]
+            x, y = wa[wa != ord("-")], wb[wb != ord("-")]
+            if len(x) and len(y):
+                t3 = time.perf_counter()
+                path, _ = O.nw_align(code[x], code[y])
+                cpu_s += time.perf_counter() - t3
+                cpu_cells += len(x) * len(y)
+                i = j = 0
+                xa, xb = [], []
+                for e in path:
+                    xa.append(x[i] if e in "MD" else ord("-"))
+                    xb.append(y[j] if e in "MI" else ord("-"))
+                    i += e in "MD"
+                    j += e in "MI"
+                wa, wb = np.array(xa, np.uint8), np.array(xb, np.uint8)
+                checked += 1
+            outa.append(wa)
+            outb.append(wb)
+            at = hi
+        outa.append(fa[at:])
+        outb.append(fb[at:])
+        same = same and np.concatenate(outa).tobytes() == final[k][0] and np.concatenate(outb).tobytes() == final[k][1]
+    return {"workload": "%d stand-in LCBs of two genomes, %.2f M columns (divergence 2-25%%, one-sided gap runs)"
+                        % (RF_NLCB, cols / 1e6),
+            "value": round(cols / 1e6 / (t2 - t0), 3), "unit": "M columns/s (both passes)",
+            "gapped_alignment_ms": round(1e3 * (t1 - t0), 2), "refinement_ms": round(1e3 * (t2 - t1), 2),
+            "timing": "host wall clock around each pass (window and range planning on the host, one batched "
+                      "gap-DP call and the GPU row rebuild per pass)",
+            "refinement_identical_to_oracle_on_sample": bool(same),
+            "oracle_sample": "every refinement range of 10 LCBs (%d problems)" % checked,
+            "cpu_baseline": {"value": round(cpu_cells / cpu_s / 1e9, 4) if cpu_s else None, "unit": "GCUPS",
+                             "cores": 1, "kind": "port", "sample": "the oracle's NWSmall on the same ranges"}}
+
+
 def mds42_section(ctx, dev, stream, flush):
     """Anchoring on the reference's own recoded E. coli fixture pair
     (tests/golden/mds42.npz, 3.98 Mbp each): device-resident throughput and
@@ -731,6 +872,17 @@ def run_gb300(args, world, rank, local):
             gs = line["gap_search"]
             line.update({"value": gs["value"], "unit": gs["unit"], "ms_per_step": gs["ms"]})
 
+    if args.only in ("all", "outside"):
+        line["outside_lcbs"] = outside_lcbs_section(ctx, dev, rank)
+        if args.only == "outside":
+            ol = line["outside_lcbs"]
+            line.update({"value": ol["value"], "unit": ol["unit"], "ms_per_step": ol["ms"]})
+    if args.only in ("all", "refine"):
+        line["refinement"] = refinement_section(ctx, rank)
+        if args.only == "refine":
+            rf = line["refinement"]
+            line.update({"value": rf["value"], "unit": rf["unit"]})
+
     lut_sec = None
     if args.only in ("all", "lut"):
         lut_sec = lut_section(ctx, args, dev, stream, rank, flush)
@@ -778,7 +930,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--skip-cpu-baseline", action="store_true")
-    ap.add_argument("--only", choices=["all", "anchor", "gapdp", "gapsearch", "lut"], default="all",
+    ap.add_argument("--only", choices=["all", "anchor", "gapdp", "gapsearch", "outside", "refine", "lut"],
+                    default="all",
                     help="run one half only (small cases for profiler captures)")
     ap.add_argument("--pair", choices=["recoded", "small"], default="recoded",
                     help="genome pair: recoded 4.6 Mbp (default) or the 1 Mbp plain-method pair")

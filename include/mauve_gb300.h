@@ -269,6 +269,25 @@ int mvg_refine_windows(const uint8_t* row_a, const uint8_t* row_b, uint64_t ncol
 int mvg_refine_fast_ranges(const uint8_t* row_a, const uint8_t* row_b, uint64_t ncols, double max_window_size,
                            int64_t* ranges, uint64_t cap, uint64_t* n);
 
+/* Both gapped-alignment passes of a two-genome progressiveMauve run over
+ * many LCBs in one call: doGappedAlignment (LM/ProgressiveAligner.cpp:
+ * 1242-1290) with refineAlignment (:1119-1230).  passes bit 0: the
+ * gapped-alignment pass (profile_aln = true; every window that is not a gap
+ * window and holds bases of both genomes realigned as ProfileAlignFast
+ * (anchored) does, LM/MuscleInterface.cpp:1053-1109); bit 1: the final
+ * iterative-refinement pass (profile_aln = false; mvg_refine_fast_ranges'
+ * column windows realigned as RefineFast does).  Each pass plans on the
+ * host, runs all problems of all LCBs in one batched gap-DP call and
+ * rebuilds their rows on the GPU.  LCB k is columns col_off[k] ..
+ * col_off[k+1]-1 of rows_a / rows_b ('-' gaps, bases A/C/G/T in either case
+ * where a problem needs them, else MVG_ERR_BAD_BASE).  Out: the new rows in
+ * out_a / out_b, LCB k at out_off[k] .. out_off[k+1]-1 (out_off has nlcb+1
+ * entries and is set even when MVG_ERR_CAPACITY reports that the rows need
+ * more than cap columns). */
+int mvg_gapped_alignment(mvg_handle h, const uint8_t* rows_a, const uint8_t* rows_b, const uint64_t* col_off,
+                         int64_t nlcb, double max_window_size, int passes, uint8_t* out_a, uint8_t* out_b,
+                         uint64_t* out_off, uint64_t cap);
+
 /* ------------------------------------------------ search outside LCBs */
 
 /* Match lists below are 3 int64 per match: libMems' signed 1-based start in

@@ -20,6 +20,7 @@
 
 #include <vector>
 
+#include "lcb_host.h"
 #include "mvg_internal.h"
 
 namespace mvg {
@@ -113,13 +114,9 @@ float ceil_score(float x) { return (float)(x > kSmoothCeil ? kSmoothCeil : x); }
 
 using namespace mvg;
 
-extern "C" int mvg_anchor_columns(const uint8_t* row_a, const uint8_t* row_b, uint64_t ncols, uint32_t* cols,
-                                  uint64_t cap, uint64_t* ncols_out) {
-  if (!ncols_out || (ncols && (!row_a || !row_b)) || (cap && !cols)) return report_error(MVG_ERR_ARG, "null argument");
-  if (ncols >= (1ull << 31)) return report_error(MVG_ERR_ARG, "window longer than 2^31 columns");
-  *ncols_out = 0;
-  const unsigned n = (unsigned)ncols;
-  if (n == 0) return 0;
+void mvg::anchor_columns(const uint8_t* row_a, const uint8_t* row_b, unsigned n, std::vector<unsigned>& out) {
+  out.clear();
+  if (n == 0) return;
   std::vector<float> score, smooth(n, 0.0f);
   column_scores(row_a, row_b, n, score);
   // WindowSmooth
@@ -143,7 +140,6 @@ extern "C" int mvg_anchor_columns(const uint8_t* row_a, const uint8_t* row_b, ui
   }
   // MergeBestCols: two candidates within a window keep the better scoring;
   // more keep the one nearest the first, among all but the window's last
-  uint64_t m = 0;
   for (size_t k = 0; k < best.size();) {
     const unsigned first = best[k];
     unsigned within = 0;
@@ -168,10 +164,19 @@ extern "C" int mvg_anchor_columns(const uint8_t* row_a, const uint8_t* row_b, ui
       }
       anchor = closest;
     }
-    if (m < cap) cols[m] = anchor;
-    ++m;
+    out.push_back(anchor);
     k += within + 1;
   }
+}
+
+extern "C" int mvg_anchor_columns(const uint8_t* row_a, const uint8_t* row_b, uint64_t ncols, uint32_t* cols,
+                                  uint64_t cap, uint64_t* ncols_out) {
+  if (!ncols_out || (ncols && (!row_a || !row_b)) || (cap && !cols)) return report_error(MVG_ERR_ARG, "null argument");
+  if (ncols >= (1ull << 31)) return report_error(MVG_ERR_ARG, "window longer than 2^31 columns");
+  std::vector<unsigned> found;
+  anchor_columns(row_a, row_b, (unsigned)ncols, found);
+  const uint64_t m = found.size();
+  for (uint64_t k = 0; k < m && k < cap; ++k) cols[k] = found[k];
   *ncols_out = m;
   if (m > cap) return report_error(MVG_ERR_CAPACITY, "anchor column buffer too small");
   return 0;

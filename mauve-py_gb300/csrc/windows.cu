@@ -29,6 +29,7 @@
 #include <list>
 #include <vector>
 
+#include "lcb_host.h"
 #include "mvg_internal.h"
 
 namespace mvg {
@@ -40,17 +41,15 @@ constexpr double kMinWindowSize = 200;    // min_window_size (:58)
 constexpr double kMinDensity = .5;        // min_density (:60)
 constexpr double kMaxDensity = .9;        // max_density (:61)
 
-struct Window {
-  uint64_t lo, hi;  // columns [lo, hi)
-  bool gap;
-  int density;  // IsDenseEnough's class of the final window: 0, 1 or 2
-};
+using Window = LcbWindow;
 
 // RefineW's window widths by density class (refineAlignment with
 // profile_aln = false, :1201-1212: RefineFast(w), RefineFast(w, 500),
 // RefineFast(w, 200)); 0 = no change (RefineVert needs three sequences,
 // MU/refinevert.cpp:60-61).
 constexpr uint64_t kRefineWidth[3] = {0, 500, 200};
+
+}  // namespace
 
 // refineAlignment's windows of one LCB (removeLargeGapsPP, then halving by
 // IsDenseEnough), each with its density class.
@@ -132,7 +131,8 @@ std::vector<Window> lcb_windows(const uint8_t* row_a, const uint8_t* row_b, uint
   return std::vector<Window>(wins.begin(), wins.end());
 }
 
-}  // namespace
+uint64_t refine_width(int density) { return kRefineWidth[density]; }
+
 }  // namespace mvg
 
 using namespace mvg;

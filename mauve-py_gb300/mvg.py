@@ -51,7 +51,8 @@ EXPORTS = ["mvg_create", "mvg_destroy", "mvg_last_error", "mvg_stream", "mvg_ker
            "mvg_xmfa_write", "mvg_xmfa_write_dev", "mvg_set_mlp_tcgen05", "mvg_mlp_tcgen05_passes",
            "mvg_set_dp_checkpoint", "mvg_set_band_whole_full_rows", "mvg_set_ring_max_rows",
            "mvg_recursion_gaps", "mvg_anchor_columns", "mvg_refine_windows", "mvg_search_lcb_gaps",
-           "mvg_refine_fast_ranges", "mvg_search_lcb_gaps_dev", "mvg_lcb_gap_finish", "mvg_transpose_matches", "mvg_eliminate_overlaps"]
+           "mvg_refine_fast_ranges", "mvg_gapped_alignment", "mvg_search_lcb_gaps_dev", "mvg_lcb_gap_finish",
+           "mvg_transpose_matches", "mvg_eliminate_overlaps"]
 
 TUNING_PATH = os.path.join(HERE, "dp_tuning.json")
 
@@ -102,6 +103,7 @@ def load_library(path=LIB_PATH):
         "mvg_anchor_columns": (ci, [vp, vp, u64, vp, u64, ctypes.POINTER(u64)]),
         "mvg_refine_windows": (ci, [vp, vp, u64, ctypes.c_double, vp, u64, ctypes.POINTER(u64)]),
         "mvg_refine_fast_ranges": (ci, [vp, vp, u64, ctypes.c_double, vp, u64, ctypes.POINTER(u64)]),
+        "mvg_gapped_alignment": (ci, [vp, vp, vp, vp, i64, ctypes.c_double, ci, vp, vp, vp, u64]),
         "mvg_search_lcb_gaps": (ci, [vp, vp, u64, vp, u64, vp, u64, vp, u64, vp, u64, ctypes.POINTER(u64),
                                      ctypes.POINTER(ctypes.c_uint32)]),
         "mvg_search_lcb_gaps_dev": (ci, [vp, vp, u64, vp, u64, vp, u64, vp, u64, vp, u64, ctypes.POINTER(u64),
@@ -721,97 +723,60 @@ class Context:
             out.append((b"".join(ra), b"".join(rb)))
         return out
 
+    def _gapped(self, lcbs, max_window_size, passes):
+        """mvg_gapped_alignment over a list of (row A, row B)."""
+        rows = [(_u8(ra), _u8(rb)) for ra, rb in lcbs]
+        for ra, rb in rows:
+            if len(ra) != len(rb):
+                raise ValueError("rows of different length")
+        if not rows:
+            return []
+        ra = np.concatenate([r[0] for r in rows])
+        rb = np.concatenate([r[1] for r in rows])
+        off = np.zeros(len(rows) + 1, np.uint64)
+        off[1:] = np.cumsum([len(r[0]) for r in rows])
+        out_off = np.zeros(len(rows) + 1, np.uint64)
+        cap = int(len(ra) * 1.25) + 1024
+        while True:
+            oa, ob = np.zeros(cap, np.uint8), np.zeros(cap, np.uint8)
+            rc = load_library().mvg_gapped_alignment(self._h, _ptr(ra), _ptr(rb), _ptr(off), len(rows),
+                                                     float(max_window_size), int(passes), _ptr(oa), _ptr(ob),
+                                                     _ptr(out_off), cap)
+            if rc == MVG_ERR_CAPACITY and int(out_off[-1]) > cap:
+                cap = int(out_off[-1])
+                continue
+            _check(rc)
+            return [(oa[out_off[k]:out_off[k + 1]].tobytes(), ob[out_off[k]:out_off[k + 1]].tobytes())
+                    for k in range(len(rows))]
+
     def refine_alignment(self, lcbs, max_window_size=20000.0):
         """The gapped-alignment pass of refineAlignment for LCBs of two
         genomes (LM/ProgressiveAligner.cpp:1119-1230 with profile_aln, as
-        doGappedAlignment calls it at step 8 of alignProfileToProfile): each
-        LCB cut into windows (mvg_refine_windows), every window that is not a
-        gap window and holds bases of both genomes realigned with
-        anchored_realign (all windows of all LCBs in one batch), and each
-        LCB's windows concatenated.  lcbs: list of (row A, row B).  Returns
-        the new (row A, row B) bytes of each LCB."""
-        jobs, plan = [], []
-        for ra, rb in lcbs:
-            a, b = _u8(ra), _u8(rb)
-            parts = []
-            for lo, hi, gap in refine_windows(a, b, max_window_size).tolist():
-                wa, wb = a[lo:hi], b[lo:hi]
-                if not gap and (wa != ord("-")).any() and (wb != ord("-")).any():
-                    parts.append(len(jobs))
-                    jobs.append((wa, wb))
-                else:
-                    parts.append((wa.tobytes(), wb.tobytes()))
-            plan.append(parts)
-        done = self.anchored_realign(jobs) if jobs else []
-        out = []
-        for parts in plan:
-            rows = [done[p] if isinstance(p, int) else p for p in parts]
-            out.append((b"".join(r[0] for r in rows), b"".join(r[1] for r in rows)))
-        return out
-
-    def _realign_ranges(self, jobs):
-        """Global NWSmall of each job's bases (job: (row A, row B) column
-        range), all in one gap-DP call on the GPU, rows rebuilt on the GPU;
-        a job with bases of one genome only keeps its columns.  Returns the
-        (row A, row B) bytes of each job."""
-        code = np.full(256, 255, np.uint8)
-        for i, ch in enumerate(b"ACGT"):
-            code[ch] = code[ch | 0x20] = i
-        sa, sb, oa, ob, slot = [], [], [0], [0], []
-        for wa, wb in jobs:
-            a, b = wa[wa != ord("-")], wb[wb != ord("-")]
-            if len(a) == 0 or len(b) == 0:
-                slot.append((wa.tobytes(), wb.tobytes()))
-                continue
-            if (code[a] == 255).any() or (code[b] == 255).any():
-                raise ValueError("the gap DP takes A, C, G and T only")
-            slot.append(len(oa) - 1)
-            sa.append(a)
-            sb.append(b)
-            oa.append(oa[-1] + len(a))
-            ob.append(ob[-1] + len(b))
-        rows = []
-        if len(oa) > 1:
-            chars_a, chars_b = np.concatenate(sa), np.concatenate(sb)
-            _, paths = self.gap_align_batch(code[chars_a], oa, code[chars_b], ob)
-            rows = self.path_rows(chars_a, oa, chars_b, ob, paths)
-        return [rows[s] if isinstance(s, int) else s for s in slot]
+        doGappedAlignment calls it at step 8 of alignProfileToProfile;
+        mvg_gapped_alignment, pass 1): each LCB cut into windows
+        (mvg_refine_windows), every window that is not a gap window and holds
+        bases of both genomes realigned as ProfileAlignFast(anchored) does
+        (all windows of all LCBs in one gap-DP call), and each LCB's windows
+        concatenated.  lcbs: list of (row A, row B).  Returns the new
+        (row A, row B) bytes of each LCB."""
+        return self._gapped(lcbs, max_window_size, 1)
 
     def iterative_refine(self, lcbs, max_window_size=20000.0):
         """The final iterative-refinement pass for LCBs of two genomes
         (refineAlignment with profile_aln = false,
         LM/ProgressiveAligner.cpp:1119-1230, as alignProfileToProfile ends
-        with it, :3750-3755): RefineFast's column windows (refine_fast_ranges)
-        of every LCB realigned from their bases in one gap-DP call, the other
-        columns kept.  lcbs: list of (row A, row B).  Returns the new
-        (row A, row B) bytes of each LCB."""
-        jobs, plan = [], []
-        for ra, rb in lcbs:
-            a, b = _u8(ra), _u8(rb)
-            parts, at = [], 0
-            for lo, hi in refine_fast_ranges(a, b, max_window_size).tolist():
-                if lo > at:
-                    parts.append((a[at:lo].tobytes(), b[at:lo].tobytes()))
-                parts.append(len(jobs))
-                jobs.append((a[lo:hi], b[lo:hi]))
-                at = hi
-            if at < len(a):
-                parts.append((a[at:].tobytes(), b[at:].tobytes()))
-            plan.append(parts)
-        done = self._realign_ranges(jobs) if jobs else []
-        out = []
-        for parts in plan:
-            rows = [done[p] if isinstance(p, int) else p for p in parts]
-            out.append((b"".join(r[0] for r in rows), b"".join(r[1] for r in rows)))
-        return out
+        with it, :3750-3755; mvg_gapped_alignment, pass 2): RefineFast's
+        column windows (refine_fast_ranges) of every LCB realigned from their
+        bases in one gap-DP call, the other columns kept.  lcbs: list of
+        (row A, row B).  Returns the new (row A, row B) bytes of each LCB."""
+        return self._gapped(lcbs, max_window_size, 2)
 
     def gapped_alignment(self, lcbs, max_window_size=20000.0, refine=True):
-        """Both passes a two-genome progressiveMauve run makes over its LCBs:
-        the gapped-alignment pass (refine_alignment) and, unless refine is
-        False, the final iterative refinement (iterative_refine) on its
+        """Both passes a two-genome progressiveMauve run makes over its LCBs
+        in one call (mvg_gapped_alignment): the gapped-alignment pass and,
+        unless refine is False, the final iterative refinement on its
         output."""
-        out = self.refine_alignment(lcbs, max_window_size)
-        return self.iterative_refine(out, max_window_size) if refine else out
+        return self._gapped(lcbs, max_window_size, 3 if refine else 1)
 
     def xmfa_write(self, file_a, file_b, starts, lengths, rows_a, rows_b, col_off, backbone_file=""):
         """WriteStandardAlignment for pairwise blocks; returns the XMFA text (bytes)."""
