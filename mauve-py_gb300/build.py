@@ -18,8 +18,11 @@ LIBDIR = os.path.join(HERE, "lib")
 OBJDIR = os.path.join(LIBDIR, "obj")
 LIB = os.path.join(LIBDIR, "libmauve_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
-         "-I" + os.path.join(ROOT, "include")]
+# -ffp-contract=off: the host restatements of the reference's float and
+# double arithmetic (anchor-column scores, window densities) must round as
+# the reference does, with no fused multiply-add on hosts that have one.
+FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2", "-Xcompiler",
+         "-ffp-contract=off", "-I" + os.path.join(ROOT, "include")]
 
 
 def nvcc():

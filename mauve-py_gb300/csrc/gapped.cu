@@ -18,7 +18,10 @@
 // the LCBs' rows on the host.
 #include <stdint.h>
 
+#include <algorithm>
+#include <atomic>
 #include <cstring>
+#include <thread>
 #include <vector>
 
 #include "lcb_host.h"
@@ -44,34 +47,36 @@ uint8_t base_code(uint8_t c) {
 // A piece of an LCB's new rows: either a gap-DP problem's rows or literal
 // columns.
 struct Piece {
-  int64_t prob;            // problem index, or -1 for literal columns
+  int64_t prob;            // problem index (within its LCB's plan until merged), or -1
   std::vector<uint8_t> a;  // literal rows (prob < 0)
   std::vector<uint8_t> b;
 };
 
+// The plan of one LCB: its pieces in column order and its problems' bases.
 struct Plan {
-  std::vector<std::vector<Piece>> lcb;  // pieces per LCB, in column order
+  std::vector<Piece> pieces;
   std::vector<uint8_t> chars_a, chars_b, codes_a, codes_b;
   std::vector<uint64_t> off_a{0}, off_b{0};
+  int rc = 0;
 
-  int add_problem(std::vector<Piece>& out, const uint8_t* ra, const uint8_t* rb, uint64_t lo, uint64_t hi) {
+  int add_problem(const uint8_t* ra, const uint8_t* rb, uint64_t lo, uint64_t hi) {
     for (uint64_t c = lo; c < hi; ++c) {
       for (int q = 0; q < 2; ++q) {
         const uint8_t ch = (q ? rb : ra)[c];
         if (is_gap_char(ch)) continue;
         const uint8_t code = base_code(ch);
-        if (code > 3) return report_error(MVG_ERR_BAD_BASE, "the gap DP takes A, C, G and T only");
+        if (code > 3) return MVG_ERR_BAD_BASE;
         (q ? chars_b : chars_a).push_back(ch);
         (q ? codes_b : codes_a).push_back(code);
       }
     }
-    out.push_back(Piece{(int64_t)off_a.size() - 1, {}, {}});
+    pieces.push_back(Piece{(int64_t)off_a.size() - 1, {}, {}});
     off_a.push_back(chars_a.size());
     off_b.push_back(chars_b.size());
     return 0;
   }
-  static void add_literal(std::vector<Piece>& out, const uint8_t* ra, const uint8_t* rb, uint64_t lo, uint64_t hi) {
-    if (hi > lo) out.push_back(Piece{-1, std::vector<uint8_t>(ra + lo, ra + hi), std::vector<uint8_t>(rb + lo, rb + hi)});
+  void add_literal(const uint8_t* ra, const uint8_t* rb, uint64_t lo, uint64_t hi) {
+    if (hi > lo) pieces.push_back(Piece{-1, std::vector<uint8_t>(ra + lo, ra + hi), std::vector<uint8_t>(rb + lo, rb + hi)});
   }
   int64_t nprob() const { return (int64_t)off_a.size() - 1; }
 };
@@ -83,11 +88,11 @@ uint64_t bases_in(const uint8_t* r, uint64_t lo, uint64_t hi) {
 }
 
 // Pass 1 plan for one LCB.
-int plan_anchored(Plan& p, std::vector<Piece>& out, const uint8_t* ra, const uint8_t* rb, uint64_t n, double maxw) {
+int plan_anchored(Plan& p, const uint8_t* ra, const uint8_t* rb, uint64_t n, double maxw) {
   std::vector<unsigned> cols;
   for (const LcbWindow& w : lcb_windows(ra, rb, n, maxw)) {
     if (w.gap || !bases_in(ra, w.lo, w.hi) || !bases_in(rb, w.lo, w.hi)) {
-      Plan::add_literal(out, ra, rb, w.lo, w.hi);
+      p.add_literal(ra, rb, w.lo, w.hi);
       continue;
     }
     anchor_columns(ra + w.lo, rb + w.lo, (unsigned)(w.hi - w.lo), cols);
@@ -97,7 +102,7 @@ int plan_anchored(Plan& p, std::vector<Piece>& out, const uint8_t* ra, const uin
       if (hi > lo) {
         const uint64_t na = bases_in(ra, lo, hi), nb = bases_in(rb, lo, hi);
         if (na && nb) {
-          if (int rc = p.add_problem(out, ra, rb, lo, hi)) return rc;
+          if (int rc = p.add_problem(ra, rb, lo, hi)) return rc;
         } else {  // the other genome's bases against gaps
           Piece piece{-1, {}, {}};
           for (uint64_t c = lo; c < hi; ++c) {
@@ -106,7 +111,7 @@ int plan_anchored(Plan& p, std::vector<Piece>& out, const uint8_t* ra, const uin
             piece.a.push_back(na ? ch : (uint8_t)'-');
             piece.b.push_back(na ? (uint8_t)'-' : ch);
           }
-          if (!piece.a.empty()) out.push_back(std::move(piece));
+          if (!piece.a.empty()) p.pieces.push_back(std::move(piece));
         }
       }
       lo = hi > lo ? hi : lo;
@@ -116,29 +121,73 @@ int plan_anchored(Plan& p, std::vector<Piece>& out, const uint8_t* ra, const uin
 }
 
 // Pass 2 plan for one LCB.
-int plan_refine(Plan& p, std::vector<Piece>& out, const uint8_t* ra, const uint8_t* rb, uint64_t n, double maxw) {
+int plan_refine(Plan& p, const uint8_t* ra, const uint8_t* rb, uint64_t n, double maxw) {
   uint64_t at = 0;
   for (const LcbWindow& w : lcb_windows(ra, rb, n, maxw)) {
     const uint64_t width = refine_width(w.density);
     if (w.gap || width == 0) continue;
     for (uint64_t lo = w.lo; lo < w.hi; lo += width) {
       const uint64_t hi = lo + width < w.hi ? lo + width : w.hi;
-      Plan::add_literal(out, ra, rb, at, lo);
+      p.add_literal(ra, rb, at, lo);
       if (bases_in(ra, lo, hi) && bases_in(rb, lo, hi)) {
-        if (int rc = p.add_problem(out, ra, rb, lo, hi)) return rc;
+        if (int rc = p.add_problem(ra, rb, lo, hi)) return rc;
       } else {
-        Plan::add_literal(out, ra, rb, lo, hi);
+        p.add_literal(ra, rb, lo, hi);
       }
       at = hi;
     }
   }
-  Plan::add_literal(out, ra, rb, at, n);
+  p.add_literal(ra, rb, at, n);
   return 0;
+}
+
+// Runs fn(k) for k in [0, n) on up to 16 host threads claiming one index at
+// a time (LCBs differ in size).
+template <class F>
+void for_each_lcb(size_t n, F&& fn) {
+  const size_t hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  const size_t nt = std::min(hw, n);
+  std::atomic<size_t> next{0};
+  auto worker = [&]() {
+    for (size_t k; (k = next.fetch_add(1)) < n;) fn(k);
+  };
+  if (nt <= 1) {
+    worker();
+    return;
+  }
+  std::vector<std::thread> pool;
+  for (size_t t = 0; t < nt; ++t) pool.emplace_back(worker);
+  for (std::thread& th : pool) th.join();
+}
+
+// The problems of every LCB's plan, concatenated in LCB order.
+struct Batch {
+  std::vector<uint8_t> chars_a, chars_b, codes_a, codes_b;
+  std::vector<uint64_t> off_a{0}, off_b{0};
+  std::vector<int64_t> base;  // first problem of each LCB
+  int64_t nprob() const { return (int64_t)off_a.size() - 1; }
+};
+
+void merge(const std::vector<Plan>& plans, Batch& b) {
+  b.base.assign(plans.size() + 1, 0);
+  for (size_t k = 0; k < plans.size(); ++k) {
+    const Plan& p = plans[k];
+    b.base[k + 1] = b.base[k] + p.nprob();
+    const uint64_t oa = b.chars_a.size(), ob = b.chars_b.size();
+    b.chars_a.insert(b.chars_a.end(), p.chars_a.begin(), p.chars_a.end());
+    b.chars_b.insert(b.chars_b.end(), p.chars_b.begin(), p.chars_b.end());
+    b.codes_a.insert(b.codes_a.end(), p.codes_a.begin(), p.codes_a.end());
+    b.codes_b.insert(b.codes_b.end(), p.codes_b.begin(), p.codes_b.end());
+    for (int64_t q = 1; q <= p.nprob(); ++q) {
+      b.off_a.push_back(oa + p.off_a[q]);
+      b.off_b.push_back(ob + p.off_b[q]);
+    }
+  }
 }
 
 // Runs every problem of a plan on the GPU; rows_a/rows_b get each problem's
 // rows at row_off[k].
-int solve(Ctx* c, const Plan& p, std::vector<uint8_t>& rows_a, std::vector<uint8_t>& rows_b,
+int solve(Ctx* c, const Batch& p, std::vector<uint8_t>& rows_a, std::vector<uint8_t>& rows_b,
           std::vector<uint64_t>& row_off) {
   const int64_t np = p.nprob();
   row_off.assign(np + 1, 0);
@@ -196,38 +245,50 @@ int solve(Ctx* c, const Plan& p, std::vector<uint8_t>& rows_a, std::vector<uint8
   return 0;
 }
 
-// One pass over all LCBs: plan, solve, splice.  rows/col_off in, out.
+// One pass over all LCBs: plan (host threads, one LCB at a time), solve,
+// splice.  rows/col_off in, out.
 int run_pass(Ctx* c, bool anchored, double maxw, std::vector<uint8_t>& ra, std::vector<uint8_t>& rb,
              std::vector<uint64_t>& col_off) {
   const size_t nlcb = col_off.size() - 1;
-  Plan p;
-  p.lcb.resize(nlcb);
-  for (size_t k = 0; k < nlcb; ++k) {
+  std::vector<Plan> plans(nlcb);
+  for_each_lcb(nlcb, [&](size_t k) {
     const uint64_t lo = col_off[k], n = col_off[k + 1] - lo;
-    const int rc = anchored ? plan_anchored(p, p.lcb[k], ra.data() + lo, rb.data() + lo, n, maxw)
-                            : plan_refine(p, p.lcb[k], ra.data() + lo, rb.data() + lo, n, maxw);
-    if (rc) return rc;
-  }
+    plans[k].rc = anchored ? plan_anchored(plans[k], ra.data() + lo, rb.data() + lo, n, maxw)
+                           : plan_refine(plans[k], ra.data() + lo, rb.data() + lo, n, maxw);
+  });
+  for (const Plan& p : plans)
+    if (p.rc) return report_error(p.rc, "the gap DP takes A, C, G and T only");
+  Batch batch;
+  merge(plans, batch);
   std::vector<uint8_t> pa, pb;
   std::vector<uint64_t> poff;
-  if (int rc = solve(c, p, pa, pb, poff)) return rc;
-  std::vector<uint8_t> na, nb;
-  std::vector<uint64_t> noff(1, 0);
-  na.reserve(ra.size());
-  nb.reserve(rb.size());
+  if (int rc = solve(c, batch, pa, pb, poff)) return rc;
+  // each LCB's new length, then the splice into place (host threads)
+  std::vector<uint64_t> noff(nlcb + 1, 0);
   for (size_t k = 0; k < nlcb; ++k) {
-    for (const Piece& piece : p.lcb[k]) {
+    uint64_t len = 0;
+    for (const Piece& piece : plans[k].pieces)
+      len += piece.prob < 0 ? piece.a.size()
+                            : poff[batch.base[k] + piece.prob + 1] - poff[batch.base[k] + piece.prob];
+    noff[k + 1] = noff[k] + len;
+  }
+  std::vector<uint8_t> na(noff[nlcb]), nb(noff[nlcb]);
+  for_each_lcb(nlcb, [&](size_t k) {
+    uint64_t at = noff[k];
+    for (const Piece& piece : plans[k].pieces) {
       if (piece.prob < 0) {
-        na.insert(na.end(), piece.a.begin(), piece.a.end());
-        nb.insert(nb.end(), piece.b.begin(), piece.b.end());
+        std::memcpy(na.data() + at, piece.a.data(), piece.a.size());
+        std::memcpy(nb.data() + at, piece.b.data(), piece.b.size());
+        at += piece.a.size();
       } else {
-        const uint64_t o = poff[piece.prob], e = poff[piece.prob + 1];
-        na.insert(na.end(), pa.begin() + o, pa.begin() + e);
-        nb.insert(nb.end(), pb.begin() + o, pb.begin() + e);
+        const int64_t g = batch.base[k] + piece.prob;
+        const uint64_t o = poff[g], len = poff[g + 1] - o;
+        std::memcpy(na.data() + at, pa.data() + o, len);
+        std::memcpy(nb.data() + at, pb.data() + o, len);
+        at += len;
       }
     }
-    noff.push_back(na.size());
-  }
+  });
   ra.swap(na);
   rb.swap(nb);
   col_off.swap(noff);

@@ -120,6 +120,7 @@ constexpr int kChunk = 1024;  // seeds staged per chunk (dynamic shared memory)
 // kClusterCtas CTAs (k_bucket_replay_cluster); one whose entries outgrow the
 // per-CTA copy is marked kRedo and replayed by k_bucket_replay instead.
 constexpr uint32_t kClusterBucket = 16384;
+static_assert(kBigBucket < 0x8000u && kClusterBucket < 0x8000u, "bucket thresholds must be exact in the bucket order");
 constexpr int kClusterCtas = 8;
 constexpr int kLocalCap = 1536;
 constexpr uint32_t kRedo = 0xffffffffu;
@@ -515,9 +516,20 @@ __global__ void k_bucket_bounds(const uint32_t* __restrict__ sorted_bucket, int6
   }
 }
 
+// Largest-first order of the buckets on 16-bit keys (two radix passes
+// instead of four): counts below 32,768 exactly, larger ones in steps of
+// 128 up to about 4.2 M (clamped above).  The key never decreases with the
+// count, and every threshold the replay tests on this order (kBigBucket,
+// kClusterBucket) is exact, so those tests stay monotone along it; buckets
+// of equal key keep index order.
+__device__ __forceinline__ uint32_t lpt_key16(uint32_t c) {
+  const uint32_t k = c < 0x8000u ? c : 0x8000u + min(0x7fffu, (c - 0x8000u) >> 7);
+  return 0xffffu - k;
+}
+
 __global__ void k_lpt_keys(const uint32_t* __restrict__ cnt, uint32_t* __restrict__ key, uint32_t* __restrict__ id) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < kTableSize; i += gridDim.x * blockDim.x) {
-    key[i] = 0xffffffffu - cnt[i];
+    key[i] = lpt_key16(cnt[i]);
     id[i] = i;
   }
 }
@@ -648,7 +660,7 @@ int pairwise_matches_dev(Ctx* c, const uint8_t* d_a, uint64_t na, const uint8_t*
   c->launches++;
   k_lpt_keys<<<grid_for(kTableSize, 256), 256, 0, c->stream>>>(bcount, lk0, li0);
   c->launches++;
-  which = sort_pairs<uint32_t>(lk0, li0, lk1, li1, kTableSize, 32, sscr, c->stream, &c->launches, c->d_err);
+  which = sort_pairs<uint32_t>(lk0, li0, lk1, li1, kTableSize, 16, sscr, c->stream, &c->launches, c->d_err);
   const uint32_t* border = which ? li1 : li0;
   MatchCtx mc;
   mc.g[0] = ga;
