@@ -139,6 +139,23 @@ def dist_setup(n_gpus):
     return world, rank, local
 
 
+def max_over_ranks(x, world, device):
+    """The slowest rank's time (the job's time): an all-reduce MAX over the
+    process group (NCCL on the GPUs; any backend works)."""
+    if world == 1:
+        return x
+    import torch
+    t = torch.tensor([x], device=device, dtype=torch.float64)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_pair_seed(rank):
+    """Each rank aligns its own genome pair (replicas, weak scaling): the
+    recoded pair's generator seed for a rank."""
+    return 1 + rank
+
+
 def seeds_for(a, b):
     import oracle as O
     w = O.default_seed_weight((len(a) + len(b)) // 2)
@@ -679,12 +696,8 @@ def run_gb300(args, world, rank, local):
     dev = torch.device("cuda", local)
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
 
-    def max_over_ranks(x):
-        if world == 1:
-            return x
-        t = torch.tensor([x], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        return float(t.item())
+    def mor(x):
+        return max_over_ranks(x, world, dev)
 
     line = {"metric": METRIC, "unit": "Mbp/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8/int64",
@@ -697,7 +710,7 @@ def run_gb300(args, world, rank, local):
             a, b = synth.genome_pair_small(seed=rank)
             workload = "plain-method pair: 1 Mbp i.i.d. GC 0.50, A = B + 0.5% subs, 50 indels, 2 x 10 kbp inversions"
         else:
-            a, b = synth.genome_pair_recoded(seed=1 + rank)
+            a, b = synth.genome_pair_recoded(seed=replica_pair_seed(rank))
             workload = WORKLOAD
         seed, w = seeds_for(a, b)
         na, nb = len(a), len(b)
@@ -732,7 +745,7 @@ def run_gb300(args, world, rank, local):
                 stage_tot[name] = stage_tot.get(name, 0.0) + t
         torch.cuda.synchronize()
         launches += ctx.kernel_launches() - launches0
-        tot_ms = max_over_ranks(sum(e0.elapsed_time(e1) for e0, e1 in ev))
+        tot_ms = mor(sum(e0.elapsed_time(e1) for e0, e1 in ev))
         if world > 1:
             torch.distributed.barrier()
         clocks_anchor = sampler.stop()
@@ -764,7 +777,7 @@ def run_gb300(args, world, rank, local):
             t0 = time.perf_counter()
             n_e2e = e2e_step()
             e2e_s += time.perf_counter() - t0
-        e2e_s = max_over_ranks(e2e_s)
+        e2e_s = mor(e2e_s)
         assert n_e2e == nmatch
         e2e_value = world * args.steps * (na + nb) / 1e6 / e2e_s
 
@@ -843,7 +856,7 @@ def run_gb300(args, world, rank, local):
         launches += ctx.kernel_launches() - launches0
         clocks_dp = sampler.stop()
         ctx.set_profiling(False)
-        dp_ms = max_over_ranks(sum(e0.elapsed_time(e1) for e0, e1 in dp_ev) / dp_steps)
+        dp_ms = mor(sum(e0.elapsed_time(e1) for e0, e1 in dp_ev) / dp_steps)
         gcups = world * cells / (dp_ms / 1e3) / 1e9
         int32_peak = ctx.probe_int32_peak()
         dp_kernel_ms = dp_stage.get("dp", 0.0) / dp_steps
