@@ -11,9 +11,9 @@ value = (|A| + |B|) / step time, in Mbp/s, inputs resident in HBM.
 e2e   = the same through the host-buffer C-ABI call (copies inside).
 
 `value` covers the anchoring stages only: the metric's "Mbp/s aligned"
-(FASTA to XMFA) would also take the reference's host steps between the GPU
-calls (LCB selection, backbone, XMFA writer), which are not built here;
-the line says so in "value_scope".
+(FASTA to XMFA) would also take LCB selection with breakpoint elimination
+and the backbone HMM, which are not built here; the line says so in
+"value_scope".
 
 Measured in the same run, each with its own check:
   gap_dp          the batched gap DP on the whole 200,000-pair batch (lengths
@@ -55,8 +55,9 @@ GAP_WORKLOAD = ("batched gap DP: the 200,000-pair batch, lengths log-uniform 10-
 GAP_NPROB = 200_000
 VALUE_SCOPE = ("anchoring Mbp/s: pack, coding-seed keys and sort, unique-seed join, hashing and the "
                "extension/containment replay to the reference's match list, for both genomes; 'Mbp/s aligned' "
-               "(FASTA to XMFA) is not measured: the reference's host steps between the GPU calls (LCB "
-               "selection, backbone HMM, refinement, XMFA writer) are not built here")
+               "(FASTA to XMFA) is not measured: LCB selection with breakpoint elimination and the backbone HMM "
+               "are not built here (the gap search, the search outside LCBs, both gapped-alignment passes and "
+               "the LUT are, each measured in its own section)")
 L2_FLUSH_BYTES = 256 << 20
 OPS_PER_CELL = 10  # D: 2 add + max, I: 2 add + max, M: add + 2 max + add
 
