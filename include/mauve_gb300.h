@@ -288,6 +288,42 @@ int mvg_gapped_alignment(mvg_handle h, const uint8_t* rows_a, const uint8_t* row
                          int64_t nlcb, double max_window_size, int passes, uint8_t* out_a, uint8_t* out_b,
                          uint64_t* out_off, uint64_t cap);
 
+/* -------------------------------------------------- backbone detection */
+
+/* Parameters of the backbone-detection HMM, the members of the reference's
+ * Params (LM/HomologyHMM/homology.h:169-177) in order. */
+typedef struct mvg_hmm_params {
+  double start_homologous;
+  double go_homologous;
+  double go_unrelated;
+  double go_stop_from_unrelated;
+  double go_stop_from_homologous;
+  double emit_homologous[8];
+  double emit_unrelated[8];
+} mvg_hmm_params;
+
+/* The parameters applyBackbone uses (MA/progressiveMauve.cpp:226-238):
+ * getAdaptedHoxdMatrixParameters(gc_content), then go_homologous and
+ * go_unrelated set, then adaptToPercentIdentity(pct_identity)
+ * (LM/HomologyHMM/parameters.h).  progressiveMauve's defaults: 1e-5, 1e-9,
+ * 0.7.  MVG_ERR_ARG unless 0 < pct_identity <= 1 (the reference throws). */
+int mvg_hmm_backbone_params(double gc_content, double go_homologous, double go_unrelated, double pct_identity,
+                            mvg_hmm_params* out);
+
+/* Homologous segments of two-genome alignments: findHssHomologyHMM
+ * (LM/Islands.h:122-196) for every LCB, as detectAndApplyBackbone runs it
+ * (LM/Backbone.cpp:1081-1088, left and right homologous both set): column
+ * emission symbols, the HMM's forward and backward passes in HMMoC's
+ * extended-exponent arithmetic, posterior >= 0.9, and the homologous column
+ * ranges.  Host only (one LCB per host thread).  LCB k is columns
+ * col_off[k] .. col_off[k+1]-1 of rows_a / rows_b.  Out: 2 int64 per
+ * segment (first and last column, inclusive, relative to the LCB), LCB k's
+ * segments at seg_off[k] .. seg_off[k+1]-1 (seg_off has nlcb+1 entries);
+ * *nsegs the total, MVG_ERR_CAPACITY when above cap. */
+int mvg_homologous_segments(const uint8_t* rows_a, const uint8_t* rows_b, const uint64_t* col_off, int64_t nlcb,
+                            const mvg_hmm_params* params, int left_homologous, int right_homologous, int64_t* segs,
+                            uint64_t cap, uint64_t* nsegs, uint64_t* seg_off);
+
 /* ------------------------------------------------ search outside LCBs */
 
 /* Match lists below are 3 int64 per match: libMems' signed 1-based start in

@@ -52,9 +52,23 @@ EXPORTS = ["mvg_create", "mvg_destroy", "mvg_last_error", "mvg_stream", "mvg_ker
            "mvg_set_dp_checkpoint", "mvg_set_band_whole_full_rows", "mvg_set_ring_max_rows",
            "mvg_recursion_gaps", "mvg_anchor_columns", "mvg_refine_windows", "mvg_search_lcb_gaps",
            "mvg_refine_fast_ranges", "mvg_gapped_alignment", "mvg_search_lcb_gaps_dev", "mvg_lcb_gap_finish",
-           "mvg_transpose_matches", "mvg_eliminate_overlaps"]
+           "mvg_transpose_matches", "mvg_eliminate_overlaps", "mvg_hmm_backbone_params",
+           "mvg_homologous_segments"]
 
 TUNING_PATH = os.path.join(HERE, "dp_tuning.json")
+
+
+class HmmParams(ctypes.Structure):
+    """mvg_hmm_params: the backbone-detection HMM's parameters (the members
+    of the reference's Params, libMems/HomologyHMM/homology.h:169-177)."""
+    _fields_ = [("start_homologous", ctypes.c_double), ("go_homologous", ctypes.c_double),
+                ("go_unrelated", ctypes.c_double), ("go_stop_from_unrelated", ctypes.c_double),
+                ("go_stop_from_homologous", ctypes.c_double), ("emit_homologous", ctypes.c_double * 8),
+                ("emit_unrelated", ctypes.c_double * 8)]
+
+    def to_array(self):
+        return np.array([self.start_homologous, self.go_homologous, self.go_unrelated, self.go_stop_from_unrelated,
+                         self.go_stop_from_homologous, *self.emit_homologous, *self.emit_unrelated], np.float64)
 
 
 def load_library(path=LIB_PATH):
@@ -104,6 +118,10 @@ def load_library(path=LIB_PATH):
         "mvg_refine_windows": (ci, [vp, vp, u64, ctypes.c_double, vp, u64, ctypes.POINTER(u64)]),
         "mvg_refine_fast_ranges": (ci, [vp, vp, u64, ctypes.c_double, vp, u64, ctypes.POINTER(u64)]),
         "mvg_gapped_alignment": (ci, [vp, vp, vp, vp, i64, ctypes.c_double, ci, vp, vp, vp, u64]),
+        "mvg_hmm_backbone_params": (ci, [ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                         ctypes.POINTER(HmmParams)]),
+        "mvg_homologous_segments": (ci, [vp, vp, vp, i64, ctypes.POINTER(HmmParams), ci, ci, vp, u64,
+                                         ctypes.POINTER(u64), vp]),
         "mvg_search_lcb_gaps": (ci, [vp, vp, u64, vp, u64, vp, u64, vp, u64, vp, u64, ctypes.POINTER(u64),
                                      ctypes.POINTER(ctypes.c_uint32)]),
         "mvg_search_lcb_gaps_dev": (ci, [vp, vp, u64, vp, u64, vp, u64, vp, u64, vp, u64, ctypes.POINTER(u64),
@@ -346,6 +364,42 @@ def refine_fast_ranges(row_a, row_b, max_window_size=20000.0):
             continue
         _check(rc)
         return r[:2 * int(n.value)].reshape(-1, 2)
+
+
+def hmm_backbone_params(gc_content, go_homologous=0.00001, go_unrelated=0.000000001, pct_identity=0.7):
+    """The backbone HMM's parameters as progressiveMauve's applyBackbone sets
+    them (mauveAligner/src/progressiveMauve.cpp:226-238; its defaults)."""
+    p = HmmParams()
+    _check(load_library().mvg_hmm_backbone_params(float(gc_content), float(go_homologous), float(go_unrelated),
+                                                   float(pct_identity), ctypes.byref(p)))
+    return p
+
+
+def homologous_segments(lcbs, params, left_homologous=True, right_homologous=True):
+    """findHssHomologyHMM for LCBs of two genomes (no GPU needed; see
+    mvg_homologous_segments): for each (row A, row B), the homologous column
+    ranges as int64[k, 2] (first, last column, inclusive)."""
+    rows = [(_u8(ra), _u8(rb)) for ra, rb in lcbs]
+    if not rows:
+        return []
+    ra = np.concatenate([r[0] for r in rows])
+    rb = np.concatenate([r[1] for r in rows])
+    off = np.zeros(len(rows) + 1, np.uint64)
+    off[1:] = np.cumsum([len(r[0]) for r in rows])
+    seg_off = np.zeros(len(rows) + 1, np.uint64)
+    n = ctypes.c_uint64(0)
+    cap = max(16, len(ra) // 64)
+    L = load_library()
+    while True:
+        segs = np.zeros(2 * cap, np.int64)
+        rc = L.mvg_homologous_segments(_ptr(ra), _ptr(rb), _ptr(off), len(rows), ctypes.byref(params),
+                                       int(bool(left_homologous)), int(bool(right_homologous)), _ptr(segs), cap,
+                                       ctypes.byref(n), _ptr(seg_off))
+        if rc == MVG_ERR_CAPACITY:
+            cap = int(n.value)
+            continue
+        _check(rc)
+        return [segs[2 * int(seg_off[k]):2 * int(seg_off[k + 1])].reshape(-1, 2) for k in range(len(rows))]
 
 
 def anchored_problems(row_a, row_b):
