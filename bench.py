@@ -27,6 +27,8 @@ Measured in the same run, each with its own check:
                   per genome), checked against the oracle's matcher
   refinement      both gapped-alignment passes over 120 stand-in LCBs
                   (oracle-checked on the refinement ranges of 10 LCBs)
+  backbone_detection  the backbone HMM's homologous segments of 20 LCBs
+                  (host code, host threads; planted islands checked)
   index_lut       buildIndex's LUT step
 
     python bench.py [--gpus N --steps K --warmup W] [--impl gb300|reference]
@@ -538,6 +540,48 @@ def refinement_section(ctx, rank):
                              "cores": 1, "kind": "port", "sample": "the oracle's NWSmall on the same ranges"}}
 
 
+BB_NLCB = 20
+
+
+def backbone_section(rank):
+    """Backbone detection's homology HMM over 20 LCBs of 200,000 columns (a
+    sequence and a 5%-substituted copy with one unrelated 10,000-column
+    island each): all LCBs in one call (host threads), then each LCB on its
+    own (one thread, as the reference runs the step); the islands found
+    checked against where they were planted."""
+    import mvg
+    rng = np.random.default_rng(180 + rank)
+    acgt = np.frombuffer(b"ACGT", np.uint8)
+    lcbs = []
+    for _ in range(BB_NLCB):
+        a = acgt[rng.integers(0, 4, 200_000)]
+        b = a.copy()
+        sub = rng.random(len(b)) < 0.05
+        b[sub] = acgt[rng.integers(0, 4, int(sub.sum()))]
+        b[50_000:60_000] = acgt[rng.integers(0, 4, 10_000)]
+        lcbs.append((a, b))
+    p = mvg.hmm_backbone_params(0.5)
+    mvg.homologous_segments(lcbs[:2], p)  # warm-up
+    t0 = time.perf_counter()
+    segs = mvg.homologous_segments(lcbs, p)
+    t = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    for lcb in lcbs[:4]:
+        mvg.homologous_segments([lcb], p)
+    t1 = (time.perf_counter() - t0) * BB_NLCB / 4
+    cols = float(sum(len(x[0]) for x in lcbs))
+    # two homologous stretches around each island, their edges within a few
+    # hundred columns of the planted ones (chance matches extend them)
+    found = all(len(sg) == 2 and abs(int(sg[0][1]) - 50_000) < 300 and abs(int(sg[1][0]) - 60_000) < 300
+                for sg in segs)
+    return {"workload": "%d LCBs x 200,000 columns (5%% substitutions, one 10 kbp unrelated island each), "
+                        "progressiveMauve's default HMM parameters" % BB_NLCB,
+            "value": round(cols / 1e6 / t, 2), "unit": "M columns/s (host threads)", "ms": round(1e3 * t, 2),
+            "islands_found": bool(found),
+            "single_thread": {"value": round(cols / 1e6 / t1, 2), "unit": "M columns/s",
+                              "sample": "4 of the LCBs one at a time (one host thread, as the reference runs it)"}}
+
+
 def mds42_section(ctx, dev, stream, flush):
     """Anchoring on the reference's own recoded E. coli fixture pair
     (tests/golden/mds42.npz, 3.98 Mbp each): device-resident throughput and
@@ -897,6 +941,12 @@ def run_gb300(args, world, rank, local):
             rf = line["refinement"]
             line.update({"value": rf["value"], "unit": rf["unit"]})
 
+    if args.only in ("all", "backbone"):
+        line["backbone_detection"] = backbone_section(rank)
+        if args.only == "backbone":
+            bb = line["backbone_detection"]
+            line.update({"value": bb["value"], "unit": bb["unit"], "ms_per_step": bb["ms"]})
+
     lut_sec = None
     if args.only in ("all", "lut"):
         lut_sec = lut_section(ctx, args, dev, stream, rank, flush)
@@ -944,7 +994,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--skip-cpu-baseline", action="store_true")
-    ap.add_argument("--only", choices=["all", "anchor", "gapdp", "gapsearch", "outside", "refine", "lut"],
+    ap.add_argument("--only", choices=["all", "anchor", "gapdp", "gapsearch", "outside", "refine", "backbone", "lut"],
                     default="all",
                     help="run one half only (small cases for profiler captures)")
     ap.add_argument("--pair", choices=["recoded", "small"], default="recoded",
