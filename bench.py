@@ -490,6 +490,13 @@ def refinement_section(ctx, rank):
         ra, rb = ra[~both], rb[~both]
         lcbs.append((ra, rb))
     cols = float(sum(len(x[0]) for x in lcbs))
+    # the recursion's gap enumeration over the same LCBs (host; each LCB as
+    # if at genome position 1 of genomes just long enough)
+    t0 = time.perf_counter()
+    for ra, rb in lcbs:
+        na, nb = int((ra != ord("-")).sum()), int((rb != ord("-")).sum())
+        mvg.recursion_gaps(ra, rb, 1, False, 1, False, na, nb)
+    rec_s = time.perf_counter() - t0
     ctx.gapped_alignment(lcbs[:4])  # warm-up
     t0 = time.perf_counter()
     first = ctx.refine_alignment(lcbs)
@@ -535,6 +542,9 @@ def refinement_section(ctx, rank):
             "timing": "host wall clock around each pass (window and range planning on the host, one batched "
                       "gap-DP call and the GPU row rebuild per pass)",
             "refinement_identical_to_oracle_on_sample": bool(same),
+            "recursion_gaps": {"value": round(cols / 1e6 / rec_s, 2), "unit": "M columns/s",
+                               "timing": "host wall clock, one mvg_recursion_gaps call per LCB through the Python "
+                                         "binding (one thread)"},
             "oracle_sample": "every refinement range of 10 LCBs (%d problems)" % checked,
             "cpu_baseline": {"value": round(cpu_cells / cpu_s / 1e9, 4) if cpu_s else None, "unit": "GCUPS",
                              "cores": 1, "kind": "port", "sample": "the oracle's NWSmall on the same ranges"}}
