@@ -367,6 +367,19 @@ int mvg_transpose_matches(const int64_t* matches, uint64_t n, unsigned seq, cons
 /* EliminateOverlaps (LM/Aligner.cpp:62-176) for two-genome matches.  Host
  * only. */
 int mvg_eliminate_overlaps(const int64_t* matches, uint64_t n, int64_t* out, uint64_t cap, uint64_t* count);
+/* LCBs of a two-genome match list for collinear genomes: the collinear
+ * branch of alignProfileToProfile (LM/ProgressiveAligner.cpp:2281-2303) --
+ * IdentifyBreakpoints, ComputeLCBs_v2, SimpleGetLCBCoverage weights,
+ * breakpoint penalty 100 + their sum, computeLCBAdjacencies_v3, greedy
+ * breakpoint elimination (greedyBreakpointElimination_v4 with a collinear
+ * SimpleBreakpointScorer) and filterMatches_v2.  matches: n (start A, start
+ * B, length) triples, both starts nonzero.  Out: the surviving LCBs' matches
+ * concatenated into out (room for n triples), LCB k at
+ * [lcb_off[k], lcb_off[k + 1]) (*nlcb LCBs; MVG_ERR_CAPACITY when
+ * *nlcb + 1 > lcb_cap), and the deleted matches in deleted (room for n
+ * triples, *ndeleted of them).  Host only. */
+int mvg_collinear_lcbs(const int64_t* matches, uint64_t n, int64_t* out, uint64_t* lcb_off, uint64_t lcb_cap,
+                       uint64_t* nlcb, int64_t* deleted, uint64_t* ndeleted);
 
 /* ------------------------------------------------ band-proposal network */
 

@@ -53,7 +53,7 @@ EXPORTS = ["mvg_create", "mvg_destroy", "mvg_last_error", "mvg_stream", "mvg_ker
            "mvg_recursion_gaps", "mvg_anchor_columns", "mvg_refine_windows", "mvg_search_lcb_gaps",
            "mvg_refine_fast_ranges", "mvg_gapped_alignment", "mvg_search_lcb_gaps_dev", "mvg_lcb_gap_finish",
            "mvg_transpose_matches", "mvg_eliminate_overlaps", "mvg_hmm_backbone_params",
-           "mvg_homologous_segments"]
+           "mvg_homologous_segments", "mvg_collinear_lcbs"]
 
 TUNING_PATH = os.path.join(HERE, "dp_tuning.json")
 
@@ -129,6 +129,7 @@ def load_library(path=LIB_PATH):
         "mvg_lcb_gap_finish": (ci, [vp, u64, vp, u64, vp, u64, vp, u64, ctypes.POINTER(u64)]),
         "mvg_transpose_matches": (ci, [vp, u64, ctypes.c_uint, vp, u64, vp, u64, ctypes.POINTER(u64)]),
         "mvg_eliminate_overlaps": (ci, [vp, u64, vp, u64, ctypes.POINTER(u64)]),
+        "mvg_collinear_lcbs": (ci, [vp, u64, vp, vp, u64, ctypes.POINTER(u64), vp, ctypes.POINTER(u64)]),
         "mvg_set_mlp_tcgen05": (ci, [vp, ci]),
         "mvg_mlp_tcgen05_passes": (ci, [vp, ctypes.POINTER(ctypes.c_uint64)]),
         "mvg_set_dp_coop_strips": (ci, [vp, ci]),
@@ -285,6 +286,26 @@ def eliminate_overlaps(matches):
     L = load_library()
     return _host_matches(lambda out, cap, cnt: L.mvg_eliminate_overlaps(_ptr(m), len(m), _ptr(out), cap,
                                                                         ctypes.byref(cnt)), len(m))
+
+
+def collinear_lcbs(matches):
+    """LCBs of a two-genome match list for collinear genomes, with greedy
+    breakpoint elimination (the collinear branch of alignProfileToProfile,
+    libMems/ProgressiveAligner.cpp:2281-2303; no GPU needed).  Returns (the
+    LCBs, each an int64[k, 3] match list in the reference's order, the
+    deleted matches as int64[d, 3])."""
+    m = _matches(matches)
+    L = load_library()
+    n = len(m)
+    out = np.zeros(3 * max(n, 1), np.int64)
+    deleted = np.zeros(3 * max(n, 1), np.int64)
+    off = np.zeros(n + 2, np.uint64)
+    nlcb, ndel = ctypes.c_uint64(0), ctypes.c_uint64(0)
+    _check(L.mvg_collinear_lcbs(_ptr(m), n, _ptr(out), _ptr(off), len(off), ctypes.byref(nlcb), _ptr(deleted),
+                                ctypes.byref(ndel)))
+    o = off[:nlcb.value + 1].astype(np.int64)
+    rows = out.reshape(-1, 3)
+    return [rows[o[k]:o[k + 1]].copy() for k in range(nlcb.value)], deleted[:3 * ndel.value].reshape(-1, 3)
 
 
 def lcb_gap_finish(matches, regions_a, regions_b):
