@@ -592,6 +592,46 @@ def backbone_section(rank):
                               "sample": "4 of the LCBs one at a time (one host thread, as the reference runs it)"}}
 
 
+def collinear_lcbs_section(rank):
+    """LCBs with greedy breakpoint elimination for collinear genomes (host,
+    one thread, a sequential heap of moves as in the reference) on a
+    synthetic two-genome match list: 300 blocks of 100-1,500 bp, shuffled
+    and 30% inverted in genome B, ungapped 9-40 bp matches along each, and
+    2,000 random matches; checked that the LCBs and the deleted list
+    partition the input."""
+    import mvg
+    rng = np.random.default_rng(190 + rank)
+    nblk = 300
+    lens = rng.integers(100, 1500, nblk)
+    inv = rng.random(nblk) < 0.3
+    pos_a = np.concatenate([[1], 1 + np.cumsum(lens)[:-1]])
+    pos_b, p = np.zeros(nblk, np.int64), 1
+    for k in rng.permutation(nblk):
+        pos_b[k] = p
+        p += int(lens[k]) + 10
+    m = []
+    for k in range(nblk):
+        x = 0
+        while x < lens[k] - 20:
+            L = min(int(rng.integers(9, 40)), int(lens[k] - x))
+            m.append((pos_a[k] + x, -(pos_b[k] + lens[k] - x - L) if inv[k] else pos_b[k] + x, L))
+            x += L + int(rng.integers(0, 30))
+    for _ in range(2000):
+        L = int(rng.integers(9, 30))
+        m.append((int(rng.integers(1, pos_a[-1] + lens[-1] - L)), int(rng.integers(1, p)) * int(rng.choice([-1, 1])),
+                  L))
+    m = np.array(m, np.int64)[rng.permutation(len(m))]
+    mvg.collinear_lcbs(m[:1000])  # warm-up
+    t0 = time.perf_counter()
+    lcbs, deleted = mvg.collinear_lcbs(m)
+    t = time.perf_counter() - t0
+    key = sorted(map(tuple, np.concatenate(lcbs + [deleted]).tolist()))
+    return {"workload": "%d matches: %d blocks shuffled and 30%% inverted, 2,000 random matches" % (len(m), nblk),
+            "value": round(len(m) / 1e3 / t, 1), "unit": "k matches/s (one host thread)", "ms": round(1e3 * t, 2),
+            "lcbs": len(lcbs), "deleted": int(len(deleted)),
+            "partition_ok": key == sorted(map(tuple, m.tolist()))}
+
+
 def mds42_section(ctx, dev, stream, flush):
     """Anchoring on the reference's own recoded E. coli fixture pair
     (tests/golden/mds42.npz, 3.98 Mbp each): device-resident throughput and
@@ -957,6 +997,12 @@ def run_gb300(args, world, rank, local):
             bb = line["backbone_detection"]
             line.update({"value": bb["value"], "unit": bb["unit"], "ms_per_step": bb["ms"]})
 
+    if args.only in ("all", "lcbs"):
+        line["collinear_lcbs"] = collinear_lcbs_section(rank)
+        if args.only == "lcbs":
+            cl = line["collinear_lcbs"]
+            line.update({"value": cl["value"], "unit": cl["unit"], "ms_per_step": cl["ms"]})
+
     lut_sec = None
     if args.only in ("all", "lut"):
         lut_sec = lut_section(ctx, args, dev, stream, rank, flush)
@@ -1004,7 +1050,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--skip-cpu-baseline", action="store_true")
-    ap.add_argument("--only", choices=["all", "anchor", "gapdp", "gapsearch", "outside", "refine", "backbone", "lut"],
+    ap.add_argument("--only", choices=["all", "anchor", "gapdp", "gapsearch", "outside", "refine", "backbone", "lcbs",
+                                         "lut"],
                     default="all",
                     help="run one half only (small cases for profiler captures)")
     ap.add_argument("--pair", choices=["recoded", "small"], default="recoded",
