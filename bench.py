@@ -632,6 +632,66 @@ def collinear_lcbs_section(rank):
             "partition_ok": key == sorted(map(tuple, m.tolist()))}
 
 
+def xmfa_section(ctx, dev, rank):
+    """The XMFA writer (WriteStandardAlignment for pairwise blocks) on a
+    genome-sized alignment: 64 blocks, 4.6 Mbp per genome (2% substitutions,
+    0.05% indels), every other block on the reverse strand of genome B.
+    value: the rows resident on the device, the text assembled there and
+    copied into pinned host memory, wall clock with the call's host planning;
+    e2e: the host-rows call a user makes (rows copied in, text returned as
+    bytes).  Checked by reading the text back with the buildIndex XMFA
+    reader: every block's coordinates, strands and rows."""
+    import torch
+
+    import buildindex
+    import synth
+    gs, rs, off, rg, rr, _, _ = synth.lut_alignment_fast(41 + rank, n_ref=LUT_NREF, sub=0.02, indel=0.0005,
+                                                          nblocks=64)
+    nb = len(off) - 1
+    rs = np.where(np.arange(nb) % 2 == 1, -rs, rs)
+    starts = np.stack([gs, rs], 1).reshape(-1)
+    lens = np.array([[int((x[int(off[b]):int(off[b + 1])] != ord("-")).sum()) for x in (rg, rr)] for b in range(nb)],
+                    np.int64).reshape(-1)
+    names = ("genome.fasta", "reference.fasta")
+    d_a, d_b = torch.from_numpy(rg).to(dev), torch.from_numpy(rr).to(dev)
+    need = ctx.xmfa_write_dev(*names, starts, lens, d_a.data_ptr(), d_b.data_ptr(), off)
+    out = torch.empty(need, dtype=torch.uint8, pin_memory=True)
+
+    def dev_step():
+        return ctx.xmfa_write_dev(*names, starts, lens, d_a.data_ptr(), d_b.data_ptr(), off, out.data_ptr(), need)
+
+    launches0 = ctx.kernel_launches()
+    for _ in range(3):
+        dev_step()
+    launches = (ctx.kernel_launches() - launches0) / 3
+    wall, e2e = [], []
+    for _ in range(5):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        dev_step()
+        wall.append(time.perf_counter() - t0)
+    for _ in range(3):
+        t0 = time.perf_counter()
+        text = ctx.xmfa_write(*names, starts, lens, rg, rr, off)
+        e2e.append(time.perf_counter() - t0)
+    same = out.numpy().tobytes() == text
+    groups = buildindex.parse_xmfa_text(text.decode())
+    ok = len(groups) == nb
+    for b, grp in enumerate(groups if ok else []):
+        for q, sub in enumerate(grp.alignments):
+            s, n = int(starts[2 * b + q]), int(lens[2 * b + q])
+            row = (rg, rr)[q][int(off[b]):int(off[b + 1])].tobytes().decode()
+            ok = ok and sub.start_idx == abs(s) and sub.end_idx == abs(s) + n - 1 and sub.seq == row and \
+                sub.strand == ("+" if s > 0 else "-")
+    t, te = sorted(wall)[2], sorted(e2e)[1]
+    return {"workload": "XMFA of %d blocks, %d columns, 4.6 Mbp per genome (%d bytes of text)" % (nb, len(rg), need),
+            "value": round(need / 1e6 / t, 1), "unit": "MB/s of XMFA text", "ms": round(1e3 * t, 3),
+            "e2e": {"value": round(need / 1e6 / te, 1), "unit": "MB/s of XMFA text", "ms": round(1e3 * te, 3),
+                    "h2d_bytes_per_step": int(2 * len(rg)), "d2h_bytes_per_step": int(need)},
+            "gpu_launches_per_step": launches, "device_and_host_paths_identical": bool(same),
+            "reads_back": bool(ok)}
+
+
 def mds42_section(ctx, dev, stream, flush):
     """Anchoring on the reference's own recoded E. coli fixture pair
     (tests/golden/mds42.npz, 3.98 Mbp each): device-resident throughput and
@@ -997,6 +1057,12 @@ def run_gb300(args, world, rank, local):
             bb = line["backbone_detection"]
             line.update({"value": bb["value"], "unit": bb["unit"], "ms_per_step": bb["ms"]})
 
+    if args.only in ("all", "xmfa"):
+        line["xmfa_writer"] = xmfa_section(ctx, dev, rank)
+        if args.only == "xmfa":
+            xw = line["xmfa_writer"]
+            line.update({"value": xw["value"], "unit": xw["unit"], "ms_per_step": xw["ms"]})
+
     if args.only in ("all", "lcbs"):
         line["collinear_lcbs"] = collinear_lcbs_section(rank)
         if args.only == "lcbs":
@@ -1051,7 +1117,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--skip-cpu-baseline", action="store_true")
     ap.add_argument("--only", choices=["all", "anchor", "gapdp", "gapsearch", "outside", "refine", "backbone", "lcbs",
-                                         "lut"],
+                                         "xmfa", "lut"],
                     default="all",
                     help="run one half only (small cases for profiler captures)")
     ap.add_argument("--pair", choices=["recoded", "small"], default="recoded",

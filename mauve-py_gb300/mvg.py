@@ -871,6 +871,23 @@ class Context:
         _check(L.mvg_xmfa_write(*args, out, int(cnt.value), ctypes.byref(cnt)))
         return out.raw[:cnt.value]
 
+    def xmfa_write_dev(self, file_a, file_b, starts, lengths, d_rows_a, d_rows_b, col_off, out_ptr=None, cap=0,
+                       backbone_file=""):
+        """The writer with the rows in device memory (raw pointers), the text
+        written into the caller's host buffer out_ptr of cap bytes.  Returns
+        the text length; with no buffer (cap 0) only the length needed."""
+        starts = np.ascontiguousarray(starts, np.int64).reshape(-1)
+        lengths = np.ascontiguousarray(lengths, np.int64).reshape(-1)
+        col_off = np.ascontiguousarray(col_off, np.uint64)
+        cnt = ctypes.c_uint64(0)
+        wait_producers()
+        rc = load_library().mvg_xmfa_write_dev(self._h, file_a.encode(), file_b.encode(), backbone_file.encode(),
+                                               len(col_off) - 1, _ptr(starts), _ptr(lengths), d_rows_a, d_rows_b,
+                                               _ptr(col_off), out_ptr, cap, ctypes.byref(cnt))
+        if not (rc == MVG_ERR_CAPACITY and not cap):
+            _check(rc)
+        return int(cnt.value)
+
     def gap_align_batch_raw(self, seq_a, off_a, seq_b, off_b, scores, paths, path_off, path_len):
         """Host-buffer call with caller-owned numpy outputs (no per-call Python decoding)."""
         n = len(off_a) - 1
