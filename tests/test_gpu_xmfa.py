@@ -72,3 +72,28 @@ def test_xmfa_reads_back(ctx):
             assert sub.seq_num == q + 1 and sub.start_idx == abs(s) and sub.end_idx == abs(s) + lengths[2 * b + q] - 1
             assert sub.strand == ("+" if s > 0 else "-")
             assert sub.seq == (ra if q == 0 else rb)[int(cols[b]):int(cols[b + 1])].tobytes().decode()
+
+
+def test_xmfa_device_rows_into_pinned_memory(ctx):
+    """Context.xmfa_write_dev with the rows in device memory writes the
+    reference's text into a pinned host buffer; with no buffer it returns
+    the size needed, and a buffer one byte short is refused."""
+    import torch
+    g = load_golden("xmfa.npz")
+    for k in range(int(g["count"])):
+        (ra, rb), lengths = fill_rows((g["ga"], g["gb"]), g["starts%d" % k], g["cols%d" % k],
+                                      [g["ra%d" % k], g["rb%d" % k]])
+        names = (g["fa%d" % k].tobytes().decode(), g["fb%d" % k].tobytes().decode())
+        bb = g["bb%d" % k].tobytes().decode()
+        d_a = torch.from_numpy(np.concatenate([ra, np.zeros(1, np.uint8)])).cuda()
+        d_b = torch.from_numpy(np.concatenate([rb, np.zeros(1, np.uint8)])).cuda()
+        args = (*names, g["starts%d" % k], lengths, d_a.data_ptr(), d_b.data_ptr(), g["cols%d" % k])
+        need = ctx.xmfa_write_dev(*args, backbone_file=bb)
+        want = g["text%d" % k].tobytes()
+        assert need == len(want)
+        out = torch.zeros(need + 1, dtype=torch.uint8, pin_memory=True)
+        if need > 1:
+            with pytest.raises(OverflowError):
+                ctx.xmfa_write_dev(*args, out.data_ptr(), need - 1, backbone_file=bb)
+        assert ctx.xmfa_write_dev(*args, out.data_ptr(), need, backbone_file=bb) == need
+        assert out[:need].numpy().tobytes() == want, "case %d" % k
