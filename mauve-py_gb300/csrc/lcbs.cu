@@ -343,12 +343,13 @@ struct Scorer {
     for (const Lcb& l : adjs) total_weight += l.weight;
   }
   double score() const { return total_weight - (double)bp_count * bp_penalty; }
+  // scratch of move(), kept between calls so that scoring allocates nothing
+  std::vector<std::pair<uint32_t, uint32_t>> mv_remaps;
+  std::vector<uint32_t> mv_impact;
   double move(size_t i) {
     const double cur = score();
-    std::vector<std::pair<uint32_t, uint32_t>> remaps;
-    std::vector<uint32_t> impact;
-    const uint32_t bp_removed = remove_and_coalesce(i, adjs, scores, remaps, impact);
-    undo_removal(adjs, remaps);
+    const uint32_t bp_removed = remove_and_coalesce(i, adjs, scores, mv_remaps, mv_impact);
+    undo_removal(adjs, mv_remaps);
     const double bp_score = (double)(bp_count - bp_removed) * bp_penalty;
     const double move_score = total_weight - adjs[i].weight - bp_score;
     const double diff = move_score - cur;
