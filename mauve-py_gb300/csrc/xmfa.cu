@@ -23,6 +23,8 @@
 //   =
 #include <string.h>
 
+#include <algorithm>
+
 #include <string>
 #include <vector>
 
@@ -38,21 +40,24 @@ struct XmfaPiece {
   int32_t pad;
 };
 
-// One block of threads per piece; a row's column c goes to dst + c + c/80,
-// with a newline after every 80th column and after the last.
+// Pieces along grid.y, each piece's output bytes spread over grid.x: output
+// byte o of a row piece is column (o / 81) * 80 + o % 81 of the row, or the
+// newline that ends every 80 columns and the last, partial line.
 __global__ void k_xmfa_assemble(const XmfaPiece* __restrict__ pieces, int64_t npieces, const uint8_t* __restrict__ blob,
                                 const uint8_t* __restrict__ rows_a, const uint8_t* __restrict__ rows_b,
                                 uint8_t* __restrict__ out) {
-  for (int64_t k = blockIdx.x; k < npieces; k += gridDim.x) {
+  const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
+  for (int64_t k = blockIdx.y; k < npieces; k += gridDim.y) {
     const XmfaPiece pc = pieces[k];
+    const uint64_t first = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (pc.row < 0) {
-      for (uint64_t i = threadIdx.x; i < pc.len; i += blockDim.x) out[pc.dst + i] = blob[pc.src + i];
+      for (uint64_t i = first; i < pc.len; i += step) out[pc.dst + i] = blob[pc.src + i];
     } else {
       const uint8_t* r = (pc.row == 0 ? rows_a : rows_b) + pc.src;
-      for (uint64_t c = threadIdx.x; c < pc.len; c += blockDim.x) {
-        const uint64_t d = pc.dst + c + c / 80;
-        out[d] = r[c];
-        if (c % 80 == 79 || c + 1 == pc.len) out[d + 1] = '\n';
+      const uint64_t nout = pc.len + (pc.len + 79) / 80;
+      for (uint64_t o = first; o < nout; o += step) {
+        const uint64_t line = o / 81, pos = o - line * 81, c = line * 80 + pos;
+        out[pc.dst + o] = (pos == 80 || c == pc.len) ? (uint8_t)'\n' : r[c];
       }
     }
   }
@@ -155,8 +160,11 @@ extern "C" int mvg_xmfa_write_dev(mvg_handle h, const char* file_a, const char* 
   if (int rc = h2d_async(c, d_pieces, pieces.data(), pieces.size() * sizeof(XmfaPiece), c->stream)) return rc;
   if (int rc = h2d_async(c, d_blob, blob.data(), blob.size(), c->stream)) return rc;
   const int64_t np = (int64_t)pieces.size();
-  k_xmfa_assemble<<<(unsigned)std::min<int64_t>(np, 65535), 256, 0, c->stream>>>(d_pieces, np, d_blob, d_rows_a,
-                                                                                 d_rows_b, d_out);
+  uint64_t widest = 0;  // output bytes of the largest piece
+  for (const XmfaPiece& pc : pieces) widest = std::max(widest, pc.row < 0 ? pc.len : pc.len + (pc.len + 79) / 80);
+  const dim3 grid((unsigned)std::min<uint64_t>(std::max<uint64_t>((widest + 1023) / 1024, 1), 1024),
+                  (unsigned)std::min<int64_t>(np, 65535));
+  k_xmfa_assemble<<<grid, 256, 0, c->stream>>>(d_pieces, np, d_blob, d_rows_a, d_rows_b, d_out);
   c->launches++;
   MVG_CUDA_TRY(cudaGetLastError());
   MVG_CUDA_TRY(cudaMemcpyAsync(out, d_out, total, cudaMemcpyDeviceToHost, c->stream));
